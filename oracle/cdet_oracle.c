@@ -1,0 +1,703 @@
+/*
+ * CPU restatement of the reference CDet Renyi-2 integrand (the oracle).
+ *
+ * TEST INFRASTRUCTURE ONLY (see cdet_oracle.h). Each function cites the
+ * reference file:line it restates; all paths are relative to the reference
+ * project (Boyuan-Shi-0607/cdet-renyi-entanglement-hpc). Compile with
+ * -ffp-contract=off: the operation order below is the reference's, and every
+ * multiply and add must round separately, exactly as on an x86-64 build.
+ */
+#include "cdet_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORACLE_BAD_INPUT 4
+#define ORACLE_MAX_ORDER 24
+
+/* ---------------------------------------------------------------- layout --- */
+
+/* replica_sitepair_index (replica_chebyshev_tables.h:365-382). */
+static uint64_t sitepair_index(int ra, int rb, int x1, int y1, int x2, int y2, int n1, int n2) {
+    return (((((uint64_t)ra * 2u + (uint64_t)rb) * (uint64_t)n1 + (uint64_t)x1) * (uint64_t)n2 +
+             (uint64_t)y1) * (uint64_t)n1 + (uint64_t)x2) * (uint64_t)n2 + (uint64_t)y2;
+}
+
+static double clamp_unit(double value) {
+    /* clamp_to_unit_interval (g_funcs.h:300-309) */
+    if (value < -1.0) return -1.0;
+    if (value > 1.0) return 1.0;
+    return value;
+}
+
+/* prepare_green_lookup_descriptor (g_funcs.h:609-653). The returned index is
+ * the corner index on the corner path and the coefficient block base
+ * (sitepair * nu * nv) otherwise. */
+int oracle_lookup_descriptor(int ra, int rb, double tau1, double tau2, int x1, int y1, int x2,
+                             int y2, double beta, double branch_eps, int nu, int nv, int n1,
+                             int n2, int upper, int* use_corner, uint64_t* index, double* u,
+                             double* v) {
+    const uint64_t sp = sitepair_index(ra, rb, x1, y1, x2, y2, n1, n2);
+    *u = 0.0;
+    *v = 0.0;
+    if (upper) {
+        if (tau1 < branch_eps) {
+            *use_corner = 1;
+            *index = sp;
+            return 0;
+        }
+        *u = clamp_unit(2.0 * tau1 / beta - 1.0);
+        *v = clamp_unit(2.0 * tau2 / tau1 - 1.0);
+    } else {
+        if (tau2 < branch_eps) {
+            *use_corner = 1;
+            *index = sp;
+            return 0;
+        }
+        *u = clamp_unit(2.0 * tau2 / beta - 1.0);
+        *v = clamp_unit(2.0 * tau1 / tau2 - 1.0);
+    }
+    *use_corner = 0;
+    *index = sp * (uint64_t)nu * (uint64_t)nv;
+    return 0;
+}
+
+/* clenshaw_from_contiguous_coeffs / clenshaw_pair_from_contiguous_coeffs
+ * (g_funcs.h:395-463): sum_{k<=degree} c[k] T_k(x). */
+static double clenshaw(const double* c, int degree, double x) {
+    if (degree < 0) return 0.0;
+    if (degree == 0) return c[0];
+    if (degree == 1) return c[0] + c[1] * x;
+    const double two_x = 2.0 * x;
+    double b1 = 0.0, b2 = 0.0;
+    for (int k = degree; k >= 1; --k) {
+        const double bk = c[k] + two_x * b1 - b2;
+        b2 = b1;
+        b1 = bk;
+    }
+    return c[0] + b1 * x - b2;
+}
+
+/* chebyshev_sum_2d_pair_from_ptrs (g_funcs.h:687-763): a Clenshaw sum along v
+ * on every row of the nu x nv block (row-major, v fastest), then one along u
+ * over the row values. The fixed-degree specialisations (:561-578) perform
+ * the same operations in the same order. */
+static double chebyshev_2d(const double* block, double u, double v, int nu, int nv) {
+    double rows[512];
+    for (int a = 0; a < nu; ++a) rows[a] = clenshaw(block + (size_t)a * (size_t)nv, nv - 1, v);
+    return clenshaw(rows, nu - 1, u);
+}
+
+/* evaluate_green_pair_descriptor (g_funcs.h:793-818). */
+void oracle_green_pair(const oracle_table* up, const oracle_table* down, int upper,
+                       int use_corner, uint64_t index, double u, double v, int nu, int nv,
+                       double* up_value, double* down_value) {
+    if (use_corner) {
+        *up_value = upper ? up->upper_corners[index] : up->lower_corners[index];
+        *down_value = upper ? down->upper_corners[index] : down->lower_corners[index];
+        return;
+    }
+    const double* cu = (upper ? up->upper_coeffs : up->lower_coeffs) + index;
+    const double* cd = (upper ? down->upper_coeffs : down->lower_coeffs) + index;
+    *up_value = chebyshev_2d(cu, u, v, nu, nv);
+    *down_value = chebyshev_2d(cd, u, v, nu, nv);
+}
+
+/* ---------------------------------------------------------- vertex decode --- */
+
+typedef struct vertex {
+    double tau, tau_unit;
+    int x, y, replica;
+} vertex;
+
+/* sampled_coordinate_to_index (g_funcs.h:315-342): floor then clamp to
+ * [0, extent-1]. The reference throws std::overflow_error outside the int
+ * range; non-finite input is undefined there. Both are reported here. */
+static int coordinate_to_index(double coordinate, int extent, int* bad) {
+    if (!isfinite(coordinate) || coordinate <= -2147483648.0 || coordinate >= 2147483648.0) {
+        *bad = 1;
+        return 0;
+    }
+    int index = (int)floor(coordinate);
+    if (index < 0) index = 0;
+    if (index >= extent) index = extent - 1;
+    return index;
+}
+
+/* Vertex decode of integrand_temp_typed (integrand_replica_randomly_sampled.h:422-432)
+ * with sampled_replica_from_unit_coordinate_typed (:142-153). */
+static int decode_vertices(const oracle_scalars* s, const double* args, int order,
+                           int replica_count, vertex* out) {
+    int bad = 0;
+    for (int i = 0; i < order; ++i) {
+        const double* a = args + 4 * i;
+        if (!isfinite(a[0])) bad = 1;
+        out[i].tau_unit = a[0];
+        out[i].tau = s->beta * a[0];
+        out[i].x = coordinate_to_index((double)s->n1 * a[1], s->n1, &bad);
+        out[i].y = coordinate_to_index((double)s->n2 * a[2], s->n2, &bad);
+        if (replica_count <= 1) {
+            out[i].replica = 0;
+        } else {
+            int r = coordinate_to_index((double)replica_count * a[3], replica_count, &bad);
+            out[i].replica = r < 0 ? 0 : (r > replica_count - 1 ? replica_count - 1 : r);
+        }
+    }
+    return bad;
+}
+
+/* Green-matrix fill of integrand_temp_typed (:434-484) and of the all-subset
+ * variant (:698-776): entry (i,j) of each spin matrix is the table value at
+ * (vertex i, vertex j), the diagonal gets the crossed alpha shift, and every
+ * entry is multiplied by sqrt(U*N1*N2*beta). diag_up/diag_down (optional)
+ * receive the shifted, unscaled diagonal the all-subset singletons use. */
+static void fill_from_vertices(const oracle_scalars* s, const oracle_table* tu,
+                               const oracle_table* td, const vertex* vx, int order,
+                               double* mat_up, double* mat_down, double* diag_up,
+                               double* diag_down) {
+    for (int idx = 0; idx < order * order; ++idx) {
+        const int i = idx / order;
+        const int j = idx - i * order;
+        const int upper = (i != j) && (vx[i].tau_unit > vx[j].tau_unit);
+        int corner;
+        uint64_t index;
+        double u, v, up, down;
+        oracle_lookup_descriptor(vx[i].replica, vx[j].replica, vx[i].tau, vx[j].tau, vx[i].x,
+                                 vx[i].y, vx[j].x, vx[j].y, s->beta, s->branch_eps, s->cheb_nu,
+                                 s->cheb_nv, s->n1, s->n2, upper, &corner, &index, &u, &v);
+        oracle_green_pair(tu, td, upper, corner, index, u, v, s->cheb_nu, s->cheb_nv, &up, &down);
+        if (i == j) {
+            if (diag_up) diag_up[i] = up + s->diag_up_shift;
+            if (diag_down) diag_down[i] = down + s->diag_down_shift;
+            up += s->diag_up_shift;
+            down += s->diag_down_shift;
+        }
+        mat_up[idx] = up * s->scale;
+        mat_down[idx] = down * s->scale;
+    }
+}
+
+int oracle_fill_green(const oracle_scalars* s, const oracle_table* up, const oracle_table* down,
+                      const double* unit_vertices, int order, int replica_count, double* mat_up,
+                      double* mat_down, double* diag_up, double* diag_down) {
+    vertex vx[ORACLE_MAX_ORDER];
+    if (order < 1 || order > ORACLE_MAX_ORDER) return ORACLE_BAD_INPUT;
+    if (decode_vertices(s, unit_vertices, order, replica_count, vx)) return ORACLE_BAD_INPUT;
+    fill_from_vertices(s, up, down, vx, order, mat_up, mat_down, diag_up, diag_down);
+    return 0;
+}
+
+/* ------------------------------------------------------ principal minors --- */
+
+/* determinant_principal_minor_from_buffer (fast_principle_minors.h:39-105):
+ * partial-pivot LU of the principal submatrix selected by mask. */
+static double minor_by_lu(const double* a, int n, uint64_t mask) {
+    int idx[64];
+    int k = 0;
+    for (int i = 0; i < n; ++i)
+        if (mask & ((uint64_t)1 << i)) idx[k++] = i;
+    if (k == 0) return 1.0;
+    double m[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER];
+    for (int r = 0; r < k; ++r)
+        for (int c = 0; c < k; ++c) m[r * k + c] = a[idx[r] * n + idx[c]];
+    double det = 1.0;
+    int sign = 1;
+    for (int col = 0; col < k; ++col) {
+        int pivot_row = col;
+        double pivot_abs = fabs(m[col * k + col]);
+        for (int row = col + 1; row < k; ++row) {
+            const double cand = fabs(m[row * k + col]);
+            if (cand > pivot_abs) {
+                pivot_abs = cand;
+                pivot_row = row;
+            }
+        }
+        if (pivot_abs == 0.0) return 0.0;
+        if (pivot_row != col) {
+            for (int c = col; c < k; ++c) {
+                const double t = m[col * k + c];
+                m[col * k + c] = m[pivot_row * k + c];
+                m[pivot_row * k + c] = t;
+            }
+            sign = -sign;
+        }
+        const double pivot = m[col * k + col];
+        det *= pivot;
+        for (int row = col + 1; row < k; ++row) {
+            const double factor = m[row * k + col] / pivot;
+            if (factor == 0.0) continue;
+            m[row * k + col] = 0.0;
+            for (int c = col + 1; c < k; ++c) m[row * k + c] = fma(-factor, m[col * k + c], m[row * k + c]);
+        }
+    }
+    return sign < 0 ? -det : det;
+}
+
+/* determinant_principal_minors_from_buffer (fast_principle_minors.h:107-115). */
+void oracle_minors_by_lu(const double* a, int n, double* pm_out) {
+    const uint64_t count = (uint64_t)1 << n;
+    for (uint64_t mask = 1; mask < count; ++mask) pm_out[mask - 1] = minor_by_lu(a, n, mask);
+}
+
+/* mat2pm_from_buffer (fast_principle_minors.h:120-246): all principal minors
+ * of A + pI by a level-by-level Schur-complement recursion, a prefix product,
+ * then removal of the uniform shift p by multilinearity. A pivot with
+ * |a+p| <= tol*max|A| (or 0) sends the whole matrix to the LU fallback.
+ * Returns 1 when the fallback ran, 0 otherwise, -1 on a bad n. */
+int oracle_mat2pm(const double* a, int n, double tol, double shift, double* pm_out) {
+    if (n <= 0 || n > ORACLE_MAX_ORDER) return -1;
+    const uint64_t subset_count = (uint64_t)1 << n;
+    const int matrix_size = n * n;
+    for (uint64_t i = 0; i + 1 < subset_count; ++i) pm_out[i] = 0.0;
+
+    double max_abs = 0.0;
+    for (int i = 0; i < matrix_size; ++i) {
+        const double e = fabs(a[i]);
+        if (e > max_abs) max_abs = e;
+    }
+    const int explicit_shift = !(shift < 0.0);
+    const double p = explicit_shift ? shift : max_abs / (double)matrix_size;
+    if (max_abs == 0.0 && p == 0.0) return 0;
+    const double fallback_eps = (tol > 0.0 && max_abs > 0.0) ? tol * max_abs : 0.0;
+
+    size_t list_size = (size_t)matrix_size;
+    for (int level = 0; level < n - 1; ++level) {
+        const size_t ns = (size_t)(n - level - 1);
+        const size_t cand = ((size_t)1 << (level + 1)) * ns * ns;
+        if (cand > list_size) list_size = cand;
+    }
+    double* old_list = (double*)malloc(list_size * sizeof(double));
+    double* new_list = (double*)malloc(list_size * sizeof(double));
+    double* shifted = (double*)malloc(subset_count * sizeof(double));
+    memcpy(old_list, a, (size_t)matrix_size * sizeof(double));
+    for (uint64_t i = 0; i < subset_count; ++i) shifted[i] = p;
+    shifted[0] = 1.0;
+    shifted[1] += old_list[0];
+
+    size_t minor_index = 2;
+    int fell_back = 0;
+    for (int level = 0; level < n - 1 && !fell_back; ++level) {
+        const size_t old_size = (size_t)(n - level);
+        const size_t old_msize = old_size * old_size;
+        const size_t new_size = old_size - 1;
+        const size_t new_msize = new_size * new_size;
+        const size_t sets = (size_t)1 << level;
+        for (size_t set = 0; set < sets; ++set) {
+            size_t dst_without = set * new_msize;
+            const size_t src = set * old_msize;
+            const size_t first_column = src + old_size;
+            size_t dst_with = dst_without + sets * new_msize;
+            const double pivot = old_list[src] + p;
+            const double pivot_abs = fabs(pivot);
+            if (pivot_abs == 0.0 || (fallback_eps > 0.0 && pivot_abs <= fallback_eps)) {
+                fell_back = 1;
+                break;
+            }
+            const double inverse = 1.0 / pivot;
+            size_t row_start = first_column + 1;
+            size_t column_start = first_column;
+            for (size_t row = 0; row < new_size; ++row) {
+                size_t top_row = src + 1;
+                const double factor = old_list[column_start] * inverse;
+                for (size_t col = 0; col < new_size; ++col) {
+                    const double base = old_list[row_start];
+                    new_list[dst_without] = base;
+                    new_list[dst_with] = fma(-old_list[top_row], factor, base);
+                    ++top_row;
+                    ++row_start;
+                    ++dst_without;
+                    ++dst_with;
+                }
+                ++row_start;
+                column_start += old_size;
+            }
+        }
+        if (fell_back) break;
+        for (size_t m = 0; m < 2 * sets; ++m) shifted[minor_index++] += new_list[m * new_msize];
+        double* t = old_list;
+        old_list = new_list;
+        new_list = t;
+    }
+    if (fell_back) {
+        free(old_list);
+        free(new_list);
+        free(shifted);
+        oracle_minors_by_lu(a, n, pm_out);
+        return 1;
+    }
+
+    uint64_t step = 1;
+    for (int level = 0; level < n; ++level) {
+        for (uint64_t set = step + 1; set < 2 * step; ++set) shifted[set] *= shifted[set - step];
+        step <<= 1;
+    }
+    step = subset_count;
+    for (int level = n; level > 0; --level) {
+        const uint64_t half = step >> 1;
+        for (uint64_t set = step - 1;; --set) {
+            for (uint64_t ss = set; ss < subset_count; ss += step)
+                shifted[ss] = fma(-p, shifted[ss - half], shifted[ss]);
+            if (set == half) break;
+        }
+        step = half;
+    }
+    for (uint64_t mask = 1; mask < subset_count; ++mask) pm_out[mask - 1] = shifted[mask];
+    free(old_list);
+    free(new_list);
+    free(shifted);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ CDet --- */
+
+static int popcount64(uint64_t x) {
+    int c = 0;
+    while (x) {
+        x &= x - 1;
+        ++c;
+    }
+    return c;
+}
+
+/* compute_dp_ztransform (integrand_replica_randomly_sampled.h:226-290): the
+ * connected sum of a[m] = up[m-1]*down[m-1] anchored at vertex 0, masks taken
+ * in popcount order, with the roundoff filter |acc| < eps0*safety*sum|terms|. */
+double oracle_ztransform(const double* up, const double* down, int n, double eps0,
+                         double safety) {
+    const uint64_t count = (uint64_t)1 << n;
+    double* a = (double*)malloc(count * sizeof(double));
+    double* dp = (double*)calloc(count, sizeof(double));
+    const double threshold = eps0 * safety;
+    const int filter = threshold > 0.0;
+    a[0] = 0.0;
+    for (uint64_t m = 1; m < count; ++m) a[m] = up[m - 1] * down[m - 1];
+    for (int i = 0; i < n; ++i) dp[(uint64_t)1 << i] = a[(uint64_t)1 << i];
+    for (int bits = 2; bits <= n; ++bits) {
+        for (uint64_t mask = 0; mask < count; ++mask) {
+            if (popcount64(mask) != bits) continue;
+            double acc = a[mask];
+            double rhs = fabs(a[mask]);
+            if (mask & 1u) {
+                for (uint64_t sub = (mask - 1) & mask; sub; sub = (sub - 1) & mask) {
+                    if ((sub & 1u) == 0u) continue;
+                    const double term = dp[sub] * a[mask ^ sub];
+                    acc = acc - term;
+                    rhs += fabs(term);
+                }
+                if (filter && fabs(acc) < threshold * rhs) acc = 0.0;
+            }
+            dp[mask] = acc;
+        }
+    }
+    const double result = dp[count - 1];
+    free(a);
+    free(dp);
+    return result;
+}
+
+/* compute_dp_ztransform_all_subsets (:292-347): every mask anchored at its
+ * lowest set bit. dp_out has 2^n entries, dp_out[0] = 0. */
+void oracle_ztransform_all(const double* up, const double* down, int n, double eps0,
+                           double safety, double* dp) {
+    const uint64_t count = (uint64_t)1 << n;
+    double* a = (double*)calloc(count, sizeof(double));
+    const double threshold = eps0 * safety;
+    const int filter = threshold > 0.0;
+    for (uint64_t m = 0; m < count; ++m) dp[m] = 0.0;
+    for (uint64_t m = 1; m < count; ++m) a[m] = up[m - 1] * down[m - 1];
+    for (int i = 0; i < n; ++i) dp[(uint64_t)1 << i] = a[(uint64_t)1 << i];
+    for (int bits = 2; bits <= n; ++bits) {
+        for (uint64_t mask = 0; mask < count; ++mask) {
+            if (popcount64(mask) != bits) continue;
+            const uint64_t anchor = mask & (~mask + 1);
+            double acc = a[mask];
+            double rhs = fabs(a[mask]);
+            for (uint64_t sub = (mask - 1) & mask; sub; sub = (sub - 1) & mask) {
+                if ((sub & anchor) == 0u) continue;
+                const double term = dp[sub] * a[mask ^ sub];
+                acc = acc - term;
+                rhs += fabs(term);
+            }
+            if (filter && fabs(acc) < threshold * rhs) acc = 0.0;
+            dp[mask] = acc;
+        }
+    }
+    free(a);
+}
+
+/* ----------------------------------------------------------- double-double --- */
+
+/* DoubleDouble arithmetic (utility/types.h:30-182): Dekker/Knuth error-free
+ * transforms in the arrangement the reference uses. */
+typedef struct dd {
+    double hi, lo;
+} dd;
+
+static double two_sum(double a, double b, double* err) {
+    const double s = a + b;
+    const double bb = s - a;
+    *err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+static double quick_two_sum(double a, double b, double* err) {
+    const double s = a + b;
+    *err = b - (s - a);
+    return s;
+}
+static double two_prod(double a, double b, double* err) {
+    const double p = a * b;
+    *err = fma(a, b, -p);
+    return p;
+}
+static dd dd_make(double hi, double lo) {
+    dd r = {hi, lo};
+    return r;
+}
+static dd dd_add(dd x, dd y) {
+    double s2, t2;
+    double s1 = two_sum(x.hi, y.hi, &s2);
+    const double t1 = two_sum(x.lo, y.lo, &t2);
+    s2 += t1;
+    s1 = quick_two_sum(s1, s2, &s2);
+    s2 += t2;
+    dd r;
+    r.hi = quick_two_sum(s1, s2, &r.lo);
+    return r;
+}
+static dd dd_sub(dd x, dd y) { return dd_add(x, dd_make(-y.hi, -y.lo)); }
+static dd dd_mul(dd x, dd y) {
+    double e;
+    const double p = two_prod(x.hi, y.hi, &e);
+    e += x.hi * y.lo + x.lo * y.hi + x.lo * y.lo;
+    dd r;
+    r.hi = quick_two_sum(p, e, &r.lo);
+    return r;
+}
+static dd dd_div(dd x, dd y) {
+    const double q1 = x.hi / y.hi;
+    const dd r = dd_sub(x, dd_mul(dd_make(q1, 0.0), y));
+    const double q2 = (r.hi + r.lo) / y.hi;
+    dd q = dd_add(dd_make(q1, 0.0), dd_make(q2, 0.0));
+    const double s = q.hi + q.lo;
+    q.lo = q.lo - (s - q.hi);
+    q.hi = s;
+    return q;
+}
+static int dd_finite(dd x) { return isfinite(x.hi) && isfinite(x.lo); }
+
+/* cdet_order_prefactor<DoubleDouble> (integrand_replica_randomly_sampled.h:155-159):
+ * (-r)^n / (n! * N1 * N2). (-r)^n is an exact power (r is 1 or 2). */
+void oracle_prefactor_dd(int order, int n1, int n2, int replica_count, double* hi, double* lo) {
+    double power = 1.0;
+    for (int i = 0; i < order; ++i) power *= -(double)replica_count;
+    dd factorial = dd_make(1.0, 0.0);
+    for (int i = 1; i <= order; ++i) factorial = dd_mul(factorial, dd_make((double)i, 0.0));
+    const dd den = dd_mul(dd_mul(factorial, dd_make((double)n1, 0.0)), dd_make((double)n2, 0.0));
+    const dd q = dd_div(dd_make(power, 0.0), den);
+    *hi = q.hi;
+    *lo = q.lo;
+}
+
+/* cdet_order_prefactor<double> (:160-170): long double on the host. */
+double oracle_prefactor_ld(int order, int n1, int n2, int replica_count) {
+    long double num = 1.0L;
+    for (int i = 0; i < order; ++i) num *= -(long double)replica_count;
+    long double den = (long double)n1 * (long double)n2;
+    for (int i = 2; i <= order; ++i) den *= (long double)i;
+    return (double)(num / den);
+}
+
+/* ------------------------------------------------------------- integrand --- */
+
+static double order1_raw(const oracle_scalars* s, double shifted_up, double shifted_down,
+                         int replica_count) {
+    /* order1_density_integrand_from_sampled_vertex (:173-213) and the
+     * all-subset singletons (:835-846). */
+    const double counterterm = s->diag_up_shift * s->diag_down_shift;
+    return (double)(-replica_count) * s->u * s->beta * (shifted_up * shifted_down - counterterm);
+}
+
+/* One table set of integrand_temp_typed (:349-547): fill, minors of both
+ * spins, anchored CDet, DD prefactor. */
+static int integrand_one_set(const oracle_scalars* s, const oracle_table* tu,
+                             const oracle_table* td, const double* args, int order,
+                             int replica_count, dd* value) {
+    vertex vx[ORACLE_MAX_ORDER];
+    double mu[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER], md[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER];
+    if (decode_vertices(s, args, order, replica_count, vx)) return ORACLE_BAD_INPUT;
+    fill_from_vertices(s, tu, td, vx, order, mu, md, NULL, NULL);
+    const size_t count = ((size_t)1 << order) - 1;
+    double* pu = (double*)malloc(count * sizeof(double));
+    double* pd = (double*)malloc(count * sizeof(double));
+    int status = 0;
+    if (oracle_mat2pm(mu, order, s->tol_fpm, s->fpm_shift, pu) == 1) status |= ORACLE_FPM_FALLBACK;
+    if (oracle_mat2pm(md, order, s->tol_fpm, s->fpm_shift, pd) == 1) status |= ORACLE_FPM_FALLBACK;
+    const double c = oracle_ztransform(pu, pd, order, s->z_eps0, s->z_safety);
+    free(pu);
+    free(pd);
+    dd pref;
+    oracle_prefactor_dd(order, s->n1, s->n2, replica_count, &pref.hi, &pref.lo);
+    *value = dd_mul(pref, dd_make(c, 0.0));
+    if (!dd_finite(*value)) status |= ORACLE_NONFINITE;
+    return status;
+}
+
+/* evaluate_cdet_density_integrand_double (cdet_integrand_evaluator.h:542-560)
+ * through evaluate_cdet_density_integrand_for_real (:233-263) and the
+ * order-1 branch (:171-201): twisted (r=2) minus twice ordinary (r=1) in
+ * double-double, rounded to double. */
+int oracle_integrand(const oracle_scalars* s, const oracle_tables* t, const double* args,
+                     int order, double* value) {
+    *value = 0.0;
+    if (order <= 0 || order > ORACLE_MAX_ORDER) return ORACLE_BAD_INPUT;
+    dd twisted, ordinary;
+    int status = 0;
+    if (order == 1) {
+        vertex vx[2];
+        double v[2];
+        const oracle_table* tabs[2][2] = {{&t->twisted_up, &t->twisted_down},
+                                          {&t->ordinary_up, &t->ordinary_down}};
+        for (int set = 0; set < 2; ++set) {
+            const int r = set == 0 ? 2 : 1;
+            if (decode_vertices(s, args, 1, r, vx)) return ORACLE_BAD_INPUT;
+            int corner;
+            uint64_t index;
+            double u, w, up, down;
+            oracle_lookup_descriptor(vx[0].replica, vx[0].replica, vx[0].tau, vx[0].tau, vx[0].x,
+                                     vx[0].y, vx[0].x, vx[0].y, s->beta, s->branch_eps,
+                                     s->cheb_nu, s->cheb_nv, s->n1, s->n2, 0, &corner, &index,
+                                     &u, &w);
+            oracle_green_pair(tabs[set][0], tabs[set][1], 0, corner, index, u, w, s->cheb_nu,
+                              s->cheb_nv, &up, &down);
+            v[set] = order1_raw(s, up + s->diag_up_shift, down + s->diag_down_shift, r);
+        }
+        twisted = dd_make(v[0], 0.0);
+        ordinary = dd_make(v[1], 0.0);
+    } else {
+        status |= integrand_one_set(s, &t->twisted_up, &t->twisted_down, args, order, 2, &twisted);
+        status |= integrand_one_set(s, &t->ordinary_up, &t->ordinary_down, args, order, 1,
+                                    &ordinary);
+        if (status & ORACLE_BAD_INPUT) return status;
+    }
+    const dd result = dd_sub(twisted, dd_mul(dd_make(2.0, 0.0), ordinary));
+    *value = result.hi + result.lo;
+    return status;
+}
+
+/* integrand_all_subset_values_typed_into (:549-878) for one table set. */
+static int all_subsets_one_set(const oracle_scalars* s, const oracle_table* tu,
+                               const oracle_table* td, const double* args, int n,
+                               int replica_count, double* values) {
+    vertex vx[ORACLE_MAX_ORDER];
+    double mu[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER], md[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER];
+    double du[ORACLE_MAX_ORDER], ddn[ORACLE_MAX_ORDER];
+    if (decode_vertices(s, args, n, replica_count, vx)) return ORACLE_BAD_INPUT;
+    fill_from_vertices(s, tu, td, vx, n, mu, md, du, ddn);
+    const size_t count = (size_t)1 << n;
+    double* pu = (double*)malloc(count * sizeof(double));
+    double* pd = (double*)malloc(count * sizeof(double));
+    double* dp = (double*)malloc(count * sizeof(double));
+    int status = 0;
+    if (oracle_mat2pm(mu, n, s->tol_fpm, s->fpm_shift, pu) == 1) status |= ORACLE_FPM_FALLBACK;
+    if (oracle_mat2pm(md, n, s->tol_fpm, s->fpm_shift, pd) == 1) status |= ORACLE_FPM_FALLBACK;
+    oracle_ztransform_all(pu, pd, n, s->z_eps0, s->z_safety, dp);
+    values[0] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double v = order1_raw(s, du[i], ddn[i], replica_count);
+        if (!isfinite(v)) status |= ORACLE_NONFINITE;
+        values[(size_t)1 << i] = v;
+    }
+    double pref[ORACLE_MAX_ORDER + 1];
+    for (int k = 2; k <= n; ++k) pref[k] = oracle_prefactor_ld(k, s->n1, s->n2, replica_count);
+    for (size_t mask = 1; mask < count; ++mask) {
+        const int k = popcount64(mask);
+        if (k <= 1) continue;
+        const double v = pref[k] * dp[mask];
+        if (!isfinite(v)) status |= ORACLE_NONFINITE;
+        values[mask] = v;
+    }
+    free(pu);
+    free(pd);
+    free(dp);
+    return status;
+}
+
+/* evaluate_cdet_density_all_subset_integrands_double_into
+ * (cdet_integrand_evaluator.h:562-583, :304-351): twisted values minus twice
+ * the ordinary values, mask by mask, in double. */
+int oracle_all_subsets(const oracle_scalars* s, const oracle_tables* t, const double* args,
+                       int n, double* values) {
+    if (n <= 1 || n > ORACLE_MAX_ORDER) return ORACLE_BAD_INPUT;
+    const size_t count = (size_t)1 << n;
+    double* ordinary = (double*)malloc(count * sizeof(double));
+    int status = all_subsets_one_set(s, &t->twisted_up, &t->twisted_down, args, n, 2, values);
+    status |= all_subsets_one_set(s, &t->ordinary_up, &t->ordinary_down, args, n, 1, ordinary);
+    if (!(status & ORACLE_BAD_INPUT))
+        for (size_t m = 0; m < count; ++m) values[m] -= 2.0 * ordinary[m];
+    free(ordinary);
+    return status;
+}
+
+/* ---------------------------------------------------------- thread batch --- */
+
+typedef struct batch_job {
+    const oracle_scalars* s;
+    const oracle_tables* t;
+    const double* vertices;
+    const int32_t* orders;
+    int max_order;
+    int all_subsets;
+    int64_t begin, end;
+    double* values;
+    int32_t* status;
+} batch_job;
+
+static void* batch_worker(void* arg) {
+    batch_job* job = (batch_job*)arg;
+    for (int64_t c = job->begin; c < job->end; ++c) {
+        const double* v = job->vertices + (size_t)c * (size_t)job->max_order * 4u;
+        int st;
+        if (job->all_subsets) {
+            st = oracle_all_subsets(job->s, job->t, v, job->max_order,
+                                    job->values + (size_t)c * ((size_t)1 << job->max_order));
+        } else {
+            st = oracle_integrand(job->s, job->t, v, job->orders[c], job->values + c);
+        }
+        if (job->status) job->status[c] = st;
+    }
+    return NULL;
+}
+
+static int run_batch(batch_job proto, int64_t batch, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t tid[256];
+    batch_job jobs[256];
+    for (int w = 0; w < threads; ++w) {
+        jobs[w] = proto;
+        jobs[w].begin = batch * w / threads;
+        jobs[w].end = batch * (w + 1) / threads;
+        if (pthread_create(&tid[w], NULL, batch_worker, &jobs[w]) != 0) {
+            for (int k = 0; k < w; ++k) pthread_join(tid[k], NULL);
+            return -1;
+        }
+    }
+    for (int w = 0; w < threads; ++w) pthread_join(tid[w], NULL);
+    return 0;
+}
+
+int oracle_integrand_batch(const oracle_scalars* s, const oracle_tables* t,
+                           const double* unit_vertices, const int32_t* orders, int64_t batch,
+                           int max_order, double* values, int32_t* status, int threads) {
+    batch_job proto = {s, t, unit_vertices, orders, max_order, 0, 0, 0, values, status};
+    return run_batch(proto, batch, threads);
+}
+
+int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
+                             const double* unit_vertices, int envelope_order, int64_t batch,
+                             double* values, int32_t* status, int threads) {
+    batch_job proto = {s, t, unit_vertices, NULL, envelope_order, 1, 0, 0, values, status};
+    return run_batch(proto, batch, threads);
+}

@@ -1,0 +1,107 @@
+/*
+ * CPU restatement of the reference CDet Renyi-2 integrand (the oracle).
+ *
+ * TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg call this library as the checker. The product path never
+ * links or loads it.
+ *
+ * Built with -ffp-contract=off so that every floating-point operation is the
+ * separately rounded IEEE operation the reference performs when compiled for
+ * x86-64 (no FMA contraction there; explicit std::fma calls stay fused). The
+ * result is the same bits on x86-64 and aarch64 hosts.
+ *
+ * Pinned against the reference build in oracle/_ref/ through the golden
+ * vectors in tests/golden/ (see tests/golden/make_golden.py).
+ */
+#ifndef CDET_ORACLE_H
+#define CDET_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Runtime scalars of one parameter set (IntegrandRuntimeScalars<double>,
+ * integrand_replica_randomly_sampled.h:41-51, built by
+ * make_integrand_runtime_scalars, :98-119). */
+typedef struct oracle_scalars {
+    int32_t n1, n2;           /* lattice extents N1, N2 */
+    int32_t cheb_nu, cheb_nv; /* Chebyshev coefficients per axis */
+    double beta;              /* inverse temperature */
+    double u;                 /* Hubbard U */
+    double branch_eps;        /* BRANCH_EPSILON */
+    double scale;             /* sqrt(U*N1*N2*beta) */
+    double diag_up_shift;     /* alpha_down / U (added to the up diagonal) */
+    double diag_down_shift;   /* alpha_up / U (added to the down diagonal) */
+    double tol_fpm;           /* TOL_FPM */
+    double fpm_shift;         /* FPM_GLOBAL_SHIFT, < 0 means auto */
+    double z_eps0;            /* ZTRANSFORM_EPSILON0 (2e-16 for double) */
+    double z_safety;          /* ZTRANSFORM_SAFETY_FACTOR */
+} oracle_scalars;
+
+/* One PiecewiseChebyshevTable<double> (replica_chebyshev_tables.h:25-33). */
+typedef struct oracle_table {
+    const double* upper_coeffs;
+    const double* lower_coeffs;
+    const double* upper_corners;
+    const double* lower_corners;
+} oracle_table;
+
+/* The four resident tables: twisted up, twisted down, ordinary up, ordinary
+ * down (parameters.h:81-84). */
+typedef struct oracle_tables {
+    oracle_table twisted_up, twisted_down, ordinary_up, ordinary_down;
+} oracle_tables;
+
+/* Status bits returned per configuration. */
+enum {
+    ORACLE_OK = 0,
+    ORACLE_NONFINITE = 1,   /* the reference throws "Value is not finite" */
+    ORACLE_FPM_FALLBACK = 2 /* at least one whole-matrix pivoted-LU fallback */
+};
+
+int oracle_lookup_descriptor(int ra, int rb, double tau1, double tau2, int x1, int y1, int x2,
+                             int y2, double beta, double branch_eps, int nu, int nv, int n1,
+                             int n2, int upper, int* use_corner, uint64_t* index, double* u,
+                             double* v);
+
+void oracle_green_pair(const oracle_table* up, const oracle_table* down, int upper,
+                       int use_corner, uint64_t index, double u, double v, int nu, int nv,
+                       double* up_value, double* down_value);
+
+int oracle_fill_green(const oracle_scalars* s, const oracle_table* up, const oracle_table* down,
+                      const double* unit_vertices, int order, int replica_count, double* mat_up,
+                      double* mat_down, double* diag_up, double* diag_down);
+
+int oracle_mat2pm(const double* a, int n, double tol, double shift, double* pm_out);
+void oracle_minors_by_lu(const double* a, int n, double* pm_out);
+
+double oracle_ztransform(const double* up, const double* down, int n, double eps0,
+                         double safety);
+void oracle_ztransform_all(const double* up, const double* down, int n, double eps0,
+                           double safety, double* dp_out);
+
+void oracle_prefactor_dd(int order, int n1, int n2, int replica_count, double* hi, double* lo);
+double oracle_prefactor_ld(int order, int n1, int n2, int replica_count);
+
+int oracle_integrand(const oracle_scalars* s, const oracle_tables* t,
+                     const double* unit_vertices, int order, double* value);
+int oracle_all_subsets(const oracle_scalars* s, const oracle_tables* t,
+                       const double* unit_vertices, int envelope_order, double* values);
+
+/* Batched single-order integrand with `threads` POSIX threads; each thread
+ * takes a contiguous slice. unit_vertices is [batch][max_order][4]. */
+int oracle_integrand_batch(const oracle_scalars* s, const oracle_tables* t,
+                           const double* unit_vertices, const int32_t* orders, int64_t batch,
+                           int max_order, double* values, int32_t* status, int threads);
+int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
+                             const double* unit_vertices, int envelope_order, int64_t batch,
+                             double* values, int32_t* status, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,295 @@
+// C-ABI harness around the reference's own integrand headers.
+//
+// TEST INFRASTRUCTURE ONLY. This file is compiled by oracle/Makefile against
+// the unmodified reference headers (include/cdet/*.h of
+// Boyuan-Shi-0607/cdet-renyi-entanglement-hpc) and the quad-precision Boost
+// stand-in in oracle/boost_shim/. The result, oracle/_ref/libcdet_ref.so, is
+// used by tests/golden/make_golden.py to produce golden vectors and to pin the
+// C restatement in oracle/cdet_oracle.c. Nothing in the product links it.
+//
+// Every entry point mirrors one reference function:
+//   ref_configure          -> the process globals of parameters.h:11-33 and
+//                             ztransform_roundoff_config() (precision_config.h:284)
+//   ref_build_tables       -> load_data_into_resident_tables<double,double>()
+//                             (load_data.h:49-99)
+//   ref_get/set_table      -> g_table_{up,down,ordinary_up,ordinary_down}
+//                             (parameters.h:81-84)
+//   ref_eval_integrand     -> evaluate_cdet_density_integrand_double
+//                             (cdet_integrand_evaluator.h:542-560)
+//   ref_eval_all_subsets   -> evaluate_cdet_density_all_subset_integrands_double_into
+//                             (cdet_integrand_evaluator.h:562-583)
+//   ref_mat2pm             -> mat2pm_from_buffer (fast_principle_minors.h:120-246)
+//   ref_minors_by_lu       -> determinant_principal_minors_from_buffer (:107-115)
+//   ref_ztransform[_all]   -> compute_dp_ztransform[_all_subsets]
+//                             (integrand_replica_randomly_sampled.h:226-347)
+//   ref_lookup_descriptor  -> prepare_green_lookup_descriptor (g_funcs.h:609-653)
+//   ref_green_replica      -> ReplicaGreenCalculator::green_replica_matrix
+//                             (replica_free_greens.h:314-331), the direct kernel
+//                             solve the Chebyshev accuracy audit compares with.
+
+#include "cdet/cdet_integrand_evaluator.h"
+#include "cdet/load_data.h"
+#include "cdet/mcmcmc_sampler.h"
+
+#include <cstdint>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+std::string g_last_error;
+
+ResidentGreenFunctionTable& table_slot(int kind) {
+    switch (kind) {
+        case 0: return g_table_up;
+        case 1: return g_table_down;
+        case 2: return g_table_ordinary_up;
+        case 3: return g_table_ordinary_down;
+    }
+    throw std::runtime_error("table kind must be 0..3");
+}
+
+template <typename F>
+int guarded(F&& body) {
+    try {
+        body();
+        return 0;
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return 1;
+    }
+}
+
+std::vector<UnitVertex> unpack_vertices(const double* unit_vertices, int order) {
+    std::vector<UnitVertex> vertices(static_cast<std::size_t>(order));
+    for (int i = 0; i < order; ++i) {
+        vertices[static_cast<std::size_t>(i)] = UnitVertex{
+            unit_vertices[4 * i + 0], unit_vertices[4 * i + 1],
+            unit_vertices[4 * i + 2], unit_vertices[4 * i + 3]};
+    }
+    return vertices;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error() { return g_last_error.c_str(); }
+
+int ref_configure(int n1, int n2, const char* beta_s, const char* mu_s, const char* u_s,
+                  const char* alpha_up_s, const char* alpha_down_s, int pbc_flag,
+                  const char* mask_name, int square_radius, int nu, int nv,
+                  const char* branch_eps_s, const char* tol_fpm_s, const char* fpm_shift_s,
+                  const char* z_eps0_s, const char* z_safety_s) {
+    return guarded([&] {
+        N1 = n1;
+        N2 = n2;
+        beta = MP_Real(beta_s);
+        mu = MP_Real(mu_s);
+        U = MP_Real(u_s);
+        alpha_shift_up = MP_Real(alpha_up_s);
+        alpha_shift_down = MP_Real(alpha_down_s);
+        pbc = pbc_flag != 0;
+        subregion_mask_name = mask_name;
+        subregion_square_radius = square_radius;
+        cheb_nu = nu;
+        cheb_nv = nv;
+        branch_epsilon = MP_Real(branch_eps_s);
+        tol_fpm = MP_Real(tol_fpm_s);
+        fpm_global_shift = std::string(fpm_shift_s) == "auto" ? MP_Real(-1) : MP_Real(fpm_shift_s);
+        green_table_drop_bits = 0;
+        load_data_real_name = "double";
+        vector_real_name = "double";
+        integrand_real_name = "double";
+        load_data_workflow = "resident";
+        load_data_calculator_cache = "off";
+        mcmcmc_table_backend = "resident";
+        table_build_threads = 1;
+        internal_integrand_threads = 1;
+        load_data_condition_check_mode = LinearSolveConditionCheckMode::Off;
+        if (std::string(z_eps0_s) == "auto") {
+            ztransform_roundoff_config().set_epsilon0_auto();
+        } else {
+            ztransform_roundoff_config().set_epsilon0_literal(z_eps0_s);
+        }
+        ztransform_roundoff_config().set_safety_factor_literal(z_safety_s);
+    });
+}
+
+int ref_set_precision(const char* vector_real, const char* integrand_real) {
+    return guarded([&] {
+        vector_real_name = vector_real;
+        integrand_real_name = integrand_real;
+    });
+}
+
+int ref_build_tables(int threads) {
+    return guarded([&] {
+        table_build_threads = threads;
+        load_data_into_resident_tables<double, double>();
+    });
+}
+
+std::size_t ref_coeff_count() {
+    return replica_sitepair_count(N1, N2) * static_cast<std::size_t>(cheb_nu) *
+           static_cast<std::size_t>(cheb_nv);
+}
+
+std::size_t ref_corner_count() { return replica_sitepair_count(N1, N2); }
+
+int ref_get_table(int kind, double* upper, double* lower, double* upper_corners,
+                  double* lower_corners) {
+    return guarded([&] {
+        const auto& table = std::get<GreenFunctionTableDouble>(table_slot(kind));
+        std::memcpy(upper, table.upper_coeffs.data(), table.upper_coeffs.size() * sizeof(double));
+        std::memcpy(lower, table.lower_coeffs.data(), table.lower_coeffs.size() * sizeof(double));
+        std::memcpy(upper_corners, table.upper_corners.data(),
+                    table.upper_corners.size() * sizeof(double));
+        std::memcpy(lower_corners, table.lower_corners.data(),
+                    table.lower_corners.size() * sizeof(double));
+    });
+}
+
+int ref_set_table(int kind, const double* upper, const double* lower, const double* upper_corners,
+                  const double* lower_corners) {
+    return guarded([&] {
+        GreenFunctionTableDouble table;
+        const std::size_t coeffs = ref_coeff_count();
+        const std::size_t corners = ref_corner_count();
+        table.upper_coeffs.assign(upper, upper + coeffs);
+        table.lower_coeffs.assign(lower, lower + coeffs);
+        table.upper_corners.assign(upper_corners, upper_corners + corners);
+        table.lower_corners.assign(lower_corners, lower_corners + corners);
+        table_slot(kind) = std::move(table);
+    });
+}
+
+int ref_eval_integrand(const double* unit_vertices, int order, double* out) {
+    return guarded([&] {
+        *out = evaluate_cdet_density_integrand_double(unpack_vertices(unit_vertices, order));
+    });
+}
+
+// Single-order integrand over a batch of configurations, one std::thread per
+// worker with its own contiguous slice (the reference integrand is re-entrant;
+// mcmcmc_sampler.h:1101-1110 calls it from one thread per chain). Returns the
+// number of configurations that raised.
+int ref_eval_integrand_batch(const double* unit_vertices, const int* orders, int batch,
+                             int max_order, double* out, int threads) {
+    if (threads < 1) threads = 1;
+    std::vector<int> failures(static_cast<std::size_t>(threads), 0);
+    std::vector<std::thread> workers;
+    for (int worker = 0; worker < threads; ++worker) {
+        workers.emplace_back([&, worker] {
+            const long begin = static_cast<long>(batch) * worker / threads;
+            const long end = static_cast<long>(batch) * (worker + 1) / threads;
+            for (long c = begin; c < end; ++c) {
+                try {
+                    out[c] = evaluate_cdet_density_integrand_double(
+                        unpack_vertices(unit_vertices + c * max_order * 4, orders[c]));
+                } catch (const std::exception&) {
+                    out[c] = std::numeric_limits<double>::quiet_NaN();
+                    ++failures[static_cast<std::size_t>(worker)];
+                }
+            }
+        });
+    }
+    for (auto& worker : workers) worker.join();
+    int total = 0;
+    for (int f : failures) total += f;
+    return total;
+}
+
+int ref_eval_all_subsets(const double* unit_vertices, int envelope_order, double* out) {
+    return guarded([&] {
+        std::vector<double> values;
+        evaluate_cdet_density_all_subset_integrands_double_into(
+            unpack_vertices(unit_vertices, envelope_order), values);
+        std::memcpy(out, values.data(), values.size() * sizeof(double));
+    });
+}
+
+int ref_mat2pm(const double* matrix, int n, double tol, double shift, double* out) {
+    return guarded([&] {
+        const std::vector<double> pm = mat2pm_from_buffer<double>(matrix, n, tol, shift);
+        std::memcpy(out, pm.data(), pm.size() * sizeof(double));
+    });
+}
+
+int ref_minors_by_lu(const double* matrix, int n, double* out) {
+    return guarded([&] {
+        const std::vector<double> pm = determinant_principal_minors_from_buffer<double>(matrix, n);
+        std::memcpy(out, pm.data(), pm.size() * sizeof(double));
+    });
+}
+
+double ref_ztransform(const double* up, const double* down, int n, double eps0, double safety) {
+    const std::size_t count = (std::size_t{1} << n) - 1;
+    const std::vector<double> u(up, up + count), d(down, down + count);
+    return compute_dp_ztransform<double>(u, d, n, eps0, safety);
+}
+
+int ref_ztransform_all(const double* up, const double* down, int n, double eps0, double safety,
+                       double* out) {
+    return guarded([&] {
+        const std::size_t count = (std::size_t{1} << n) - 1;
+        const std::vector<double> u(up, up + count), d(down, down + count);
+        const std::vector<double> dp = compute_dp_ztransform_all_subsets<double>(u, d, n, eps0, safety);
+        std::memcpy(out, dp.data(), dp.size() * sizeof(double));
+    });
+}
+
+int ref_lookup_descriptor(int ra, int rb, double tau1, double tau2, int x1, int y1, int x2, int y2,
+                          double beta_value, double branch_eps, int nu, int nv, int n1, int n2,
+                          int upper, int* use_corner, unsigned long long* index, double* u,
+                          double* v) {
+    return guarded([&] {
+        const auto d = prepare_green_lookup_descriptor<double>(
+            ra, rb, tau1, tau2, x1, y1, x2, y2, beta_value, branch_eps, nu, nv, n1, n2, upper != 0);
+        *use_corner = d.use_corner ? 1 : 0;
+        *index = d.use_corner ? d.corner_index : d.coeff_base_index;
+        *u = d.u;
+        *v = d.v;
+    });
+}
+
+int ref_green_replica(int n1, int n2, double beta_value, double mu_value, int pbc_flag,
+                      const char* mask_name, int square_radius, int ra, int rb, double tau,
+                      double tau_prime, int upper, double* out) {
+    return guarded([&] {
+        load_data_condition_check_mode = LinearSolveConditionCheckMode::Off;
+        const ReplicaSubregionMask mask = parse_subregion_mask(mask_name);
+        ReplicaGreenCalculator<double> calculator(n1, n2, beta_value, mu_value, pbc_flag != 0, mask,
+                                                  square_radius);
+        const auto matrix = calculator.green_replica_matrix(
+            ra, rb, tau, tau_prime, upper ? TriangleBranch::Upper : TriangleBranch::Lower);
+        const int sites = n1 * n2;
+        for (int i = 0; i < sites; ++i) {
+            for (int j = 0; j < sites; ++j) {
+                out[i * sites + j] = matrix(i, j);
+            }
+        }
+    });
+}
+
+// sample_uniform_unit_vertex (mcmcmc_sampler.h:187-190) drawn `count` times
+// from std::mt19937_64(seed); out is [count][4] = tau, x, y, replica.
+void ref_sample_vertices(unsigned long long seed, int count, double* out) {
+    std::mt19937_64 rng(seed);
+    for (int i = 0; i < count; ++i) {
+        const UnitVertex v = sample_uniform_unit_vertex(rng);
+        out[4 * i + 0] = v.tau;
+        out[4 * i + 1] = v.x;
+        out[4 * i + 2] = v.y;
+        out[4 * i + 3] = v.replica;
+    }
+}
+
+unsigned long long ref_fpm_fallbacks() { return snapshot_cdet_runtime_counters().fpm_fallbacks; }
+
+void ref_reset_counters() { reset_cdet_runtime_counters(); }
+
+}  // extern "C"
