@@ -1,0 +1,203 @@
+"""Host-side mirror of the reference integrand interface, on the GB300 kernels.
+
+``CdetIntegrand`` holds one parameter set and its four resident tables in HBM
+and exposes the reference's two entry points with the reference's names,
+argument meaning and errors:
+
+* ``evaluate_cdet_density_integrand_double(vertices)``
+  (cdet_integrand_evaluator.h:542-560)
+* ``evaluate_cdet_density_all_subset_integrands_double_into(vertices, values)``
+  (:562-583) and the by-value form (:585-590)
+
+plus batched forms on host or device buffers, which the C ABI
+(include/cdet_gb300.h) provides and which a driver that evaluates many
+proposals per step calls instead of one configuration at a time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from collections import namedtuple
+from typing import Dict, Iterable, List, Optional, Sequence
+
+import numpy as np
+
+from . import lib as L
+from .params import CdetParams
+
+# UnitVertex (cdet_integrand_evaluator.h:16-21): tau, x, y, replica in [0, 1).
+UnitVertex = namedtuple("UnitVertex", ["tau", "x", "y", "replica"])
+
+
+def _as_vertex_array(vertices) -> np.ndarray:
+    if isinstance(vertices, np.ndarray):
+        arr = vertices
+    else:
+        arr = np.array([[v.tau, v.x, v.y, v.replica] if isinstance(v, UnitVertex) else list(v)
+                        for v in vertices], dtype=np.float64)
+    return np.ascontiguousarray(arr, dtype=np.float64).reshape(-1, 4)
+
+
+def _ptr(obj) -> int:
+    """Address of a numpy array or a torch tensor (host or device)."""
+    if hasattr(obj, "data_ptr"):
+        return obj.data_ptr()
+    return obj.ctypes.data
+
+
+class CdetIntegrand:
+    """The CDet integrand of one parameter set on one CUDA device.
+
+    ``tables`` maps the four kinds (twisted_up, twisted_down, ordinary_up,
+    ordinary_down) to dicts with float64 arrays ``upper``, ``lower``,
+    ``upper_corners``, ``lower_corners``. CUDA torch tensors are used in place
+    (the caller keeps them alive); numpy arrays and CPU tensors are copied to
+    HBM. Kinds whose dict is the same object as another kind's are aliased, as
+    the reference does when ALPHA_UP == ALPHA_DOWN.
+    """
+
+    def __init__(self, params: CdetParams, tables: Dict[str, Dict], device: int = 0):
+        self.params = params
+        self.scalars = params.runtime_scalars()
+        self._lib = L.load()
+        self._ctx = C.c_void_p()
+        rs = L.RuntimeScalars(**{k: self.scalars[k] for k, _ in L.RuntimeScalars._fields_})
+        L.check(self._lib.cdet_create(C.byref(rs), device, C.byref(self._ctx)))
+        self._keep = []
+        sites = params.sites
+        self.coeff_count = 4 * sites * sites * params.cheb_nu * params.cheb_nv
+        self.corner_count = 4 * sites * sites
+        seen = {}
+        for kind, name in enumerate(L.KIND_NAMES):
+            t = tables[name]
+            if id(t) in seen:
+                L.check(self._lib.cdet_alias_table(self._ctx, kind, seen[id(t)]))
+                continue
+            seen[id(t)] = kind
+            self._set_table(kind, t)
+
+    def _set_table(self, kind: int, t: Dict) -> None:
+        arrays = [t["upper"], t["lower"], t["upper_corners"], t["lower_corners"]]
+        on_device = all(hasattr(a, "is_cuda") and a.is_cuda for a in arrays)
+        if on_device:
+            for a in arrays:
+                if a.dtype.__str__() != "torch.float64" or not a.is_contiguous():
+                    raise ValueError("device tables must be contiguous float64 tensors")
+            self._keep.append(arrays)
+            view = L.TableView(*[a.data_ptr() for a in arrays])
+            L.check(self._lib.cdet_bind_device_table(self._ctx, kind, C.byref(view),
+                                                     self.coeff_count, self.corner_count))
+        else:
+            host = [np.ascontiguousarray(a.detach().cpu().numpy() if hasattr(a, "detach") else a,
+                                         dtype=np.float64) for a in arrays]
+            view = L.TableView(*[h.ctypes.data for h in host])
+            L.check(self._lib.cdet_upload_table(self._ctx, kind, C.byref(view),
+                                                self.coeff_count, self.corner_count))
+
+    def close(self) -> None:
+        if self._ctx:
+            self._lib.cdet_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+            self._keep = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ batched ---
+    def reserve(self, batch: int, max_order: int) -> None:
+        L.check(self._lib.cdet_reserve(self._ctx, int(batch), int(max_order)))
+
+    def integrand_batch(self, vertices: np.ndarray, orders: Sequence[int], check: bool = False):
+        """Host buffers: vertices [batch][max_order][4], orders [batch].
+        Returns (values [batch], status [batch])."""
+        v = np.ascontiguousarray(vertices, dtype=np.float64)
+        o = np.ascontiguousarray(orders, dtype=np.int32)
+        batch, max_order = v.shape[0], v.shape[1]
+        values = np.zeros(batch)
+        status = np.zeros(batch, dtype=np.int32)
+        rc = self._lib.cdet_integrand_host(self._ctx, v.ctypes.data, o.ctypes.data, batch,
+                                           max_order, values.ctypes.data, status.ctypes.data)
+        if rc not in (L.CDET_OK, L.CDET_ERR_VALUE) or (check and rc != L.CDET_OK):
+            L.check(rc)
+        return values, status
+
+    def all_subsets_batch(self, vertices: np.ndarray, check: bool = False):
+        """Host buffers: vertices [batch][envelope][4]. Returns
+        (values [batch][2^envelope], status [batch])."""
+        v = np.ascontiguousarray(vertices, dtype=np.float64)
+        batch, env = v.shape[0], v.shape[1]
+        values = np.zeros((batch, 1 << env))
+        status = np.zeros(batch, dtype=np.int32)
+        rc = self._lib.cdet_all_subsets_host(self._ctx, v.ctypes.data, env, batch,
+                                             values.ctypes.data, status.ctypes.data)
+        if rc not in (L.CDET_OK, L.CDET_ERR_VALUE) or (check and rc != L.CDET_OK):
+            L.check(rc)
+        return values, status
+
+    def integrand_device(self, vertices, orders, values, status, stream=None) -> None:
+        """Device buffers (torch CUDA tensors or raw addresses), asynchronous
+        on ``stream`` (a torch.cuda.Stream, a cudaStream_t address or None)."""
+        batch, max_order = int(vertices.shape[0]), int(vertices.shape[1])
+        L.check(self._lib.cdet_integrand_device(self._ctx, _ptr(vertices), _ptr(orders), batch,
+                                                max_order, _ptr(values), _ptr(status),
+                                                _stream_handle(stream)))
+
+    def all_subsets_device(self, vertices, values, status, stream=None) -> None:
+        batch, env = int(vertices.shape[0]), int(vertices.shape[1])
+        L.check(self._lib.cdet_all_subsets_device(self._ctx, _ptr(vertices), env, batch,
+                                                  _ptr(values), _ptr(status),
+                                                  _stream_handle(stream)))
+
+    def counters(self):
+        calls, fallbacks = C.c_uint64(), C.c_uint64()
+        L.check(self._lib.cdet_counters(self._ctx, C.byref(calls), C.byref(fallbacks)))
+        return calls.value, fallbacks.value
+
+    def last_launch_count(self) -> int:
+        return int(self._lib.cdet_last_launch_count(self._ctx))
+
+    # --------------------------------------------- reference entry points ---
+    def evaluate_cdet_density_integrand_double(self, vertices) -> float:
+        v = _as_vertex_array(vertices)
+        order = v.shape[0]
+        if order <= 0:
+            raise RuntimeError("The replica integrand is defined only for order >= 1")
+        values, status = self.integrand_batch(v[None], [order])
+        if status[0] & L.CONFIG_BAD_INPUT:
+            raise RuntimeError("Error (integrand): vertex coordinates rejected")
+        if status[0] & L.CONFIG_NONFINITE:
+            raise RuntimeError("Error (integrand): Value is not finite")
+        return float(values[0])
+
+    def evaluate_cdet_density_all_subset_integrands_double_into(self, vertices, values: List[float]) -> None:
+        v = _as_vertex_array(vertices)
+        env = v.shape[0]
+        if env <= 1:
+            raise RuntimeError("The all-subset replica integrand is defined only for envelope order >= 2")
+        out, status = self.all_subsets_batch(v[None])
+        if status[0] & L.CONFIG_BAD_INPUT:
+            raise RuntimeError("Error (all-subset integrand): vertex coordinates rejected")
+        if status[0] & L.CONFIG_NONFINITE:
+            raise RuntimeError("Error (all-subset integrand): Value is not finite")
+        values[:] = out[0].tolist()
+
+    def evaluate_cdet_density_all_subset_integrands_double(self, vertices) -> List[float]:
+        values: List[float] = []
+        self.evaluate_cdet_density_all_subset_integrands_double_into(vertices, values)
+        return values
+
+
+def _stream_handle(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def subset_vertices(full_vertices, mask: int) -> np.ndarray:
+    """subset_vertices (cdet_integrand_evaluator.h:592-602)."""
+    v = _as_vertex_array(full_vertices)
+    return v[[i for i in range(v.shape[0]) if (mask >> i) & 1]]

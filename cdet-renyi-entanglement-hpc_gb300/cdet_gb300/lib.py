@@ -1,0 +1,90 @@
+"""ctypes binding of libcdet_gb300.so (the C ABI in include/cdet_gb300.h).
+
+There is no fallback: if the library is missing or does not load, every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB_PATH
+
+CDET_OK = 0
+CDET_ERR_INVALID = 1
+CDET_ERR_STATE = 2
+CDET_ERR_CUDA = 3
+CDET_ERR_VALUE = 4
+
+CONFIG_NONFINITE = 1
+CONFIG_FPM_FALLBACK = 2
+CONFIG_BAD_INPUT = 4
+
+TWISTED_UP, TWISTED_DOWN, ORDINARY_UP, ORDINARY_DOWN = 0, 1, 2, 3
+KIND_NAMES = ("twisted_up", "twisted_down", "ordinary_up", "ordinary_down")
+
+# Every symbol include/cdet_gb300.h declares.
+EXPORTED = (
+    "cdet_create", "cdet_destroy", "cdet_upload_table", "cdet_bind_device_table",
+    "cdet_alias_table", "cdet_reserve", "cdet_integrand_device", "cdet_all_subsets_device",
+    "cdet_integrand_host", "cdet_all_subsets_host", "cdet_counters", "cdet_last_error",
+    "cdet_last_launch_count",
+)
+
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int32)
+
+
+class RuntimeScalars(C.Structure):
+    _fields_ = [("n1", C.c_int32), ("n2", C.c_int32), ("cheb_nu", C.c_int32),
+                ("cheb_nv", C.c_int32), ("beta", C.c_double), ("u", C.c_double),
+                ("branch_eps", C.c_double), ("scale", C.c_double),
+                ("diag_up_shift", C.c_double), ("diag_down_shift", C.c_double),
+                ("tol_fpm", C.c_double), ("fpm_shift", C.c_double),
+                ("z_eps0", C.c_double), ("z_safety", C.c_double)]
+
+
+class TableView(C.Structure):
+    _fields_ = [("upper_coeffs", C.c_void_p), ("lower_coeffs", C.c_void_p),
+                ("upper_corners", C.c_void_p), ("lower_corners", C.c_void_p)]
+
+
+_LIB = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads the library (once) and declares the prototypes."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build it with __graft_entry__.build() (nvcc, sm_103a); "
+            "the CDet integrand has no CPU fallback")
+    lib = C.CDLL(path)
+    vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int
+    lib.cdet_create.argtypes = [C.POINTER(RuntimeScalars), i32, C.POINTER(vp)]
+    lib.cdet_destroy.argtypes = [vp]
+    lib.cdet_destroy.restype = None
+    lib.cdet_upload_table.argtypes = [vp, i32, C.POINTER(TableView), C.c_size_t, C.c_size_t]
+    lib.cdet_bind_device_table.argtypes = [vp, i32, C.POINTER(TableView), C.c_size_t, C.c_size_t]
+    lib.cdet_alias_table.argtypes = [vp, i32, i32]
+    lib.cdet_reserve.argtypes = [vp, i64, i32]
+    lib.cdet_integrand_device.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp]
+    lib.cdet_all_subsets_device.argtypes = [vp, vp, i32, i64, vp, vp, vp]
+    lib.cdet_integrand_host.argtypes = [vp, vp, vp, i64, i32, vp, vp]
+    lib.cdet_all_subsets_host.argtypes = [vp, vp, i32, i64, vp, vp]
+    lib.cdet_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.cdet_last_error.restype = C.c_char_p
+    lib.cdet_last_launch_count.argtypes = [vp]
+    _LIB = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().cdet_last_error().decode()
+
+
+def check(rc: int) -> None:
+    if rc != CDET_OK:
+        raise RuntimeError(last_error() or f"cdet call failed with code {rc}")

@@ -1,0 +1,454 @@
+// C ABI of the GB300 CDet integrand (declared in include/cdet_gb300.h).
+//
+// Host side: context and table bookkeeping, the order prefactors (computed on
+// the host exactly as the reference does), device scratch, and the launch of
+// the FP64 kernels in cdet_kernels.cu. The host compiler runs with
+// -ffp-contract=off so the double-double prefactor arithmetic below rounds
+// every operation separately, as the reference's DoubleDouble does.
+#include "cdet_gb300.h"
+#include "cdet_kernels.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& message) {
+    g_last_error = message;
+    return code;
+}
+
+int cuda_fail(cudaError_t err, const char* what) {
+    return fail(CDET_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+// DoubleDouble (utility/types.h:30-182), host side.
+struct HostDD {
+    double hi, lo;
+};
+double h_two_sum(double a, double b, double& e) {
+    const double s = a + b;
+    const double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+    return s;
+}
+double h_quick_two_sum(double a, double b, double& e) {
+    const double s = a + b;
+    e = b - (s - a);
+    return s;
+}
+HostDD h_add(HostDD x, HostDD y) {
+    double s2, t2;
+    double s1 = h_two_sum(x.hi, y.hi, s2);
+    const double t1 = h_two_sum(x.lo, y.lo, t2);
+    s2 += t1;
+    s1 = h_quick_two_sum(s1, s2, s2);
+    s2 += t2;
+    HostDD r;
+    r.hi = h_quick_two_sum(s1, s2, r.lo);
+    return r;
+}
+HostDD h_mul(HostDD x, HostDD y) {
+    const double p = x.hi * y.hi;
+    double e = std::fma(x.hi, y.hi, -p);
+    e += x.hi * y.lo + x.lo * y.hi + x.lo * y.lo;
+    HostDD r;
+    r.hi = h_quick_two_sum(p, e, r.lo);
+    return r;
+}
+HostDD h_div(HostDD x, HostDD y) {
+    const double q1 = x.hi / y.hi;
+    const HostDD prod = h_mul(HostDD{q1, 0.0}, y);
+    const HostDD r = h_add(x, HostDD{-prod.hi, -prod.lo});
+    const double q2 = (r.hi + r.lo) / y.hi;
+    HostDD q = h_add(HostDD{q1, 0.0}, HostDD{q2, 0.0});
+    const double s = q.hi + q.lo;
+    q.lo = q.lo - (s - q.hi);
+    q.hi = s;
+    return q;
+}
+
+// cdet_order_prefactor<DoubleDouble> (integrand_replica_randomly_sampled.h:155-159):
+// (-r)^n / (n! N1 N2); (-r)^n is exact for r in {1, 2}.
+HostDD prefactor_dd(int order, int n1, int n2, int r) {
+    double power = 1.0;
+    for (int i = 0; i < order; ++i) power *= -static_cast<double>(r);
+    HostDD factorial{1.0, 0.0};
+    for (int i = 1; i <= order; ++i) factorial = h_mul(factorial, HostDD{static_cast<double>(i), 0.0});
+    const HostDD den = h_mul(h_mul(factorial, HostDD{static_cast<double>(n1), 0.0}),
+                             HostDD{static_cast<double>(n2), 0.0});
+    return h_div(HostDD{power, 0.0}, den);
+}
+
+// cdet_order_prefactor<double> (:160-170), in the host's long double.
+double prefactor_ld(int order, int n1, int n2, int r) {
+    long double num = 1.0L;
+    for (int i = 0; i < order; ++i) num *= -static_cast<long double>(r);
+    long double den = static_cast<long double>(n1) * static_cast<long double>(n2);
+    for (int i = 2; i <= order; ++i) den *= static_cast<long double>(i);
+    return static_cast<double>(num / den);
+}
+
+struct TableSlot {
+    cdet::TableDev dev{};
+    void* owned = nullptr;  // device allocation made by cdet_upload_table
+    int alias_of = -1;      // kind this slot shares, or -1
+    bool ready = false;
+};
+
+}  // namespace
+
+struct cdet_context {
+    int device = 0;
+    int sm_count = 0;
+    cdet_runtime_scalars scalars{};
+    size_t coeff_count = 0, corner_count = 0;
+    TableSlot tables[4];
+    // scratch
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int64_t scratch_batch = 0;
+    int scratch_order = 0;
+    size_t ws_warps = 0;
+    // staging for the host-buffer entry points
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    uint64_t calls = 0, fallbacks = 0;
+    int last_launches = 0;
+};
+
+namespace {
+
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int device) {
+        cudaGetDevice(&previous_);
+        if (previous_ != device) cudaSetDevice(device);
+        device_ = device;
+    }
+    ~DeviceGuard() {
+        if (previous_ != device_) cudaSetDevice(previous_);
+    }
+
+private:
+    int previous_ = 0, device_ = 0;
+};
+
+const cdet::TableDev* resolve(const cdet_context* ctx, int kind) {
+    const TableSlot& slot = ctx->tables[kind];
+    if (slot.alias_of >= 0) return resolve(ctx, slot.alias_of);
+    return slot.ready ? &slot.dev : nullptr;
+}
+
+bool valid_kind(int kind) { return kind >= 0 && kind < 4; }
+
+size_t expected_coeffs(const cdet_runtime_scalars& s) {
+    const size_t sites = static_cast<size_t>(s.n1) * s.n2;
+    return 4 * sites * sites * static_cast<size_t>(s.cheb_nu) * s.cheb_nv;
+}
+size_t expected_corners(const cdet_runtime_scalars& s) {
+    const size_t sites = static_cast<size_t>(s.n1) * s.n2;
+    return 4 * sites * sites;
+}
+
+void release_slot(TableSlot& slot) {
+    if (slot.owned) cudaFree(slot.owned);
+    slot = TableSlot{};
+}
+
+int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
+    if (ctx->scratch && batch <= ctx->scratch_batch && max_order <= ctx->scratch_order) return CDET_OK;
+    const int64_t new_batch = batch > ctx->scratch_batch ? batch : ctx->scratch_batch;
+    const int new_order = max_order > ctx->scratch_order ? max_order : ctx->scratch_order;
+    const size_t ws_warps = static_cast<size_t>(ctx->sm_count) * 8;
+    const size_t bytes = cdet::scratch_bytes(new_batch, new_order, ws_warps);
+    if (ctx->scratch) {
+        cudaDeviceSynchronize();
+        cudaFree(ctx->scratch);
+        ctx->scratch = nullptr;
+    }
+    cudaError_t err = cudaMalloc(&ctx->scratch, bytes);
+    if (err != cudaSuccess) {
+        ctx->scratch_batch = 0;
+        ctx->scratch_order = 0;
+        return cuda_fail(err, "cudaMalloc(scratch)");
+    }
+    ctx->scratch_bytes = bytes;
+    ctx->scratch_batch = new_batch;
+    ctx->scratch_order = new_order;
+    ctx->ws_warps = ws_warps;
+    return CDET_OK;
+}
+
+int build_problem(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                  int64_t batch, int max_order, int all_subsets, double* values,
+                  int32_t* status, cdet::Problem* p) {
+    const cdet_runtime_scalars& s = ctx->scalars;
+    p->s = cdet::Scalars{s.n1, s.n2, s.cheb_nu, s.cheb_nv, s.beta, s.u, s.branch_eps, s.scale,
+                         s.diag_up_shift, s.diag_down_shift, s.tol_fpm, s.fpm_shift, s.z_eps0,
+                         s.z_safety};
+    const int kinds[2][2] = {{CDET_TWISTED_UP, CDET_TWISTED_DOWN},
+                             {CDET_ORDINARY_UP, CDET_ORDINARY_DOWN}};
+    for (int set = 0; set < 2; ++set) {
+        const cdet::TableDev* up = resolve(ctx, kinds[set][0]);
+        const cdet::TableDev* down = resolve(ctx, kinds[set][1]);
+        if (!up || !down) return fail(CDET_ERR_STATE, "Green-function tables have not been uploaded");
+        p->up[set] = *up;
+        p->down[set] = *down;
+        p->same_spin[set] = (up->upper == down->upper && up->lower == down->lower &&
+                             up->upper_corners == down->upper_corners &&
+                             up->lower_corners == down->lower_corners &&
+                             s.diag_up_shift == s.diag_down_shift)
+                                ? 1
+                                : 0;
+    }
+    p->vertices = vertices;
+    p->orders = orders;
+    p->batch = batch;
+    p->max_order = max_order;
+    p->all_subsets = all_subsets;
+    for (int set = 0; set < 2; ++set) {
+        const int r = set == 0 ? 2 : 1;
+        for (int n = 0; n <= cdet::kMaxOrder; ++n) {
+            const HostDD dd = n >= 1 ? prefactor_dd(n, s.n1, s.n2, r) : HostDD{0.0, 0.0};
+            p->pref_dd[set][n] = cdet::DDPair{dd.hi, dd.lo};
+            p->pref_ld[set][n] = n >= 2 ? prefactor_ld(n, s.n1, s.n2, r) : 0.0;
+        }
+    }
+    p->values = values;
+    p->status = status;
+    return CDET_OK;
+}
+
+int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
+        int max_order, int all_subsets, double* values, int32_t* status, cudaStream_t stream) {
+    if (batch < 0) return fail(CDET_ERR_INVALID, "batch must be non-negative");
+    if (batch == 0) return CDET_OK;
+    if (!vertices || !values || !status || (!all_subsets && !orders))
+        return fail(CDET_ERR_INVALID, "null buffer");
+    int rc = ensure_scratch(ctx, batch, max_order);
+    if (rc != CDET_OK) return rc;
+    cdet::Problem p;
+    rc = build_problem(ctx, vertices, orders, batch, max_order, all_subsets, values, status, &p);
+    if (rc != CDET_OK) return rc;
+    cdet::Scratch w;
+    cdet::carve_scratch(ctx->scratch, ctx->scratch_batch, ctx->scratch_order, ctx->ws_warps, &w);
+    // The carve above is for the reserved (batch, order); the kernels index
+    // with the call's max_order, which only needs less.
+    cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMemsetAsync(status)");
+    err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+    ctx->last_launches = 4;  // status memset + 3 kernels
+    return CDET_OK;
+}
+
+int run_host(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
+             int order_arg, int all_subsets, double* values, int32_t* status) {
+    if (batch <= 0) return batch == 0 ? CDET_OK : fail(CDET_ERR_INVALID, "batch must be non-negative");
+    if (!vertices || !values || !status || (!all_subsets && !orders))
+        return fail(CDET_ERR_INVALID, "null buffer");
+    const size_t vbytes = static_cast<size_t>(batch) * order_arg * 4 * sizeof(double);
+    const size_t obytes = all_subsets ? 0 : static_cast<size_t>(batch) * sizeof(int32_t);
+    const size_t out_count = all_subsets ? static_cast<size_t>(batch) << order_arg : static_cast<size_t>(batch);
+    const size_t valbytes = out_count * sizeof(double);
+    const size_t sbytes = static_cast<size_t>(batch) * sizeof(int32_t);
+    auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
+    const size_t need = up(vbytes) + up(obytes) + up(valbytes) + up(sbytes);
+    if (need > ctx->staging_bytes) {
+        if (ctx->staging) cudaFree(ctx->staging);
+        ctx->staging = nullptr;
+        cudaError_t err = cudaMalloc(&ctx->staging, need);
+        if (err != cudaSuccess) {
+            ctx->staging_bytes = 0;
+            return cuda_fail(err, "cudaMalloc(staging)");
+        }
+        ctx->staging_bytes = need;
+    }
+    char* base = static_cast<char*>(ctx->staging);
+    double* d_v = reinterpret_cast<double*>(base);
+    int32_t* d_o = reinterpret_cast<int32_t*>(base + up(vbytes));
+    double* d_val = reinterpret_cast<double*>(base + up(vbytes) + up(obytes));
+    int32_t* d_s = reinterpret_cast<int32_t*>(base + up(vbytes) + up(obytes) + up(valbytes));
+    cudaStream_t stream = nullptr;
+    cudaError_t err = cudaMemcpyAsync(d_v, vertices, vbytes, cudaMemcpyHostToDevice, stream);
+    if (err == cudaSuccess && obytes)
+        err = cudaMemcpyAsync(d_o, orders, obytes, cudaMemcpyHostToDevice, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMemcpyAsync(H2D)");
+    int rc = run(ctx, d_v, all_subsets ? nullptr : d_o, batch, order_arg, all_subsets, d_val, d_s, stream);
+    if (rc != CDET_OK) return rc;
+    err = cudaMemcpyAsync(values, d_val, valbytes, cudaMemcpyDeviceToHost, stream);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(status, d_s, sbytes, cudaMemcpyDeviceToHost, stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+    if (err != cudaSuccess) return cuda_fail(err, "evaluation");
+    ctx->calls += static_cast<uint64_t>(batch);
+    bool flagged = false;
+    for (int64_t c = 0; c < batch; ++c) {
+        if (status[c] & CDET_CONFIG_FPM_FALLBACK) ++ctx->fallbacks;
+        if (status[c] & (CDET_CONFIG_NONFINITE | CDET_CONFIG_BAD_INPUT)) flagged = true;
+    }
+    if (flagged) return fail(CDET_ERR_VALUE, "Error (integrand): Value is not finite or input rejected");
+    return CDET_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cdet_last_error(void) { return g_last_error.c_str(); }
+
+int cdet_create(const cdet_runtime_scalars* scalars, int device, cdet_context** out) {
+    if (!scalars || !out) return fail(CDET_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const cdet_runtime_scalars& s = *scalars;
+    if (s.n1 < 1 || s.n2 < 1 || s.cheb_nu < 1 || s.cheb_nv < 1)
+        return fail(CDET_ERR_INVALID, "lattice extents and Chebyshev sizes must be positive");
+    int count = 0;
+    cudaError_t err = cudaGetDeviceCount(&count);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return fail(CDET_ERR_INVALID, "no such CUDA device");
+    DeviceGuard guard(device);
+    cdet_context* ctx = new cdet_context();
+    ctx->device = device;
+    ctx->scalars = s;
+    ctx->coeff_count = expected_coeffs(s);
+    ctx->corner_count = expected_corners(s);
+    err = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (err != cudaSuccess) {
+        delete ctx;
+        return cuda_fail(err, "cudaDeviceGetAttribute");
+    }
+    *out = ctx;
+    return CDET_OK;
+}
+
+void cdet_destroy(cdet_context* ctx) {
+    if (!ctx) return;
+    DeviceGuard guard(ctx->device);
+    cudaDeviceSynchronize();
+    for (TableSlot& slot : ctx->tables) release_slot(slot);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->staging) cudaFree(ctx->staging);
+    delete ctx;
+}
+
+int cdet_upload_table(cdet_context* ctx, int kind, const cdet_table_view* t, size_t coeff_count,
+                      size_t corner_count) {
+    if (!ctx || !t || !valid_kind(kind)) return fail(CDET_ERR_INVALID, "bad argument");
+    if (coeff_count != ctx->coeff_count || corner_count != ctx->corner_count)
+        return fail(CDET_ERR_INVALID, "table size does not match N1, N2, CHEB_NU, CHEB_NV");
+    if (!t->upper_coeffs || !t->lower_coeffs || !t->upper_corners || !t->lower_corners)
+        return fail(CDET_ERR_INVALID, "null table array");
+    DeviceGuard guard(ctx->device);
+    TableSlot& slot = ctx->tables[kind];
+    release_slot(slot);
+    const size_t cb = coeff_count * sizeof(double), kb = corner_count * sizeof(double);
+    void* mem = nullptr;
+    cudaError_t err = cudaMalloc(&mem, 2 * cb + 2 * kb);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(table)");
+    char* base = static_cast<char*>(mem);
+    const void* src[4] = {t->upper_coeffs, t->lower_coeffs, t->upper_corners, t->lower_corners};
+    const size_t off[4] = {0, cb, 2 * cb, 2 * cb + kb};
+    const size_t len[4] = {cb, cb, kb, kb};
+    for (int k = 0; k < 4; ++k) {
+        err = cudaMemcpy(base + off[k], src[k], len[k], cudaMemcpyHostToDevice);
+        if (err != cudaSuccess) {
+            cudaFree(mem);
+            return cuda_fail(err, "cudaMemcpy(table)");
+        }
+    }
+    slot.owned = mem;
+    slot.dev = cdet::TableDev{reinterpret_cast<const double*>(base), reinterpret_cast<const double*>(base + cb),
+                              reinterpret_cast<const double*>(base + 2 * cb),
+                              reinterpret_cast<const double*>(base + 2 * cb + kb)};
+    slot.ready = true;
+    return CDET_OK;
+}
+
+int cdet_bind_device_table(cdet_context* ctx, int kind, const cdet_table_view* t,
+                           size_t coeff_count, size_t corner_count) {
+    if (!ctx || !t || !valid_kind(kind)) return fail(CDET_ERR_INVALID, "bad argument");
+    if (coeff_count != ctx->coeff_count || corner_count != ctx->corner_count)
+        return fail(CDET_ERR_INVALID, "table size does not match N1, N2, CHEB_NU, CHEB_NV");
+    if (!t->upper_coeffs || !t->lower_coeffs || !t->upper_corners || !t->lower_corners)
+        return fail(CDET_ERR_INVALID, "null table array");
+    TableSlot& slot = ctx->tables[kind];
+    release_slot(slot);
+    slot.dev = cdet::TableDev{t->upper_coeffs, t->lower_coeffs, t->upper_corners, t->lower_corners};
+    slot.ready = true;
+    return CDET_OK;
+}
+
+int cdet_alias_table(cdet_context* ctx, int kind, int source_kind) {
+    if (!ctx || !valid_kind(kind) || !valid_kind(source_kind) || kind == source_kind)
+        return fail(CDET_ERR_INVALID, "bad argument");
+    for (int k = source_kind; k >= 0; k = ctx->tables[k].alias_of)
+        if (k == kind) return fail(CDET_ERR_INVALID, "alias cycle");
+    TableSlot& slot = ctx->tables[kind];
+    release_slot(slot);
+    slot.alias_of = source_kind;
+    return CDET_OK;
+}
+
+int cdet_reserve(cdet_context* ctx, int64_t batch, int max_order) {
+    if (!ctx || batch < 1 || max_order < 1 || max_order > cdet::kMaxOrder)
+        return fail(CDET_ERR_INVALID, "bad argument");
+    DeviceGuard guard(ctx->device);
+    return ensure_scratch(ctx, batch, max_order);
+}
+
+int cdet_integrand_device(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                          int64_t batch, int max_order, double* values, int32_t* status,
+                          void* stream) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (max_order < 1 || max_order > cdet::kMaxOrder)
+        return fail(CDET_ERR_INVALID, "The replica integrand is defined only for order >= 1 (max 24 here)");
+    DeviceGuard guard(ctx->device);
+    return run(ctx, vertices, orders, batch, max_order, 0, values, status,
+               static_cast<cudaStream_t>(stream));
+}
+
+int cdet_all_subsets_device(cdet_context* ctx, const double* vertices, int envelope_order,
+                            int64_t batch, double* values, int32_t* status, void* stream) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (envelope_order <= 1 || envelope_order > cdet::kMaxOrder)
+        return fail(CDET_ERR_INVALID,
+                    "The all-subset replica integrand is defined only for envelope order >= 2 (max 24 here)");
+    DeviceGuard guard(ctx->device);
+    return run(ctx, vertices, nullptr, batch, envelope_order, 1, values, status,
+               static_cast<cudaStream_t>(stream));
+}
+
+int cdet_integrand_host(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                        int64_t batch, int max_order, double* values, int32_t* status) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (max_order < 1 || max_order > cdet::kMaxOrder)
+        return fail(CDET_ERR_INVALID, "The replica integrand is defined only for order >= 1 (max 24 here)");
+    DeviceGuard guard(ctx->device);
+    return run_host(ctx, vertices, orders, batch, max_order, 0, values, status);
+}
+
+int cdet_all_subsets_host(cdet_context* ctx, const double* vertices, int envelope_order,
+                          int64_t batch, double* values, int32_t* status) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (envelope_order <= 1 || envelope_order > cdet::kMaxOrder)
+        return fail(CDET_ERR_INVALID,
+                    "The all-subset replica integrand is defined only for envelope order >= 2 (max 24 here)");
+    DeviceGuard guard(ctx->device);
+    return run_host(ctx, vertices, nullptr, batch, envelope_order, 1, values, status);
+}
+
+int cdet_counters(const cdet_context* ctx, uint64_t* integrand_calls, uint64_t* fpm_fallbacks) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (integrand_calls) *integrand_calls = ctx->calls;
+    if (fpm_fallbacks) *fpm_fallbacks = ctx->fallbacks;
+    return CDET_OK;
+}
+
+int cdet_last_launch_count(const cdet_context* ctx) { return ctx ? ctx->last_launches : 0; }
+
+}  // extern "C"

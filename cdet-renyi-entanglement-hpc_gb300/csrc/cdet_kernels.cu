@@ -1,0 +1,583 @@
+// FP64 CDet integrand kernels for sm_103a.
+//
+// Three launches per batch of vertex configurations:
+//
+//  1. green_assembly_fp64: one thread per Green-matrix entry (configuration,
+//     table set, i, j). It decodes the two vertices, forms the lookup
+//     descriptor and evaluates the 2-D Chebyshev sum of the spin-up (and, when
+//     the tables differ, spin-down) block by the reference's Clenshaw
+//     recurrences, rows in descending order with the outer recurrence fused.
+//  2. principal_minors_fp64: one warp per (configuration, table set). The
+//     warp runs the shifted Schur-complement recursion of mat2pm level by
+//     level, lanes spread over (set, row, column) work items, then the prefix
+//     product and the shift removal, and writes a[mask] = pm_up * pm_down into
+//     a lane-interleaved array for step 3.
+//  3. cdet_fp64: one lane per configuration, 32 configurations per warp. Each
+//     lane runs the connected-sum recursion of its configuration serially, in
+//     the reference's mask and submask order, so the FP64 pipe always runs
+//     full warps. It then applies the prefactors and forms
+//     twisted - 2 * ordinary.
+//
+// On GB300 the FP64 pipe retires about 504 G lane-operations per second and a
+// partially active warp costs as much as a full one, so all three kernels keep
+// every lane of every FP64 instruction busy.
+#include "cdet_device.cuh"
+#include "cdet_kernels.cuh"
+
+#include <algorithm>
+
+namespace cdet {
+
+namespace {
+
+// sampled_coordinate_to_index (g_funcs.h:315-342) on value*extent; flags
+// values the reference would reject (non-finite, outside the int range).
+__device__ __forceinline__ int coordinate_index(double scaled, int extent, bool& bad) {
+    if (!(scaled > -2147483648.0 && scaled < 2147483648.0)) {
+        bad = true;
+        return 0;
+    }
+    int index = static_cast<int>(floor(scaled));
+    if (index < 0) index = 0;
+    if (index >= extent) index = extent - 1;
+    return index;
+}
+
+struct Vertex {
+    double tau, tau_unit;
+    int x, y, replica;
+};
+
+// Vertex decode of integrand_temp_typed (integrand_replica_randomly_sampled.h:422-432).
+__device__ __forceinline__ Vertex decode_vertex(const double* __restrict__ v, const Scalars& s,
+                                                int replica_count, bool& bad) {
+    Vertex out;
+    const double tu = __ldg(v + 0);
+    if (!isfinite(tu)) bad = true;
+    out.tau_unit = tu;
+    out.tau = dmul(s.beta, tu);
+    out.x = coordinate_index(dmul(static_cast<double>(s.n1), __ldg(v + 1)), s.n1, bad);
+    out.y = coordinate_index(dmul(static_cast<double>(s.n2), __ldg(v + 2)), s.n2, bad);
+    out.replica = replica_count <= 1
+                      ? 0
+                      : coordinate_index(dmul(static_cast<double>(replica_count), __ldg(v + 3)),
+                                         replica_count, bad);
+    return out;
+}
+
+__device__ __forceinline__ double clamp_unit(double value) {
+    if (value < -1.0) return -1.0;
+    if (value > 1.0) return 1.0;
+    return value;
+}
+
+// ------------------------------------------------------ 1. assembly -------
+__global__ void __launch_bounds__(128) green_assembly_fp64(const __grid_constant__ Problem p,
+                                                          const __grid_constant__ Scratch w) {
+    const int nmax = p.max_order;
+    const int64_t per_set = static_cast<int64_t>(nmax) * nmax;
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= p.batch * 2 * per_set) return;
+    const int64_t c = idx / (2 * per_set);
+    const int64_t rem = idx - c * 2 * per_set;
+    const int set = static_cast<int>(rem / per_set);
+    const int pair = static_cast<int>(rem - set * per_set);
+    const int i = pair / nmax;
+    const int j = pair - i * nmax;
+    const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
+    if (n < 1 || n > nmax) {
+        if (rem == 0) atomicOr(p.status + c, kStatusBadInput);
+        return;
+    }
+    if (i >= n || j >= n) return;
+
+    const Scalars& s = p.s;
+    const int replica_count = set == 0 ? 2 : 1;
+    bool bad = false;
+    const double* vbase = p.vertices + c * static_cast<int64_t>(nmax) * 4;
+    const Vertex vi = decode_vertex(vbase + 4 * i, s, replica_count, bad);
+    const Vertex vj = decode_vertex(vbase + 4 * j, s, replica_count, bad);
+    if (bad) {
+        atomicOr(p.status + c, kStatusBadInput);
+        return;
+    }
+
+    // prepare_green_lookup_descriptor (g_funcs.h:609-653).
+    const bool upper = (i != j) && (vi.tau_unit > vj.tau_unit);
+    const uint64_t sitepair =
+        ((((static_cast<uint64_t>(vi.replica) * 2u + static_cast<uint64_t>(vj.replica)) * s.n1 +
+           vi.x) * s.n2 + vi.y) * s.n1 + vj.x) * s.n2 + vj.y;
+    const double t_outer = upper ? vi.tau : vj.tau;  // the later time of the pair
+    const double t_inner = upper ? vj.tau : vi.tau;
+    const TableDev& tu = p.up[set];
+    const TableDev& td = p.down[set];
+    const bool one_spin = p.same_spin[set] != 0;
+    double up, down;
+    if (t_outer < s.branch_eps) {
+        up = __ldg((upper ? tu.upper_corners : tu.lower_corners) + sitepair);
+        down = one_spin ? up : __ldg((upper ? td.upper_corners : td.lower_corners) + sitepair);
+    } else {
+        const double u = clamp_unit(dsub(ddiv(dmul(2.0, t_outer), s.beta), 1.0));
+        const double v = clamp_unit(dsub(ddiv(dmul(2.0, t_inner), t_outer), 1.0));
+        const uint64_t base = sitepair * static_cast<uint64_t>(s.nu) * static_cast<uint64_t>(s.nv);
+        const double* bu = (upper ? tu.upper : tu.lower) + base;
+        OuterClenshaw ou;
+        ou.init(s.nu - 1, u);
+        if (one_spin) {
+            for (int a = s.nu - 1; a >= 0; --a)
+                ou.push(a, clenshaw_row(bu + static_cast<int64_t>(a) * s.nv, s.nv - 1, v));
+            up = down = ou.result();
+        } else {
+            const double* bd = (upper ? td.upper : td.lower) + base;
+            OuterClenshaw od;
+            od.init(s.nu - 1, u);
+            for (int a = s.nu - 1; a >= 0; --a) {
+                double ru, rd;
+                clenshaw_row_pair(bu + static_cast<int64_t>(a) * s.nv,
+                                  bd + static_cast<int64_t>(a) * s.nv, s.nv - 1, v, ru, rd);
+                ou.push(a, ru);
+                od.push(a, rd);
+            }
+            up = ou.result();
+            down = od.result();
+        }
+    }
+    // fill_pair_range (integrand_replica_randomly_sampled.h:467-473).
+    const int64_t mslot = (c * 2 + set) * 2;
+    if (i == j) {
+        up = dadd(up, s.diag_up_shift);
+        down = dadd(down, s.diag_down_shift);
+        w.diag[mslot * nmax + i] = up;
+        w.diag[(mslot + 1) * nmax + i] = down;
+    }
+    w.green[mslot * per_set + i * n + j] = dmul(up, s.scale);
+    w.green[(mslot + 1) * per_set + i * n + j] = dmul(down, s.scale);
+}
+
+// ------------------------------------------------- 2. principal minors ----
+struct WsLayout {
+    int list;      // doubles per Schur-complement list
+    size_t a, old_list, new_list, aux, shifted_up, shifted_down, total;
+};
+
+__host__ __device__ inline WsLayout ws_layout(int nmax) {
+    WsLayout l;
+    size_t list = static_cast<size_t>(nmax) * nmax;
+    for (int level = 0; level < nmax - 1; ++level) {
+        const size_t ns = static_cast<size_t>(nmax - level - 1);
+        const size_t cand = (static_cast<size_t>(1) << (level + 1)) * ns * ns;
+        if (cand > list) list = cand;
+    }
+    l.list = static_cast<int>(list);
+    const size_t subsets = static_cast<size_t>(1) << nmax;
+    auto even = [](size_t x) { return (x + 1) & ~static_cast<size_t>(1); };
+    l.a = 0;
+    l.old_list = even(static_cast<size_t>(nmax) * nmax);
+    l.new_list = l.old_list + even(list);
+    l.aux = l.new_list + even(list);
+    l.shifted_up = l.aux + even(subsets / 2 + 2);
+    l.shifted_down = l.shifted_up + subsets;
+    l.total = l.shifted_down + subsets;
+    return l;
+}
+
+// Partial-pivot LU minor of the principal submatrix selected by mask
+// (determinant_principal_minor_from_buffer, fast_principle_minors.h:39-105);
+// m is this lane's n*n scratch.
+__device__ double minor_by_lu(const double* a, int n, uint32_t mask, double* m) {
+    int idx[kMaxOrder];
+    int k = 0;
+    for (int i = 0; i < n; ++i)
+        if (mask & (1u << i)) idx[k++] = i;
+    if (k == 0) return 1.0;
+    for (int r = 0; r < k; ++r)
+        for (int c = 0; c < k; ++c) m[r * k + c] = a[idx[r] * n + idx[c]];
+    double det = 1.0;
+    int sign = 1;
+    for (int col = 0; col < k; ++col) {
+        int pivot_row = col;
+        double pivot_abs = fabs(m[col * k + col]);
+        for (int row = col + 1; row < k; ++row) {
+            const double cand = fabs(m[row * k + col]);
+            if (cand > pivot_abs) {
+                pivot_abs = cand;
+                pivot_row = row;
+            }
+        }
+        if (pivot_abs == 0.0) return 0.0;
+        if (pivot_row != col) {
+            for (int c = col; c < k; ++c) {
+                const double t = m[col * k + c];
+                m[col * k + c] = m[pivot_row * k + c];
+                m[pivot_row * k + c] = t;
+            }
+            sign = -sign;
+        }
+        const double pivot = m[col * k + col];
+        det = dmul(det, pivot);
+        for (int row = col + 1; row < k; ++row) {
+            const double factor = ddiv(m[row * k + col], pivot);
+            if (factor == 0.0) continue;
+            m[row * k + col] = 0.0;
+            for (int c = col + 1; c < k; ++c)
+                m[row * k + c] = dfma(-factor, m[col * k + c], m[row * k + c]);
+        }
+    }
+    return sign < 0 ? -det : det;
+}
+
+// mat2pm_from_buffer (fast_principle_minors.h:120-246) for one matrix, by a
+// whole warp. On return shifted[mask] (mask >= 1) holds the principal minor
+// of the rows/columns in mask. Returns true when a pivot sent the matrix to
+// the whole-matrix LU fallback (which this function then also runs).
+__device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_param,
+                            const WsLayout& lay, double* ws, double* shifted, double* lu_lane,
+                            int lane) {
+    const int msize = n * n;
+    const uint32_t subsets = 1u << n;
+    double max_abs = 0.0;
+    for (int k = lane; k < msize; k += kWarp) {
+        const double e = fabs(A[k]);
+        if (e > max_abs) max_abs = e;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_xor_sync(0xffffffffu, max_abs, off);
+        if (o > max_abs) max_abs = o;
+    }
+    const bool explicit_shift = !(shift_param < 0.0);
+    const double p = explicit_shift ? shift_param : ddiv(max_abs, static_cast<double>(msize));
+    if (max_abs == 0.0 && p == 0.0) {
+        for (uint32_t m = lane; m < subsets; m += kWarp) shifted[m] = 0.0;
+        __syncwarp();
+        return false;
+    }
+    const double fallback_eps = (tol > 0.0 && max_abs > 0.0) ? dmul(tol, max_abs) : 0.0;
+
+    double* old_list = ws + lay.old_list;
+    double* new_list = ws + lay.new_list;
+    double* inv = ws + lay.aux;
+    for (int k = lane; k < msize; k += kWarp) old_list[k] = A[k];
+    for (uint32_t m = lane; m < subsets; m += kWarp) shifted[m] = m == 0 ? 1.0 : p;
+    __syncwarp();
+    if (lane == 0) shifted[1] = dadd(shifted[1], old_list[0]);
+
+    uint32_t minor_index = 2;
+    bool fell_back = false;
+    for (int level = 0; level < n - 1; ++level) {
+        const int old_size = n - level;
+        const int old_msize = old_size * old_size;
+        const int new_size = old_size - 1;
+        const int new_msize = new_size * new_size;
+        const int sets = 1 << level;
+        // pivots of this level, one per set
+        bool bad_pivot = false;
+        for (int set = lane; set < sets; set += kWarp) {
+            const double pivot = dadd(old_list[set * old_msize], p);
+            const double pa = fabs(pivot);
+            if (pa == 0.0 || (fallback_eps > 0.0 && pa <= fallback_eps)) bad_pivot = true;
+            inv[set] = ddiv(1.0, pivot);
+        }
+        if (__any_sync(0xffffffffu, bad_pivot)) {
+            fell_back = true;
+            break;
+        }
+        __syncwarp();
+        // first-column factors, one per (set, row)
+        double* factor = inv + sets;
+        for (int item = lane; item < sets * new_size; item += kWarp) {
+            const int set = item / new_size;
+            const int row = item - set * new_size;
+            factor[item] = dmul(old_list[set * old_msize + (row + 1) * old_size], inv[set]);
+        }
+        __syncwarp();
+        // submatrix without the pivot, and its Schur complement
+        const int items = sets * new_msize;
+        for (int item = lane; item < items; item += kWarp) {
+            const int set = item / new_msize;
+            const int e = item - set * new_msize;
+            const int row = e / new_size;
+            const int col = e - row * new_size;
+            const int src = set * old_msize;
+            const double base = old_list[src + (row + 1) * old_size + col + 1];
+            new_list[item] = base;
+            new_list[items + item] = dfma(-old_list[src + 1 + col], factor[set * new_size + row], base);
+        }
+        __syncwarp();
+        for (int m = lane; m < 2 * sets; m += kWarp)
+            shifted[minor_index + m] = dadd(shifted[minor_index + m], new_list[m * new_msize]);
+        minor_index += 2 * sets;
+        double* t = old_list;
+        old_list = new_list;
+        new_list = t;
+        __syncwarp();
+    }
+    if (fell_back) {
+        // determinant_principal_minors_from_buffer (fast_principle_minors.h:107-115)
+        for (uint32_t m = 1 + lane; m < subsets; m += kWarp) shifted[m] = minor_by_lu(A, n, m, lu_lane);
+        __syncwarp();
+        return true;
+    }
+    // prefix product over levels
+    for (uint32_t step = 1; step < subsets; step <<= 1) {
+        for (uint32_t set = step + 1 + lane; set < 2 * step; set += kWarp)
+            shifted[set] = dmul(shifted[set], shifted[set - step]);
+        __syncwarp();
+    }
+    // remove the uniform shift by multilinearity
+    for (uint32_t step = subsets; step > 1; step >>= 1) {
+        const uint32_t half = step >> 1;
+        for (uint32_t q = lane; q < subsets / 2; q += kWarp) {
+            const uint32_t t = q / half;
+            const uint32_t ss = t * step + half + (q - t * half);
+            shifted[ss] = dfma(-p, shifted[ss - half], shifted[ss]);
+        }
+        __syncwarp();
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(128) principal_minors_fp64(const __grid_constant__ Problem p,
+                                                            const __grid_constant__ Scratch w,
+                                                            int use_smem) {
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int warp_in_block = threadIdx.x / kWarp;
+    const int warps_per_block = blockDim.x / kWarp;
+    const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
+    const int64_t total_warps = static_cast<int64_t>(gridDim.x) * warps_per_block;
+    const int nmax = p.max_order;
+    const WsLayout lay = ws_layout(nmax);
+    double* ws = use_smem ? smem + static_cast<size_t>(warp_in_block) * lay.total
+                          : w.ws_global + static_cast<size_t>(global_warp) * lay.total;
+    double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
+    const uint32_t full = 1u << nmax;
+    const int64_t items = p.batch * 2;
+    for (int64_t item = global_warp; item < items; item += total_warps) {
+        const int64_t c = item >> 1;
+        const int set = static_cast<int>(item & 1);
+        const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
+        if (n < 2 || n > nmax) continue;  // order 1 needs no minors; bad orders are flagged by step 1
+        const double* green = w.green + (c * 2 + set) * 2 * static_cast<int64_t>(nmax) * nmax;
+        double* A = ws + lay.a;
+        bool fb = false;
+        for (int k = lane; k < n * n; k += kWarp) A[k] = green[k];
+        __syncwarp();
+        fb |= mat2pm_warp(A, n, p.s.tol_fpm, p.s.fpm_shift, lay, ws, ws + lay.shifted_up, lu_lane, lane);
+        const bool one_spin = p.same_spin[set] != 0;
+        if (!one_spin) {
+            for (int k = lane; k < n * n; k += kWarp) A[k] = green[static_cast<int64_t>(nmax) * nmax + k];
+            __syncwarp();
+            fb |= mat2pm_warp(A, n, p.s.tol_fpm, p.s.fpm_shift, lay, ws, ws + lay.shifted_down,
+                              lu_lane, lane);
+        }
+        const double* su = ws + lay.shifted_up;
+        const double* sd = one_spin ? su : ws + lay.shifted_down;
+        // a[mask] = up[mask-1] * down[mask-1] (integrand_replica_randomly_sampled.h:254-257)
+        double* a = w.a_int + ((c >> 5) * 2 + set) * static_cast<int64_t>(full) * kWarp + (c & 31);
+        for (uint32_t m = lane; m < (1u << n); m += kWarp)
+            a[static_cast<int64_t>(m) * kWarp] = m == 0 ? 0.0 : dmul(su[m], sd[m]);
+        if (fb && lane == 0) atomicOr(p.status + c, kStatusFpmFallback);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------- 3. CDet -------
+// compute_dp_ztransform (integrand_replica_randomly_sampled.h:226-290) for
+// this lane's configuration: only masks holding vertex 0 are reduced.
+__device__ double cdet_single(const double* a, double* dp, int n, double threshold) {
+    const bool filter = threshold > 0.0;
+    dp[1 * kWarp] = a[1 * kWarp];
+    for (int bits = 2; bits <= n; ++bits) {
+        // masks = 1 | (rest << 1) with popcount(rest) = bits-1, increasing
+        const uint32_t rest_limit = 1u << (n - 1);
+        for (uint32_t rest = (1u << (bits - 1)) - 1u; rest < rest_limit; rest = next_same_popcount(rest)) {
+            const uint32_t mask = (rest << 1) | 1u;
+            double acc = a[mask * kWarp];
+            double rhs = fabs(acc);
+            // submasks holding vertex 0, in the reference's descending order
+            for (uint32_t s = (rest - 1u) & rest;; s = (s - 1u) & rest) {
+                const uint32_t sub = (s << 1) | 1u;
+                const double term = dmul(dp[sub * kWarp], a[(mask ^ sub) * kWarp]);
+                acc = dsub(acc, term);
+                rhs = dadd(rhs, fabs(term));
+                if (s == 0) break;
+            }
+            if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
+            dp[mask * kWarp] = acc;
+            if (bits == n) break;  // only one mask at the top level
+        }
+    }
+    return dp[((1u << n) - 1u) * kWarp];
+}
+
+// compute_dp_ztransform_all_subsets (:292-347): every mask, anchored at its
+// lowest vertex.
+__device__ void cdet_all(const double* a, double* dp, int n, double threshold) {
+    const bool filter = threshold > 0.0;
+    dp[0] = 0.0;
+    for (int i = 0; i < n; ++i) dp[(1u << i) * kWarp] = a[(1u << i) * kWarp];
+    const uint32_t limit = 1u << n;
+    for (int bits = 2; bits <= n; ++bits) {
+        for (uint32_t mask = (1u << bits) - 1u; mask < limit; mask = next_same_popcount(mask)) {
+            const uint32_t anchor = mask & (~mask + 1u);
+            const uint32_t rest = mask ^ anchor;
+            double acc = a[mask * kWarp];
+            double rhs = fabs(acc);
+            for (uint32_t s = (rest - 1u) & rest;; s = (s - 1u) & rest) {
+                const uint32_t sub = s | anchor;
+                const double term = dmul(dp[sub * kWarp], a[(mask ^ sub) * kWarp]);
+                acc = dsub(acc, term);
+                rhs = dadd(rhs, fabs(term));
+                if (s == 0) break;
+            }
+            if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
+            dp[mask * kWarp] = acc;
+            if (bits == n) break;
+        }
+    }
+}
+
+// order1_density_integrand_from_sampled_vertex (:173-213): shifted diagonal
+// values of one vertex -> (-r) U beta (up*down - shift_up*shift_down).
+__device__ __forceinline__ double order1_value(const Scalars& s, double su, double sd, int r) {
+    const double counter = dmul(s.diag_up_shift, s.diag_down_shift);
+    return dmul(dmul(dmul(static_cast<double>(-r), s.u), s.beta), dsub(dmul(su, sd), counter));
+}
+
+__global__ void __launch_bounds__(128) cdet_fp64(const __grid_constant__ Problem p,
+                                                const __grid_constant__ Scratch w) {
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= p.batch) return;
+    const int lane = static_cast<int>(c & 31);
+    const int nmax = p.max_order;
+    const int64_t full = int64_t{1} << nmax;
+    const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
+    if (n < 1 || n > nmax) return;
+    const Scalars& s = p.s;
+    const double threshold = dmul(s.z_eps0, s.z_safety);
+    const int64_t g = c >> 5;
+    int32_t status = 0;
+    const double* diag = w.diag + c * 2 * 2 * nmax;  // [set][spin][i]
+
+    if (!p.all_subsets) {
+        DD value[2];
+        for (int set = 0; set < 2; ++set) {
+            const int r = set == 0 ? 2 : 1;
+            if (n == 1) {
+                // order-1 branch (cdet_integrand_evaluator.h:171-201): no finiteness check
+                const double raw = order1_value(s, diag[(set * 2) * nmax], diag[(set * 2 + 1) * nmax], r);
+                value[set] = DD{raw, 0.0};
+            } else {
+                const double* a = w.a_int + (g * 2 + set) * full * kWarp + lane;
+                double* dp = w.dp_int + (g * 2 + set) * full * kWarp + lane;
+                const double cset = cdet_single(a, dp, n, threshold);
+                const DDPair pf = p.pref_dd[set][n];
+                value[set] = dd_mul(DD{pf.hi, pf.lo}, DD{cset, 0.0});
+                if (!dd_finite(value[set])) status |= kStatusNonFinite;
+            }
+        }
+        const DD result = dd_sub(value[0], dd_mul(DD{2.0, 0.0}, value[1]));
+        p.values[c] = dadd(result.hi, result.lo);
+    } else {
+        // integrand_all_subset_values_typed_into (:826-877) per set, then
+        // values[mask] -= 2 * ordinary[mask] (cdet_integrand_evaluator.h:346-350)
+        double* out = p.values + c * full;
+        for (int set = 0; set < 2; ++set) {
+            const int r = set == 0 ? 2 : 1;
+            const double* a = w.a_int + (g * 2 + set) * full * kWarp + lane;
+            double* dp = w.dp_int + (g * 2 + set) * full * kWarp + lane;
+            cdet_all(a, dp, n, threshold);
+            const uint32_t count = 1u << n;
+            for (uint32_t mask = 0; mask < count; ++mask) {
+                const int k = __popc(mask);
+                double v;
+                if (k == 0) {
+                    v = 0.0;
+                } else if (k == 1) {
+                    const int i = __ffs(mask) - 1;
+                    v = order1_value(s, diag[(set * 2) * nmax + i], diag[(set * 2 + 1) * nmax + i], r);
+                } else {
+                    v = dmul(p.pref_ld[set][k], dp[static_cast<int64_t>(mask) * kWarp]);
+                }
+                if (!isfinite(v)) status |= kStatusNonFinite;
+                if (set == 0) out[mask] = v;
+                else out[mask] = dsub(out[mask], dmul(2.0, v));
+            }
+        }
+    }
+    if (status) atomicOr(p.status + c, status);
+}
+
+}  // namespace
+
+size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).total; }
+
+size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps) {
+    const size_t groups = static_cast<size_t>((batch + 31) / 32);
+    const size_t n2 = static_cast<size_t>(max_order) * max_order;
+    const size_t subsets = static_cast<size_t>(1) << max_order;
+    size_t total = 0;
+    total += static_cast<size_t>(batch) * 4 * n2;                   // green
+    total += static_cast<size_t>(batch) * 4 * max_order;            // diag
+    total += 2 * groups * 2 * subsets * kWarp;                      // a_int, dp_int
+    total += ws_warps * minors_workspace_doubles(max_order);        // minors workspace
+    total += ws_warps * kWarp * n2;                                 // LU fallback scratch
+    return total * sizeof(double) + 64 * 6;
+}
+
+void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out) {
+    const size_t groups = static_cast<size_t>((batch + 31) / 32);
+    const size_t n2 = static_cast<size_t>(max_order) * max_order;
+    const size_t subsets = static_cast<size_t>(1) << max_order;
+    char* cursor = static_cast<char*>(base);
+    auto take = [&](size_t doubles) {
+        double* ptr = reinterpret_cast<double*>(cursor);
+        cursor += ((doubles * sizeof(double) + 63) / 64) * 64;
+        return ptr;
+    };
+    out->green = take(static_cast<size_t>(batch) * 4 * n2);
+    out->diag = take(static_cast<size_t>(batch) * 4 * max_order);
+    out->a_int = take(groups * 2 * subsets * kWarp);
+    out->dp_int = take(groups * 2 * subsets * kWarp);
+    out->ws_global = take(ws_warps * minors_workspace_doubles(max_order));
+    out->lu_scratch = take(ws_warps * kWarp * n2);
+    out->ws_warps = ws_warps;
+}
+
+cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_count,
+                                  cudaStream_t stream) {
+    if (p.batch <= 0) return cudaSuccess;
+    const int64_t entries = p.batch * 2 * static_cast<int64_t>(p.max_order) * p.max_order;
+    const int threads = 128;
+    green_assembly_fp64<<<static_cast<unsigned>((entries + threads - 1) / threads), threads, 0,
+                          stream>>>(p, w);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+
+    // Minors: the per-warp workspace goes to shared memory when four warps'
+    // worth fits a block, otherwise to the global workspace.
+    const size_t ws_bytes = minors_workspace_doubles(p.max_order) * sizeof(double);
+    const size_t smem_budget = 200 * 1024;
+    const int warps_per_block = 4;
+    const bool use_smem = ws_bytes * warps_per_block <= smem_budget;
+    const int64_t items = p.batch * 2;
+    int64_t blocks = (items + warps_per_block - 1) / warps_per_block;
+    const int64_t max_blocks = static_cast<int64_t>(w.ws_warps) / warps_per_block;
+    blocks = std::min<int64_t>(blocks, std::max<int64_t>(1, max_blocks));
+    const size_t smem = use_smem ? ws_bytes * warps_per_block : 0;
+    if (smem > 48 * 1024) {
+        err = cudaFuncSetAttribute(principal_minors_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem));
+        if (err != cudaSuccess) return err;
+    }
+    principal_minors_fp64<<<static_cast<unsigned>(blocks), warps_per_block * kWarp, smem, stream>>>(
+        p, w, use_smem ? 1 : 0);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+
+    cdet_fp64<<<static_cast<unsigned>((p.batch + threads - 1) / threads), threads, 0, stream>>>(p, w);
+    (void)sm_count;
+    return cudaGetLastError();
+}
+
+}  // namespace cdet

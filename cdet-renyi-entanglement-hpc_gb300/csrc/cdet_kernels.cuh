@@ -1,0 +1,72 @@
+// Kernel argument blocks and launchers shared by the C-ABI translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace cdet {
+
+constexpr int kMaxOrder = 24;  // largest order (envelope) any kernel accepts
+
+// Status bits per configuration (the reference throws or counts instead).
+constexpr int32_t kStatusNonFinite = 1;    // "Value is not finite" (integrand_replica_randomly_sampled.h:543-545)
+constexpr int32_t kStatusFpmFallback = 2;  // whole-matrix LU fallback ran (fast_principle_minors.h:180-186)
+constexpr int32_t kStatusBadInput = 4;     // order out of range or a vertex coordinate the decode rejects
+
+// IntegrandRuntimeScalars<double> (integrand_replica_randomly_sampled.h:41-51).
+struct Scalars {
+    int32_t n1, n2, nu, nv;
+    double beta, u, branch_eps, scale, diag_up_shift, diag_down_shift;
+    double tol_fpm, fpm_shift, z_eps0, z_safety;
+};
+
+// One PiecewiseChebyshevTable<double> resident in HBM.
+struct TableDev {
+    const double* upper;
+    const double* lower;
+    const double* upper_corners;
+    const double* lower_corners;
+};
+
+struct DDPair {
+    double hi, lo;
+};
+
+// Device scratch of one evaluation: per configuration the Green matrices of
+// both table sets and spins, their shifted diagonals, and the subset arrays
+// a[mask] and dp[mask] of the CDet recursion laid out lane-interleaved for
+// 32-configuration groups.
+struct Scratch {
+    double* green;      // [batch][2 sets][2 spins][max_order^2]
+    double* diag;       // [batch][2][2][max_order]
+    double* a_int;      // [groups][2][2^max_order][32]
+    double* dp_int;     // [groups][2][2^max_order][32]
+    double* ws_global;  // per-warp minors workspace when it does not fit shared memory
+    double* lu_scratch; // per-lane LU fallback scratch, [warps][32][max_order^2]
+    size_t ws_warps;    // warps the global workspace holds
+};
+
+struct Problem {
+    Scalars s;
+    TableDev up[2], down[2];  // set 0 = twisted (r=2), set 1 = ordinary (r=1)
+    int same_spin[2];         // up/down tables and diagonal shifts identical: compute spin up only
+    const double* vertices;   // [batch][max_order][4]: tau, x, y, replica in [0,1)
+    const int32_t* orders;    // [batch] (single-order mode); ignored for all-subsets
+    int64_t batch;
+    int max_order;
+    int all_subsets;          // 0: one value per configuration; 1: 2^max_order values
+    DDPair pref_dd[2][kMaxOrder + 1];   // cdet_order_prefactor<DoubleDouble>, [set][order]
+    double pref_ld[2][kMaxOrder + 1];   // cdet_order_prefactor<double> (host long double)
+    double* values;
+    int32_t* status;
+};
+
+size_t minors_workspace_doubles(int max_order);
+size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps);
+void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out);
+cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& scratch, int sm_count,
+                                  cudaStream_t stream);
+
+}  // namespace cdet

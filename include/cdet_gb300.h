@@ -1,0 +1,154 @@
+/*
+ * cdet_gb300.h - C ABI of the GB300 (sm_103a) CDet Renyi-2 integrand.
+ *
+ * Drop-in boundary for the integrand of Boyuan-Shi-0607/cdet-renyi-entanglement-hpc.
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to that project). All arguments are plain pointers and sizes; the
+ * library owns no host state beyond the opaque context. Errors are status
+ * codes (the reference throws std::runtime_error) with the message available
+ * from cdet_last_error(); include/cdet_gb300.hpp re-throws them with the
+ * reference's messages.
+ *
+ * Numerics: every kernel evaluates the reference's FP64 operations in the
+ * reference's order without contraction, so on equal inputs the values equal
+ * the reference compiled for x86-64 bit for bit.
+ */
+#ifndef CDET_GB300_H
+#define CDET_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CDET_GB300_ABI_VERSION 1
+
+/* Return codes of every entry point. */
+enum cdet_result {
+    CDET_OK = 0,
+    CDET_ERR_INVALID = 1, /* bad argument: null pointer, size or order out of range */
+    CDET_ERR_STATE = 2,   /* a table the call needs is not uploaded */
+    CDET_ERR_CUDA = 3,    /* a CUDA runtime call failed; see cdet_last_error() */
+    CDET_ERR_VALUE = 4    /* at least one configuration is flagged in `status` */
+};
+
+/* Per-configuration status bits written to the `status` arrays. */
+enum cdet_config_status {
+    CDET_CONFIG_NONFINITE = 1,    /* integrand_replica_randomly_sampled.h:543-545, 842-844, 873-875 */
+    CDET_CONFIG_FPM_FALLBACK = 2, /* fast_principle_minors.h:180-186 (counted, not an error) */
+    CDET_CONFIG_BAD_INPUT = 4     /* order outside [1, 24], or a coordinate the decode rejects */
+};
+
+/* Table kinds: the four resident tables g_table_up, g_table_down,
+ * g_table_ordinary_up, g_table_ordinary_down (include/cdet/parameters.h:81-84). */
+enum cdet_table_kind {
+    CDET_TWISTED_UP = 0,
+    CDET_TWISTED_DOWN = 1,
+    CDET_ORDINARY_UP = 2,
+    CDET_ORDINARY_DOWN = 3
+};
+
+/* IntegrandRuntimeScalars<double> (integrand_replica_randomly_sampled.h:41-51)
+ * as built by make_integrand_runtime_scalars (:98-119) and the z-transform
+ * roundoff filter of ztransform_roundoff_config() (precision_config.h:208-287). */
+typedef struct cdet_runtime_scalars {
+    int32_t n1, n2;            /* N1, N2 */
+    int32_t cheb_nu, cheb_nv;  /* CHEB_NU, CHEB_NV (coefficients per axis) */
+    double beta;               /* beta */
+    double u;                  /* U */
+    double branch_eps;         /* BRANCH_EPSILON */
+    double scale;              /* sqrt(U * N1 * N2 * beta) */
+    double diag_up_shift;      /* ALPHA_DOWN / U, added to the spin-up diagonal */
+    double diag_down_shift;    /* ALPHA_UP / U, added to the spin-down diagonal */
+    double tol_fpm;            /* TOL_FPM */
+    double fpm_shift;          /* FPM_GLOBAL_SHIFT; negative means auto (max|A| / n^2) */
+    double z_eps0;             /* ZTRANSFORM_EPSILON0 (2e-16 when auto) */
+    double z_safety;           /* ZTRANSFORM_SAFETY_FACTOR (0 disables the filter) */
+} cdet_runtime_scalars;
+
+/* One PiecewiseChebyshevTable<double> (replica_chebyshev_tables.h:25-33):
+ * coefficients [4*S*S][nu][nv] per branch and corners [4*S*S], S = N1*N2,
+ * indexed by replica_sitepair_index (replica_chebyshev_tables.h:365-400). */
+typedef struct cdet_table_view {
+    const double* upper_coeffs;
+    const double* lower_coeffs;
+    const double* upper_corners;
+    const double* lower_corners;
+} cdet_table_view;
+
+typedef struct cdet_context cdet_context;
+
+/* Creates a context on CUDA device `device` for one parameter set. Replaces
+ * the process globals the integrand reads (include/cdet/parameters.h:11-33)
+ * and the cached scalars of cached_integrand_runtime_scalars_for_real
+ * (cdet_integrand_evaluator.h:73-96). */
+int cdet_create(const cdet_runtime_scalars* scalars, int device, cdet_context** out);
+
+/* Releases the context and every device buffer it owns. */
+void cdet_destroy(cdet_context* ctx);
+
+/* Copies one table from host memory into HBM. Replaces the assignment of
+ * g_table_* by load_data_into_resident_tables (load_data.h:49-99).
+ * coeff_count = 4*S*S*nu*nv, corner_count = 4*S*S. */
+int cdet_upload_table(cdet_context* ctx, int kind, const cdet_table_view* host_table,
+                      size_t coeff_count, size_t corner_count);
+
+/* Uses a table that already lives in device memory (no copy); the caller
+ * keeps it alive. Same layout and sizes as cdet_upload_table. */
+int cdet_bind_device_table(cdet_context* ctx, int kind, const cdet_table_view* device_table,
+                           size_t coeff_count, size_t corner_count);
+
+/* Makes `kind` share the table of `source_kind`, as load_data does when
+ * ALPHA_UP == ALPHA_DOWN (load_data.h:70-91). When a set's up and down
+ * tables are shared and the two diagonal shifts are equal the spin-down
+ * Green matrix equals the spin-up one and is not evaluated twice. */
+int cdet_alias_table(cdet_context* ctx, int kind, int source_kind);
+
+/* Sizes the device scratch for batches up to `batch` configurations of
+ * order (or envelope) up to `max_order`, so that later calls of that size
+ * allocate nothing. */
+int cdet_reserve(cdet_context* ctx, int64_t batch, int max_order);
+
+/* Batched single-order integrand on device buffers, asynchronous on `stream`
+ * (a cudaStream_t; NULL = legacy default stream). For configuration c with
+ * order orders[c] (1..max_order), vertices[c][i][0..3] hold the unit-cube
+ * coordinates tau, x, y, replica of vertex i. values[c] receives
+ * evaluate_cdet_density_integrand_double (cdet_integrand_evaluator.h:542-560);
+ * status[c] receives cdet_config_status bits (zeroed by the call). */
+int cdet_integrand_device(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                          int64_t batch, int max_order, double* values, int32_t* status,
+                          void* stream);
+
+/* Batched all-subset integrand on device buffers, asynchronous on `stream`.
+ * values[c][mask] (2^envelope_order per configuration, values[c][0] = 0)
+ * receives evaluate_cdet_density_all_subset_integrands_double_into
+ * (cdet_integrand_evaluator.h:562-583). envelope_order is 2..24. */
+int cdet_all_subsets_device(cdet_context* ctx, const double* vertices, int envelope_order,
+                            int64_t batch, double* values, int32_t* status, void* stream);
+
+/* Host-buffer forms of the two calls above: copy the inputs in, evaluate,
+ * copy the results out, and return when they are in host memory. Pinned
+ * host buffers make the copies asynchronous DMA. Returns CDET_ERR_VALUE when
+ * any configuration is flagged NONFINITE or BAD_INPUT. */
+int cdet_integrand_host(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                        int64_t batch, int max_order, double* values, int32_t* status);
+int cdet_all_subsets_host(cdet_context* ctx, const double* vertices, int envelope_order,
+                          int64_t batch, double* values, int32_t* status);
+
+/* Counters of the host entry points: integrand calls and whole-matrix
+ * principal-minor fallbacks (runtime_counters.h:14-51). */
+int cdet_counters(const cdet_context* ctx, uint64_t* integrand_calls, uint64_t* fpm_fallbacks);
+
+/* Message of the last failed call on this thread ("" when none). */
+const char* cdet_last_error(void);
+
+/* Kernel launches the last evaluation issued (for launch accounting). */
+int cdet_last_launch_count(const cdet_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CDET_GB300_H */
