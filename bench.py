@@ -1,0 +1,362 @@
+"""Benchmark of the CDet integrand on GB300.
+
+Workload: 8x8 periodic Hubbard lattice, t=1, U=4, beta=8, mu=0, subsystem A =
+4x4 corner block (origin square, radius 2), Chebyshev degree 128, 65,536
+seeded configurations at order n = 10 per step (uniform vertices, both spins).
+One step evaluates the whole batch; `value` is configurations per second over
+the whole job with the inputs resident in HBM, `e2e` the same through the
+host-buffer C-ABI call with the host<->device copies inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--path fp64]
+  python bench.py --impl reference ...   # the CPU integrand on the host cores
+
+Under torchrun each rank evaluates its own 65,536 configurations (weak
+scaling, no collective on the data path); timing is bracketed by a barrier and
+a device synchronize and the maximum over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "cdet-renyi-entanglement-hpc_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "configs/sec at order n: batched mixed-prec vs plain FP64 on GB300 at <=1e-10 rel err"
+UNIT = "configs/s"
+WORKLOAD = {
+    "workload": "8x8 Hubbard, 4x4 corner subsystem, Chebyshev degree 128, order n=10, "
+                "65536 configurations per step (per GPU)",
+    "lattice": "8x8", "U": 4, "beta": 8, "mu": 0, "mask": "origin_square r=2",
+    "cheb_degree": 128, "order": 10, "batch_per_gpu": 65536,
+}
+BATCH = 65536
+ORDER = 10
+L2_FLUSH_BYTES = 512 << 20
+PRESET = "8x8-d128"
+
+
+def workload_params():
+    """The benchmark workload, or (--preset 6x6-d96) a 6x6 / half-lattice /
+    degree-96 case whose 1.5 GB of tables suit profiler captures."""
+    from cdet_gb300.params import CdetParams, half_lattice_mask, named_mask
+    if PRESET == "6x6-d96":
+        return CdetParams(n1=6, n2=6, beta="5", mu="0", u="4", alpha_up="0", alpha_down="0",
+                          mask_sites=half_lattice_mask(6, 6), cheb_nu=96, cheb_nv=96)
+    return CdetParams(n1=8, n2=8, beta="8", mu="0", u="4", alpha_up="0", alpha_down="0",
+                      mask_sites=named_mask("origin_square", 8, 8, 2), cheb_nu=128, cheb_nv=128)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), p.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.device_index = device_index
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device_index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.out.flush()
+        self.out.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, f[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.out.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def time_cpu_integrand(params, tables, vertices, orders, threads):
+    """The C restatement of the reference integrand (oracle/) on the host
+    cores: returns (seconds, values)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from bindings import Oracle
+    orc = Oracle(params.runtime_scalars(), tables)
+    t0 = time.perf_counter()
+    values, _ = orc.integrand_batch(vertices, orders, threads=threads)
+    return time.perf_counter() - t0, values
+
+
+def run_reference(args):
+    """--impl reference: the CPU integrand timed on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+    from cdet_gb300.synthetic import uniform_configurations
+    from cdet_gb300.tables import build_tables
+    params = workload_params()
+    device = "cuda" if torch.cuda.is_available() else "cpu"
+    tables = build_tables(params, device=device)
+    host = {k: {kk: vv.cpu().numpy() for kk, vv in t.items()} for k, t in tables.items()}
+    if tables["twisted_down"] is tables["twisted_up"]:
+        host["twisted_down"] = host["twisted_up"]
+        host["ordinary_down"] = host["ordinary_up"]
+    del tables
+    threads = cpu_threads()
+    sample = args.cpu_sample or 64 * threads
+    for w in range(args.warmup):
+        v = uniform_configurations(700 + w, max(threads, 16), ORDER)
+        time_cpu_integrand(params, host, v, np.full(v.shape[0], ORDER, np.int32), threads)
+    total = 0.0
+    for k in range(args.steps):
+        v = uniform_configurations(9000 + k, sample, ORDER)
+        dt, _ = time_cpu_integrand(params, host, v, np.full(sample, ORDER, np.int32), threads)
+        total += dt
+    value = args.steps * sample / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform vertices)",
+        "config": dict(WORKLOAD, batch_per_step=sample),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{sample} configurations per step of the workload, "
+                                   f"{threads} threads (C restatement of the reference integrand, "
+                                   "bit-identical to it on the golden vectors)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from cdet_gb300.integrand import CdetIntegrand
+    from cdet_gb300.synthetic import derive_seed, uniform_configurations
+    from cdet_gb300.tables import build_tables, table_bytes
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+
+    params = workload_params()
+    tables = build_tables(params, device=str(dev))
+    integrand = CdetIntegrand(params, tables, device=local_rank)
+    integrand.reserve(BATCH, ORDER)
+
+    # K + W distinct batches, resident in HBM before timing; each rank its own seeds
+    n_batches = args.steps + args.warmup
+    host_batches = [uniform_configurations(derive_seed(20261203, 100 + rank, s), BATCH, ORDER)
+                    for s in range(n_batches)]
+    d_vertices = [torch.from_numpy(v).to(dev) for v in host_batches]
+    d_orders = torch.full((BATCH,), ORDER, dtype=torch.int32, device=dev)
+    d_values = torch.empty(BATCH, dtype=torch.float64, device=dev)
+    d_status = torch.empty(BATCH, dtype=torch.int32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # the clock sampler starts before the warm-up so that nvidia-smi's start-up
+    # is over when the timed region begins
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(2.0)
+    # warm-up
+    for w in range(args.warmup):
+        flush.zero_()
+        integrand.integrand_device(d_vertices[args.steps + w], d_orders, d_values, d_status, stream)
+    barrier()
+
+    # timed: inputs resident in HBM
+    integrand.profile(True)
+    barrier()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for k in range(args.steps):
+        flush.zero_()  # L2 flush between steps
+        integrand.integrand_device(d_vertices[k], d_orders, d_values, d_status, stream)
+    stop.record(stream)
+    barrier()
+    clock_info = clocks.stop()
+    elapsed_ms = max_over_ranks(start.elapsed_time(stop))
+    kernel_ms, launches = integrand.profile_read()
+    integrand.profile(False)
+    status = d_status.cpu().numpy()
+    values = d_values.cpu().numpy()
+
+    # end to end through the host-buffer C-ABI call, pinned host buffers
+    pinned_v = [torch.from_numpy(v).pin_memory() for v in host_batches[:args.steps]]
+    pinned_o = torch.full((BATCH,), ORDER, dtype=torch.int32).pin_memory()
+    pinned_out = torch.empty(BATCH, dtype=torch.float64).pin_memory()
+    pinned_st = torch.empty(BATCH, dtype=torch.int32).pin_memory()
+    lib = integrand._lib
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        rc = lib.cdet_integrand_host(integrand._ctx, pinned_v[k].data_ptr(), pinned_o.data_ptr(),
+                                     BATCH, ORDER, pinned_out.data_ptr(), pinned_st.data_ptr())
+        if rc not in (0, 4):
+            raise RuntimeError("host-buffer evaluation failed")
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    # both loops end on batch steps-1: the host-buffer values must equal the device ones
+    e2e_match = bool(np.array_equal(pinned_out.numpy().view(np.uint64), values.view(np.uint64)))
+
+    total_configs = BATCH * args.steps * world
+    value = total_configs / (elapsed_ms / 1e3)
+    e2e_value = total_configs / e2e_s
+    hbm_peak, bf16_peak, peak_kind = peaks()
+
+    # roofline of the dominant kernel (Green-matrix assembly)
+    names = ["green_assembly_fp64", "principal_minors_fp64", "cdet_fp64"]
+    dom = int(np.argmax(kernel_ms))
+    per_launch_ms = kernel_ms[dom] / args.steps
+    d2 = params.cheb_nu * params.cheb_nv
+    lookups = BATCH * 2 * ORDER * ORDER  # table sets x entries (up==down tables)
+    alg_bytes = lookups * 8 * d2 + BATCH * ORDER * 4 * 8 + BATCH * 2 * 2 * ORDER * ORDER * 8
+    achieved_gbs = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    fp64_ops = lookups * 3 * d2  # mul, add, sub per coefficient (Clenshaw, no contraction)
+    fp64_peak = 504.0  # G lane-ops/s, FP64 pipe throughput measured on this GB300 pool
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform vertices, "
+        "tables from the in-tree precompute)",
+        "config": dict(WORKLOAD, path="fp64 (bit-identical to the reference)",
+                       parallelism=f"replicas x{world}",
+                       l2="flushed between steps (512 MiB write); tables 8.6 GB > L2"),
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": BATCH * ORDER * 4 * 8 + BATCH * 4,
+                "d2h_bytes_per_step": BATCH * 8 + BATCH * 4},
+        "gpu_launches": int(launches),
+        "kernels_ms_per_step": {n: ms / args.steps for n, ms in zip(names, kernel_ms)},
+        "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": achieved_gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": None,
+                     "fp64_pipe": {"achieved_gops": fp64_ops / (per_launch_ms / 1e3) / 1e9,
+                                   "peak_gops": fp64_peak,
+                                   "frac": fp64_ops / (per_launch_ms / 1e3) / 1e9 / fp64_peak}},
+        "clocks": clock_info,
+        "flagged_configs": int((status & 5).astype(bool).sum()),
+        "fpm_fallbacks": int((status & 2).astype(bool).sum()),
+    }
+    line["e2e_bit_identical"] = e2e_match
+    if PRESET != "8x8-d128":
+        line["config"]["workload"] = f"profiling preset {PRESET}, batch {BATCH}, order {ORDER}"
+
+    if rank == 0 and not args.no_cpu_baseline:
+        host = {k: {kk: vv.cpu().numpy() for kk, vv in t.items()} for k, t in tables.items()}
+        host["twisted_down"] = host["twisted_up"] if tables["twisted_down"] is tables["twisted_up"] \
+            else host["twisted_down"]
+        host["ordinary_down"] = host["ordinary_up"] if tables["ordinary_down"] is tables["ordinary_up"] \
+            else host["ordinary_down"]
+        threads = cpu_threads()
+        sample = args.cpu_sample or 64 * threads
+        v = host_batches[0][:sample]
+        dt, cpu_values = time_cpu_integrand(params, host, v, np.full(sample, ORDER, np.int32), threads)
+        gpu_first = None
+        # the GPU values of the same configurations (batch 0 = first timed step)
+        integrand.integrand_device(d_vertices[0], d_orders, d_values, d_status, stream)
+        torch.cuda.synchronize(dev)
+        gpu_first = d_values.cpu().numpy()[:sample]
+        line["cpu_baseline"] = {
+            "value": sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {sample} configurations of the first timed batch, {threads} threads, "
+                      f"{dt:.1f} s wall (C restatement of the reference integrand)",
+            "bit_identical_to_gpu": bool(np.array_equal(cpu_values.view(np.uint64),
+                                                        gpu_first.view(np.uint64))),
+        }
+    if rank == 0:
+        print(json.dumps(line))
+    integrand.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="configurations in the CPU-baseline sample (default 64 per thread)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--preset", choices=["8x8-d128", "6x6-d96"], default="8x8-d128",
+                    help="6x6-d96 is a smaller case for profiler captures, not a bench line")
+    ap.add_argument("--batch", type=int, default=65536, help="configurations per step per GPU")
+    args = ap.parse_args()
+    global PRESET, BATCH
+    PRESET, BATCH = args.preset, args.batch
+    args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -158,6 +158,18 @@ class CdetIntegrand:
     def last_launch_count(self) -> int:
         return int(self._lib.cdet_last_launch_count(self._ctx))
 
+    def profile(self, enable: bool) -> None:
+        """Record CUDA events around every kernel of later evaluations."""
+        L.check(self._lib.cdet_profile_enable(self._ctx, int(bool(enable))))
+
+    def profile_read(self):
+        """(per-kernel milliseconds [assembly, minors, cdet], launches) since
+        the last read; waits for the recorded events."""
+        ms = (C.c_double * 3)(0.0, 0.0, 0.0)
+        launches = C.c_int64(0)
+        L.check(self._lib.cdet_profile_read(self._ctx, ms, C.byref(launches)))
+        return list(ms), launches.value
+
     # --------------------------------------------- reference entry points ---
     def evaluate_cdet_density_integrand_double(self, vertices) -> float:
         v = _as_vertex_array(vertices)

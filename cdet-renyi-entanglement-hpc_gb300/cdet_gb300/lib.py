@@ -28,7 +28,7 @@ EXPORTED = (
     "cdet_create", "cdet_destroy", "cdet_upload_table", "cdet_bind_device_table",
     "cdet_alias_table", "cdet_reserve", "cdet_integrand_device", "cdet_all_subsets_device",
     "cdet_integrand_host", "cdet_all_subsets_host", "cdet_counters", "cdet_last_error",
-    "cdet_last_launch_count",
+    "cdet_last_launch_count", "cdet_profile_enable", "cdet_profile_read",
 )
 
 _DP = C.POINTER(C.c_double)
@@ -77,6 +77,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.cdet_last_error.restype = C.c_char_p
     lib.cdet_last_launch_count.argtypes = [vp]
+    lib.cdet_profile_enable.argtypes = [vp, i32]
+    lib.cdet_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     _LIB = lib
     return lib
 

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 namespace {
 
@@ -119,6 +120,11 @@ struct cdet_context {
     size_t staging_bytes = 0;
     uint64_t calls = 0, fallbacks = 0;
     int last_launches = 0;
+    // measurement hooks
+    bool profiling = false;
+    std::vector<cdet::KernelEvents> pending;  // recorded, not yet read
+    std::vector<cdet::KernelEvents> spare;    // read, reusable
+    int64_t pending_launches = 0;
 };
 
 namespace {
@@ -241,9 +247,24 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
     // with the call's max_order, which only needs less.
     cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);
     if (err != cudaSuccess) return cuda_fail(err, "cudaMemsetAsync(status)");
-    err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream);
+    cdet::KernelEvents* events = nullptr;
+    if (ctx->profiling) {
+        if (ctx->spare.empty()) {
+            cdet::KernelEvents ev{};
+            for (cudaEvent_t& e : ev.marks) {
+                err = cudaEventCreate(&e);
+                if (err != cudaSuccess) return cuda_fail(err, "cudaEventCreate");
+            }
+            ctx->spare.push_back(ev);
+        }
+        ctx->pending.push_back(ctx->spare.back());
+        ctx->spare.pop_back();
+        events = &ctx->pending.back();
+    }
+    err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events);
     if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
-    ctx->last_launches = 4;  // status memset + 3 kernels
+    ctx->last_launches = 3;  // kernels of this library (the status reset is a memset)
+    if (ctx->profiling) ctx->pending_launches += 3;
     return CDET_OK;
 }
 
@@ -330,6 +351,9 @@ void cdet_destroy(cdet_context* ctx) {
     if (!ctx) return;
     DeviceGuard guard(ctx->device);
     cudaDeviceSynchronize();
+    for (auto* list : {&ctx->pending, &ctx->spare})
+        for (auto& ev : *list)
+            for (cudaEvent_t e : ev.marks) cudaEventDestroy(e);
     for (TableSlot& slot : ctx->tables) release_slot(slot);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->staging) cudaFree(ctx->staging);
@@ -450,5 +474,31 @@ int cdet_counters(const cdet_context* ctx, uint64_t* integrand_calls, uint64_t* 
 }
 
 int cdet_last_launch_count(const cdet_context* ctx) { return ctx ? ctx->last_launches : 0; }
+
+int cdet_profile_enable(cdet_context* ctx, int enable) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    ctx->profiling = enable != 0;
+    return CDET_OK;
+}
+
+int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches) {
+    if (!ctx || !kernel_ms) return fail(CDET_ERR_INVALID, "bad argument");
+    DeviceGuard guard(ctx->device);
+    for (cdet::KernelEvents& ev : ctx->pending) {
+        cudaError_t err = cudaEventSynchronize(ev.marks[3]);
+        if (err != cudaSuccess) return cuda_fail(err, "cudaEventSynchronize");
+        for (int k = 0; k < 3; ++k) {
+            float ms = 0.0f;
+            err = cudaEventElapsedTime(&ms, ev.marks[k], ev.marks[k + 1]);
+            if (err != cudaSuccess) return cuda_fail(err, "cudaEventElapsedTime");
+            kernel_ms[k] += ms;
+        }
+        ctx->spare.push_back(ev);
+    }
+    ctx->pending.clear();
+    if (launches) *launches += ctx->pending_launches;
+    ctx->pending_launches = 0;
+    return CDET_OK;
+}
 
 }  // extern "C"

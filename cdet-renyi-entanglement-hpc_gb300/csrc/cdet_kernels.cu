@@ -545,14 +545,19 @@ void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Sc
 }
 
 cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_count,
-                                  cudaStream_t stream) {
+                                  cudaStream_t stream, const KernelEvents* events) {
     if (p.batch <= 0) return cudaSuccess;
+    auto mark = [&](int k) {
+        if (events && events->marks[k]) cudaEventRecord(events->marks[k], stream);
+    };
+    mark(0);
     const int64_t entries = p.batch * 2 * static_cast<int64_t>(p.max_order) * p.max_order;
     const int threads = 128;
     green_assembly_fp64<<<static_cast<unsigned>((entries + threads - 1) / threads), threads, 0,
                           stream>>>(p, w);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
+    mark(1);
 
     // Minors: the per-warp workspace goes to shared memory when four warps'
     // worth fits a block, otherwise to the global workspace.
@@ -574,10 +579,14 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
         p, w, use_smem ? 1 : 0);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
+    mark(2);
 
     cdet_fp64<<<static_cast<unsigned>((p.batch + threads - 1) / threads), threads, 0, stream>>>(p, w);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    mark(3);
     (void)sm_count;
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 }  // namespace cdet

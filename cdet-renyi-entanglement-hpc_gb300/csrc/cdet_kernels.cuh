@@ -66,7 +66,13 @@ struct Problem {
 size_t minors_workspace_doubles(int max_order);
 size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps);
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out);
+// Optional events recorded before the first kernel and after each kernel
+// (4 events for the 3 kernels); null entries are skipped.
+struct KernelEvents {
+    cudaEvent_t marks[4];
+};
+
 cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& scratch, int sm_count,
-                                  cudaStream_t stream);
+                                  cudaStream_t stream, const KernelEvents* events);
 
 }  // namespace cdet

@@ -147,6 +147,14 @@ const char* cdet_last_error(void);
 /* Kernel launches the last evaluation issued (for launch accounting). */
 int cdet_last_launch_count(const cdet_context* ctx);
 
+/* Measurement hooks; no counterpart in the reference. While enabled, every
+ * evaluation records CUDA events around each of its kernels on the stream it
+ * runs on. cdet_profile_read waits for the recorded events, adds the elapsed
+ * milliseconds per kernel (assembly, minors, CDet) to kernel_ms[0..2] and the
+ * number of kernel launches to *launches, and clears the record. */
+int cdet_profile_enable(cdet_context* ctx, int enable);
+int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif
