@@ -7,7 +7,7 @@ One step evaluates the whole batch; `value` is configurations per second over
 the whole job with the inputs resident in HBM, `e2e` the same through the
 host-buffer C-ABI call with the host<->device copies inside the timed region.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--path fp64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--path both|split|fp64]
   python bench.py --impl reference ...   # the CPU integrand on the host cores
 
 Under torchrun each rank evaluates its own 65,536 configurations (weak
@@ -176,7 +176,7 @@ def run_gpu(args):
     import torch.distributed as dist
     from cdet_gb300.integrand import CdetIntegrand
     from cdet_gb300.synthetic import derive_seed, uniform_configurations
-    from cdet_gb300.tables import build_tables, table_bytes
+    from cdet_gb300.tables import build_tables
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -190,6 +190,10 @@ def run_gpu(args):
     tables = build_tables(params, device=str(dev))
     integrand = CdetIntegrand(params, tables, device=local_rank)
     integrand.reserve(BATCH, ORDER)
+    paths = ["fp64", "split"] if args.path == "both" else [args.path]
+    if "split" in paths:
+        integrand.set_assembly("split")
+        integrand.prepare_split()  # slice the tables outside any timed region
 
     # K + W distinct batches, resident in HBM before timing; each rank its own seeds
     n_batches = args.steps + args.warmup
@@ -215,34 +219,41 @@ def run_gpu(args):
         return float(t.item())
 
     # the clock sampler starts before the warm-up so that nvidia-smi's start-up
-    # is over when the timed region begins
+    # is over when the timed regions begin
     clocks = ClockSampler(local_rank)
     clocks.start()
     time.sleep(2.0)
-    # warm-up
-    for w in range(args.warmup):
-        flush.zero_()
-        integrand.integrand_device(d_vertices[args.steps + w], d_orders, d_values, d_status, stream)
-    barrier()
 
-    # timed: inputs resident in HBM
-    integrand.profile(True)
-    barrier()
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record(stream)
-    for k in range(args.steps):
-        flush.zero_()  # L2 flush between steps
-        integrand.integrand_device(d_vertices[k], d_orders, d_values, d_status, stream)
-    stop.record(stream)
-    barrier()
+    def timed(path):
+        """W untimed steps, then K timed steps (CUDA events on the launching
+        stream, barrier + synchronize on both sides); returns the elapsed ms
+        (max over ranks), per-stage kernel ms, launches, last values/status."""
+        integrand.set_assembly(path)
+        for w in range(args.warmup):
+            flush.zero_()
+            integrand.integrand_device(d_vertices[args.steps + w], d_orders, d_values, d_status, stream)
+        barrier()
+        integrand.profile(True)
+        barrier()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush between steps
+            integrand.integrand_device(d_vertices[k], d_orders, d_values, d_status, stream)
+        stop.record(stream)
+        barrier()
+        elapsed = max_over_ranks(start.elapsed_time(stop))
+        stage_ms, launches = integrand.profile_read()
+        integrand.profile(False)
+        return elapsed, stage_ms, launches, d_values.cpu().numpy(), d_status.cpu().numpy()
+
+    results = {path: timed(path) for path in paths}
     clock_info = clocks.stop()
-    elapsed_ms = max_over_ranks(start.elapsed_time(stop))
-    kernel_ms, launches = integrand.profile_read()
-    integrand.profile(False)
-    status = d_status.cpu().numpy()
-    values = d_values.cpu().numpy()
+    head = "split" if "split" in paths else "fp64"
+    elapsed_ms, stage_ms, launches, values, status = results[head]
 
     # end to end through the host-buffer C-ABI call, pinned host buffers
+    integrand.set_assembly(head)
     pinned_v = [torch.from_numpy(v).pin_memory() for v in host_batches[:args.steps]]
     pinned_o = torch.full((BATCH,), ORDER, dtype=torch.int32).pin_memory()
     pinned_out = torch.empty(BATCH, dtype=torch.float64).pin_memory()
@@ -256,7 +267,7 @@ def run_gpu(args):
         rc = lib.cdet_integrand_host(integrand._ctx, pinned_v[k].data_ptr(), pinned_o.data_ptr(),
                                      BATCH, ORDER, pinned_out.data_ptr(), pinned_st.data_ptr())
         if rc not in (0, 4):
-            raise RuntimeError("host-buffer evaluation failed")
+            raise RuntimeError("host-buffer evaluation failed: " + lib.cdet_last_error().decode())
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     # both loops end on batch steps-1: the host-buffer values must equal the device ones
@@ -266,59 +277,89 @@ def run_gpu(args):
     value = total_configs / (elapsed_ms / 1e3)
     e2e_value = total_configs / e2e_s
     hbm_peak, bf16_peak, peak_kind = peaks()
+    nu, nv = params.cheb_nu, params.cheb_nv
+    lookups = BATCH * 2 * ORDER * ORDER  # table sets x entries (up and down share one table)
 
-    # roofline of the dominant kernel (Green-matrix assembly)
-    names = ["green_assembly_fp64", "principal_minors_fp64", "cdet_fp64"]
-    dom = int(np.argmax(kernel_ms))
-    per_launch_ms = kernel_ms[dom] / args.steps
-    d2 = params.cheb_nu * params.cheb_nv
-    lookups = BATCH * 2 * ORDER * ORDER  # table sets x entries (up==down tables)
-    alg_bytes = lookups * 8 * d2 + BATCH * ORDER * 4 * 8 + BATCH * 2 * 2 * ORDER * ORDER * 8
-    achieved_gbs = alg_bytes / (per_launch_ms / 1e3) / 1e9
-    fp64_ops = lookups * 3 * d2  # mul, add, sub per coefficient (Clenshaw, no contraction)
-    fp64_peak = 504.0  # G lane-ops/s, FP64 pipe throughput measured on this GB300 pool
+    def per_step(ms):
+        return {"split_prep": ms[0] / args.steps, "assembly": ms[1] / args.steps,
+                "minors": ms[2] / args.steps, "cdet": ms[3] / args.steps}
+
+    if head == "split":
+        # tcgen05 kernel: 36 bf16 slice-pair products of nu x nv per lookup
+        per_launch_ms = stage_ms[1] / args.steps
+        flops = lookups * 36 * 2.0 * nu * nv
+        achieved = flops / (per_launch_ms / 1e3) / 1e12
+        roofline = {"kernel": "split_assembly (tcgen05 bf16 slices)", "bound": "tensor",
+                    "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                    "frac": achieved / bf16_peak,
+                    "peak_source": f"{peak_kind} (MEASURED_PEAKS.json bf16_tflops, burst)",
+                    "traffic": None,
+                    "algorithmic": "lookups x 36 slice pairs x 2 x nu x nv"}
+    else:
+        per_launch_ms = stage_ms[1] / args.steps
+        alg_bytes = lookups * 8 * nu * nv
+        achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+        roofline = {"kernel": "green_assembly_fp64", "bound": "hbm", "achieved": achieved,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                    "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "traffic": None,
+                    "fp64_pipe_frac": lookups * 3.0 * nu * nv / (per_launch_ms / 1e3) / 504e9}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform vertices, "
-        "tables from the in-tree precompute)",
-        "config": dict(WORKLOAD, path="fp64 (bit-identical to the reference)",
-                       parallelism=f"replicas x{world}",
+        "vs_baseline": None,
+        "dtype": "f64 (split-bf16 tcgen05 assembly, FP64 minors and CDet)" if head == "split" else "f64",
+        "data": "synthetic (seeded uniform vertices, tables from the in-tree precompute)",
+        "config": dict(WORKLOAD, path=head, parallelism=f"replicas x{world}",
                        l2="flushed between steps (512 MiB write); tables 8.6 GB > L2"),
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": BATCH * ORDER * 4 * 8 + BATCH * 4,
                 "d2h_bytes_per_step": BATCH * 8 + BATCH * 4},
         "gpu_launches": int(launches),
-        "kernels_ms_per_step": {n: ms / args.steps for n, ms in zip(names, kernel_ms)},
-        "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": achieved_gbs,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "traffic": None,
-                     "fp64_pipe": {"achieved_gops": fp64_ops / (per_launch_ms / 1e3) / 1e9,
-                                   "peak_gops": fp64_peak,
-                                   "frac": fp64_ops / (per_launch_ms / 1e3) / 1e9 / fp64_peak}},
+        "stages_ms_per_step": per_step(stage_ms),
+        "roofline": roofline,
         "clocks": clock_info,
         "flagged_configs": int((status & 5).astype(bool).sum()),
         "fpm_fallbacks": int((status & 2).astype(bool).sum()),
+        "e2e_bit_identical": e2e_match,
     }
-    line["e2e_bit_identical"] = e2e_match
-    if PRESET != "8x8-d128":
-        line["config"]["workload"] = f"profiling preset {PRESET}, batch {BATCH}, order {ORDER}"
+    if "fp64" in results:
+        f_ms, f_stage, _, f_values, _ = results["fp64"]
+        line["fp64_path"] = {"value": total_configs / (f_ms / 1e3), "unit": UNIT,
+                             "ms_per_step": f_ms / args.steps, "stages_ms_per_step": per_step(f_stage),
+                             "bit_identical_to_reference": True}
+        if head == "split":
+            line["split_over_fp64"] = value / line["fp64_path"]["value"]
+            ok = f_values != 0
+            rel = np.abs(values[ok] - f_values[ok]) / np.abs(f_values[ok])
+            line["split_vs_fp64_rel_err_order10"] = {
+                "median": float(np.median(rel)), "p90": float(np.percentile(rel, 90)),
+                "note": "FP64 round-off floor at order 10 (any 1-ulp change of the Green entries "
+                        "moves the FP64 integrand by this much); see DESIGN.md"}
+    if rank == 0 and head == "split":
+        # Green-matrix agreement of the two assemblies on a 2048-configuration sample
+        sample = d_vertices[0][:2048].contiguous()
+        so = d_orders[:2048].contiguous()
+        integrand.set_assembly("fp64")
+        g64, _, _ = integrand.assemble(sample, so)
+        integrand.set_assembly("split")
+        gsp, _, _ = integrand.assemble(sample, so)
+        torch.cuda.synchronize(dev)
+        scale = g64.abs().amax(dim=3, keepdim=True).clamp_min(1e-300)
+        line["green_split_vs_fp64_max_rel"] = float(((gsp - g64).abs() / scale).max().item())
 
     if rank == 0 and not args.no_cpu_baseline:
         host = {k: {kk: vv.cpu().numpy() for kk, vv in t.items()} for k, t in tables.items()}
-        host["twisted_down"] = host["twisted_up"] if tables["twisted_down"] is tables["twisted_up"] \
-            else host["twisted_down"]
-        host["ordinary_down"] = host["ordinary_up"] if tables["ordinary_down"] is tables["ordinary_up"] \
-            else host["ordinary_down"]
+        if tables["twisted_down"] is tables["twisted_up"]:
+            host["twisted_down"] = host["twisted_up"]
+        if tables["ordinary_down"] is tables["ordinary_up"]:
+            host["ordinary_down"] = host["ordinary_up"]
         threads = cpu_threads()
         sample = args.cpu_sample or 64 * threads
         v = host_batches[0][:sample]
         dt, cpu_values = time_cpu_integrand(params, host, v, np.full(sample, ORDER, np.int32), threads)
-        gpu_first = None
-        # the GPU values of the same configurations (batch 0 = first timed step)
+        integrand.set_assembly("fp64")
         integrand.integrand_device(d_vertices[0], d_orders, d_values, d_status, stream)
         torch.cuda.synchronize(dev)
         gpu_first = d_values.cpu().numpy()[:sample]
@@ -326,8 +367,8 @@ def run_gpu(args):
             "value": sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"first {sample} configurations of the first timed batch, {threads} threads, "
                       f"{dt:.1f} s wall (C restatement of the reference integrand)",
-            "bit_identical_to_gpu": bool(np.array_equal(cpu_values.view(np.uint64),
-                                                        gpu_first.view(np.uint64))),
+            "bit_identical_to_gpu_fp64_path": bool(np.array_equal(cpu_values.view(np.uint64),
+                                                                  gpu_first.view(np.uint64))),
         }
     if rank == 0:
         print(json.dumps(line))
@@ -348,6 +389,8 @@ def main():
     ap.add_argument("--preset", choices=["8x8-d128", "6x6-d96"], default="8x8-d128",
                     help="6x6-d96 is a smaller case for profiler captures, not a bench line")
     ap.add_argument("--batch", type=int, default=65536, help="configurations per step per GPU")
+    ap.add_argument("--path", choices=["both", "split", "fp64"], default="both",
+                    help="both: time the FP64 form and the split form, report the split form")
     args = ap.parse_args()
     global PRESET, BATCH
     PRESET, BATCH = args.preset, args.batch

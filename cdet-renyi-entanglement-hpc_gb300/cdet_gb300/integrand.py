@@ -158,14 +158,38 @@ class CdetIntegrand:
     def last_launch_count(self) -> int:
         return int(self._lib.cdet_last_launch_count(self._ctx))
 
+    def set_assembly(self, mode: str) -> None:
+        """"fp64": the reference's Clenshaw in FP64, bit-identical (default);
+        "split": batched split-bf16 tcgen05 assembly, FP64-level accuracy."""
+        code = {"fp64": L.ASSEMBLY_FP64, "split": L.ASSEMBLY_SPLIT_BF16}[mode]
+        L.check(self._lib.cdet_set_assembly(self._ctx, code))
+
+    def prepare_split(self) -> None:
+        """Slice the tables for the split assembly now (device memory)."""
+        L.check(self._lib.cdet_prepare_split(self._ctx))
+
+    def assemble(self, vertices, orders, stream=None):
+        """Green matrices of the current assembly mode for device (torch)
+        inputs: returns (green [batch][2][2][max_order^2],
+        diag [batch][2][2][max_order], status)."""
+        import torch
+        batch, nmax = int(vertices.shape[0]), int(vertices.shape[1])
+        green = torch.zeros((batch, 2, 2, nmax * nmax), dtype=torch.float64, device=vertices.device)
+        diag = torch.zeros((batch, 2, 2, nmax), dtype=torch.float64, device=vertices.device)
+        status = torch.zeros(batch, dtype=torch.int32, device=vertices.device)
+        L.check(self._lib.cdet_assemble_device(self._ctx, _ptr(vertices), _ptr(orders), batch, nmax,
+                                               _ptr(green), _ptr(diag), _ptr(status),
+                                               _stream_handle(stream)))
+        return green, diag, status
+
     def profile(self, enable: bool) -> None:
         """Record CUDA events around every kernel of later evaluations."""
         L.check(self._lib.cdet_profile_enable(self._ctx, int(bool(enable))))
 
     def profile_read(self):
-        """(per-kernel milliseconds [assembly, minors, cdet], launches) since
-        the last read; waits for the recorded events."""
-        ms = (C.c_double * 3)(0.0, 0.0, 0.0)
+        """(per-stage milliseconds [split prep, assembly, minors, cdet],
+        launches) since the last read; waits for the recorded events."""
+        ms = (C.c_double * 4)(0.0, 0.0, 0.0, 0.0)
         launches = C.c_int64(0)
         L.check(self._lib.cdet_profile_read(self._ctx, ms, C.byref(launches)))
         return list(ms), launches.value

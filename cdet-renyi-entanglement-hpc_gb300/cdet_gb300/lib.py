@@ -29,7 +29,11 @@ EXPORTED = (
     "cdet_alias_table", "cdet_reserve", "cdet_integrand_device", "cdet_all_subsets_device",
     "cdet_integrand_host", "cdet_all_subsets_host", "cdet_counters", "cdet_last_error",
     "cdet_last_launch_count", "cdet_profile_enable", "cdet_profile_read",
+    "cdet_set_assembly", "cdet_prepare_split", "cdet_assemble_device",
 )
+
+ASSEMBLY_FP64 = 0
+ASSEMBLY_SPLIT_BF16 = 1
 
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int32)
@@ -77,6 +81,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.cdet_last_error.restype = C.c_char_p
     lib.cdet_last_launch_count.argtypes = [vp]
+    lib.cdet_set_assembly.argtypes = [vp, i32]
+    lib.cdet_prepare_split.argtypes = [vp]
+    lib.cdet_assemble_device.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp, vp]
     lib.cdet_profile_enable.argtypes = [vp, i32]
     lib.cdet_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     _LIB = lib

@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -101,6 +103,14 @@ struct TableSlot {
     bool ready = false;
 };
 
+// bf16 slices of one branch of one table (split assembly)
+struct SlicedBranch {
+    void* mem = nullptr;  // slices followed by exponents
+    const uint16_t* slices = nullptr;
+    const int32_t* exponents = nullptr;
+    size_t blocks = 0;
+};
+
 }  // namespace
 
 struct cdet_context {
@@ -120,6 +130,12 @@ struct cdet_context {
     size_t staging_bytes = 0;
     uint64_t calls = 0, fallbacks = 0;
     int last_launches = 0;
+    // split assembly
+    int assembly = CDET_ASSEMBLY_FP64;
+    std::map<std::pair<const double*, size_t>, SlicedBranch> sliced;  // (coeffs, blocks) -> slices
+    void* split_scratch = nullptr;
+    size_t split_scratch_bytes = 0;
+    int32_t* split_error = nullptr;  // device flag of the last split evaluation
     // measurement hooks
     bool profiling = false;
     std::vector<cdet::KernelEvents> pending;  // recorded, not yet read
@@ -230,8 +246,77 @@ int build_problem(cdet_context* ctx, const double* vertices, const int32_t* orde
     return CDET_OK;
 }
 
+int slice_branch(cdet_context* ctx, const double* coeffs, size_t blocks, SlicedBranch** out) {
+    auto key = std::make_pair(coeffs, blocks);
+    auto it = ctx->sliced.find(key);
+    if (it != ctx->sliced.end()) {
+        *out = &it->second;
+        return CDET_OK;
+    }
+    const cdet_runtime_scalars& s = ctx->scalars;
+    const size_t sbytes = cdet::split_slices_bytes(s.cheb_nu, s.cheb_nv, blocks);
+    SlicedBranch b;
+    cudaError_t err = cudaMalloc(&b.mem, sbytes + blocks * sizeof(int32_t) + 256);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(split slices)");
+    b.slices = static_cast<const uint16_t*>(b.mem);
+    b.exponents = reinterpret_cast<const int32_t*>(static_cast<char*>(b.mem) + sbytes);
+    b.blocks = blocks;
+    err = cdet::launch_slice_table(coeffs, s.cheb_nu, s.cheb_nv, blocks, const_cast<uint16_t*>(b.slices),
+                                   const_cast<int32_t*>(b.exponents), nullptr);
+    if (err == cudaSuccess) err = cudaDeviceSynchronize();
+    if (err != cudaSuccess) {
+        cudaFree(b.mem);
+        return cuda_fail(err, "slicing the tables");
+    }
+    auto res = ctx->sliced.emplace(key, b);
+    *out = &res.first->second;
+    return CDET_OK;
+}
+
+// The segments of the split assembly: per set, one record per distinct
+// up/down table, and per record the two branches.
+int build_split_plan(cdet_context* ctx, cdet::SplitPlan* plan) {
+    const cdet_runtime_scalars& s = ctx->scalars;
+    if (s.cheb_nu > 128 || s.cheb_nv > 128)
+        return fail(CDET_ERR_INVALID, "split assembly needs CHEB_NU and CHEB_NV <= 128");
+    *plan = cdet::SplitPlan{};
+    const size_t sites2 = static_cast<size_t>(s.n1) * s.n2 * s.n1 * s.n2;
+    const int kinds[2][2] = {{CDET_TWISTED_UP, CDET_TWISTED_DOWN}, {CDET_ORDINARY_UP, CDET_ORDINARY_DOWN}};
+    uint32_t base = 0;
+    int seg = 0;
+    for (int set = 0; set < 2; ++set) {
+        const cdet::TableDev* up = resolve(ctx, kinds[set][0]);
+        const cdet::TableDev* down = resolve(ctx, kinds[set][1]);
+        if (!up || !down) return fail(CDET_ERR_STATE, "Green-function tables have not been uploaded");
+        const bool shared = up->upper == down->upper && up->lower == down->lower;
+        const cdet::TableDev* recs[2] = {up, down};
+        plan->records_per_set[set] = shared ? 1 : 2;
+        const size_t blocks = set == 0 ? 4 * sites2 : sites2;  // ordinary: replica (0,0) only
+        for (int r = 0; r < plan->records_per_set[set]; ++r) {
+            plan->spin_mask[set][r] = shared ? 3 : (1 << r);
+            for (int br = 0; br < 2; ++br) {
+                SlicedBranch* sb = nullptr;
+                const int rc = slice_branch(ctx, br == 0 ? recs[r]->upper : recs[r]->lower, blocks, &sb);
+                if (rc != CDET_OK) return rc;
+                plan->segment_base[seg] = base;
+                plan->slices[seg] = sb->slices;
+                plan->exponents[seg] = sb->exponents;
+                plan->segment_of[set][r][br] = seg;
+                base += static_cast<uint32_t>(blocks);
+                ++seg;
+            }
+        }
+    }
+    plan->segments = seg;
+    plan->segment_base[seg] = base;
+    plan->nblocks = base;
+    plan->ksteps = (s.cheb_nv + 15) / 16;
+    return CDET_OK;
+}
+
 int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
-        int max_order, int all_subsets, double* values, int32_t* status, cudaStream_t stream) {
+        int max_order, int all_subsets, double* values, int32_t* status, cudaStream_t stream,
+        bool assembly_only = false) {
     if (batch < 0) return fail(CDET_ERR_INVALID, "batch must be non-negative");
     if (batch == 0) return CDET_OK;
     if (!vertices || !values || !status || (!all_subsets && !orders))
@@ -248,7 +333,7 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
     cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);
     if (err != cudaSuccess) return cuda_fail(err, "cudaMemsetAsync(status)");
     cdet::KernelEvents* events = nullptr;
-    if (ctx->profiling) {
+    if (ctx->profiling && !assembly_only) {
         if (ctx->spare.empty()) {
             cdet::KernelEvents ev{};
             for (cudaEvent_t& e : ev.marks) {
@@ -261,10 +346,43 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         ctx->spare.pop_back();
         events = &ctx->pending.back();
     }
-    err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events);
-    if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
-    ctx->last_launches = 3;  // kernels of this library (the status reset is a memset)
-    if (ctx->profiling) ctx->pending_launches += 3;
+    int launches = 3;
+    if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16) {
+        cdet::SplitPlan plan;
+        rc = build_split_plan(ctx, &plan);
+        if (rc != CDET_OK) return rc;
+        const size_t need = cdet::split_scratch_bytes(batch, max_order, plan.nblocks);
+        if (need > ctx->split_scratch_bytes) {
+            cudaDeviceSynchronize();
+            if (ctx->split_scratch) cudaFree(ctx->split_scratch);
+            ctx->split_scratch = nullptr;
+            ctx->split_scratch_bytes = 0;
+            err = cudaMalloc(&ctx->split_scratch, need);
+            if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(split scratch)");
+            ctx->split_scratch_bytes = need;
+        }
+        if (events && events->marks[0]) cudaEventRecord(events->marks[0], stream);
+        err = cdet::launch_split_assembly(p, w, plan, ctx->split_scratch, ctx->split_scratch_bytes,
+                                          ctx->sm_count, &ctx->split_error, stream, events);
+        if (err != cudaSuccess) return cuda_fail(err, "split assembly launch");
+        if (events && events->marks[2]) cudaEventRecord(events->marks[2], stream);
+        launches = 5 + 2;  // descriptors, scan, scatter, tiles, tensor assembly + minors, CDet
+        if (!assembly_only) {
+            err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events, false);
+            if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+        } else {
+            launches = 5;
+        }
+    } else if (!assembly_only) {
+        err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events);
+        if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+    } else {
+        launches = 1;
+        err = cdet::launch_fp64_assembly_only(p, w, stream);
+        if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+    }
+    ctx->last_launches = launches;  // kernels of this library (the status reset is a memset)
+    if (events) ctx->pending_launches += launches;
     return CDET_OK;
 }
 
@@ -306,6 +424,12 @@ int run_host(cdet_context* ctx, const double* vertices, const int32_t* orders, i
     if (err == cudaSuccess) err = cudaMemcpyAsync(status, d_s, sbytes, cudaMemcpyDeviceToHost, stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
     if (err != cudaSuccess) return cuda_fail(err, "evaluation");
+    if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16 && ctx->split_error) {
+        int32_t flag = 0;
+        err = cudaMemcpy(&flag, ctx->split_error, sizeof(flag), cudaMemcpyDeviceToHost);
+        if (err != cudaSuccess) return cuda_fail(err, "reading the split assembly status");
+        if (flag) return fail(CDET_ERR_CUDA, "split assembly: a pipeline wait timed out");
+    }
     ctx->calls += static_cast<uint64_t>(batch);
     bool flagged = false;
     for (int64_t c = 0; c < batch; ++c) {
@@ -357,6 +481,8 @@ void cdet_destroy(cdet_context* ctx) {
     for (TableSlot& slot : ctx->tables) release_slot(slot);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->staging) cudaFree(ctx->staging);
+    if (ctx->split_scratch) cudaFree(ctx->split_scratch);
+    for (auto& kv : ctx->sliced) cudaFree(kv.second.mem);
     delete ctx;
 }
 
@@ -475,6 +601,44 @@ int cdet_counters(const cdet_context* ctx, uint64_t* integrand_calls, uint64_t* 
 
 int cdet_last_launch_count(const cdet_context* ctx) { return ctx ? ctx->last_launches : 0; }
 
+int cdet_set_assembly(cdet_context* ctx, int mode) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (mode != CDET_ASSEMBLY_FP64 && mode != CDET_ASSEMBLY_SPLIT_BF16)
+        return fail(CDET_ERR_INVALID, "unknown assembly mode");
+    if (mode == CDET_ASSEMBLY_SPLIT_BF16 && (ctx->scalars.cheb_nu > 128 || ctx->scalars.cheb_nv > 128))
+        return fail(CDET_ERR_INVALID, "split assembly needs CHEB_NU and CHEB_NV <= 128");
+    ctx->assembly = mode;
+    return CDET_OK;
+}
+
+int cdet_prepare_split(cdet_context* ctx) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    DeviceGuard guard(ctx->device);
+    cdet::SplitPlan plan;
+    return build_split_plan(ctx, &plan);
+}
+
+int cdet_assemble_device(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                         int64_t batch, int max_order, double* green, double* diag,
+                         int32_t* status, void* stream) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (max_order < 1 || max_order > cdet::kMaxOrder) return fail(CDET_ERR_INVALID, "order out of range");
+    if (!green || !diag) return fail(CDET_ERR_INVALID, "null buffer");
+    DeviceGuard guard(ctx->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double scratch_dummy = 0.0;
+    int rc = run(ctx, vertices, orders, batch, max_order, 0, &scratch_dummy, status, st, true);
+    if (rc != CDET_OK) return rc;
+    cdet::Scratch w;
+    cdet::carve_scratch(ctx->scratch, ctx->scratch_batch, ctx->scratch_order, ctx->ws_warps, &w);
+    const size_t gbytes = static_cast<size_t>(batch) * 4 * max_order * max_order * sizeof(double);
+    const size_t dbytes = static_cast<size_t>(batch) * 4 * max_order * sizeof(double);
+    cudaError_t err = cudaMemcpyAsync(green, w.green, gbytes, cudaMemcpyDeviceToDevice, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(diag, w.diag, dbytes, cudaMemcpyDeviceToDevice, st);
+    if (err != cudaSuccess) return cuda_fail(err, "copying the Green matrices");
+    return CDET_OK;
+}
+
 int cdet_profile_enable(cdet_context* ctx, int enable) {
     if (!ctx) return fail(CDET_ERR_INVALID, "null context");
     ctx->profiling = enable != 0;
@@ -485,9 +649,9 @@ int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches) {
     if (!ctx || !kernel_ms) return fail(CDET_ERR_INVALID, "bad argument");
     DeviceGuard guard(ctx->device);
     for (cdet::KernelEvents& ev : ctx->pending) {
-        cudaError_t err = cudaEventSynchronize(ev.marks[3]);
+        cudaError_t err = cudaEventSynchronize(ev.marks[4]);
         if (err != cudaSuccess) return cuda_fail(err, "cudaEventSynchronize");
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < 4; ++k) {
             float ms = 0.0f;
             err = cudaEventElapsedTime(&ms, ev.marks[k], ev.marks[k + 1]);
             if (err != cudaSuccess) return cuda_fail(err, "cudaEventElapsedTime");

@@ -512,6 +512,13 @@ __global__ void __launch_bounds__(128) cdet_fp64(const __grid_constant__ Problem
 
 size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).total; }
 
+cudaError_t launch_fp64_assembly_only(const Problem& p, const Scratch& w, cudaStream_t stream) {
+    if (p.batch <= 0) return cudaSuccess;
+    const int64_t entries = p.batch * 2 * static_cast<int64_t>(p.max_order) * p.max_order;
+    green_assembly_fp64<<<static_cast<unsigned>((entries + 127) / 128), 128, 0, stream>>>(p, w);
+    return cudaGetLastError();
+}
+
 size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps) {
     const size_t groups = static_cast<size_t>((batch + 31) / 32);
     const size_t n2 = static_cast<size_t>(max_order) * max_order;
@@ -545,19 +552,25 @@ void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Sc
 }
 
 cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_count,
-                                  cudaStream_t stream, const KernelEvents* events) {
+                                  cudaStream_t stream, const KernelEvents* events, bool assembly) {
     if (p.batch <= 0) return cudaSuccess;
     auto mark = [&](int k) {
         if (events && events->marks[k]) cudaEventRecord(events->marks[k], stream);
     };
-    mark(0);
+    if (assembly) {
+        mark(0);
+        mark(1);
+    }
     const int64_t entries = p.batch * 2 * static_cast<int64_t>(p.max_order) * p.max_order;
     const int threads = 128;
-    green_assembly_fp64<<<static_cast<unsigned>((entries + threads - 1) / threads), threads, 0,
-                          stream>>>(p, w);
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) return err;
-    mark(1);
+    cudaError_t err = cudaSuccess;
+    if (assembly) {
+        green_assembly_fp64<<<static_cast<unsigned>((entries + threads - 1) / threads), threads, 0,
+                              stream>>>(p, w);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        mark(2);
+    }
 
     // Minors: the per-warp workspace goes to shared memory when four warps'
     // worth fits a block, otherwise to the global workspace.
@@ -579,12 +592,12 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
         p, w, use_smem ? 1 : 0);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    mark(2);
+    mark(3);
 
     cdet_fp64<<<static_cast<unsigned>((p.batch + threads - 1) / threads), threads, 0, stream>>>(p, w);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    mark(3);
+    mark(4);
     (void)sm_count;
     return cudaSuccess;
 }

@@ -63,16 +63,43 @@ struct Problem {
     int32_t* status;
 };
 
+// Optional events bracketing the stages of one evaluation: [0] start,
+// [1] assembly prep done (descriptors and sort of the split form; equal to
+// [0] for the FP64 form), [2] assembly done, [3] minors done, [4] CDet done.
+struct KernelEvents {
+    cudaEvent_t marks[5];
+};
+
+// Split-precision assembly plan: the sliced coefficient blocks of every table
+// the two sets use, grouped in segments (one per table and branch) whose
+// blocks are numbered consecutively from segment_base.
+struct SplitPlan {
+    int segments;
+    uint32_t segment_base[9];       // ascending; [segments] = total blocks
+    const uint16_t* slices[8];      // bf16 slices of the segment's blocks
+    const int32_t* exponents[8];    // binary exponent of each block
+    int records_per_set[2];         // 1 when up and down share one table, else 2
+    int segment_of[2][2][2];        // [set][record][0 upper, 1 lower] -> segment
+    int spin_mask[2][2];            // [set][record] -> spins the record writes
+    uint32_t nblocks;
+    int ksteps;                     // ceil(nv / 16)
+};
+
+size_t split_slices_bytes(int nu, int nv, size_t blocks);
+cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
+                               int32_t* exponents, cudaStream_t stream);
+size_t split_scratch_bytes(int64_t batch, int max_order, uint32_t nblocks);
+cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const SplitPlan& plan, void* scratch,
+                                  size_t scratch_bytes, int sm_count, int32_t** error_flag_out,
+                                  cudaStream_t stream, const KernelEvents* events);
+
+cudaError_t launch_fp64_assembly_only(const Problem& p, const Scratch& scratch, cudaStream_t stream);
 size_t minors_workspace_doubles(int max_order);
 size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps);
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out);
-// Optional events recorded before the first kernel and after each kernel
-// (4 events for the 3 kernels); null entries are skipped.
-struct KernelEvents {
-    cudaEvent_t marks[4];
-};
-
+// assembly = true launches the FP64 Green-matrix assembly first; false
+// expects the Green matrices already in scratch (split-precision assembly).
 cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& scratch, int sm_count,
-                                  cudaStream_t stream, const KernelEvents* events);
+                                  cudaStream_t stream, const KernelEvents* events, bool assembly = true);
 
 }  // namespace cdet

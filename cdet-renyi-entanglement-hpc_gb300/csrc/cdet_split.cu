@@ -1,0 +1,751 @@
+// Split-precision Green-matrix assembly on the tcgen05 tensor cores (sm_103a).
+//
+// The Chebyshev sum G = sum_{a,b} C[a][b] T_a(u) T_b(v) of one lookup is
+// evaluated for all lookups of one coefficient block together:
+//
+//   W[a][l] = sum_b C[a][b] T_b(v_l)        (tensor cores, exact)
+//   G_l     = sum_a T_a(u_l) W[a][l]          (integer epilogue, exact up to
+//                                             final rounding)
+//
+// Operands are split Ozaki-style into bf16 slices of ~7 bits each:
+// C = 2^E sum_t q_t 2^{-7t} per block (E = the block's binary exponent, nine
+// slices) and T_b(v) = sum_t' q'_t' 2^{-7t'} (eight slices). Every slice is an
+// integer of magnitude at most 128, so each bf16 x bf16 product is exact and
+// the FP32 accumulation of all products of one level tau = t + t' over
+// K <= 128 stays below 2^24: the accumulators of levels 2..8 in tensor memory
+// hold exact integers; level 9 also takes the ninth coefficient slice, stored
+// pre-scaled by 2^-7, and rounds below 2^-65 of the block scale. Products of
+// levels 10 and above are dropped (weight 2^-70 each). The epilogue combines the levels in 64-bit fixed point, multiplies
+// by T_a(u) in Q62 fixed point and sums over a in 128-bit integers, so the
+// only roundings are the slice truncation (2^-57), the fixed-point scalings
+// (2^-56), the Q62 Chebyshev recurrences of the two bases (2^-63 per step)
+// and the final conversion to double: FP64-level accuracy without the FP64
+// pipe.
+//
+// Pipeline per evaluation: split_descriptors (one thread per vertex pair:
+// branch, u, v, block ids; corner entries written directly), a counting sort
+// of lookups by block (histogram, single-CTA scan, scatter), a tile list of
+// up to 64 lookups of one block, and split_assembly, a persistent kernel with
+// one CTA per SM that runs the tcgen05 GEMM of each tile. A-operand slices
+// stream from HBM with bulk asynchronous copies (cp.async.bulk) into a
+// two-stage shared-memory ring; the basis slices are generated in shared
+// memory by the CTA's threads.
+#include "cdet_device.cuh"
+#include "cdet_kernels.cuh"
+
+#include <algorithm>
+
+namespace cdet {
+
+namespace {
+
+constexpr int kSlices = 8;          // slices of the basis operand
+constexpr int kSlicesA = 9;         // slices of the coefficient operand (the ninth pre-scaled by 2^-7)
+constexpr int kLevels = 8;          // accumulator levels tau = 2..9
+constexpr int kTileN = 64;          // lookups per tile (MMA N)
+constexpr int kRows = 128;          // MMA M (Chebyshev rows a, zero padded)
+constexpr int kKStep = 16;          // MMA K (bf16)
+constexpr int kThreads = 128;       // one thread per TMEM lane / row a
+constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
+
+// bytes of one A stage: 9 slices x 128 rows x 16 k x bf16
+constexpr uint32_t kAStageBytes = kSlicesA * kRows * kKStep * 2;      // 36 KiB
+// bytes of the B operand of one K step: 8 slices x 64 lookups x 16 k x bf16
+constexpr uint32_t kBStepBytes = kSlices * kTileN * kKStep * 2;       // 16 KiB
+
+// ----------------------------------------------------------- PTX helpers --
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor, K-major, no swizzle: core matrices of
+// 8 rows x 16 bytes; lbo = byte stride between core matrices along K, sbo =
+// byte stride between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+    d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+    d |= static_cast<uint64_t>(1) << 46;
+    return d;
+}
+
+// kind::f16 instruction descriptor: bf16 x bf16 -> f32, K-major A and B.
+__host__ __device__ constexpr uint32_t mma_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+           (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes));
+}
+
+// Wait for the phase with the given parity, for at most kWaitCycles SM
+// clocks; returns false on timeout (the caller records an error and stops).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done = 0;
+    const long long start = clock64();
+    while (true) {
+        asm volatile(
+            "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity));
+        if (done) return true;
+        if (clock64() - start > kWaitCycles) return false;
+    }
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;}\n" ::"r"(tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+        smem_addr(bar)));
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(addr));
+}
+
+// ------------------------------------------------------ fixed-point helpers --
+// round(x * 2^frac) as int64 for |x| <= 1, by integer operations on the bits.
+__device__ __forceinline__ int64_t fixed_from_double(double x, int frac) {
+    const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(x));
+    const int e = static_cast<int>((bits >> 52) & 0x7FF);
+    if (e == 0) return 0;
+    const int64_t mant = static_cast<int64_t>((bits & ((uint64_t{1} << 52) - 1)) | (uint64_t{1} << 52));
+    const int shift = e - 1075 + frac;
+    int64_t v;
+    if (shift >= 0) v = mant << shift;
+    else if (shift > -60) v = (mant + (int64_t{1} << (-shift - 1))) >> (-shift);
+    else v = 0;
+    return (bits >> 63) ? -v : v;
+}
+
+// One step of the Chebyshev recurrence T_{k+1} = 2 u T_k - T_{k-1} in Q62
+// fixed point (u, T in [-1, 1] scaled by 2^62). The 128-bit product is
+// rounded to Q62; the wrap-around 64-bit arithmetic is exact because the
+// result lies in [-1, 1]. The rounding error per step is 2^-63 and grows at
+// most like k^2 (about 2^-50 at degree 128), 2^11 below the FP64 recurrence.
+__device__ __forceinline__ int64_t cheb_step_q62(int64_t ufix, int64_t t, int64_t tprev) {
+    const uint64_t lo = static_cast<uint64_t>(ufix) * static_cast<uint64_t>(t);
+    uint64_t hi = static_cast<uint64_t>(__mul64hi(ufix, t));
+    const uint64_t lo2 = lo + (uint64_t{1} << 60);
+    hi += lo2 < lo ? 1u : 0u;
+    const uint64_t twice = (hi << 3) | (lo2 >> 61);  // round(2 u t) in Q62, modulo 2^64
+    return static_cast<int64_t>(twice - static_cast<uint64_t>(tprev));
+}
+
+// bf16 bit pattern of a small integer (|q| <= 128), exact.
+__device__ __forceinline__ uint16_t bf16_of_int(int q) {
+    const float f = __int_as_float(0x4B400000 + q) - 12582912.0f;
+    return static_cast<uint16_t>(__float_as_uint(f) >> 16);
+}
+
+// Offset (in bf16 elements) of element (row, k) inside one K-major
+// no-swizzle operand of `rows` rows and 16 k: [row group][k chunk][8][8].
+__device__ __forceinline__ int core_offset(int row, int k) {
+    return (row >> 3) * 128 + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
+}
+
+// ---------------------------------------------------------- table slicing --
+// One block of nu x nv FP64 coefficients -> kSlicesA bf16 slices laid out as
+// [kstep][slice][core layout of 128 rows x 16 k], and the block exponent.
+// Slices 1..8 are integers q_t (weight 2^-7t); slice 9 is stored as
+// q_9 * 2^-7 (exact in bf16) so that its one product, with the first basis
+// slice, accumulates at level 9 with the right weight. Nine slices leave a
+// truncation of 2^-64 of the block scale per coefficient.
+__global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ coeffs, int nu, int nv,
+                                                    int ksteps, uint16_t* __restrict__ out,
+                                                    int32_t* __restrict__ exponents) {
+    const int64_t block = blockIdx.x;
+    const double* c = coeffs + block * static_cast<int64_t>(nu) * nv;
+    __shared__ double red[256];
+    double m = 0.0;
+    for (int i = threadIdx.x; i < nu * nv; i += blockDim.x) m = fmax(m, fabs(c[i]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    int e = 0;
+    if (red[0] > 0.0) frexp(red[0], &e);  // max < 2^e
+    if (threadIdx.x == 0) exponents[block] = e;
+    uint16_t* dst = out + block * static_cast<int64_t>(ksteps) * kSlicesA * kRows * kKStep;
+    const int total = kRows * ksteps * kKStep;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+        const int a = i / (ksteps * kKStep);
+        const int b = i - a * (ksteps * kKStep);
+        double r = (a < nu && b < nv) ? ldexp(c[a * nv + b], -e) : 0.0;  // |r| < 1
+        const int ks = b / kKStep, k = b - ks * kKStep;
+        uint16_t* base = dst + static_cast<int64_t>(ks) * kSlicesA * kRows * kKStep + core_offset(a, k);
+        for (int t = 0; t < kSlicesA; ++t) {
+            // exact: r * 128 has the same significand, and subtracting the
+            // nearest integer leaves the (representable) remainder
+            const double scaled = r * 128.0;
+            const double q = rint(scaled);
+            r = scaled - q;
+            base[t * kRows * kKStep] = t < kSlices ? bf16_of_int(static_cast<int>(q))
+                                                   : static_cast<uint16_t>(__float_as_uint(static_cast<float>(q) * 0.0078125f) >> 16);
+        }
+    }
+}
+
+// ------------------------------------------------------------ descriptors --
+struct SplitRecordArrays {
+    uint32_t* key;    // block id, or kNoKey
+    double* u;
+    double* v;
+    uint64_t* info;   // c | set<<32 | spinmask<<33 | i<<35 | j<<40 | n<<45
+};
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint64_t pack_info(int64_t c, int set, int spins, int i, int j, int n) {
+    return static_cast<uint64_t>(c) | (static_cast<uint64_t>(set) << 32) |
+           (static_cast<uint64_t>(spins) << 33) | (static_cast<uint64_t>(i) << 35) |
+           (static_cast<uint64_t>(j) << 40) | (static_cast<uint64_t>(n) << 45);
+}
+
+__device__ __forceinline__ int coordinate_index_s(double scaled, int extent, bool& bad) {
+    if (!(scaled > -2147483648.0 && scaled < 2147483648.0)) {
+        bad = true;
+        return 0;
+    }
+    int index = static_cast<int>(floor(scaled));
+    if (index < 0) index = 0;
+    if (index >= extent) index = extent - 1;
+    return index;
+}
+
+__device__ __forceinline__ double clamp_unit_s(double value) {
+    if (value < -1.0) return -1.0;
+    if (value > 1.0) return 1.0;
+    return value;
+}
+
+// One thread per (configuration, i, j): branch and (u, v) are shared by both
+// table sets; the corner path is evaluated here, every other lookup becomes a
+// record keyed by its coefficient block. Record slots are fixed:
+// ((c * nmax^2 + pair) * 2 + set) * 2 + spin_record.
+__global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__ Problem p,
+                                                         const __grid_constant__ Scratch w,
+                                                         const __grid_constant__ SplitPlan plan,
+                                                         SplitRecordArrays rec, uint32_t* counts) {
+    const int nmax = p.max_order;
+    const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= p.batch * per_c) return;
+    const int64_t c = idx / per_c;
+    const int pair = static_cast<int>(idx - c * per_c);
+    const int i = pair / nmax, j = pair - (pair / nmax) * nmax;
+    const int64_t slot0 = idx * 4;
+    for (int k = 0; k < 4; ++k) rec.key[slot0 + k] = kNoKey;
+    const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
+    if (n < 1 || n > nmax) {
+        if (pair == 0) atomicOr(p.status + c, kStatusBadInput);
+        return;
+    }
+    if (i >= n || j >= n) return;
+    const Scalars& s = p.s;
+    const double* vb = p.vertices + c * static_cast<int64_t>(nmax) * 4;
+    bool bad = false;
+    const double tui = __ldg(vb + 4 * i), tuj = __ldg(vb + 4 * j);
+    if (!isfinite(tui) || !isfinite(tuj)) bad = true;
+    const double taui = dmul(s.beta, tui), tauj = dmul(s.beta, tuj);
+    const int xi = coordinate_index_s(dmul(static_cast<double>(s.n1), __ldg(vb + 4 * i + 1)), s.n1, bad);
+    const int yi = coordinate_index_s(dmul(static_cast<double>(s.n2), __ldg(vb + 4 * i + 2)), s.n2, bad);
+    const int xj = coordinate_index_s(dmul(static_cast<double>(s.n1), __ldg(vb + 4 * j + 1)), s.n1, bad);
+    const int yj = coordinate_index_s(dmul(static_cast<double>(s.n2), __ldg(vb + 4 * j + 2)), s.n2, bad);
+    const int ri = coordinate_index_s(dmul(2.0, __ldg(vb + 4 * i + 3)), 2, bad);
+    const int rj = coordinate_index_s(dmul(2.0, __ldg(vb + 4 * j + 3)), 2, bad);
+    if (bad) {
+        atomicOr(p.status + c, kStatusBadInput);
+        return;
+    }
+    const bool upper = (i != j) && (tui > tuj);
+    const double t_outer = upper ? taui : tauj;
+    const double t_inner = upper ? tauj : taui;
+    const bool corner = t_outer < s.branch_eps;
+    double u = 0.0, v = 0.0;
+    if (!corner) {
+        u = clamp_unit_s(dsub(ddiv(dmul(2.0, t_outer), s.beta), 1.0));
+        v = clamp_unit_s(dsub(ddiv(dmul(2.0, t_inner), t_outer), 1.0));
+    }
+    const uint64_t site_part =
+        ((static_cast<uint64_t>(xi) * s.n2 + yi) * s.n1 + xj) * s.n2 + yj;
+    const uint64_t sites2 = static_cast<uint64_t>(s.n1) * s.n2 * s.n1 * s.n2;
+    for (int set = 0; set < 2; ++set) {
+        const uint64_t sitepair =
+            set == 0 ? (static_cast<uint64_t>(ri) * 2 + rj) * sites2 + site_part : site_part;
+        const int64_t mslot = (c * 2 + set) * 2;
+        if (corner) {
+            const TableDev& tu = p.up[set];
+            const TableDev& td = p.down[set];
+            double up = __ldg((upper ? tu.upper_corners : tu.lower_corners) + sitepair);
+            double down = p.same_spin[set] ? up
+                                           : __ldg((upper ? td.upper_corners : td.lower_corners) + sitepair);
+            if (i == j) {
+                up = dadd(up, s.diag_up_shift);
+                down = dadd(down, s.diag_down_shift);
+                w.diag[mslot * nmax + i] = up;
+                w.diag[(mslot + 1) * nmax + i] = down;
+            }
+            w.green[mslot * per_c + i * n + j] = dmul(up, s.scale);
+            w.green[(mslot + 1) * per_c + i * n + j] = dmul(down, s.scale);
+            continue;
+        }
+        for (int r = 0; r < plan.records_per_set[set]; ++r) {
+            const int seg = plan.segment_of[set][r][upper ? 0 : 1];
+            const uint32_t key = plan.segment_base[seg] + static_cast<uint32_t>(sitepair);
+            const int64_t slot = slot0 + set * 2 + r;
+            rec.key[slot] = key;
+            rec.u[slot] = u;
+            rec.v[slot] = v;
+            rec.info[slot] = pack_info(c, set, plan.spin_mask[set][r], i, j, n);
+            atomicAdd(counts + key, 1u);
+        }
+    }
+}
+
+// Exclusive scan of block counts (offsets) and of their 64-lookup tile counts
+// (tile offsets); one CTA of 1024 threads. totals[0] = lookups, totals[1] = tiles.
+__global__ void __launch_bounds__(1024) split_scan(const uint32_t* __restrict__ counts, uint32_t nblocks,
+                                                   uint32_t* __restrict__ offsets,
+                                                   uint32_t* __restrict__ tile_offsets,
+                                                   uint32_t* __restrict__ cursors,
+                                                   uint32_t* __restrict__ totals) {
+    __shared__ uint32_t s_sum[1024], s_tiles[1024];
+    const uint32_t per = (nblocks + 1023) / 1024;
+    const uint32_t begin = threadIdx.x * per;
+    const uint32_t end = min(nblocks, begin + per);
+    uint32_t sum = 0, tiles = 0;
+    for (uint32_t b = begin; b < end; ++b) {
+        sum += counts[b];
+        tiles += (counts[b] + kTileN - 1) / kTileN;
+    }
+    s_sum[threadIdx.x] = sum;
+    s_tiles[threadIdx.x] = tiles;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t a = 0, t = 0;
+        if (threadIdx.x >= static_cast<unsigned>(off)) {
+            a = s_sum[threadIdx.x - off];
+            t = s_tiles[threadIdx.x - off];
+        }
+        __syncthreads();
+        s_sum[threadIdx.x] += a;
+        s_tiles[threadIdx.x] += t;
+        __syncthreads();
+    }
+    uint32_t run = s_sum[threadIdx.x] - sum, trun = s_tiles[threadIdx.x] - tiles;
+    for (uint32_t b = begin; b < end; ++b) {
+        offsets[b] = run;
+        tile_offsets[b] = trun;
+        cursors[b] = 0;
+        run += counts[b];
+        trun += (counts[b] + kTileN - 1) / kTileN;
+    }
+    if (threadIdx.x == 1023) {
+        totals[0] = s_sum[1023];
+        totals[1] = s_tiles[1023];
+    }
+}
+
+struct SplitTile {
+    uint32_t block, start, count, pad;
+};
+
+// Scatter records into block order and emit the tile list.
+__global__ void __launch_bounds__(256) split_scatter(const SplitRecordArrays rec, int64_t nrec,
+                                                     const uint32_t* __restrict__ offsets,
+                                                     uint32_t* __restrict__ cursors,
+                                                     SplitRecordArrays sorted) {
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= nrec) return;
+    const uint32_t key = rec.key[idx];
+    if (key == kNoKey) return;
+    const uint32_t pos = offsets[key] + atomicAdd(cursors + key, 1u);
+    sorted.u[pos] = rec.u[idx];
+    sorted.v[pos] = rec.v[idx];
+    sorted.info[pos] = rec.info[idx];
+}
+
+__global__ void __launch_bounds__(256) split_tiles(const uint32_t* __restrict__ counts, uint32_t nblocks,
+                                                   const uint32_t* __restrict__ offsets,
+                                                   const uint32_t* __restrict__ tile_offsets,
+                                                   SplitTile* __restrict__ tiles) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nblocks) return;
+    const uint32_t n = counts[b];
+    uint32_t t = tile_offsets[b];
+    for (uint32_t s = 0; s < n; s += kTileN, ++t) tiles[t] = SplitTile{b, offsets[b] + s, min(kTileN * 1u, n - s), 0};
+}
+
+// ------------------------------------------------------------- assembly --
+struct SplitShared {
+    // A ring (2 x 36 KiB), reused by the epilogue for the Q62 u-basis
+    alignas(1024) uint16_t a_stage[2][kAStageBytes / 2];
+    // B operand for all K steps of the tile (up to 8 x 16 KiB), reused by the
+    // epilogue for the per-row products
+    alignas(1024) uint16_t b_all[8][kBStepBytes / 2];
+    double u[kTileN];
+    double v[kTileN];
+    uint64_t info[kTileN];
+    uint64_t full[2];
+    uint64_t empty[2];
+    uint64_t acc_done;
+    uint32_t tmem_base;
+    uint32_t error;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) split_assembly(const __grid_constant__ Problem p,
+                                                              const __grid_constant__ Scratch w,
+                                                              const __grid_constant__ SplitPlan plan,
+                                                              const SplitRecordArrays sorted,
+                                                              const SplitTile* __restrict__ tiles,
+                                                              const uint32_t* __restrict__ totals,
+                                                              int32_t* __restrict__ error_flag) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    SplitShared& sh = *reinterpret_cast<SplitShared*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int nmax = p.max_order;
+    const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
+    const Scalars& s = p.s;
+    const int ksteps = plan.ksteps;
+    const int nu = s.nu;
+
+    if (tid == 0) {
+        mbar_init(&sh.full[0], 1);
+        mbar_init(&sh.full[1], 1);
+        mbar_init(&sh.empty[0], 1);
+        mbar_init(&sh.empty[1], 1);
+        mbar_init(&sh.acc_done, 1);
+        sh.error = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+            smem_addr(&sh.tmem_base)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = sh.tmem_base;
+    const uint32_t idesc = mma_idesc(kRows, kTileN);
+    uint32_t full_use[2] = {0, 0}, empty_use[2] = {0, 0}, acc_use = 0;
+    const uint32_t ntiles = totals[1];
+
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const SplitTile tl = tiles[tile];
+        // segment of this block: table pointer and exponent
+        int seg = 0;
+        while (seg + 1 < plan.segments && tl.block >= plan.segment_base[seg + 1]) ++seg;
+        const uint32_t local = tl.block - plan.segment_base[seg];
+        const uint16_t* a_src = plan.slices[seg] + static_cast<int64_t>(local) * ksteps * (kAStageBytes / 2);
+        const int exponent = plan.exponents[seg][local];
+
+        // lookups of the tile
+        if (tid < kTileN) {
+            const bool live = tid < static_cast<int>(tl.count);
+            sh.u[tid] = live ? sorted.u[tl.start + tid] : 0.0;
+            sh.v[tid] = live ? sorted.v[tl.start + tid] : 0.0;
+            sh.info[tid] = live ? sorted.info[tl.start + tid] : ~uint64_t{0};
+        }
+        __syncthreads();
+        if (sh.error) break;  // a wait timed out: leave the remaining tiles
+        // first A stage can stream while the basis is generated (the stage was
+        // last read through the generic proxy by the previous epilogue)
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;");
+            mbar_expect_tx(&sh.full[0], kAStageBytes);
+            bulk_copy_g2s(sh.a_stage[0], a_src, kAStageBytes, &sh.full[0]);
+        }
+        // B operand: T_b(v_l) split into 8 slices, two threads per lookup
+        {
+            const int l = tid & (kTileN - 1);
+            const int half = tid >> 6;
+            const int kpad = ksteps * kKStep;
+            const int b_begin = half * (kpad / 2), b_end = b_begin + kpad / 2;
+            const int64_t vfix = fixed_from_double(sh.v[l], 62);
+            int64_t tprev = int64_t{1} << 62, tcur = vfix;  // T_0, T_1
+            for (int b = 0; b < b_end; ++b) {
+                int64_t tb;
+                if (b == 0) {
+                    tb = int64_t{1} << 62;
+                } else if (b == 1) {
+                    tb = vfix;
+                } else {
+                    tb = cheb_step_q62(vfix, tcur, tprev);
+                    tprev = tcur;
+                    tcur = tb;
+                }
+                if (b < b_begin) continue;
+                // Q62 -> Q56, rounded; padding columns b >= nv are zero
+                int64_t x = b < s.nv ? (tb + 32) >> 6 : 0;
+                const int ks = b / kKStep, k = b - ks * kKStep;
+                uint16_t* dst = sh.b_all[ks] + core_offset(l, k);
+                for (int t = 0; t < kSlices; ++t) {
+                    const int shift = 49 - 7 * t;
+                    int64_t q = shift > 0 ? (x + (int64_t{1} << (shift - 1))) >> shift : x;
+                    x -= q * (int64_t{1} << shift);
+                    dst[t * kTileN * kKStep] = bf16_of_int(static_cast<int>(q));
+                }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        __syncthreads();
+
+        // MMA issue: 36 slice pairs per K step into 8 exact levels
+        if (tid == 0) {
+            for (int ks = 0; ks < ksteps; ++ks) {
+                const int st = ks & 1;
+                if (ks + 1 < ksteps) {
+                    const int nx = (ks + 1) & 1;
+                    if (ks + 1 >= 2) {
+                        if (!mbar_wait(&sh.empty[nx], empty_use[nx] & 1)) {
+                            sh.error = 1;
+                            break;
+                        }
+                        ++empty_use[nx];
+                    }
+                    mbar_expect_tx(&sh.full[nx], kAStageBytes);
+                    bulk_copy_g2s(sh.a_stage[nx], a_src + static_cast<int64_t>(ks + 1) * (kAStageBytes / 2),
+                                  kAStageBytes, &sh.full[nx]);
+                }
+                if (!mbar_wait(&sh.full[st], full_use[st] & 1)) {
+                    sh.error = 1;
+                    break;
+                }
+                ++full_use[st];
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t a_base = smem_addr(sh.a_stage[st]);
+                const uint32_t b_base = smem_addr(sh.b_all[ks]);
+                for (int t = 1; t <= kSlices; ++t) {
+                    for (int tp = 1; t + tp <= kSlices + 1; ++tp) {
+                        const int level = t + tp - 2;
+                        const uint64_t ad = smem_desc(a_base + (t - 1) * (kRows * kKStep * 2), 128, 256);
+                        const uint64_t bd = smem_desc(b_base + (tp - 1) * (kTileN * kKStep * 2), 128, 256);
+                        mma_bf16(tmem + level * kTileN, ad, bd, idesc, (ks > 0 || t > 1) ? 1u : 0u);
+                    }
+                }
+                // ninth coefficient slice (pre-scaled) x first basis slice -> level 9
+                mma_bf16(tmem + (kLevels - 1) * kTileN,
+                         smem_desc(a_base + kSlices * (kRows * kKStep * 2), 128, 256),
+                         smem_desc(b_base, 128, 256), idesc, 1u);
+                mma_commit(&sh.empty[st]);
+            }
+            mma_commit(&sh.acc_done);
+        }
+        // everyone waits for the accumulators
+        if (!mbar_wait(&sh.acc_done, acc_use & 1)) sh.error = 1;
+        ++acc_use;
+        if (tid == 0) {
+            // balance the empty barriers: ksteps commits went to empty[ks & 1];
+            // the in-loop waits consumed those of steps 0..ksteps-3
+            for (int ks = (ksteps > 2 ? ksteps - 2 : 0); ks < ksteps; ++ks) {
+                const int st = ks & 1;
+                if (!mbar_wait(&sh.empty[st], empty_use[st] & 1)) sh.error = 1;
+                ++empty_use[st];
+            }
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+
+        // u basis in Q62 fixed point, [l][a ^ (l & 31)], in the A ring
+        int64_t* ubasis = reinterpret_cast<int64_t*>(sh.a_stage[0]);
+        if (tid < kTileN) {
+            const int l = tid;
+            const int64_t ufix = fixed_from_double(sh.u[l], 62);
+            int64_t tprev = int64_t{1} << 62, tcur = ufix;
+            for (int a = 0; a < kRows; ++a) {
+                int64_t ta;
+                if (a == 0) {
+                    ta = int64_t{1} << 62;
+                } else if (a == 1) {
+                    ta = ufix;
+                } else {
+                    ta = cheb_step_q62(ufix, tcur, tprev);
+                    tprev = tcur;
+                    tcur = ta;
+                }
+                ubasis[l * kRows + (a ^ (l & 31))] = a < nu ? ta : 0;
+            }
+        }
+        __syncthreads();
+
+        // epilogue: row a = tid; combine levels, multiply by T_a(u_l), store
+        int64_t* prod = reinterpret_cast<int64_t*>(sh.b_all[0]);
+        const int a = tid;
+        const uint32_t lane_base = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+        for (int l0 = 0; l0 < kTileN; l0 += 16) {
+            uint32_t acc[kLevels][16];
+#pragma unroll
+            for (int lev = 0; lev < kLevels; ++lev) tmem_ld16(lane_base + lev * kTileN + l0, acc[lev]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int l = l0 + j;
+                int64_t p[kLevels];
+#pragma unroll
+                for (int lev = 0; lev < kLevels; ++lev) p[lev] = __float2int_rn(__uint_as_float(acc[lev][j]));
+                // W * 2^55 = sum_tau P_tau 2^(55 - 7 tau), tau = 2..9
+                int64_t wfix = p[0] * (int64_t{1} << 41) + p[1] * (int64_t{1} << 34) +
+                               p[2] * (int64_t{1} << 27) + p[3] * (int64_t{1} << 20) +
+                               p[4] * (int64_t{1} << 13) + p[5] * 64 + ((p[6] * 128 + p[7] + 128) >> 8);
+                const int64_t tf = ubasis[l * kRows + (a ^ (l & 31))];
+                // (wfix * tf) >> 62, rounded
+                const uint64_t lo = static_cast<uint64_t>(wfix) * static_cast<uint64_t>(tf);
+                int64_t hi = __mul64hi(wfix, tf);
+                const uint64_t lo2 = lo + (uint64_t{1} << 61);
+                hi += lo2 < lo ? 1 : 0;
+                const int64_t term = static_cast<int64_t>((static_cast<uint64_t>(hi) << 2) | (lo2 >> 62));
+                prod[l * kRows + (a ^ (l & 31))] = term;
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+
+        // column sums in 128-bit integers and the write-back
+        if (tid < kTileN && tid < static_cast<int>(tl.count)) {
+            const int l = tid;
+            uint64_t lo = 0;
+            int64_t hi = 0;
+            for (int r = 0; r < kRows; ++r) {
+                const int64_t t = prod[l * kRows + (r ^ (l & 31))];
+                const uint64_t nlo = lo + static_cast<uint64_t>(t);
+                hi += (t < 0 ? -1 : 0) + (nlo < lo ? 1 : 0);
+                lo = nlo;
+            }
+            double value;
+            const int64_t lo_signed = static_cast<int64_t>(lo);
+            if ((hi == 0 && lo_signed >= 0) || (hi == -1 && lo_signed < 0)) {
+                value = static_cast<double>(lo_signed);
+            } else {
+                value = static_cast<double>(hi) * 18446744073709551616.0 + static_cast<double>(lo);
+            }
+            value = ldexp(value, exponent - 55);
+            const uint64_t info = sh.info[l];
+            const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
+            const int set = static_cast<int>((info >> 32) & 1);
+            const int spins = static_cast<int>((info >> 33) & 3);
+            const int i = static_cast<int>((info >> 35) & 31);
+            const int j = static_cast<int>((info >> 40) & 31);
+            const int n = static_cast<int>((info >> 45) & 31);
+            const int64_t mslot = (c * 2 + set) * 2;
+            for (int spin = 0; spin < 2; ++spin) {
+                if (!(spins & (1 << spin))) continue;
+                double g = value;
+                if (i == j) {
+                    g = dadd(g, spin == 0 ? s.diag_up_shift : s.diag_down_shift);
+                    w.diag[(mslot + spin) * nmax + i] = g;
+                }
+                w.green[(mslot + spin) * per_c + i * n + j] = dmul(g, s.scale);
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && sh.error) atomicExch(error_flag, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+}
+
+}  // namespace
+
+size_t split_slices_bytes(int nu, int nv, size_t blocks) {
+    const int ksteps = (nv + kKStep - 1) / kKStep;
+    return blocks * static_cast<size_t>(ksteps) * kAStageBytes;
+}
+
+cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
+                               int32_t* exponents, cudaStream_t stream) {
+    if (blocks == 0) return cudaSuccess;
+    const int ksteps = (nv + kKStep - 1) / kKStep;
+    slice_blocks<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(coeffs, nu, nv, ksteps, slices, exponents);
+    return cudaGetLastError();
+}
+
+size_t split_scratch_bytes(int64_t batch, int max_order, uint32_t nblocks) {
+    const size_t nrec = static_cast<size_t>(batch) * max_order * max_order * 4;
+    size_t total = 0;
+    total += nrec * (4 + 8 + 8 + 8);          // unsorted records
+    total += nrec * (8 + 8 + 8);              // sorted records
+    total += static_cast<size_t>(nblocks) * 4 * 4;  // counts, offsets, tile offsets, cursors
+    total += (nrec / kTileN + nblocks + 1) * sizeof(SplitTile);  // tiles
+    total += 64;                              // totals, error flag
+    return total + 16 * 256;
+}
+
+cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const SplitPlan& plan, void* scratch,
+                                  size_t scratch_bytes, int sm_count, int32_t** error_flag_out,
+                                  cudaStream_t stream, const KernelEvents* events) {
+    const int64_t pairs = p.batch * static_cast<int64_t>(p.max_order) * p.max_order;
+    const int64_t nrec = pairs * 4;
+    char* cursor = static_cast<char*>(scratch);
+    auto take = [&](size_t bytes) {
+        void* ptr = cursor;
+        cursor += (bytes + 255) & ~static_cast<size_t>(255);
+        return ptr;
+    };
+    SplitRecordArrays rec{static_cast<uint32_t*>(take(nrec * 4)), static_cast<double*>(take(nrec * 8)),
+                          static_cast<double*>(take(nrec * 8)), static_cast<uint64_t*>(take(nrec * 8))};
+    SplitRecordArrays sorted{nullptr, static_cast<double*>(take(nrec * 8)), static_cast<double*>(take(nrec * 8)),
+                             static_cast<uint64_t*>(take(nrec * 8))};
+    uint32_t* counts = static_cast<uint32_t*>(take(plan.nblocks * 4u));
+    uint32_t* offsets = static_cast<uint32_t*>(take(plan.nblocks * 4u));
+    uint32_t* tile_offsets = static_cast<uint32_t*>(take(plan.nblocks * 4u));
+    uint32_t* cursors = static_cast<uint32_t*>(take(plan.nblocks * 4u));
+    SplitTile* tiles = static_cast<SplitTile*>(take((nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile)));
+    uint32_t* totals = static_cast<uint32_t*>(take(16));
+    int32_t* error_flag = static_cast<int32_t*>(take(16));
+    if (static_cast<size_t>(cursor - static_cast<char*>(scratch)) > scratch_bytes) return cudaErrorInvalidValue;
+    if (error_flag_out) *error_flag_out = error_flag;
+
+    cudaError_t err = cudaMemsetAsync(counts, 0, plan.nblocks * 4u, stream);
+    if (err != cudaSuccess) return err;
+    err = cudaMemsetAsync(error_flag, 0, 4, stream);
+    if (err != cudaSuccess) return err;
+    split_descriptors<<<static_cast<unsigned>((pairs + 127) / 128), 128, 0, stream>>>(p, w, plan, rec, counts);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    split_scan<<<1, 1024, 0, stream>>>(counts, plan.nblocks, offsets, tile_offsets, cursors, totals);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    split_scatter<<<static_cast<unsigned>((nrec + 255) / 256), 256, 0, stream>>>(rec, nrec, offsets, cursors,
+                                                                                 sorted);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    split_tiles<<<(plan.nblocks + 255) / 256, 256, 0, stream>>>(counts, plan.nblocks, offsets, tile_offsets,
+                                                                tiles);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if (events && events->marks[1]) cudaEventRecord(events->marks[1], stream);
+    const size_t smem = sizeof(SplitShared);
+    err = cudaFuncSetAttribute(split_assembly, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (err != cudaSuccess) return err;
+    split_assembly<<<sm_count, kThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, error_flag);
+    return cudaGetLastError();
+}
+
+}  // namespace cdet

@@ -147,11 +147,45 @@ const char* cdet_last_error(void);
 /* Kernel launches the last evaluation issued (for launch accounting). */
 int cdet_last_launch_count(const cdet_context* ctx);
 
+/* Green-matrix assembly modes (cdet_set_assembly). */
+enum cdet_assembly_mode {
+    /* The reference's Clenshaw recurrences in FP64 on the CUDA cores: every
+     * value bit-identical to the reference integrand (the drop-in default). */
+    CDET_ASSEMBLY_FP64 = 0,
+    /* Batched split-precision assembly on the tcgen05 tensor cores: lookups
+     * grouped by coefficient block, each block's Chebyshev contraction as
+     * eight-slice bf16 products with exact FP32 accumulation and an integer
+     * epilogue (FP64-level accuracy, not bit-identical). Minors and the CDet
+     * recursion stay FP64. Needs CHEB_NU and CHEB_NV <= 128. */
+    CDET_ASSEMBLY_SPLIT_BF16 = 1
+};
+
+/* Selects the assembly of later evaluations. Replaces the VECTOR_REAL /
+ * INTEGRAND_REAL precision switch (cdet_integrand_evaluator.h:431-465) with
+ * the two GB300 assembly forms above. */
+int cdet_set_assembly(cdet_context* ctx, int mode);
+
+/* Builds the bf16 slices of every uploaded table for the split assembly
+ * (otherwise done by the first split evaluation). Allocates about twice the
+ * FP64 table size of device memory. */
+int cdet_prepare_split(cdet_context* ctx);
+
+/* Runs only the Green-matrix assembly of the current mode, for testing:
+ * green[c][set][spin][i*n+j] and diag[c][set][spin][i] (set 0 twisted,
+ * 1 ordinary; spin 0 up, 1 down; n = orders[c]) receive the matrices the
+ * integrand's fill step builds (integrand_replica_randomly_sampled.h:434-484),
+ * including the diagonal shifts and the scale. Device buffers, asynchronous. */
+int cdet_assemble_device(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                         int64_t batch, int max_order, double* green, double* diag,
+                         int32_t* status, void* stream);
+
 /* Measurement hooks; no counterpart in the reference. While enabled, every
- * evaluation records CUDA events around each of its kernels on the stream it
- * runs on. cdet_profile_read waits for the recorded events, adds the elapsed
- * milliseconds per kernel (assembly, minors, CDet) to kernel_ms[0..2] and the
- * number of kernel launches to *launches, and clears the record. */
+ * evaluation records CUDA events between its stages on the stream it runs
+ * on. cdet_profile_read waits for the recorded events, adds the elapsed
+ * milliseconds per stage to kernel_ms[0..3] (0: descriptors and sort of the
+ * split assembly, 1: Green-matrix assembly, 2: principal minors, 3: CDet and
+ * prefactors), adds the number of kernel launches to *launches, and clears
+ * the record. */
 int cdet_profile_enable(cdet_context* ctx, int enable);
 int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches);
 

@@ -1,0 +1,121 @@
+"""The split-precision (tcgen05, bf16-slice) Green-matrix assembly.
+
+Its Green matrices must agree with the FP64 Clenshaw assembly to
+|G_split - G_fp64| <= 2e-15 * max|G| per matrix set: both are FP64-level
+evaluations of the same Chebyshev series. (Against an exact evaluation of the
+series the split form's error is below 6e-17 of the block scale at degrees 16
+and 64, no larger than the Clenshaw sum's.)
+
+Integrand values are compared only where that is meaningful. Any ulp-level
+change of the Green entries re-rolls the round-off of the FP64 minors and
+CDet recursion; on the 8x8 lattice a 1e-15 relative perturbation moves the
+FP64 integrand by a median 2e-13 at order 2, 3e-10 at order 4 and 3e-7 at
+order 6, whatever the perturbation's size. So order 1 (a product of two
+diagonal entries) is held to 1e-13, the rest to those noise levels.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from cdet_gb300.integrand import CdetIntegrand  # noqa: E402
+from cdet_gb300.params import CdetParams, named_mask  # noqa: E402
+from cdet_gb300.synthetic import uniform_configurations  # noqa: E402
+from cdet_gb300.tables import build_tables  # noqa: E402
+from helpers import bits_equal, load_case  # noqa: E402
+
+GREEN_TOL = 2e-15
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    yield
+
+
+def _green_both(params, tables, v, orders):
+    gpu = CdetIntegrand(params, tables)
+    dv = torch.from_numpy(np.ascontiguousarray(v)).cuda()
+    do = torch.from_numpy(np.ascontiguousarray(orders, dtype=np.int32)).cuda()
+    g64, d64, s64 = gpu.assemble(dv, do)
+    gpu.set_assembly("split")
+    gsp, dsp, ssp = gpu.assemble(dv, do)
+    torch.cuda.synchronize()
+    assert int(s64.max()) == 0 and int(ssp.max()) == 0
+    return gpu, g64.cpu().numpy(), d64.cpu().numpy(), gsp.cpu().numpy(), dsp.cpu().numpy()
+
+
+def _check_green(g64, gsp, orders, nmax):
+    for c, n in enumerate(orders):
+        for set_ in range(2):
+            for spin in range(2):
+                a = g64[c, set_, spin, : n * n]
+                b = gsp[c, set_, spin, : n * n]
+                scale = max(np.max(np.abs(a)), 1e-300)
+                assert np.max(np.abs(a - b)) <= GREEN_TOL * scale, (c, set_, spin)
+
+
+@pytest.mark.parametrize("d", [16, 64, 128])
+def test_split_green_matches_fp64(d):
+    params = CdetParams(n1=4, n2=4, beta="6", mu="0", u="2",
+                        mask_sites=named_mask("origin_square", 4, 4, 1), cheb_nu=d, cheb_nv=d)
+    tables = build_tables(params, device="cuda")
+    v = uniform_configurations(300 + d, 256, 8)
+    orders = np.full(256, 8, dtype=np.int32)
+    _, g64, d64, gsp, dsp = _green_both(params, tables, v, orders)
+    _check_green(g64, gsp, orders, 8)
+    scale = np.max(np.abs(d64))
+    assert np.max(np.abs(d64 - dsp)) <= GREEN_TOL * scale
+
+
+def test_split_unaliased_padded_and_corners():
+    """Four distinct tables (alpha_up != alpha_down: two records per set),
+    degree 18 (K and M padding), and vertices at tau = 0 (corner path)."""
+    params, tables, data = load_case("physical_2x2")
+    v = data["single.vertices"]
+    orders = data["single.orders"]
+    gpu, g64, d64, gsp, dsp = _green_both(params, tables, v, orders)
+    _check_green(g64, gsp, orders, 8)
+    # order 1 is a function of the diagonal only: 1e-13; order 2: the FP64
+    # noise level of the minors and CDet recursion
+    gpu.set_assembly("split")
+    split_vals, st = gpu.integrand_batch(v, orders)
+    ref = data["single.values"]
+    # twisted - 2 * ordinary cancels, so order 1 uses the reference audit's
+    # form: |a - b| <= tol * max(1, |a|, |b|) (tests/audit_test_utils.h:17-28)
+    close = np.abs(split_vals - ref) / np.maximum(1.0, np.maximum(np.abs(split_vals), np.abs(ref)))
+    assert np.max(close[orders == 1]) <= 1e-13
+    rel = np.abs(split_vals - ref) / np.maximum(np.abs(ref), 1e-300)
+    assert np.median(rel[orders == 2]) <= 1e-11
+
+
+def test_split_deterministic_and_full_path():
+    params = CdetParams(n1=3, n2=3, beta="4", mu="0", u="2",
+                        mask_sites=named_mask("first_column", 3, 3), cheb_nu=64, cheb_nv=64)
+    tables = build_tables(params, device="cuda")
+    gpu = CdetIntegrand(params, tables)
+    gpu.set_assembly("split")
+    gpu.prepare_split()
+    v = uniform_configurations(77, 8192, 4)
+    orders = np.full(8192, 4, dtype=np.int32)
+    a, st = gpu.integrand_batch(v, orders)
+    b, _ = gpu.integrand_batch(v, orders)
+    assert st.max() == 0 and bits_equal(a, b)
+    gpu.set_assembly("fp64")
+    ref, _ = gpu.integrand_batch(v, orders)
+    rel = np.abs(a - ref) / np.maximum(np.abs(ref), 1e-300)
+    assert np.median(rel) <= 1e-9  # order 4: the FP64 noise level
+    # all-subsets through the split assembly
+    gpu.set_assembly("split")
+    env = uniform_configurations(78, 64, 6)
+    sa, _ = gpu.all_subsets_batch(env)
+    gpu.set_assembly("fp64")
+    fa, _ = gpu.all_subsets_batch(env)
+    singles = [1 << i for i in range(6)]
+    a_, b_ = sa[:, singles], fa[:, singles]
+    close = np.abs(a_ - b_) / np.maximum(1.0, np.maximum(np.abs(a_), np.abs(b_)))
+    assert np.max(close) <= 1e-13
