@@ -144,6 +144,15 @@ class CdetIntegrand:
                                                 max_order, _ptr(values), _ptr(status),
                                                 _stream_handle(stream)))
 
+    def integrand_device_noalloc(self, vertices, orders, values, status, stream=None) -> int:
+        """cdet_integrand_device_noalloc: the FP64 form on the library's fixed
+        static scratch, allocating no device memory. Returns the C-ABI code
+        (0 on success); the message of a failure is in lib.last_error()."""
+        batch, max_order = int(vertices.shape[0]), int(vertices.shape[1])
+        return int(self._lib.cdet_integrand_device_noalloc(self._ctx, _ptr(vertices), _ptr(orders), batch,
+                                                           max_order, _ptr(values), _ptr(status),
+                                                           _stream_handle(stream)))
+
     def all_subsets_device(self, vertices, values, status, stream=None) -> None:
         batch, env = int(vertices.shape[0]), int(vertices.shape[1])
         L.check(self._lib.cdet_all_subsets_device(self._ctx, _ptr(vertices), env, batch,

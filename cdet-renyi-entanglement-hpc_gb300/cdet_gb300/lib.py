@@ -30,6 +30,7 @@ EXPORTED = (
     "cdet_integrand_host", "cdet_all_subsets_host", "cdet_counters", "cdet_last_error",
     "cdet_last_launch_count", "cdet_profile_enable", "cdet_profile_read",
     "cdet_set_assembly", "cdet_prepare_split", "cdet_assemble_device",
+    "cdet_integrand_device_noalloc",
 )
 
 ASSEMBLY_FP64 = 0
@@ -81,6 +82,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.cdet_last_error.restype = C.c_char_p
     lib.cdet_last_launch_count.argtypes = [vp]
+    lib.cdet_integrand_device_noalloc.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp]
     lib.cdet_set_assembly.argtypes = [vp, i32]
     lib.cdet_prepare_split.argtypes = [vp]
     lib.cdet_assemble_device.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp, vp]

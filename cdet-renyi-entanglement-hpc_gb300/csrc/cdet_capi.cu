@@ -442,6 +442,33 @@ int run_host(cdet_context* ctx, const double* vertices, const int32_t* orders, i
 
 }  // namespace
 
+namespace cdet {
+
+// Runs the FP64 form on scratch memory the caller provides (at least
+// scratch_bytes(batch, max_order, ws_warps) bytes), allocating nothing and
+// recording no profiling events. Used by the no-allocation entry point.
+int run_fp64_on_scratch(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
+                        int max_order, double* values, int32_t* status, void* scratch, size_t ws_warps,
+                        cudaStream_t stream) {
+    Problem p;
+    int rc = build_problem(ctx, vertices, orders, batch, max_order, 0, values, status, &p);
+    if (rc != CDET_OK) return rc;
+    Scratch w;
+    carve_scratch(scratch, batch, max_order, ws_warps, &w);
+    cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMemsetAsync(status)");
+    err = launch_fp64_integrand(p, w, ctx->sm_count, stream, nullptr);
+    if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+    ctx->last_launches = 3;
+    return CDET_OK;
+}
+
+int fail_with(int code, const char* message) { return fail(code, message); }
+int context_device(const cdet_context* ctx) { return ctx->device; }
+int context_sm_count(const cdet_context* ctx) { return ctx->sm_count; }
+
+}  // namespace cdet
+
 extern "C" {
 
 const char* cdet_last_error(void) { return g_last_error.c_str(); }

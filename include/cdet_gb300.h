@@ -128,6 +128,23 @@ int cdet_integrand_device(cdet_context* ctx, const double* vertices, const int32
 int cdet_all_subsets_device(cdet_context* ctx, const double* vertices, int envelope_order,
                             int64_t batch, double* values, int32_t* status, void* stream);
 
+/* No counterpart in the reference. The single-order FP64 integrand of
+ * cdet_integrand_device, for callers that cannot let the library allocate
+ * device memory: a driver that captures its step into a CUDA graph (no
+ * allocation is allowed during stream capture), or a process that has given
+ * HBM to its tables or to its own pool. Its scratch is a fixed 64 MiB array
+ * of device memory held by every GPU that loads the library; batches that
+ * need more (about 1,200 configurations of order 10, or more at lower order)
+ * are rejected with CDET_ERR_INVALID and a message. Tables must already be
+ * on the device (cdet_bind_device_table allocates nothing). The first call
+ * on a device looks up the array's device address, so it should come before
+ * any stream capture. All calls share the array: calls that overlap on the
+ * GPU race, so keep them on one stream or order them. Always the FP64
+ * assembly (the split assembly needs allocations). */
+int cdet_integrand_device_noalloc(cdet_context* ctx, const double* vertices, const int32_t* orders,
+                                  int64_t batch, int max_order, double* values, int32_t* status,
+                                  void* stream);
+
 /* Host-buffer forms of the two calls above: copy the inputs in, evaluate,
  * copy the results out, and return when they are in host memory. Pinned
  * host buffers make the copies asynchronous DMA. Returns CDET_ERR_VALUE when

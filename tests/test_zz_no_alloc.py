@@ -1,0 +1,71 @@
+"""cdet_integrand_device_noalloc: the FP64 integrand on fixed static scratch.
+
+For callers that must not let the library allocate device memory (a driver
+capturing its step into a CUDA graph, or a process that has handed HBM to its
+tables or to its own pool). Through the C ABI, two calls in a row must equal
+the ordinary entry point bit for bit (the FP64 form's tolerance in every other
+test). The first call on a device is the set-up call: it looks up the
+array's device address, which loads the library's module holding the array
+(the 64 MiB then stays with the GPU until exit). The two calls after it must
+leave the device's free memory unchanged. A batch too large for the fixed
+scratch must be refused with a message. This file sorts last so that a
+run stopping at the first failure has already run every other test.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from cdet_gb300 import lib as L  # noqa: E402
+from cdet_gb300.integrand import CdetIntegrand  # noqa: E402
+from cdet_gb300.params import CdetParams, named_mask  # noqa: E402
+from cdet_gb300.synthetic import truncated_geometric_orders, uniform_configurations  # noqa: E402
+from cdet_gb300.tables import build_tables  # noqa: E402
+
+
+def test_noalloc_matches_device_entry_twice():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    params = CdetParams(n1=4, n2=4, beta="6", mu="0", u="2",
+                        mask_sites=named_mask("origin_square", 4, 4, 1), cheb_nu=32, cheb_nv=32)
+    tables = build_tables(params, device="cuda")  # device tables: bound, not copied
+    gpu = CdetIntegrand(params, tables)
+    batch, nmax = 512, 8
+    v = torch.from_numpy(uniform_configurations(4242, batch, nmax)).cuda()
+    o = torch.from_numpy(truncated_geometric_orders(4243, batch, 0.3, nmax)).cuda()
+    ref_values = torch.empty(batch, dtype=torch.float64, device="cuda")
+    ref_status = torch.empty(batch, dtype=torch.int32, device="cuda")
+    gpu.integrand_device(v, o, ref_values, ref_status)
+    values = [torch.full((batch,), float("nan"), dtype=torch.float64, device="cuda") for _ in range(3)]
+    status = [torch.full((batch,), -1, dtype=torch.int32, device="cuda") for _ in range(3)]
+    # set-up call (first on this device)
+    assert gpu.integrand_device_noalloc(v, o, values[0], status[0]) == L.CDET_OK, L.last_error()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for k in (1, 2):
+        rc = gpu.integrand_device_noalloc(v, o, values[k], status[k])
+        assert rc == L.CDET_OK, L.last_error()
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before  # the calls allocate nothing on the device
+    want = ref_values.cpu().numpy().view(np.uint64)
+    for k in range(3):
+        assert np.array_equal(values[k].cpu().numpy().view(np.uint64), want)
+        assert np.array_equal(status[k].cpu().numpy(), ref_status.cpu().numpy())
+
+
+def test_noalloc_rejects_oversized_batch():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    params = CdetParams(n1=3, n2=3, beta="4", mu="0", u="2",
+                        mask_sites=named_mask("first_column", 3, 3), cheb_nu=8, cheb_nv=8)
+    gpu = CdetIntegrand(params, build_tables(params, device="cuda"))
+    batch, nmax = 65536, 10
+    v = torch.zeros((batch, nmax, 4), dtype=torch.float64, device="cuda")
+    o = torch.full((batch,), nmax, dtype=torch.int32, device="cuda")
+    out = torch.empty(batch, dtype=torch.float64, device="cuda")
+    st = torch.empty(batch, dtype=torch.int32, device="cuda")
+    rc = gpu.integrand_device_noalloc(v, o, out, st)
+    assert rc == L.CDET_ERR_INVALID
+    assert "split the batch" in L.last_error()
