@@ -28,8 +28,9 @@
 // up to 64 lookups of one block, and split_assembly, a persistent kernel with
 // one CTA per SM that runs the tcgen05 GEMM of each tile. A-operand slices
 // stream from HBM with bulk asynchronous copies (cp.async.bulk) into a
-// two-stage shared-memory ring; the basis slices are generated in shared
-// memory by the CTA's threads.
+// three-stage shared-memory ring; the basis slices are generated in shared
+// memory by four producer warps while a single thread issues the MMAs and
+// four epilogue warps drain the previous tile.
 #include "cdet_device.cuh"
 #include "cdet_kernels.cuh"
 
@@ -45,7 +46,6 @@ constexpr int kLevels = 8;          // accumulator levels tau = 2..9
 constexpr int kTileN = 64;          // lookups per tile (MMA N)
 constexpr int kRows = 128;          // MMA M (Chebyshev rows a, zero padded)
 constexpr int kKStep = 16;          // MMA K (bf16)
-constexpr int kThreads = 128;       // one thread per TMEM lane / row a
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
 
 // bytes of one A stage: 9 slices x 128 rows x 16 k x bf16
@@ -119,15 +119,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
         smem_addr(bar)));
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15])
-        : "r"(addr));
 }
 
 // ------------------------------------------------------ fixed-point helpers --
@@ -406,49 +397,149 @@ __global__ void __launch_bounds__(256) split_tiles(const uint32_t* __restrict__ 
 }
 
 // ------------------------------------------------------------- assembly --
-struct SplitShared {
-    // A ring (2 x 36 KiB), reused by the epilogue for the Q62 u-basis
-    alignas(1024) uint16_t a_stage[2][kAStageBytes / 2];
-    // B operand for all K steps of the tile (up to 8 x 16 KiB), reused by the
-    // epilogue for the per-row products
-    alignas(1024) uint16_t b_all[8][kBStepBytes / 2];
+// Warp-specialised persistent kernel, one CTA of 10 warps per SM:
+//   warps 0-3  basis producers: the eight bf16 slices of T_b(v) for each
+//              K step of a tile, into a two-stage ring (16-byte stores of
+//              whole core-matrix rows, conflict-free);
+//   warps 4-7  epilogue: the Q62 u-basis of the tile (while the MMAs run),
+//              then the TMEM levels row by row (warp w reads lanes
+//              32(w-4)..), combined in fixed point and summed over rows
+//              through a shared-memory stage, and the Green entries written;
+//   warp 8     one thread streams the coefficient slices of every K step
+//              into a three-stage ring with cp.async.bulk;
+//   warp 9     one thread issues the 37 tcgen05.mma of each K step and
+//              owns the 512 TMEM columns (eight levels x 64 lookups).
+// The accumulators are single-buffered: the MMAs of a tile start when the
+// epilogue has released the previous tile's TMEM.
+constexpr int kAStages = 3;
+constexpr int kBStages = 2;
+constexpr int kMetaBufs = 3;
+constexpr int kProducerWarps = 4;
+constexpr int kEpilogueWarps = 4;
+constexpr int kWarpCopy = 8;
+constexpr int kWarpMma = 9;
+constexpr int kAssemblyThreads = 320;
+constexpr int kRedChunk = 8;  // lookups per epilogue reduction chunk
+constexpr uint32_t kEpiBarrier = 1;  // named barrier of the epilogue warps
+
+struct TileMeta {
     double u[kTileN];
-    double v[kTileN];
     uint64_t info[kTileN];
-    uint64_t full[2];
-    uint64_t empty[2];
-    uint64_t acc_done;
+    uint32_t count;
+    int32_t exponent;
+    uint32_t pad[2];
+};
+
+struct SplitShared {
+    alignas(1024) uint16_t a_ring[kAStages][kAStageBytes / 2];  // 3 x 36 KiB
+    alignas(1024) uint16_t b_ring[kBStages][kBStepBytes / 2];   // 2 x 16 KiB
+    alignas(16) int64_t ubasis[kTileN * kRows];                 // 64 KiB, [l][a ^ (l & 31)]
+    alignas(16) int64_t red[kRedChunk * kRows];                 // 8 KiB, [j][row]
+    TileMeta meta[kMetaBufs];
+    uint64_t a_full[kAStages], a_empty[kAStages];
+    uint64_t b_full[kBStages], b_empty[kBStages];
+    uint64_t meta_full[kMetaBufs], meta_empty[kMetaBufs];
+    uint64_t acc_full, acc_empty;
+    uint64_t drain;  // last commit of the MMA thread, waited on before dealloc
     uint32_t tmem_base;
     uint32_t error;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) split_assembly(const __grid_constant__ Problem p,
-                                                              const __grid_constant__ Scratch w,
-                                                              const __grid_constant__ SplitPlan plan,
-                                                              const SplitRecordArrays sorted,
-                                                              const SplitTile* __restrict__ tiles,
-                                                              const uint32_t* __restrict__ totals,
-                                                              int32_t* __restrict__ error_flag) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void epilogue_sync() {
+    asm volatile("bar.sync %0, %1;" ::"n"(kEpiBarrier), "n"(kEpilogueWarps * 32) : "memory");
+}
+
+// Barrier of the epilogue warps that also ORs a predicate over them: every
+// epilogue thread gets the same answer, so they leave the tile loop together
+// and none is left waiting at a named barrier.
+__device__ __forceinline__ bool epilogue_any(bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{.reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.or.pred q, %2, %3, p; selp.u32 %0, 1, 0, q;}"
+        : "=r"(r)
+        : "r"(static_cast<uint32_t>(pred)), "n"(kEpiBarrier), "n"(kEpilogueWarps * 32)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ bool failed(const SplitShared& sh) {
+    return *static_cast<const volatile uint32_t*>(&sh.error) != 0;
+}
+
+__device__ __forceinline__ void tile_source(const SplitPlan& plan, uint32_t block, int ksteps,
+                                            const uint16_t** a_src, int* exponent) {
+    int seg = 0;
+    while (seg + 1 < plan.segments && block >= plan.segment_base[seg + 1]) ++seg;
+    const uint32_t local = block - plan.segment_base[seg];
+    *a_src = plan.slices[seg] + static_cast<int64_t>(local) * ksteps * (kAStageBytes / 2);
+    *exponent = plan.exponents[seg][local];
+}
+
+// Next value of a Q62 Chebyshev sequence: T_0 = 1, T_1 = x, then the recurrence.
+struct ChebQ62 {
+    int64_t x, prev, cur;
+    int next_index;
+    __device__ __forceinline__ void init(int64_t xfix) {
+        x = xfix;
+        prev = int64_t{1} << 62;
+        cur = xfix;
+        next_index = 0;
+    }
+    __device__ __forceinline__ int64_t next() {
+        int64_t t;
+        if (next_index == 0) {
+            t = int64_t{1} << 62;
+        } else if (next_index == 1) {
+            t = x;
+        } else {
+            t = cheb_step_q62(x, cur, prev);
+            prev = cur;
+            cur = t;
+        }
+        ++next_index;
+        return t;
+    }
+};
+
+__global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __grid_constant__ Problem p,
+                                                                      const __grid_constant__ Scratch w,
+                                                                      const __grid_constant__ SplitPlan plan,
+                                                                      const SplitRecordArrays sorted,
+                                                                      const SplitTile* __restrict__ tiles,
+                                                                      const uint32_t* __restrict__ totals,
+                                                                      int32_t* __restrict__ error_flag) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SplitShared& sh = *reinterpret_cast<SplitShared*>(smem_raw);
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
-    const int nmax = p.max_order;
-    const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
-    const Scalars& s = p.s;
+    const int lane = tid & 31;
     const int ksteps = plan.ksteps;
-    const int nu = s.nu;
+    const uint32_t ntiles = totals[1];
 
     if (tid == 0) {
-        mbar_init(&sh.full[0], 1);
-        mbar_init(&sh.full[1], 1);
-        mbar_init(&sh.empty[0], 1);
-        mbar_init(&sh.empty[1], 1);
-        mbar_init(&sh.acc_done, 1);
+        for (int i = 0; i < kAStages; ++i) {
+            mbar_init(&sh.a_full[i], 1);
+            mbar_init(&sh.a_empty[i], 1);
+        }
+        for (int i = 0; i < kBStages; ++i) {
+            mbar_init(&sh.b_full[i], kProducerWarps * 32);
+            mbar_init(&sh.b_empty[i], 1);
+        }
+        for (int i = 0; i < kMetaBufs; ++i) {
+            mbar_init(&sh.meta_full[i], kProducerWarps * 32);
+            mbar_init(&sh.meta_empty[i], kEpilogueWarps * 32);
+        }
+        mbar_init(&sh.acc_full, 1);
+        mbar_init(&sh.acc_empty, kEpilogueWarps * 32);
+        mbar_init(&sh.drain, 1);
         sh.error = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    if (warp == 0) {
+    if (warp == kWarpMma) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
             smem_addr(&sh.tmem_base)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -457,222 +548,271 @@ __global__ void __launch_bounds__(kThreads, 1) split_assembly(const __grid_const
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = sh.tmem_base;
-    const uint32_t idesc = mma_idesc(kRows, kTileN);
-    uint32_t full_use[2] = {0, 0}, empty_use[2] = {0, 0}, acc_use = 0;
-    const uint32_t ntiles = totals[1];
 
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const SplitTile tl = tiles[tile];
-        // segment of this block: table pointer and exponent
-        int seg = 0;
-        while (seg + 1 < plan.segments && tl.block >= plan.segment_base[seg + 1]) ++seg;
-        const uint32_t local = tl.block - plan.segment_base[seg];
-        const uint16_t* a_src = plan.slices[seg] + static_cast<int64_t>(local) * ksteps * (kAStageBytes / 2);
-        const int exponent = plan.exponents[seg][local];
-
-        // lookups of the tile
-        if (tid < kTileN) {
-            const bool live = tid < static_cast<int>(tl.count);
-            sh.u[tid] = live ? sorted.u[tl.start + tid] : 0.0;
-            sh.v[tid] = live ? sorted.v[tl.start + tid] : 0.0;
-            sh.info[tid] = live ? sorted.info[tl.start + tid] : ~uint64_t{0};
-        }
-        __syncthreads();
-        if (sh.error) break;  // a wait timed out: leave the remaining tiles
-        // first A stage can stream while the basis is generated (the stage was
-        // last read through the generic proxy by the previous epilogue)
-        if (tid == 0) {
-            asm volatile("fence.proxy.async.shared::cta;");
-            mbar_expect_tx(&sh.full[0], kAStageBytes);
-            bulk_copy_g2s(sh.a_stage[0], a_src, kAStageBytes, &sh.full[0]);
-        }
-        // B operand: T_b(v_l) split into 8 slices, two threads per lookup
-        {
-            const int l = tid & (kTileN - 1);
-            const int half = tid >> 6;
-            const int kpad = ksteps * kKStep;
-            const int b_begin = half * (kpad / 2), b_end = b_begin + kpad / 2;
-            const int64_t vfix = fixed_from_double(sh.v[l], 62);
-            int64_t tprev = int64_t{1} << 62, tcur = vfix;  // T_0, T_1
-            for (int b = 0; b < b_end; ++b) {
-                int64_t tb;
-                if (b == 0) {
-                    tb = int64_t{1} << 62;
-                } else if (b == 1) {
-                    tb = vfix;
-                } else {
-                    tb = cheb_step_q62(vfix, tcur, tprev);
-                    tprev = tcur;
-                    tcur = tb;
-                }
-                if (b < b_begin) continue;
-                // Q62 -> Q56, rounded; padding columns b >= nv are zero
-                int64_t x = b < s.nv ? (tb + 32) >> 6 : 0;
-                const int ks = b / kKStep, k = b - ks * kKStep;
-                uint16_t* dst = sh.b_all[ks] + core_offset(l, k);
-                for (int t = 0; t < kSlices; ++t) {
-                    const int shift = 49 - 7 * t;
-                    int64_t q = shift > 0 ? (x + (int64_t{1} << (shift - 1))) >> shift : x;
-                    x -= q * (int64_t{1} << shift);
-                    dst[t * kTileN * kKStep] = bf16_of_int(static_cast<int>(q));
-                }
+    if (warp < kProducerWarps) {
+        // ---------------------------------------------- basis producers --
+        const int l = tid >> 1;  // lookup of this thread
+        const int h = tid & 1;   // which 8 of the 16 k of a step
+        uint32_t b_cnt = 0, tile_cnt = 0;
+        for (uint32_t tile = blockIdx.x; tile < ntiles && !failed(sh); tile += gridDim.x, ++tile_cnt) {
+            const SplitTile tl = tiles[tile];
+            const int mb = static_cast<int>(tile_cnt % kMetaBufs);
+            if (tile_cnt >= kMetaBufs && !mbar_wait(&sh.meta_empty[mb], ((tile_cnt / kMetaBufs) - 1) & 1)) {
+                sh.error = 1;
+                break;
             }
-        }
-        asm volatile("fence.proxy.async.shared::cta;");
-        __syncthreads();
-
-        // MMA issue: 36 slice pairs per K step into 8 exact levels
-        if (tid == 0) {
-            for (int ks = 0; ks < ksteps; ++ks) {
-                const int st = ks & 1;
-                if (ks + 1 < ksteps) {
-                    const int nx = (ks + 1) & 1;
-                    if (ks + 1 >= 2) {
-                        if (!mbar_wait(&sh.empty[nx], empty_use[nx] & 1)) {
-                            sh.error = 1;
-                            break;
-                        }
-                        ++empty_use[nx];
-                    }
-                    mbar_expect_tx(&sh.full[nx], kAStageBytes);
-                    bulk_copy_g2s(sh.a_stage[nx], a_src + static_cast<int64_t>(ks + 1) * (kAStageBytes / 2),
-                                  kAStageBytes, &sh.full[nx]);
-                }
-                if (!mbar_wait(&sh.full[st], full_use[st] & 1)) {
+            const bool live = static_cast<uint32_t>(l) < tl.count;
+            const double v = live ? sorted.v[tl.start + l] : 0.0;
+            if (h == 0) {
+                sh.meta[mb].u[l] = live ? sorted.u[tl.start + l] : 0.0;
+                sh.meta[mb].info[l] = live ? sorted.info[tl.start + l] : ~uint64_t{0};
+            }
+            if (tid == 0) {
+                const uint16_t* a_src;
+                int exponent;
+                tile_source(plan, tl.block, ksteps, &a_src, &exponent);
+                sh.meta[mb].count = tl.count;
+                sh.meta[mb].exponent = exponent;
+            }
+            mbar_arrive(&sh.meta_full[mb]);
+            ChebQ62 cheb;
+            cheb.init(fixed_from_double(v, 62));
+            for (int ks = 0; ks < ksteps; ++ks, ++b_cnt) {
+                const int sb = static_cast<int>(b_cnt % kBStages);
+                if (b_cnt >= kBStages && !mbar_wait(&sh.b_empty[sb], ((b_cnt / kBStages) - 1) & 1)) {
                     sh.error = 1;
                     break;
                 }
-                ++full_use[st];
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t a_base = smem_addr(sh.a_stage[st]);
-                const uint32_t b_base = smem_addr(sh.b_all[ks]);
-                for (int t = 1; t <= kSlices; ++t) {
-                    for (int tp = 1; t + tp <= kSlices + 1; ++tp) {
-                        const int level = t + tp - 2;
-                        const uint64_t ad = smem_desc(a_base + (t - 1) * (kRows * kKStep * 2), 128, 256);
-                        const uint64_t bd = smem_desc(b_base + (tp - 1) * (kTileN * kKStep * 2), 128, 256);
-                        mma_bf16(tmem + level * kTileN, ad, bd, idesc, (ks > 0 || t > 1) ? 1u : 0u);
+                int64_t x[8];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int b = ks * kKStep + i;
+                    const int64_t tb = cheb.next();
+                    if ((i >> 3) == h) x[i & 7] = b < p.s.nv ? (tb + 32) >> 6 : 0;  // Q56
+                }
+                uint32_t packed[kSlices][4];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    int64_t xi = x[i];
+#pragma unroll
+                    for (int t = 0; t < kSlices; ++t) {
+                        const int shift = 49 - 7 * t;
+                        const int64_t q = shift > 0 ? (xi + (int64_t{1} << (shift - 1))) >> shift : xi;
+                        xi -= q * (int64_t{1} << shift);
+                        const uint32_t bits = bf16_of_int(static_cast<int>(q));
+                        if (i & 1) packed[t][i >> 1] |= bits << 16;
+                        else packed[t][i >> 1] = bits;
                     }
                 }
-                // ninth coefficient slice (pre-scaled) x first basis slice -> level 9
-                mma_bf16(tmem + (kLevels - 1) * kTileN,
-                         smem_desc(a_base + kSlices * (kRows * kKStep * 2), 128, 256),
-                         smem_desc(b_base, 128, 256), idesc, 1u);
-                mma_commit(&sh.empty[st]);
-            }
-            mma_commit(&sh.acc_done);
-        }
-        // everyone waits for the accumulators
-        if (!mbar_wait(&sh.acc_done, acc_use & 1)) sh.error = 1;
-        ++acc_use;
-        if (tid == 0) {
-            // balance the empty barriers: ksteps commits went to empty[ks & 1];
-            // the in-loop waits consumed those of steps 0..ksteps-3
-            for (int ks = (ksteps > 2 ? ksteps - 2 : 0); ks < ksteps; ++ks) {
-                const int st = ks & 1;
-                if (!mbar_wait(&sh.empty[st], empty_use[st] & 1)) sh.error = 1;
-                ++empty_use[st];
-            }
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-
-        // u basis in Q62 fixed point, [l][a ^ (l & 31)], in the A ring
-        int64_t* ubasis = reinterpret_cast<int64_t*>(sh.a_stage[0]);
-        if (tid < kTileN) {
-            const int l = tid;
-            const int64_t ufix = fixed_from_double(sh.u[l], 62);
-            int64_t tprev = int64_t{1} << 62, tcur = ufix;
-            for (int a = 0; a < kRows; ++a) {
-                int64_t ta;
-                if (a == 0) {
-                    ta = int64_t{1} << 62;
-                } else if (a == 1) {
-                    ta = ufix;
-                } else {
-                    ta = cheb_step_q62(ufix, tcur, tprev);
-                    tprev = tcur;
-                    tcur = ta;
+                uint16_t* base = sh.b_ring[sb] + core_offset(l, 8 * h);
+#pragma unroll
+                for (int t = 0; t < kSlices; ++t) {
+                    const uint32_t addr = smem_addr(base + t * kTileN * kKStep);
+                    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(packed[t][0]),
+                                 "r"(packed[t][1]), "r"(packed[t][2]), "r"(packed[t][3])
+                                 : "memory");
                 }
-                ubasis[l * kRows + (a ^ (l & 31))] = a < nu ? ta : 0;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(&sh.b_full[sb]);
             }
         }
-        __syncthreads();
-
-        // epilogue: row a = tid; combine levels, multiply by T_a(u_l), store
-        int64_t* prod = reinterpret_cast<int64_t*>(sh.b_all[0]);
-        const int a = tid;
-        const uint32_t lane_base = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-        for (int l0 = 0; l0 < kTileN; l0 += 16) {
-            uint32_t acc[kLevels][16];
-#pragma unroll
-            for (int lev = 0; lev < kLevels; ++lev) tmem_ld16(lane_base + lev * kTileN + l0, acc[lev]);
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int l = l0 + j;
-                int64_t p[kLevels];
-#pragma unroll
-                for (int lev = 0; lev < kLevels; ++lev) p[lev] = __float2int_rn(__uint_as_float(acc[lev][j]));
-                // W * 2^55 = sum_tau P_tau 2^(55 - 7 tau), tau = 2..9
-                int64_t wfix = p[0] * (int64_t{1} << 41) + p[1] * (int64_t{1} << 34) +
-                               p[2] * (int64_t{1} << 27) + p[3] * (int64_t{1} << 20) +
-                               p[4] * (int64_t{1} << 13) + p[5] * 64 + ((p[6] * 128 + p[7] + 128) >> 8);
-                const int64_t tf = ubasis[l * kRows + (a ^ (l & 31))];
-                // (wfix * tf) >> 62, rounded
-                const uint64_t lo = static_cast<uint64_t>(wfix) * static_cast<uint64_t>(tf);
-                int64_t hi = __mul64hi(wfix, tf);
-                const uint64_t lo2 = lo + (uint64_t{1} << 61);
-                hi += lo2 < lo ? 1 : 0;
-                const int64_t term = static_cast<int64_t>((static_cast<uint64_t>(hi) << 2) | (lo2 >> 62));
-                prod[l * kRows + (a ^ (l & 31))] = term;
+    } else if (warp < kProducerWarps + kEpilogueWarps) {
+        // ------------------------------------------------------ epilogue --
+        const int e = tid - kProducerWarps * 32;  // row a of this thread
+        const uint32_t lane_base = tmem + (static_cast<uint32_t>((warp & 3) * 32) << 16);
+        const int nu = p.s.nu;
+        const int nmax = p.max_order;
+        const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
+        uint32_t tile_cnt = 0;
+        for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tile_cnt) {
+            const int mb = static_cast<int>(tile_cnt % kMetaBufs);
+            const bool meta_ok = mbar_wait(&sh.meta_full[mb], (tile_cnt / kMetaBufs) & 1);
+            if (epilogue_any(!meta_ok || failed(sh))) {
+                sh.error = 1;
+                break;
             }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-
-        // column sums in 128-bit integers and the write-back
-        if (tid < kTileN && tid < static_cast<int>(tl.count)) {
-            const int l = tid;
-            uint64_t lo = 0;
-            int64_t hi = 0;
-            for (int r = 0; r < kRows; ++r) {
-                const int64_t t = prod[l * kRows + (r ^ (l & 31))];
-                const uint64_t nlo = lo + static_cast<uint64_t>(t);
-                hi += (t < 0 ? -1 : 0) + (nlo < lo ? 1 : 0);
-                lo = nlo;
-            }
-            double value;
-            const int64_t lo_signed = static_cast<int64_t>(lo);
-            if ((hi == 0 && lo_signed >= 0) || (hi == -1 && lo_signed < 0)) {
-                value = static_cast<double>(lo_signed);
-            } else {
-                value = static_cast<double>(hi) * 18446744073709551616.0 + static_cast<double>(lo);
-            }
-            value = ldexp(value, exponent - 55);
-            const uint64_t info = sh.info[l];
-            const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
-            const int set = static_cast<int>((info >> 32) & 1);
-            const int spins = static_cast<int>((info >> 33) & 3);
-            const int i = static_cast<int>((info >> 35) & 31);
-            const int j = static_cast<int>((info >> 40) & 31);
-            const int n = static_cast<int>((info >> 45) & 31);
-            const int64_t mslot = (c * 2 + set) * 2;
-            for (int spin = 0; spin < 2; ++spin) {
-                if (!(spins & (1 << spin))) continue;
-                double g = value;
-                if (i == j) {
-                    g = dadd(g, spin == 0 ? s.diag_up_shift : s.diag_down_shift);
-                    w.diag[(mslot + spin) * nmax + i] = g;
+            const TileMeta& meta = sh.meta[mb];
+            // u basis of the tile, two threads per lookup, each storing half of a
+            {
+                const int l = e >> 1, half = e & 1;
+                ChebQ62 cheb;
+                cheb.init(fixed_from_double(meta.u[l], 62));
+                for (int a = 0; a < kRows; ++a) {
+                    const int64_t ta = cheb.next();
+                    if ((a >> 6) == half) sh.ubasis[l * kRows + (a ^ (l & 31))] = a < nu ? ta : 0;
                 }
-                w.green[(mslot + spin) * per_c + i * n + j] = dmul(g, s.scale);
+            }
+            const bool acc_ok = mbar_wait(&sh.acc_full, tile_cnt & 1);
+            if (epilogue_any(!acc_ok)) {  // also orders the u-basis stores before their reads
+                sh.error = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t count = meta.count;
+            const int exponent = meta.exponent;
+            for (int l0 = 0; l0 < kTileN; l0 += kRedChunk) {
+                uint32_t acc[kLevels][8];
+#pragma unroll
+                for (int lev = 0; lev < kLevels; ++lev) {
+                    const uint32_t addr = lane_base + lev * kTileN + l0;
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                 : "=r"(acc[lev][0]), "=r"(acc[lev][1]), "=r"(acc[lev][2]), "=r"(acc[lev][3]),
+                                   "=r"(acc[lev][4]), "=r"(acc[lev][5]), "=r"(acc[lev][6]), "=r"(acc[lev][7])
+                                 : "r"(addr));
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                for (int j = 0; j < kRedChunk; ++j) {
+                    const int l = l0 + j;
+                    int64_t pl[kLevels];
+#pragma unroll
+                    for (int lev = 0; lev < kLevels; ++lev) pl[lev] = __float2int_rn(__uint_as_float(acc[lev][j]));
+                    const int64_t wfix = pl[0] * (int64_t{1} << 41) + pl[1] * (int64_t{1} << 34) +
+                                         pl[2] * (int64_t{1} << 27) + pl[3] * (int64_t{1} << 20) +
+                                         pl[4] * (int64_t{1} << 13) + pl[5] * 64 + ((pl[6] * 128 + pl[7] + 128) >> 8);
+                    const int64_t tf = sh.ubasis[l * kRows + (e ^ (l & 31))];
+                    const uint64_t lo = static_cast<uint64_t>(wfix) * static_cast<uint64_t>(tf);
+                    int64_t hi = __mul64hi(wfix, tf);
+                    const uint64_t lo2 = lo + (uint64_t{1} << 61);
+                    hi += lo2 < lo ? 1 : 0;
+                    sh.red[j * kRows + e] =
+                        static_cast<int64_t>((static_cast<uint64_t>(hi) << 2) | (lo2 >> 62));
+                }
+                epilogue_sync();
+                // 16 threads per lookup sum 8 rows each (rows part + 16 i), then 4 shuffle levels
+                {
+                    const int j = e >> 4, part = e & 15;
+                    uint64_t slo = 0;
+                    int64_t shi = 0;
+#pragma unroll
+                    for (int i = 0; i < kRows / 16; ++i) {
+                        const int64_t t = sh.red[j * kRows + part + 16 * i];
+                        const uint64_t nlo = slo + static_cast<uint64_t>(t);
+                        shi += (t < 0 ? -1 : 0) + (nlo < slo ? 1 : 0);
+                        slo = nlo;
+                    }
+#pragma unroll
+                    for (int off = 8; off > 0; off >>= 1) {
+                        const uint64_t olo = __shfl_xor_sync(0xffffffffu, slo, off);
+                        const int64_t ohi = __shfl_xor_sync(0xffffffffu, shi, off);
+                        const uint64_t nlo = slo + olo;
+                        shi += ohi + (nlo < slo ? 1 : 0);
+                        slo = nlo;
+                    }
+                    const int l = l0 + j;
+                    if (part == 0 && static_cast<uint32_t>(l) < count) {
+                        double value;
+                        const int64_t lo_signed = static_cast<int64_t>(slo);
+                        if ((shi == 0 && lo_signed >= 0) || (shi == -1 && lo_signed < 0)) {
+                            value = static_cast<double>(lo_signed);
+                        } else {
+                            value = static_cast<double>(shi) * 18446744073709551616.0 + static_cast<double>(slo);
+                        }
+                        value = ldexp(value, exponent - 55);
+                        const uint64_t info = meta.info[l];
+                        const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
+                        const int set = static_cast<int>((info >> 32) & 1);
+                        const int spins = static_cast<int>((info >> 33) & 3);
+                        const int i = static_cast<int>((info >> 35) & 31);
+                        const int jj = static_cast<int>((info >> 40) & 31);
+                        const int n = static_cast<int>((info >> 45) & 31);
+                        const int64_t mslot = (c * 2 + set) * 2;
+                        for (int spin = 0; spin < 2; ++spin) {
+                            if (!(spins & (1 << spin))) continue;
+                            double g = value;
+                            if (i == jj) {
+                                g = dadd(g, spin == 0 ? p.s.diag_up_shift : p.s.diag_down_shift);
+                                w.diag[(mslot + spin) * nmax + i] = g;
+                            }
+                            w.green[(mslot + spin) * per_c + i * n + jj] = dmul(g, p.s.scale);
+                        }
+                    }
+                }
+                epilogue_sync();
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(&sh.acc_empty);
+            mbar_arrive(&sh.meta_empty[mb]);
+        }
+    } else if (warp == kWarpCopy) {
+        // ----------------------------------------- coefficient streaming --
+        if (lane == 0) {
+            uint32_t a_cnt = 0;
+            for (uint32_t tile = blockIdx.x; tile < ntiles && !failed(sh); tile += gridDim.x) {
+                const SplitTile tl = tiles[tile];
+                const uint16_t* a_src;
+                int exponent;
+                tile_source(plan, tl.block, ksteps, &a_src, &exponent);
+                for (int ks = 0; ks < ksteps; ++ks, ++a_cnt) {
+                    const int st = static_cast<int>(a_cnt % kAStages);
+                    if (a_cnt >= kAStages && !mbar_wait(&sh.a_empty[st], ((a_cnt / kAStages) - 1) & 1)) {
+                        sh.error = 1;
+                        break;
+                    }
+                    mbar_expect_tx(&sh.a_full[st], kAStageBytes);
+                    bulk_copy_g2s(sh.a_ring[st], a_src + static_cast<int64_t>(ks) * (kAStageBytes / 2),
+                                  kAStageBytes, &sh.a_full[st]);
+                }
+            }
+            // copies still in flight (only after an error) land before the CTA exits
+            for (uint32_t st = 0; st < static_cast<uint32_t>(kAStages); ++st) {
+                if (a_cnt <= st) continue;
+                const uint32_t last = a_cnt - 1 - (a_cnt - 1 - st) % kAStages;
+                if (!mbar_wait(&sh.a_full[st], (last / kAStages) & 1)) sh.error = 1;
             }
         }
-        __syncthreads();
+    } else if (warp == kWarpMma) {
+        // ---------------------------------------------------- MMA issue --
+        if (lane == 0) {
+            const uint32_t idesc = mma_idesc(kRows, kTileN);
+            uint32_t a_cnt = 0, b_cnt = 0, tile_cnt = 0;
+            for (uint32_t tile = blockIdx.x; tile < ntiles && !failed(sh); tile += gridDim.x, ++tile_cnt) {
+                if (tile_cnt > 0 && !mbar_wait(&sh.acc_empty, (tile_cnt - 1) & 1)) {
+                    sh.error = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                for (int ks = 0; ks < ksteps; ++ks, ++a_cnt, ++b_cnt) {
+                    const int sa = static_cast<int>(a_cnt % kAStages);
+                    const int sb = static_cast<int>(b_cnt % kBStages);
+                    if (!mbar_wait(&sh.a_full[sa], (a_cnt / kAStages) & 1) ||
+                        !mbar_wait(&sh.b_full[sb], (b_cnt / kBStages) & 1)) {
+                        sh.error = 1;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t a_base = smem_addr(sh.a_ring[sa]);
+                    const uint32_t b_base = smem_addr(sh.b_ring[sb]);
+                    for (int t = 1; t <= kSlices; ++t) {
+                        for (int tp = 1; t + tp <= kSlices + 1; ++tp) {
+                            const int level = t + tp - 2;
+                            mma_bf16(tmem + level * kTileN,
+                                     smem_desc(a_base + (t - 1) * (kRows * kKStep * 2), 128, 256),
+                                     smem_desc(b_base + (tp - 1) * (kTileN * kKStep * 2), 128, 256), idesc,
+                                     (ks > 0 || t > 1) ? 1u : 0u);
+                        }
+                    }
+                    mma_bf16(tmem + (kLevels - 1) * kTileN, smem_desc(a_base + kSlices * (kRows * kKStep * 2), 128, 256),
+                             smem_desc(b_base, 128, 256), idesc, 1u);
+                    mma_commit(&sh.a_empty[sa]);
+                    mma_commit(&sh.b_empty[sb]);
+                }
+                mma_commit(&sh.acc_full);
+            }
+            // every MMA issued has completed before the columns are freed
+            if (tile_cnt > 0) {
+                mma_commit(&sh.drain);
+                if (!mbar_wait(&sh.drain, 0)) sh.error = 1;
+            }
+        }
     }
-    if (tid == 0 && sh.error) atomicExch(error_flag, 1);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+    if (tid == 0 && sh.error) atomicExch(error_flag, 1);
+    if (warp == kWarpMma) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+    }
 }
 
 }  // namespace
@@ -744,7 +884,7 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     const size_t smem = sizeof(SplitShared);
     err = cudaFuncSetAttribute(split_assembly, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (err != cudaSuccess) return err;
-    split_assembly<<<sm_count, kThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, error_flag);
+    split_assembly<<<sm_count, kAssemblyThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, error_flag);
     return cudaGetLastError();
 }
 
