@@ -7,20 +7,27 @@
 //   G_l     = sum_a T_a(u_l) W[a][l]          (integer epilogue, exact up to
 //                                             final rounding)
 //
-// Operands are split Ozaki-style into bf16 slices of ~7 bits each:
-// C = 2^E sum_t q_t 2^{-7t} per block (E = the block's binary exponent, nine
-// slices) and T_b(v) = sum_t' q'_t' 2^{-7t'} (eight slices). Every slice is an
-// integer of magnitude at most 128, so each bf16 x bf16 product is exact and
-// the FP32 accumulation of all products of one level tau = t + t' over
-// K <= 128 stays below 2^24: the accumulators of levels 2..8 in tensor memory
-// hold exact integers; level 9 also takes the ninth coefficient slice, stored
-// pre-scaled by 2^-7, and rounds below 2^-65 of the block scale. Products of
-// levels 10 and above are dropped (weight 2^-70 each). The epilogue combines the levels in 64-bit fixed point, multiplies
-// by T_a(u) in Q62 fixed point and sums over a in 128-bit integers, so the
-// only roundings are the slice truncation (2^-57), the fixed-point scalings
-// (2^-56), the Q62 Chebyshev recurrences of the two bases (2^-63 per step)
-// and the final conversion to double: FP64-level accuracy without the FP64
-// pipe.
+// Operands are split Ozaki-style into fp16 slices of balanced 8-bit digits:
+// C = 2^E sum_t q_t 2^{-8t} per block (E = the block's binary exponent, eight
+// digits, |q_1| <= 256, |q_t| <= 128) and T_b(v) = sum_t' q'_t' 2^{-8t'}
+// (seven digits of the Q56 fixed-point value). Every product of two digits is
+// an exact integer below 2^16, and the FP32 accumulation of the products of
+// one level tau = t + t' over K <= 128 stays within 2^24 for tau <= 7, so the
+// accumulators of levels 2..7 in tensor memory hold exact integers. Level 8
+// also takes the eighth coefficient digit, stored pre-scaled by 2^-8, and
+// carries weight 2^-64; products of levels 9 and above (weight 2^-72) are
+// dropped. The epilogue combines the levels in 64-bit fixed point (2^-55),
+// multiplies by T_a(u) in Q62 fixed point and sums over a in 128-bit
+// integers. Against an exact evaluation of the series the result is within
+// 5e-16 of the block's largest coefficient at degree 16 and 2.4e-16 at degree
+// 64 (the FP64 Clenshaw sum: 2e-15): FP64-level accuracy without the FP64 pipe.
+//
+// Both bases come from the stride-2 Chebyshev recurrence
+// T_{n+2} = 2 T_2 T_n - T_{n-2} in Q62 fixed point, one thread of a pair for
+// the even and one for the odd degrees. To let each thread write whole
+// core-matrix rows, the coefficient slices order each K step of 16 columns as
+// the eight even b followed by the eight odd b; the contraction over k is
+// indifferent to the order.
 //
 // Pipeline per evaluation: split_descriptors (one thread per vertex pair:
 // branch, u, v, block ids; corner entries written directly), a counting sort
@@ -34,24 +41,30 @@
 #include "cdet_device.cuh"
 #include "cdet_kernels.cuh"
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 namespace cdet {
 
 namespace {
 
-constexpr int kSlices = 8;          // slices of the basis operand
-constexpr int kSlicesA = 9;         // slices of the coefficient operand (the ninth pre-scaled by 2^-7)
-constexpr int kLevels = 8;          // accumulator levels tau = 2..9
+constexpr int kSlices = 7;          // slices of the basis operand
+constexpr int kSlicesA = 8;         // slices of the coefficient operand (the eighth pre-scaled by 2^-8)
+constexpr int kLevels = 7;          // accumulator levels tau = 2..8
 constexpr int kTileN = 64;          // lookups per tile (MMA N)
 constexpr int kRows = 128;          // MMA M (Chebyshev rows a, zero padded)
 constexpr int kKStep = 16;          // MMA K (bf16)
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
 
-// bytes of one A stage: 9 slices x 128 rows x 16 k x bf16
-constexpr uint32_t kAStageBytes = kSlicesA * kRows * kKStep * 2;      // 36 KiB
-// bytes of the B operand of one K step: 8 slices x 64 lookups x 16 k x bf16
-constexpr uint32_t kBStepBytes = kSlices * kTileN * kKStep * 2;       // 16 KiB
+// bytes of one A stage: 8 slices x 128 rows x 16 k x fp16
+constexpr uint32_t kAStageBytes = kSlicesA * kRows * kKStep * 2;      // 32 KiB
+// bytes of the B operand of one K step: 7 slices x 64 lookups x 16 k x fp16
+constexpr uint32_t kBStepBytes = kSlices * kTileN * kKStep * 2;       // 14 KiB
+// Q56 basis value -> byte digits: +128 on each of the six low bytes makes
+// every byte a balanced digit plus 128; +256 at bit 56 makes the top field
+// (bits 48 and up) the leading digit plus 256, in [0, 512].
+constexpr uint64_t kDigitBias = 0x0100808080808080ull;
 
 // ----------------------------------------------------------- PTX helpers --
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -69,10 +82,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return d;
 }
 
-// kind::f16 instruction descriptor: bf16 x bf16 -> f32, K-major A and B.
+// kind::f16 instruction descriptor: f16 x f16 -> f32, K-major A and B.
 __host__ __device__ constexpr uint32_t mma_idesc(int m, int n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
-           (static_cast<uint32_t>(m >> 4) << 24);
+    return (1u << 4) | (static_cast<uint32_t>(n >> 3) << 17) | (static_cast<uint32_t>(m >> 4) << 24);
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -108,7 +120,7 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
         : "memory");
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc,
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t adesc, uint64_t bdesc,
                                          uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
@@ -150,25 +162,45 @@ __device__ __forceinline__ int64_t cheb_step_q62(int64_t ufix, int64_t t, int64_
     return static_cast<int64_t>(twice - static_cast<uint64_t>(tprev));
 }
 
-// bf16 bit pattern of a small integer (|q| <= 128), exact.
-__device__ __forceinline__ uint16_t bf16_of_int(int q) {
-    const float f = __int_as_float(0x4B400000 + q) - 12582912.0f;
-    return static_cast<uint16_t>(__float_as_uint(f) >> 16);
+// Two fp16 digits (the same slice of two consecutive k) from the biased
+// basis values ya, yb. Slice 1 is the top field (bits 48..57, leading digit
+// + 256); slices 2..7 are bytes 5..0 (digit + 128). A field f < 1024 placed
+// in the mantissa of 1024 is the fp16 number 1024 + f; one packed
+// subtraction removes 1024 and the bias exactly.
+__device__ __forceinline__ uint32_t digit_pair(uint64_t ya, uint64_t yb, int slice) {
+    uint32_t r;
+    __half2 bias;
+    if (slice == 1) {
+        r = __byte_perm(static_cast<uint32_t>(ya >> 32), static_cast<uint32_t>(yb >> 32), 0x7632) | 0x64006400u;
+        bias = __halves2half2(__ushort_as_half(0x6500), __ushort_as_half(0x6500));  // 1280
+    } else {
+        const int byte = 7 - slice;  // 5..0
+        const uint32_t wa = byte >= 4 ? static_cast<uint32_t>(ya >> 32) : static_cast<uint32_t>(ya);
+        const uint32_t wb = byte >= 4 ? static_cast<uint32_t>(yb >> 32) : static_cast<uint32_t>(yb);
+        const uint32_t bi = static_cast<uint32_t>(byte & 3);
+        r = (__byte_perm(wa, wb, bi | (bi << 4) | ((bi + 4) << 8) | ((bi + 4) << 12)) & 0x00FF00FFu) | 0x64006400u;
+        bias = __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480));  // 1152
+    }
+    __half2 h = *reinterpret_cast<__half2*>(&r);
+    h = __hsub2(h, bias);
+    return *reinterpret_cast<uint32_t*>(&h);
 }
 
-// Offset (in bf16 elements) of element (row, k) inside one K-major
+// Offset (in 16-bit elements) of element (row, k) inside one K-major
 // no-swizzle operand of `rows` rows and 16 k: [row group][k chunk][8][8].
 __device__ __forceinline__ int core_offset(int row, int k) {
     return (row >> 3) * 128 + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
 }
 
 // ---------------------------------------------------------- table slicing --
-// One block of nu x nv FP64 coefficients -> kSlicesA bf16 slices laid out as
+// One block of nu x nv FP64 coefficients -> kSlicesA fp16 slices laid out as
 // [kstep][slice][core layout of 128 rows x 16 k], and the block exponent.
-// Slices 1..8 are integers q_t (weight 2^-7t); slice 9 is stored as
-// q_9 * 2^-7 (exact in bf16) so that its one product, with the first basis
-// slice, accumulates at level 9 with the right weight. Nine slices leave a
-// truncation of 2^-64 of the block scale per coefficient.
+// Within K step ks, position k holds column b = 16 ks + 2k (k < 8) or
+// 16 ks + 2(k - 8) + 1 (k >= 8), the order in which the basis threads produce
+// T_b(v). Slices 1..7 are integers q_t (weight 2^-8t); slice 8 is stored as
+// q_8 * 2^-8 (exact in fp16) so that its one product, with the first basis
+// slice, accumulates at level 8 with the right weight. Eight digits leave a
+// truncation of 2^-65 of the block scale per coefficient.
 __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ coeffs, int nu, int nv,
                                                     int ksteps, uint16_t* __restrict__ out,
                                                     int32_t* __restrict__ exponents) {
@@ -192,16 +224,17 @@ __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ c
         const int a = i / (ksteps * kKStep);
         const int b = i - a * (ksteps * kKStep);
         double r = (a < nu && b < nv) ? ldexp(c[a * nv + b], -e) : 0.0;  // |r| < 1
-        const int ks = b / kKStep, k = b - ks * kKStep;
+        const int ks = b / kKStep, bb = b - ks * kKStep;
+        const int k = (bb & 1) * 8 + (bb >> 1);
         uint16_t* base = dst + static_cast<int64_t>(ks) * kSlicesA * kRows * kKStep + core_offset(a, k);
         for (int t = 0; t < kSlicesA; ++t) {
-            // exact: r * 128 has the same significand, and subtracting the
+            // exact: r * 256 has the same significand, and subtracting the
             // nearest integer leaves the (representable) remainder
-            const double scaled = r * 128.0;
+            const double scaled = r * 256.0;
             const double q = rint(scaled);
             r = scaled - q;
-            base[t * kRows * kKStep] = t < kSlices ? bf16_of_int(static_cast<int>(q))
-                                                   : static_cast<uint16_t>(__float_as_uint(static_cast<float>(q) * 0.0078125f) >> 16);
+            const float stored = t < kSlicesA - 1 ? static_cast<float>(q) : static_cast<float>(q) * 0.00390625f;
+            base[t * kRows * kKStep] = __half_as_ushort(__float2half_rn(stored));
         }
     }
 }
@@ -412,7 +445,7 @@ __global__ void __launch_bounds__(256) split_tiles(const uint32_t* __restrict__ 
 // The accumulators are single-buffered: the MMAs of a tile start when the
 // epilogue has released the previous tile's TMEM.
 constexpr int kAStages = 3;
-constexpr int kBStages = 2;
+constexpr int kBStages = 3;
 constexpr int kMetaBufs = 3;
 constexpr int kProducerWarps = 4;
 constexpr int kEpilogueWarps = 4;
@@ -431,8 +464,8 @@ struct TileMeta {
 };
 
 struct SplitShared {
-    alignas(1024) uint16_t a_ring[kAStages][kAStageBytes / 2];  // 3 x 36 KiB
-    alignas(1024) uint16_t b_ring[kBStages][kBStepBytes / 2];   // 2 x 16 KiB
+    alignas(1024) uint16_t a_ring[kAStages][kAStageBytes / 2];  // 3 x 32 KiB
+    alignas(1024) uint16_t b_ring[kBStages][kBStepBytes / 2];   // 3 x 14 KiB
     alignas(16) int64_t ubasis[kTileN * kRows];                 // 64 KiB, [l][a ^ (l & 31)]
     alignas(16) int64_t red[kRedChunk * kRows];                 // 8 KiB, [j][row]
     TileMeta meta[kMetaBufs];
@@ -479,28 +512,22 @@ __device__ __forceinline__ void tile_source(const SplitPlan& plan, uint32_t bloc
     *exponent = plan.exponents[seg][local];
 }
 
-// Next value of a Q62 Chebyshev sequence: T_0 = 1, T_1 = x, then the recurrence.
-struct ChebQ62 {
-    int64_t x, prev, cur;
-    int next_index;
-    __device__ __forceinline__ void init(int64_t xfix) {
-        x = xfix;
-        prev = int64_t{1} << 62;
-        cur = xfix;
-        next_index = 0;
+// T_parity, T_{parity+2}, T_{parity+4}, ... of x in Q62 fixed point, by the
+// stride-2 recurrence T_{n+2} = 2 T_2(x) T_n - T_{n-2}, started from
+// (T_{-2}, T_0) = (T_2, 1) or (T_{-1}, T_1) = (x, x). The recurrence in
+// w = T_2(x) has half the steps of the stride-1 one and its rounding error
+// grows like the square of the step count.
+struct ChebStride2 {
+    int64_t w, prev, cur;
+    __device__ __forceinline__ void init(int64_t xfix, int parity) {
+        w = cheb_step_q62(xfix, xfix, int64_t{1} << 62);  // 2 x^2 - 1
+        prev = parity ? xfix : w;
+        cur = parity ? xfix : (int64_t{1} << 62);
     }
     __device__ __forceinline__ int64_t next() {
-        int64_t t;
-        if (next_index == 0) {
-            t = int64_t{1} << 62;
-        } else if (next_index == 1) {
-            t = x;
-        } else {
-            t = cheb_step_q62(x, cur, prev);
-            prev = cur;
-            cur = t;
-        }
-        ++next_index;
+        const int64_t t = cur;
+        cur = cheb_step_q62(w, cur, prev);
+        prev = t;
         return t;
     }
 };
@@ -551,8 +578,10 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
 
     if (warp < kProducerWarps) {
         // ---------------------------------------------- basis producers --
-        const int l = tid >> 1;  // lookup of this thread
-        const int h = tid & 1;   // which 8 of the 16 k of a step
+        // lanes 0-15 of a warp: lookups 16w..16w+15, even degrees; lanes
+        // 16-31: the same lookups, odd degrees
+        const int l = warp * 16 + (lane & 15);  // lookup of this thread
+        const int h = lane >> 4;                // parity of its degrees = which 8 of the 16 k
         uint32_t b_cnt = 0, tile_cnt = 0;
         for (uint32_t tile = blockIdx.x; tile < ntiles && !failed(sh); tile += gridDim.x, ++tile_cnt) {
             const SplitTile tl = tiles[tile];
@@ -575,41 +604,30 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 sh.meta[mb].exponent = exponent;
             }
             mbar_arrive(&sh.meta_full[mb]);
-            ChebQ62 cheb;
-            cheb.init(fixed_from_double(v, 62));
+            ChebStride2 cheb;
+            cheb.init(fixed_from_double(v, 62), h);
             for (int ks = 0; ks < ksteps; ++ks, ++b_cnt) {
                 const int sb = static_cast<int>(b_cnt % kBStages);
                 if (b_cnt >= kBStages && !mbar_wait(&sh.b_empty[sb], ((b_cnt / kBStages) - 1) & 1)) {
                     sh.error = 1;
                     break;
                 }
-                int64_t x[8];
+                // k = 8h + j holds b = 16 ks + 2j + h
+                uint64_t y[8];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int b = ks * kKStep + i;
+                for (int j = 0; j < 8; ++j) {
+                    const int b = ks * kKStep + 2 * j + h;
                     const int64_t tb = cheb.next();
-                    if ((i >> 3) == h) x[i & 7] = b < p.s.nv ? (tb + 32) >> 6 : 0;  // Q56
-                }
-                uint32_t packed[kSlices][4];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    int64_t xi = x[i];
-#pragma unroll
-                    for (int t = 0; t < kSlices; ++t) {
-                        const int shift = 49 - 7 * t;
-                        const int64_t q = shift > 0 ? (xi + (int64_t{1} << (shift - 1))) >> shift : xi;
-                        xi -= q * (int64_t{1} << shift);
-                        const uint32_t bits = bf16_of_int(static_cast<int>(q));
-                        if (i & 1) packed[t][i >> 1] |= bits << 16;
-                        else packed[t][i >> 1] = bits;
-                    }
+                    const int64_t x = b < p.s.nv ? (tb + 32) >> 6 : 0;  // Q56
+                    y[j] = static_cast<uint64_t>(x) + kDigitBias;
                 }
                 uint16_t* base = sh.b_ring[sb] + core_offset(l, 8 * h);
 #pragma unroll
-                for (int t = 0; t < kSlices; ++t) {
-                    const uint32_t addr = smem_addr(base + t * kTileN * kKStep);
-                    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(packed[t][0]),
-                                 "r"(packed[t][1]), "r"(packed[t][2]), "r"(packed[t][3])
+                for (int t = 1; t <= kSlices; ++t) {
+                    const uint32_t addr = smem_addr(base + (t - 1) * kTileN * kKStep);
+                    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(digit_pair(y[0], y[1], t)),
+                                 "r"(digit_pair(y[2], y[3], t)), "r"(digit_pair(y[4], y[5], t)),
+                                 "r"(digit_pair(y[6], y[7], t))
                                  : "memory");
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -632,14 +650,14 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 break;
             }
             const TileMeta& meta = sh.meta[mb];
-            // u basis of the tile, two threads per lookup, each storing half of a
+            // u basis of the tile, two threads per lookup (even and odd degrees)
             {
-                const int l = e >> 1, half = e & 1;
-                ChebQ62 cheb;
-                cheb.init(fixed_from_double(meta.u[l], 62));
-                for (int a = 0; a < kRows; ++a) {
+                const int l = e >> 1, parity = e & 1;
+                ChebStride2 cheb;
+                cheb.init(fixed_from_double(meta.u[l], 62), parity);
+                for (int a = parity; a < kRows; a += 2) {
                     const int64_t ta = cheb.next();
-                    if ((a >> 6) == half) sh.ubasis[l * kRows + (a ^ (l & 31))] = a < nu ? ta : 0;
+                    sh.ubasis[l * kRows + (a ^ (l & 31))] = a < nu ? ta : 0;
                 }
             }
             const bool acc_ok = mbar_wait(&sh.acc_full, tile_cnt & 1);
@@ -664,12 +682,15 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
 #pragma unroll
                 for (int j = 0; j < kRedChunk; ++j) {
                     const int l = l0 + j;
-                    int64_t pl[kLevels];
+                    // W * 2^55 = sum_tau P_tau 2^(55 - 8 tau), tau = 2..8; levels
+                    // 2..6 are exact integers, 7 and 8 are folded in FP32
+                    int64_t pl[5];
 #pragma unroll
-                    for (int lev = 0; lev < kLevels; ++lev) pl[lev] = __float2int_rn(__uint_as_float(acc[lev][j]));
-                    const int64_t wfix = pl[0] * (int64_t{1} << 41) + pl[1] * (int64_t{1} << 34) +
-                                         pl[2] * (int64_t{1} << 27) + pl[3] * (int64_t{1} << 20) +
-                                         pl[4] * (int64_t{1} << 13) + pl[5] * 64 + ((pl[6] * 128 + pl[7] + 128) >> 8);
+                    for (int lev = 0; lev < 5; ++lev) pl[lev] = __float2int_rn(__uint_as_float(acc[lev][j]));
+                    const float p78 = fmaf(__uint_as_float(acc[6][j]), 0.001953125f, __uint_as_float(acc[5][j]) * 0.5f);
+                    const int64_t wfix = pl[0] * (int64_t{1} << 39) + pl[1] * (int64_t{1} << 31) +
+                                         pl[2] * (int64_t{1} << 23) + pl[3] * (int64_t{1} << 15) + pl[4] * 128 +
+                                         __float2int_rn(p78);
                     const int64_t tf = sh.ubasis[l * kRows + (e ^ (l & 31))];
                     const uint64_t lo = static_cast<uint64_t>(wfix) * static_cast<uint64_t>(tf);
                     int64_t hi = __mul64hi(wfix, tf);
@@ -784,15 +805,15 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                     const uint32_t a_base = smem_addr(sh.a_ring[sa]);
                     const uint32_t b_base = smem_addr(sh.b_ring[sb]);
                     for (int t = 1; t <= kSlices; ++t) {
-                        for (int tp = 1; t + tp <= kSlices + 1; ++tp) {
+                        for (int tp = 1; t + tp <= kLevels + 1; ++tp) {
                             const int level = t + tp - 2;
-                            mma_bf16(tmem + level * kTileN,
+                            mma_f16(tmem + level * kTileN,
                                      smem_desc(a_base + (t - 1) * (kRows * kKStep * 2), 128, 256),
                                      smem_desc(b_base + (tp - 1) * (kTileN * kKStep * 2), 128, 256), idesc,
                                      (ks > 0 || t > 1) ? 1u : 0u);
                         }
                     }
-                    mma_bf16(tmem + (kLevels - 1) * kTileN, smem_desc(a_base + kSlices * (kRows * kKStep * 2), 128, 256),
+                    mma_f16(tmem + (kLevels - 1) * kTileN, smem_desc(a_base + kSlices * (kRows * kKStep * 2), 128, 256),
                              smem_desc(b_base, 128, 256), idesc, 1u);
                     mma_commit(&sh.a_empty[sa]);
                     mma_commit(&sh.b_empty[sb]);
