@@ -98,14 +98,19 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 
 // Wait for the phase with the given parity, for at most kWaitCycles SM
 // clocks; returns false on timeout (the caller records an error and stops).
+// Each try_wait may suspend the thread until the phase completes (at most
+// kSuspendNs), so a waiting warp takes no issue slots from the warps that
+// share its scheduler.
+constexpr uint32_t kSuspendNs = 200000;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     uint32_t done = 0;
     const long long start = clock64();
     while (true) {
         asm volatile(
-            "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
+            "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p;}"
             : "=r"(done)
-            : "r"(smem_addr(bar)), "r"(parity));
+            : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendNs)
+            : "memory");
         if (done) return true;
         if (clock64() - start > kWaitCycles) return false;
     }
@@ -146,6 +151,51 @@ __device__ __forceinline__ int64_t fixed_from_double(double x, int frac) {
     else if (shift > -60) v = (mant + (int64_t{1} << (-shift - 1))) >> (-shift);
     else v = 0;
     return (bits >> 63) ? -v : v;
+}
+
+// (hi:lo) * 2^scale_exp as a double, rounded to nearest even, with integer
+// operations only (the FP64 pipe is narrow). Results outside the normal
+// range take the FP64 route.
+__device__ __forceinline__ double int128_to_double(int64_t hi, uint64_t lo, int scale_exp) {
+    const bool neg = hi < 0;
+    uint64_t mhi = static_cast<uint64_t>(hi), mlo = lo;
+    if (neg) {
+        mlo = ~mlo + 1;
+        mhi = ~mhi + (mlo == 0 ? 1 : 0);
+    }
+    if ((mhi | mlo) == 0) return 0.0;
+    const int lz = mhi ? __clzll(static_cast<long long>(mhi)) : 64 + __clzll(static_cast<long long>(mlo));
+    // normalise so that the leading one is bit 127
+    uint64_t nhi, nlo;
+    if (lz >= 64) {
+        nhi = mlo << (lz - 64);
+        nlo = 0;
+    } else if (lz > 0) {
+        nhi = (mhi << lz) | (mlo >> (64 - lz));
+        nlo = mlo << lz;
+    } else {
+        nhi = mhi;
+        nlo = mlo;
+    }
+    uint64_t mant = nhi >> 11;  // 53 bits
+    const bool round_bit = (nhi >> 10) & 1;
+    const bool sticky = ((nhi & 0x3FFu) | nlo) != 0;
+    int msb = 127 - lz;
+    if (round_bit && (sticky || (mant & 1))) {
+        ++mant;
+        if (mant >> 53) {
+            mant >>= 1;
+            ++msb;
+        }
+    }
+    const int field = msb + scale_exp + 1023;
+    if (field <= 0 || field >= 2047) {
+        const double m = static_cast<double>(mant);  // exact, 53 bits
+        return ldexp(neg ? -m : m, msb - 52 + scale_exp);
+    }
+    const uint64_t bits = (neg ? (uint64_t{1} << 63) : 0) | (static_cast<uint64_t>(field) << 52) |
+                          (mant & ((uint64_t{1} << 52) - 1));
+    return __longlong_as_double(static_cast<long long>(bits));
 }
 
 // One step of the Chebyshev recurrence T_{k+1} = 2 u T_k - T_{k-1} in Q62
@@ -468,6 +518,7 @@ struct SplitShared {
     alignas(1024) uint16_t b_ring[kBStages][kBStepBytes / 2];   // 3 x 14 KiB
     alignas(16) int64_t ubasis[kTileN * kRows];                 // 64 KiB, [l][a ^ (l & 31)]
     alignas(16) int64_t red[kRedChunk * kRows];                 // 8 KiB, [j][row]
+    alignas(16) int64_t sums[kTileN][2];                        // 1 KiB, (lo, hi) per lookup
     TileMeta meta[kMetaBufs];
     uint64_t a_full[kAStages], a_empty[kAStages];
     uint64_t b_full[kBStages], b_empty[kBStages];
@@ -650,9 +701,12 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 break;
             }
             const TileMeta& meta = sh.meta[mb];
-            // u basis of the tile, two threads per lookup (even and odd degrees)
+            // u basis of the tile, two threads per lookup (even and odd degrees):
+            // lanes 0-15 of epilogue warp q take lookups 16q.. even, lanes
+            // 16-31 the same lookups odd, so each half-warp stores to 16
+            // distinct bank pairs
             {
-                const int l = e >> 1, parity = e & 1;
+                const int l = (e >> 5) * 16 + (e & 15), parity = (e >> 4) & 1;
                 ChebStride2 cheb;
                 cheb.init(fixed_from_double(meta.u[l], 62), parity);
                 for (int a = parity; a < kRows; a += 2) {
@@ -679,6 +733,10 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                                  : "r"(addr));
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (l0 + kRedChunk == kTileN) {  // accumulators read: the next tile's MMAs may start
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    mbar_arrive(&sh.acc_empty);
+                }
 #pragma unroll
                 for (int j = 0; j < kRedChunk; ++j) {
                     const int l = l0 + j;
@@ -720,39 +778,37 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                         shi += ohi + (nlo < slo ? 1 : 0);
                         slo = nlo;
                     }
-                    const int l = l0 + j;
-                    if (part == 0 && static_cast<uint32_t>(l) < count) {
-                        double value;
-                        const int64_t lo_signed = static_cast<int64_t>(slo);
-                        if ((shi == 0 && lo_signed >= 0) || (shi == -1 && lo_signed < 0)) {
-                            value = static_cast<double>(lo_signed);
-                        } else {
-                            value = static_cast<double>(shi) * 18446744073709551616.0 + static_cast<double>(slo);
-                        }
-                        value = ldexp(value, exponent - 55);
-                        const uint64_t info = meta.info[l];
-                        const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
-                        const int set = static_cast<int>((info >> 32) & 1);
-                        const int spins = static_cast<int>((info >> 33) & 3);
-                        const int i = static_cast<int>((info >> 35) & 31);
-                        const int jj = static_cast<int>((info >> 40) & 31);
-                        const int n = static_cast<int>((info >> 45) & 31);
-                        const int64_t mslot = (c * 2 + set) * 2;
-                        for (int spin = 0; spin < 2; ++spin) {
-                            if (!(spins & (1 << spin))) continue;
-                            double g = value;
-                            if (i == jj) {
-                                g = dadd(g, spin == 0 ? p.s.diag_up_shift : p.s.diag_down_shift);
-                                w.diag[(mslot + spin) * nmax + i] = g;
-                            }
-                            w.green[(mslot + spin) * per_c + i * n + jj] = dmul(g, p.s.scale);
-                        }
+                    if (part == 0) {
+                        sh.sums[l0 + j][0] = static_cast<int64_t>(slo);
+                        sh.sums[l0 + j][1] = shi;
                     }
                 }
                 epilogue_sync();
             }
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(&sh.acc_empty);
+            // finalisation: two full warps, one lookup per lane, so that the
+            // few FP64 operations are issued once per 32 lookups
+            if (e < kTileN && static_cast<uint32_t>(e) < count) {
+                const int l = e;
+                const double value = int128_to_double(sh.sums[l][1], static_cast<uint64_t>(sh.sums[l][0]), exponent - 55);
+                const uint64_t info = meta.info[l];
+                const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
+                const int set = static_cast<int>((info >> 32) & 1);
+                const int spins = static_cast<int>((info >> 33) & 3);
+                const int i = static_cast<int>((info >> 35) & 31);
+                const int jj = static_cast<int>((info >> 40) & 31);
+                const int n = static_cast<int>((info >> 45) & 31);
+                const int64_t mslot = (c * 2 + set) * 2;
+                for (int spin = 0; spin < 2; ++spin) {
+                    if (!(spins & (1 << spin))) continue;
+                    double g = value;
+                    if (i == jj) {
+                        g = dadd(g, spin == 0 ? p.s.diag_up_shift : p.s.diag_down_shift);
+                        w.diag[(mslot + spin) * nmax + i] = g;
+                    }
+                    w.green[(mslot + spin) * per_c + i * n + jj] = dmul(g, p.s.scale);
+                }
+            }
+            epilogue_sync();  // sums and meta are reused by the next tile
             mbar_arrive(&sh.meta_empty[mb]);
         }
     } else if (warp == kWarpCopy) {
