@@ -498,12 +498,15 @@ constexpr int kAStages = 3;
 constexpr int kBStages = 3;
 constexpr int kMetaBufs = 3;
 constexpr int kProducerWarps = 4;
-constexpr int kEpilogueWarps = 4;
-constexpr int kWarpCopy = 8;
-constexpr int kWarpMma = 9;
-constexpr int kAssemblyThreads = 320;
+constexpr int kEpilogueGroups = 2;                    // each reads all 128 TMEM lanes for half the lookups
+constexpr int kEpilogueWarps = 4 * kEpilogueGroups;
+constexpr int kGroupLookups = kTileN / kEpilogueGroups;
+constexpr int kWarpCopy = kProducerWarps + kEpilogueWarps;
+constexpr int kWarpMma = kWarpCopy + 1;
+constexpr int kAssemblyThreads = (kWarpMma + 1) * 32;
 constexpr int kRedChunk = 8;  // lookups per epilogue reduction chunk
-constexpr uint32_t kEpiBarrier = 1;  // named barrier of the epilogue warps
+constexpr uint32_t kEpiBarrier = 1;       // named barrier of all epilogue warps (votes)
+constexpr uint32_t kGroupBarrier0 = 2;    // named barriers of the epilogue groups: 2, 3
 
 struct TileMeta {
     double u[kTileN];
@@ -517,7 +520,7 @@ struct SplitShared {
     alignas(1024) uint16_t a_ring[kAStages][kAStageBytes / 2];  // 3 x 32 KiB
     alignas(1024) uint16_t b_ring[kBStages][kBStepBytes / 2];   // 3 x 14 KiB
     alignas(16) int64_t ubasis[kTileN * kRows];                 // 64 KiB, [l][a ^ (l & 31)]
-    alignas(16) int64_t red[kRedChunk * kRows];                 // 8 KiB, [j][row]
+    alignas(16) int64_t red[kEpilogueGroups][kRedChunk * kRows];  // 2 x 8 KiB, [j][row]
     alignas(16) int64_t sums[kTileN][2];                        // 1 KiB, (lo, hi) per lookup
     TileMeta meta[kMetaBufs];
     uint64_t a_full[kAStages], a_empty[kAStages];
@@ -533,11 +536,12 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-__device__ __forceinline__ void epilogue_sync() {
-    asm volatile("bar.sync %0, %1;" ::"n"(kEpiBarrier), "n"(kEpilogueWarps * 32) : "memory");
+// barrier of one epilogue group (128 threads)
+__device__ __forceinline__ void group_sync(int group) {
+    asm volatile("bar.sync %0, %1;" ::"r"(kGroupBarrier0 + group), "n"(128) : "memory");
 }
 
-// Barrier of the epilogue warps that also ORs a predicate over them: every
+// Barrier of all epilogue warps that also ORs a predicate over them: every
 // epilogue thread gets the same answer, so they leave the tile loop together
 // and none is left waiting at a named barrier.
 __device__ __forceinline__ bool epilogue_any(bool pred) {
@@ -568,6 +572,28 @@ __device__ __forceinline__ void tile_source(const SplitPlan& plan, uint32_t bloc
 // (T_{-2}, T_0) = (T_2, 1) or (T_{-1}, T_1) = (x, x). The recurrence in
 // w = T_2(x) has half the steps of the stride-1 one and its rounding error
 // grows like the square of the step count.
+struct ChebStride2;
+// T_r, T_{r+4}, T_{r+8}, ... (r = 0..3) of x in Q62 fixed point, by
+// T_{n+4} = 2 T_4(x) T_n - T_{n-4}, started from (T_{r-4}, T_r) = (T_{4-r}, T_r).
+struct ChebStride4 {
+    int64_t w, prev, cur;
+    __device__ __forceinline__ void init(int64_t xfix, int r) {
+        const int64_t one = int64_t{1} << 62;
+        const int64_t t2 = cheb_step_q62(xfix, xfix, one);
+        const int64_t t3 = cheb_step_q62(xfix, t2, xfix);
+        const int64_t t4 = cheb_step_q62(xfix, t3, t2);
+        w = t4;
+        cur = r == 0 ? one : r == 1 ? xfix : r == 2 ? t2 : t3;
+        prev = r == 0 ? t4 : r == 1 ? t3 : r == 2 ? t2 : xfix;
+    }
+    __device__ __forceinline__ int64_t next() {
+        const int64_t t = cur;
+        cur = cheb_step_q62(w, cur, prev);
+        prev = t;
+        return t;
+    }
+};
+
 struct ChebStride2 {
     int64_t w, prev, cur;
     __device__ __forceinline__ void init(int64_t xfix, int parity) {
@@ -597,6 +623,12 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
     const int lane = tid & 31;
     const int ksteps = plan.ksteps;
     const uint32_t ntiles = totals[1];
+    // each CTA takes a contiguous range of the block-sorted tile list, so the
+    // later tiles of a coefficient block find its slices in L2
+    const uint32_t tile_begin =
+        static_cast<uint32_t>((static_cast<uint64_t>(ntiles) * blockIdx.x) / gridDim.x);
+    const uint32_t tile_end =
+        static_cast<uint32_t>((static_cast<uint64_t>(ntiles) * (blockIdx.x + 1)) / gridDim.x);
 
     if (tid == 0) {
         for (int i = 0; i < kAStages; ++i) {
@@ -634,7 +666,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         const int l = warp * 16 + (lane & 15);  // lookup of this thread
         const int h = lane >> 4;                // parity of its degrees = which 8 of the 16 k
         uint32_t b_cnt = 0, tile_cnt = 0;
-        for (uint32_t tile = blockIdx.x; tile < ntiles && !failed(sh); tile += gridDim.x, ++tile_cnt) {
+        for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile, ++tile_cnt) {
             const SplitTile tl = tiles[tile];
             const int mb = static_cast<int>(tile_cnt % kMetaBufs);
             if (tile_cnt >= kMetaBufs && !mbar_wait(&sh.meta_empty[mb], ((tile_cnt / kMetaBufs) - 1) & 1)) {
@@ -687,29 +719,33 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         }
     } else if (warp < kProducerWarps + kEpilogueWarps) {
         // ------------------------------------------------------ epilogue --
-        const int e = tid - kProducerWarps * 32;  // row a of this thread
+        const int e = tid - kProducerWarps * 32;       // 0..255
+        const int group = e >> 7;                      // lookups [32 group, 32 group + 32)
+        const int row = e & (kRows - 1);               // TMEM lane = Chebyshev row a
         const uint32_t lane_base = tmem + (static_cast<uint32_t>((warp & 3) * 32) << 16);
         const int nu = p.s.nu;
         const int nmax = p.max_order;
         const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
+        int64_t* red = sh.red[group];
         uint32_t tile_cnt = 0;
-        for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tile_cnt) {
+        for (uint32_t tile = tile_begin; tile < tile_end; ++tile, ++tile_cnt) {
             const int mb = static_cast<int>(tile_cnt % kMetaBufs);
             const bool meta_ok = mbar_wait(&sh.meta_full[mb], (tile_cnt / kMetaBufs) & 1);
+            // (also: every epilogue thread is done with the previous tile's u basis)
             if (epilogue_any(!meta_ok || failed(sh))) {
                 sh.error = 1;
                 break;
             }
             const TileMeta& meta = sh.meta[mb];
-            // u basis of the tile, two threads per lookup (even and odd degrees):
-            // lanes 0-15 of epilogue warp q take lookups 16q.. even, lanes
-            // 16-31 the same lookups odd, so each half-warp stores to 16
-            // distinct bank pairs
+            // u basis of the tile, four threads per lookup (degrees r mod 4);
+            // each half-warp holds 16 lookups of one residue, so its stores
+            // hit 16 distinct bank pairs
             {
-                const int l = (e >> 5) * 16 + (e & 15), parity = (e >> 4) & 1;
-                ChebStride2 cheb;
-                cheb.init(fixed_from_double(meta.u[l], 62), parity);
-                for (int a = parity; a < kRows; a += 2) {
+                const int we = e >> 5;
+                const int l = 16 * (we & 3) + (lane & 15), r = 2 * (we >> 2) + (lane >> 4);
+                ChebStride4 cheb;
+                cheb.init(fixed_from_double(meta.u[l], 62), r);
+                for (int a = r; a < kRows; a += 4) {
                     const int64_t ta = cheb.next();
                     sh.ubasis[l * kRows + (a ^ (l & 31))] = a < nu ? ta : 0;
                 }
@@ -722,7 +758,8 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t count = meta.count;
             const int exponent = meta.exponent;
-            for (int l0 = 0; l0 < kTileN; l0 += kRedChunk) {
+            for (int c0 = 0; c0 < kGroupLookups; c0 += kRedChunk) {
+                const int l0 = group * kGroupLookups + c0;
                 uint32_t acc[kLevels][8];
 #pragma unroll
                 for (int lev = 0; lev < kLevels; ++lev) {
@@ -733,7 +770,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                                  : "r"(addr));
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
-                if (l0 + kRedChunk == kTileN) {  // accumulators read: the next tile's MMAs may start
+                if (c0 + kRedChunk == kGroupLookups) {  // accumulators read: the next tile's MMAs may start
                     asm volatile("tcgen05.fence::before_thread_sync;");
                     mbar_arrive(&sh.acc_empty);
                 }
@@ -749,23 +786,22 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                     const int64_t wfix = pl[0] * (int64_t{1} << 39) + pl[1] * (int64_t{1} << 31) +
                                          pl[2] * (int64_t{1} << 23) + pl[3] * (int64_t{1} << 15) + pl[4] * 128 +
                                          __float2int_rn(p78);
-                    const int64_t tf = sh.ubasis[l * kRows + (e ^ (l & 31))];
+                    const int64_t tf = sh.ubasis[l * kRows + (row ^ (l & 31))];
                     const uint64_t lo = static_cast<uint64_t>(wfix) * static_cast<uint64_t>(tf);
                     int64_t hi = __mul64hi(wfix, tf);
                     const uint64_t lo2 = lo + (uint64_t{1} << 61);
                     hi += lo2 < lo ? 1 : 0;
-                    sh.red[j * kRows + e] =
-                        static_cast<int64_t>((static_cast<uint64_t>(hi) << 2) | (lo2 >> 62));
+                    red[j * kRows + row] = static_cast<int64_t>((static_cast<uint64_t>(hi) << 2) | (lo2 >> 62));
                 }
-                epilogue_sync();
+                group_sync(group);
                 // 16 threads per lookup sum 8 rows each (rows part + 16 i), then 4 shuffle levels
                 {
-                    const int j = e >> 4, part = e & 15;
+                    const int j = row >> 4, part = row & 15;
                     uint64_t slo = 0;
                     int64_t shi = 0;
 #pragma unroll
                     for (int i = 0; i < kRows / 16; ++i) {
-                        const int64_t t = sh.red[j * kRows + part + 16 * i];
+                        const int64_t t = red[j * kRows + part + 16 * i];
                         const uint64_t nlo = slo + static_cast<uint64_t>(t);
                         shi += (t < 0 ? -1 : 0) + (nlo < slo ? 1 : 0);
                         slo = nlo;
@@ -783,12 +819,12 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                         sh.sums[l0 + j][1] = shi;
                     }
                 }
-                epilogue_sync();
+                group_sync(group);
             }
-            // finalisation: two full warps, one lookup per lane, so that the
-            // few FP64 operations are issued once per 32 lookups
-            if (e < kTileN && static_cast<uint32_t>(e) < count) {
-                const int l = e;
+            // finalisation: the group's first warp, one lookup per lane, so
+            // that the few FP64 operations are issued once per 32 lookups
+            const int l = group * kGroupLookups + row;
+            if (row < kGroupLookups && static_cast<uint32_t>(l) < count) {
                 const double value = int128_to_double(sh.sums[l][1], static_cast<uint64_t>(sh.sums[l][0]), exponent - 55);
                 const uint64_t info = meta.info[l];
                 const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
@@ -808,14 +844,14 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                     w.green[(mslot + spin) * per_c + i * n + jj] = dmul(g, p.s.scale);
                 }
             }
-            epilogue_sync();  // sums and meta are reused by the next tile
+            group_sync(group);  // sums are reused by the next tile
             mbar_arrive(&sh.meta_empty[mb]);
         }
     } else if (warp == kWarpCopy) {
         // ----------------------------------------- coefficient streaming --
         if (lane == 0) {
             uint32_t a_cnt = 0;
-            for (uint32_t tile = blockIdx.x; tile < ntiles && !failed(sh); tile += gridDim.x) {
+            for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile) {
                 const SplitTile tl = tiles[tile];
                 const uint16_t* a_src;
                 int exponent;
@@ -843,7 +879,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         if (lane == 0) {
             const uint32_t idesc = mma_idesc(kRows, kTileN);
             uint32_t a_cnt = 0, b_cnt = 0, tile_cnt = 0;
-            for (uint32_t tile = blockIdx.x; tile < ntiles && !failed(sh); tile += gridDim.x, ++tile_cnt) {
+            for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile, ++tile_cnt) {
                 if (tile_cnt > 0 && !mbar_wait(&sh.acc_empty, (tile_cnt - 1) & 1)) {
                     sh.error = 1;
                     break;
