@@ -233,6 +233,7 @@ int build_problem(cdet_context* ctx, const double* vertices, const int32_t* orde
     p->batch = batch;
     p->max_order = max_order;
     p->all_subsets = all_subsets;
+    p->fused_cdet = ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16 ? 1 : 0;
     for (int set = 0; set < 2; ++set) {
         const int r = set == 0 ? 2 : 1;
         for (int n = 0; n <= cdet::kMaxOrder; ++n) {
@@ -453,6 +454,7 @@ int run_fp64_on_scratch(cdet_context* ctx, const double* vertices, const int32_t
     Problem p;
     int rc = build_problem(ctx, vertices, orders, batch, max_order, 0, values, status, &p);
     if (rc != CDET_OK) return rc;
+    p.fused_cdet = 0;  // the FP64 form throughout, whatever assembly the context selects
     Scratch w;
     carve_scratch(scratch, batch, max_order, ws_warps, &w);
     cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);

@@ -382,8 +382,26 @@ __global__ void __launch_bounds__(128) principal_minors_fp64(const __grid_consta
 }
 
 // ---------------------------------------------------------- 3. CDet -------
+// One pair update of the recursion: acc -= dp[s] a[m \ s] and rhs += |that
+// term|. The reference's form rounds the product, the difference and the sum
+// separately (bit-identical FP64); the fused form, used behind the split
+// assembly whose Green matrices already differ from the FP64 ones at the
+// last bits, takes two FMAs (one rounding each, one FP64 operation fewer).
+template <bool Fused>
+__device__ __forceinline__ void pair_update(double dps, double am, double& acc, double& rhs) {
+    if constexpr (Fused) {
+        acc = __fma_rn(-dps, am, acc);
+        rhs = __fma_rn(fabs(dps), fabs(am), rhs);
+    } else {
+        const double term = dmul(dps, am);
+        acc = dsub(acc, term);
+        rhs = dadd(rhs, fabs(term));
+    }
+}
+
 // compute_dp_ztransform (integrand_replica_randomly_sampled.h:226-290) for
 // this lane's configuration: only masks holding vertex 0 are reduced.
+template <bool Fused>
 __device__ double cdet_single(const double* a, double* dp, int n, double threshold) {
     const bool filter = threshold > 0.0;
     dp[1 * kWarp] = a[1 * kWarp];
@@ -397,9 +415,7 @@ __device__ double cdet_single(const double* a, double* dp, int n, double thresho
             // submasks holding vertex 0, in the reference's descending order
             for (uint32_t s = (rest - 1u) & rest;; s = (s - 1u) & rest) {
                 const uint32_t sub = (s << 1) | 1u;
-                const double term = dmul(dp[sub * kWarp], a[(mask ^ sub) * kWarp]);
-                acc = dsub(acc, term);
-                rhs = dadd(rhs, fabs(term));
+                pair_update<Fused>(dp[sub * kWarp], a[(mask ^ sub) * kWarp], acc, rhs);
                 if (s == 0) break;
             }
             if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
@@ -412,6 +428,7 @@ __device__ double cdet_single(const double* a, double* dp, int n, double thresho
 
 // compute_dp_ztransform_all_subsets (:292-347): every mask, anchored at its
 // lowest vertex.
+template <bool Fused>
 __device__ void cdet_all(const double* a, double* dp, int n, double threshold) {
     const bool filter = threshold > 0.0;
     dp[0] = 0.0;
@@ -425,9 +442,7 @@ __device__ void cdet_all(const double* a, double* dp, int n, double threshold) {
             double rhs = fabs(acc);
             for (uint32_t s = (rest - 1u) & rest;; s = (s - 1u) & rest) {
                 const uint32_t sub = s | anchor;
-                const double term = dmul(dp[sub * kWarp], a[(mask ^ sub) * kWarp]);
-                acc = dsub(acc, term);
-                rhs = dadd(rhs, fabs(term));
+                pair_update<Fused>(dp[sub * kWarp], a[(mask ^ sub) * kWarp], acc, rhs);
                 if (s == 0) break;
             }
             if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
@@ -470,7 +485,8 @@ __global__ void __launch_bounds__(128) cdet_fp64(const __grid_constant__ Problem
             } else {
                 const double* a = w.a_int + (g * 2 + set) * full * kWarp + lane;
                 double* dp = w.dp_int + (g * 2 + set) * full * kWarp + lane;
-                const double cset = cdet_single(a, dp, n, threshold);
+                const double cset = p.fused_cdet ? cdet_single<true>(a, dp, n, threshold)
+                                                 : cdet_single<false>(a, dp, n, threshold);
                 const DDPair pf = p.pref_dd[set][n];
                 value[set] = dd_mul(DD{pf.hi, pf.lo}, DD{cset, 0.0});
                 if (!dd_finite(value[set])) status |= kStatusNonFinite;
@@ -486,7 +502,8 @@ __global__ void __launch_bounds__(128) cdet_fp64(const __grid_constant__ Problem
             const int r = set == 0 ? 2 : 1;
             const double* a = w.a_int + (g * 2 + set) * full * kWarp + lane;
             double* dp = w.dp_int + (g * 2 + set) * full * kWarp + lane;
-            cdet_all(a, dp, n, threshold);
+            if (p.fused_cdet) cdet_all<true>(a, dp, n, threshold);
+            else cdet_all<false>(a, dp, n, threshold);
             const uint32_t count = 1u << n;
             for (uint32_t mask = 0; mask < count; ++mask) {
                 const int k = __popc(mask);
@@ -508,6 +525,182 @@ __global__ void __launch_bounds__(128) cdet_fp64(const __grid_constant__ Problem
     if (status) atomicOr(p.status + c, status);
 }
 
+
+// ------------------------------------------------- 3b. CDet, warp form ----
+// The single-top recursion behind the split assembly, one warp per
+// (configuration, set), a and dp in shared memory. The masks of one popcount
+// level are independent; each gets L lanes (a power of two) that split its
+// submasks on the L highest set bits and add their partial sums with
+// shuffles, so the FP64 pipe sees few idle lanes even at the top levels.
+// Each pair update is one FP64 FMA. The round-off filter's magnitude sum
+// runs in FP32 on shadow copies scaled by 2^(-e |m|) (e: binary exponent of
+// the first singleton), which keeps all terms of a mask near 1 whatever the
+// order; a shadow is clamped to the FP32 range, so an overflow can only keep a
+// value, never zero it.
+constexpr int kWarpCdetMaxOrder = 10;
+constexpr int kWarpCdetWarps = 8;
+
+__device__ const uint16_t kBinom[11][11] = {
+    {1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+    {1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+    {1, 2, 1, 0, 0, 0, 0, 0, 0, 0, 0},
+    {1, 3, 3, 1, 0, 0, 0, 0, 0, 0, 0},
+    {1, 4, 6, 4, 1, 0, 0, 0, 0, 0, 0},
+    {1, 5, 10, 10, 5, 1, 0, 0, 0, 0, 0},
+    {1, 6, 15, 20, 15, 6, 1, 0, 0, 0, 0},
+    {1, 7, 21, 35, 35, 21, 7, 1, 0, 0, 0},
+    {1, 8, 28, 56, 70, 56, 28, 8, 1, 0, 0},
+    {1, 9, 36, 84, 126, 126, 84, 36, 9, 1, 0},
+    {1, 10, 45, 120, 210, 252, 210, 120, 45, 10, 1}};
+
+// Subset of size m of {0, ..., N-1} with colex rank r, as a bit mask.
+__device__ __forceinline__ uint32_t colex_unrank(uint32_t r, int m, int N) {
+    uint32_t set = 0;
+    int hi = N - 1;
+    for (int i = m; i >= 1; --i) {
+        int c = i - 1;
+        while (c + 1 <= hi && kBinom[c + 1][i] <= r) ++c;
+        set |= 1u << c;
+        r -= kBinom[c][i];
+        hi = c - 1;
+    }
+    return set;
+}
+
+// |v| * 2^k as a float, clamped to the finite range (|k| <= 1000).
+__device__ __forceinline__ float scaled_magnitude(double v, int k) {
+    const double p2 = __longlong_as_double(static_cast<long long>(1023 + k) << 52);
+    return fminf(static_cast<float>(fabs(dmul(v, p2))), 3.0e38f);
+}
+
+__global__ void __launch_bounds__(kWarpCdetWarps * 32) cdet_split_warp(const __grid_constant__ Problem p,
+                                                                       const __grid_constant__ Scratch w) {
+    extern __shared__ __align__(16) unsigned char cdet_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nmax = p.max_order;
+    const int full_n = 1 << nmax;
+    double* a_s = reinterpret_cast<double*>(cdet_smem) + warp * 2 * full_n;
+    double* dp_s = a_s + full_n;
+    float* af_s = reinterpret_cast<float*>(reinterpret_cast<double*>(cdet_smem) + kWarpCdetWarps * 2 * full_n) +
+                  warp * 2 * full_n;
+    float* dpf_s = af_s + full_n;
+    const Scalars& s = p.s;
+    const double threshold = dmul(s.z_eps0, s.z_safety);
+    const bool filter = threshold > 0.0;
+    const float thresholdf = static_cast<float>(threshold);
+    const int64_t g = blockIdx.x;
+    for (int cl = warp; cl < kWarp; cl += kWarpCdetWarps) {
+        const int64_t c = g * kWarp + cl;
+        if (c >= p.batch) break;
+        const int n = __ldg(p.orders + c);
+        if (n < 1 || n > nmax) continue;
+        const double* diag = w.diag + c * 2 * 2 * nmax;
+        int32_t status = 0;
+        DD value_twisted{0.0, 0.0}, value_ordinary{0.0, 0.0};
+#pragma unroll
+        for (int set = 0; set < 2; ++set) {
+            const int r = set == 0 ? 2 : 1;
+            DD& value = set == 0 ? value_twisted : value_ordinary;
+            if (n == 1) {
+                value = DD{order1_value(s, diag[(set * 2) * nmax], diag[(set * 2 + 1) * nmax], r), 0.0};
+                continue;
+            }
+            const double* ag = w.a_int + (g * 2 + set) * static_cast<int64_t>(full_n) * kWarp + cl;
+            const int count = 1 << n;
+            int e = 0;
+            {
+                const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(ag[1 * kWarp]));
+                const int field = static_cast<int>((bits >> 52) & 0x7FF);
+                if (field != 0 && field != 0x7FF) e = field - 1023;
+                e = e > 90 ? 90 : (e < -90 ? -90 : e);  // |e| * nmax stays within 1000
+            }
+            for (int m = lane; m < count; m += kWarp) {
+                const double v = ag[static_cast<int64_t>(m) * kWarp];
+                a_s[m] = v;
+                af_s[m] = scaled_magnitude(v, -e * __popc(m));
+            }
+            __syncwarp();
+            if (lane == 0) {
+                dp_s[1] = a_s[1];
+                dpf_s[1] = af_s[1];
+            }
+            __syncwarp();
+            const int nbits = n - 1;
+            for (int k = 2; k <= n; ++k) {
+                const int kk = k - 1;                 // rest = mask >> 1 has kk of nbits bits
+                const int masks = kBinom[nbits][kk];
+                const int subs = 1 << kk;             // submasks of rest, rest itself included
+                for (int base = 0; base < masks;) {
+                    const int remaining = masks - base;
+                    int L = 1, take = kWarp;
+                    if (remaining < kWarp) {
+                        while (L * 2 * remaining <= kWarp && L * 2 <= subs) L *= 2;
+                        take = remaining;
+                        if (4 * L * remaining < 3 * kWarp && L * 2 <= subs) {  // < 75% of lanes busy
+                            L *= 2;
+                            take = kWarp / L;
+                        }
+                    }
+                    const int q = __ffs(L) - 1;
+                    const int idx = base + (lane >> q);
+                    const int j = lane & (L - 1);
+                    const bool active = (lane >> q) < take && idx < masks;
+                    double part = 0.0;
+                    float rpart = 0.0f;
+                    uint32_t mask = 0;
+                    if (active) {
+                        const uint32_t rest = colex_unrank(static_cast<uint32_t>(idx), kk, nbits);
+                        mask = (rest << 1) | 1u;
+                        uint32_t top = 0, low = rest;
+                        for (int t = 0; t < q; ++t) {
+                            const uint32_t hb = 1u << (31 - __clz(low));
+                            top |= hb;
+                            low ^= hb;
+                        }
+                        uint32_t fixed = 0, tb = top;
+                        for (int t = 0; t < q; ++t) {
+                            const uint32_t lb = tb & (~tb + 1u);
+                            if ((j >> t) & 1) fixed |= lb;
+                            tb ^= lb;
+                        }
+                        for (uint32_t sl = low;; sl = (sl - 1u) & low) {
+                            const uint32_t sm = fixed | sl;
+                            if (sm != rest) {
+                                const uint32_t sub = (sm << 1) | 1u;
+                                const uint32_t other = mask ^ sub;
+                                part = __fma_rn(dp_s[sub], a_s[other], part);
+                                rpart = fmaf(dpf_s[sub], af_s[other], rpart);
+                            }
+                            if (sl == 0) break;
+                        }
+                    }
+                    for (int off = 1; off < L; off <<= 1) {
+                        part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));
+                        rpart += __shfl_xor_sync(0xffffffffu, rpart, off);
+                    }
+                    if (active && j == 0) {
+                        double acc = dsub(a_s[mask], part);
+                        const float rhs = af_s[mask] + rpart;
+                        if (filter && scaled_magnitude(acc, -e * k) < thresholdf * rhs) acc = 0.0;
+                        dp_s[mask] = acc;
+                        dpf_s[mask] = scaled_magnitude(acc, -e * k);
+                    }
+                    base += take;
+                }
+                __syncwarp();
+            }
+            const DDPair pf = p.pref_dd[set][n];
+            value = dd_mul(DD{pf.hi, pf.lo}, DD{dp_s[count - 1], 0.0});
+            if (!dd_finite(value)) status |= kStatusNonFinite;
+            __syncwarp();  // the next set reuses the arrays
+        }
+        if (lane == 0) {
+            const DD result = dd_sub(value_twisted, dd_mul(DD{2.0, 0.0}, value_ordinary));
+            p.values[c] = dadd(result.hi, result.lo);
+            if (status) atomicOr(p.status + c, status);
+        }
+    }
+}
 }  // namespace
 
 size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).total; }
@@ -594,7 +787,18 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
     if (err != cudaSuccess) return err;
     mark(3);
 
-    cdet_fp64<<<static_cast<unsigned>((p.batch + threads - 1) / threads), threads, 0, stream>>>(p, w);
+    if (p.fused_cdet && !p.all_subsets && p.max_order <= kWarpCdetMaxOrder) {
+        // split assembly: warp-per-configuration recursion in shared memory
+        const size_t csmem = static_cast<size_t>(kWarpCdetWarps) * (2 * sizeof(double) + 2 * sizeof(float)) *
+                             (size_t{1} << p.max_order);
+        err = cudaFuncSetAttribute(cdet_split_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(csmem));
+        if (err != cudaSuccess) return err;
+        cdet_split_warp<<<static_cast<unsigned>((p.batch + kWarp - 1) / kWarp), kWarpCdetWarps * kWarp, csmem,
+                          stream>>>(p, w);
+    } else {
+        cdet_fp64<<<static_cast<unsigned>((p.batch + threads - 1) / threads), threads, 0, stream>>>(p, w);
+    }
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     mark(4);

@@ -57,6 +57,8 @@ struct Problem {
     int64_t batch;
     int max_order;
     int all_subsets;          // 0: one value per configuration; 1: 2^max_order values
+    int fused_cdet;           // 1: CDet pair updates as FMAs (split assembly); 0: the reference's
+                              // separately rounded multiply, subtract and add
     DDPair pref_dd[2][kMaxOrder + 1];   // cdet_order_prefactor<DoubleDouble>, [set][order]
     double pref_ld[2][kMaxOrder + 1];   // cdet_order_prefactor<double> (host long double)
     double* values;

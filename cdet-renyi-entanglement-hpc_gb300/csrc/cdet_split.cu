@@ -894,19 +894,23 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t a_base = smem_addr(sh.a_ring[sa]);
-                    const uint32_t b_base = smem_addr(sh.b_ring[sb]);
+                    // descriptors of the stage's first slices; a slice further
+                    // on is the same descriptor plus its byte offset / 16 (the
+                    // 14-bit address field cannot carry: shared memory < 256 KiB)
+                    const uint64_t a_desc = smem_desc(smem_addr(sh.a_ring[sa]), 128, 256);
+                    const uint64_t b_desc = smem_desc(smem_addr(sh.b_ring[sb]), 128, 256);
+                    const uint32_t first = ks > 0 ? 1u : 0u;
+#pragma unroll
                     for (int t = 1; t <= kSlices; ++t) {
+#pragma unroll
                         for (int tp = 1; t + tp <= kLevels + 1; ++tp) {
                             const int level = t + tp - 2;
-                            mma_f16(tmem + level * kTileN,
-                                     smem_desc(a_base + (t - 1) * (kRows * kKStep * 2), 128, 256),
-                                     smem_desc(b_base + (tp - 1) * (kTileN * kKStep * 2), 128, 256), idesc,
-                                     (ks > 0 || t > 1) ? 1u : 0u);
+                            mma_f16(tmem + level * kTileN, a_desc + (t - 1) * (kRows * kKStep * 2 / 16),
+                                    b_desc + (tp - 1) * (kTileN * kKStep * 2 / 16), idesc, t > 1 ? 1u : first);
                         }
                     }
-                    mma_f16(tmem + (kLevels - 1) * kTileN, smem_desc(a_base + kSlices * (kRows * kKStep * 2), 128, 256),
-                             smem_desc(b_base, 128, 256), idesc, 1u);
+                    mma_f16(tmem + (kLevels - 1) * kTileN, a_desc + kSlices * (kRows * kKStep * 2 / 16), b_desc,
+                            idesc, 1u);
                     mma_commit(&sh.a_empty[sa]);
                     mma_commit(&sh.b_empty[sb]);
                 }
