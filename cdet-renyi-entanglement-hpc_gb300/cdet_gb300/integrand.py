@@ -164,6 +164,16 @@ class CdetIntegrand:
         L.check(self._lib.cdet_counters(self._ctx, C.byref(calls), C.byref(fallbacks)))
         return calls.value, fallbacks.value
 
+    def diagonal_order1_density(self) -> np.ndarray:
+        """Deterministic order-1 diagonal observable of the bound tables,
+        [twisted - 2 ordinary, twisted, ordinary]
+        (diagonal_green_observable.h:237-366), bit-identical to the reference."""
+        out = np.zeros(3)
+        L.check(self._lib.cdet_diagonal_order1_density(self._ctx, float(self.params.alpha_up),
+                                                       float(self.params.alpha_down),
+                                                       out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
     def last_launch_count(self) -> int:
         return int(self._lib.cdet_last_launch_count(self._ctx))
 

@@ -30,7 +30,7 @@ EXPORTED = (
     "cdet_integrand_host", "cdet_all_subsets_host", "cdet_counters", "cdet_last_error",
     "cdet_last_launch_count", "cdet_profile_enable", "cdet_profile_read",
     "cdet_set_assembly", "cdet_prepare_split", "cdet_assemble_device",
-    "cdet_integrand_device_noalloc",
+    "cdet_integrand_device_noalloc", "cdet_diagonal_order1_density",
 )
 
 ASSEMBLY_FP64 = 0
@@ -80,6 +80,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_integrand_host.argtypes = [vp, vp, vp, i64, i32, vp, vp]
     lib.cdet_all_subsets_host.argtypes = [vp, vp, i32, i64, vp, vp]
     lib.cdet_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.cdet_diagonal_order1_density.argtypes = [vp, C.c_double, C.c_double, _DP]
     lib.cdet_last_error.restype = C.c_char_p
     lib.cdet_last_launch_count.argtypes = [vp]
     lib.cdet_integrand_device_noalloc.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp]

@@ -668,6 +668,29 @@ int cdet_assemble_device(cdet_context* ctx, const double* vertices, const int32_
     return CDET_OK;
 }
 
+int cdet_diagonal_order1_density(cdet_context* ctx, double alpha_up, double alpha_down, double* out) {
+    if (!ctx || !out) return fail(CDET_ERR_INVALID, "bad argument");
+    DeviceGuard guard(ctx->device);
+    const cdet::TableDev* tables[4];
+    for (int k = 0; k < 4; ++k) {
+        tables[k] = resolve(ctx, k);
+        if (!tables[k]) return fail(CDET_ERR_STATE, "Green-function tables have not been uploaded");
+    }
+    const cdet_runtime_scalars& s = ctx->scalars;
+    if (s.u == 0.0) return fail(CDET_ERR_INVALID, "The diagonal observable is undefined for U = 0");
+    const int sites = s.n1 * s.n2;
+    double* buf = nullptr;
+    cudaError_t err = cudaMalloc(&buf, (static_cast<size_t>(3) * sites + 4) * sizeof(double));
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(diagonal observable)");
+    double* items = buf + 4;
+    err = cdet::launch_diagonal_order1(tables, s.n1, s.n2, s.cheb_nu, s.cheb_nv, s.beta, s.u, alpha_up,
+                                       alpha_down, items, buf, nullptr);
+    if (err == cudaSuccess) err = cudaMemcpy(out, buf, 3 * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (err != cudaSuccess) return cuda_fail(err, "diagonal observable");
+    return CDET_OK;
+}
+
 int cdet_profile_enable(cdet_context* ctx, int enable) {
     if (!ctx) return fail(CDET_ERR_INVALID, "null context");
     ctx->profiling = enable != 0;

@@ -101,6 +101,13 @@ size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps);
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out);
 // assembly = true launches the FP64 Green-matrix assembly first; false
 // expects the Green matrices already in scratch (split-precision assembly).
+// Order-1 diagonal observable: items[3 * N1 * N2] scratch, out[3] = {twisted -
+// 2 ordinary, twisted, ordinary}; tables in kind order (twisted up, twisted
+// down, ordinary up, ordinary down).
+cudaError_t launch_diagonal_order1(const TableDev* const tables[4], int n1, int n2, int nu, int nv, double beta,
+                                   double u, double alpha_up, double alpha_down, double* items, double* out,
+                                   cudaStream_t stream);
+
 cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& scratch, int sm_count,
                                   cudaStream_t stream, const KernelEvents* events, bool assembly = true);
 

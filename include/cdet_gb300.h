@@ -154,6 +154,18 @@ int cdet_integrand_host(cdet_context* ctx, const double* vertices, const int32_t
 int cdet_all_subsets_host(cdet_context* ctx, const double* vertices, int envelope_order,
                           int64_t batch, double* values, int32_t* status);
 
+/* Deterministic order-1 diagonal observable from the bound tables: out[0] =
+ * the normalised first-order coefficient of ln Z_2[A] (twisted - 2 ordinary;
+ * normalized_log_partition_first_order_density_dd and
+ * diagonal_observable_density_dd, diagonal_green_observable.h:305-366),
+ * out[1] = the twisted part (replica_log_partition_first_order_density_typed,
+ * :237-273), out[2] = the ordinary part (:275-303). alpha_up and alpha_down
+ * are ALPHA_UP and ALPHA_DOWN as doubles (the shifts are formed from them in
+ * double, as the reference does). Bit-identical to the reference's double
+ * build. Blocking; fails with CDET_ERR_INVALID when U == 0 (the reference
+ * throws "The diagonal observable is undefined for U = 0"). */
+int cdet_diagonal_order1_density(cdet_context* ctx, double alpha_up, double alpha_down, double* out);
+
 /* Counters of the host entry points: integrand calls and whole-matrix
  * principal-minor fallbacks (runtime_counters.h:14-51). */
 int cdet_counters(const cdet_context* ctx, uint64_t* integrand_calls, uint64_t* fpm_fallbacks);

@@ -104,6 +104,16 @@ public:
         if (rc != CDET_OK && rc != CDET_ERR_VALUE) check(rc);
     }
 
+    // Deterministic order-1 diagonal observable of the uploaded tables
+    // (diagonal_observable_density_dd, diagonal_green_observable.h:357-366):
+    // the normalised coefficient twisted - 2 ordinary. The reference reads
+    // ALPHA_UP and ALPHA_DOWN from its globals; pass their double values.
+    double diagonal_observable_density(double alpha_up, double alpha_down) {
+        double out[3] = {0.0, 0.0, 0.0};
+        check(cdet_diagonal_order1_density(ctx_.get(), alpha_up, alpha_down, out));
+        return out[0];
+    }
+
     // Makes this object the one the free functions below use.
     void install() { current() = this; }
 

@@ -93,6 +93,7 @@ class Oracle:
         lib.oracle_prefactor_dd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _DP, _DP]
         lib.oracle_prefactor_ld.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
         lib.oracle_prefactor_ld.restype = C.c_double
+        lib.oracle_diagonal_order1.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, _DP]
         self.scalars = OracleScalars(**{k: scalars[k] for k, _ in OracleScalars._fields_})
         self._keep = {k: _as_numpy_table(tables[k]) for k in KINDS}
         tabs = {}
@@ -151,6 +152,15 @@ class Oracle:
         st = self.lib.oracle_fill_green(C.byref(self.scalars), C.byref(tu), C.byref(td), _ptr(v),
                                         n, replica_count, _ptr(mu), _ptr(md), _ptr(du), _ptr(dd))
         return mu.reshape(n, n), md.reshape(n, n), du, dd, st
+
+    def diagonal_order1(self, alpha_up: float, alpha_down: float) -> np.ndarray:
+        """[twisted - 2 ordinary, twisted, ordinary] order-1 diagonal densities."""
+        out = np.zeros(3)
+        rc = self.lib.oracle_diagonal_order1(C.byref(self.scalars), C.byref(self.tables),
+                                             float(alpha_up), float(alpha_down), _ptr(out))
+        if rc != 0:
+            raise RuntimeError("The diagonal observable is undefined for U = 0")
+        return out
 
     @staticmethod
     def _lib():
@@ -242,6 +252,7 @@ class Reference:
                                           C.c_double, C.c_int, _DP]
         lib.ref_fpm_fallbacks.restype = C.c_ulonglong
         lib.ref_sample_vertices.argtypes = [C.c_ulonglong, C.c_int, _DP]
+        lib.ref_diagonal_order1.argtypes = [_DP]
 
     def _check(self, rc):
         if rc != 0:
@@ -296,6 +307,12 @@ class Reference:
         v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 4)
         out = np.zeros(1 << v.shape[0])
         self._check(self.lib.ref_eval_all_subsets(_ptr(v), v.shape[0], _ptr(out)))
+        return out
+
+    def diagonal_order1(self) -> np.ndarray:
+        """[normalised hi, twisted, ordinary, normalised lo] from the reference."""
+        out = np.zeros(4)
+        self._check(self.lib.ref_diagonal_order1(_ptr(out)))
         return out
 
     def mat2pm(self, a, tol, shift):

@@ -701,3 +701,98 @@ int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
     batch_job proto = {s, t, unit_vertices, NULL, envelope_order, 1, 0, 0, values, status};
     return run_batch(proto, batch, threads);
 }
+
+/* ------------------------------------------ order-1 diagonal observable --- */
+
+/* chebyshev_uniform_integral_weight (diagonal_green_observable.h:57-67):
+ * integral of T_k over [-1, 1]. */
+static double uniform_integral_weight(int degree) {
+    if (degree % 2 != 0) return 0.0;
+    if (degree == 0) return 2.0;
+    const double d = (double)degree;
+    return 2.0 / (1.0 - d * d);
+}
+
+/* lower_diagonal_line_coefficients (:69-96): the lower-branch block of
+ * (replica, replica, site, site) summed over v (T_b(1) = 1), per u row. */
+static void diagonal_line(const oracle_table* t, int replica, int x, int y, int nu, int nv,
+                          int n1, int n2, double* line) {
+    const uint64_t base = sitepair_index(replica, replica, x, y, x, y, n1, n2) * (uint64_t)nu * (uint64_t)nv;
+    const double* c = t->lower_coeffs + base;
+    for (int a = 0; a < nu; ++a) {
+        double sum = 0.0;
+        for (int b = 0; b < nv; ++b) sum += c[(size_t)a * nv + b];
+        line[a] = sum;
+    }
+}
+
+/* integrate_chebyshev_line (:121-130) */
+static double integrate_line(const double* line, int nu, double beta) {
+    double integral = 0.0;
+    for (int k = 0; k < nu; ++k) integral += line[k] * uniform_integral_weight(k);
+    return beta * integral / 2.0;
+}
+
+/* integrate_chebyshev_line_product (:141-159) */
+static double integrate_line_product(const double* lhs, const double* rhs, int nu, double beta) {
+    double integral = 0.0;
+    for (int i = 0; i < nu; ++i) {
+        const double lv = lhs[i];
+        for (int j = 0; j < nu; ++j) {
+            const double rv = rhs[j];
+            const int diff = i > j ? i - j : j - i;
+            const double w = (uniform_integral_weight(i + j) + uniform_integral_weight(diff)) / 2.0;
+            integral += lv * rv * w;
+        }
+    }
+    return beta * integral / 2.0;
+}
+
+/* integrate_diagonal_shifted_product_from_tables (:161-180) */
+static double diagonal_site_term(const oracle_table* up, const oracle_table* down, int replica, int x,
+                                 int y, const oracle_scalars* s, double shift_up, double shift_down,
+                                 double* up_line, double* down_line) {
+    diagonal_line(up, replica, x, y, s->cheb_nu, s->cheb_nv, s->n1, s->n2, up_line);
+    diagonal_line(down, replica, x, y, s->cheb_nu, s->cheb_nv, s->n1, s->n2, down_line);
+    const double up_integral = integrate_line(up_line, s->cheb_nu, s->beta);
+    const double down_integral = integrate_line(down_line, s->cheb_nu, s->beta);
+    const double product = integrate_line_product(up_line, down_line, s->cheb_nu, s->beta);
+    return product + shift_up * down_integral + shift_down * up_integral;
+}
+
+int oracle_diagonal_order1(const oracle_scalars* s, const oracle_tables* t, double alpha_up,
+                           double alpha_down, double* out) {
+    if (s->u == 0.0) return 1;
+    const double shift_up = alpha_down / s->u;   /* diagonal_up_shift, :255-256 */
+    const double shift_down = alpha_up / s->u;
+    double* up_line = (double*)malloc(sizeof(double) * (size_t)s->cheb_nu);
+    double* down_line = (double*)malloc(sizeof(double) * (size_t)s->cheb_nu);
+    if (!up_line || !down_line) {
+        free(up_line);
+        free(down_line);
+        return 2;
+    }
+    const double sites = (double)s->n1 * (double)s->n2;
+    /* replica_log_partition_first_order_density_typed (:237-273) */
+    double twisted_sum = 0.0;
+    for (int replica = 0; replica < 2; ++replica)
+        for (int y = 0; y < s->n2; ++y)
+            for (int x = 0; x < s->n1; ++x)
+                twisted_sum += diagonal_site_term(&t->twisted_up, &t->twisted_down, replica, x, y, s,
+                                                  shift_up, shift_down, up_line, down_line);
+    const double twisted = -s->u * twisted_sum / sites;
+    /* ordinary_log_partition_first_order_density_typed (:275-303) */
+    double ordinary_sum = 0.0;
+    for (int y = 0; y < s->n2; ++y)
+        for (int x = 0; x < s->n1; ++x)
+            ordinary_sum += diagonal_site_term(&t->ordinary_up, &t->ordinary_down, 0, x, y, s, shift_up,
+                                               shift_down, up_line, down_line);
+    const double ordinary = -s->u * ordinary_sum / sites;
+    free(up_line);
+    free(down_line);
+    /* normalized_log_partition_first_order_density_dd (:305-323) */
+    out[0] = twisted - 2.0 * ordinary;
+    out[1] = twisted;
+    out[2] = ordinary;
+    return 0;
+}

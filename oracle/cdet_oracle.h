@@ -100,6 +100,15 @@ int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
                              const double* unit_vertices, int envelope_order, int64_t batch,
                              double* values, int32_t* status, int threads);
 
+/* Deterministic order-1 diagonal observable (diagonal_green_observable.h:237-327):
+ * out[0] = twisted - 2 * ordinary (the normalised first-order coefficient of
+ * ln Z_2[A]), out[1] = the twisted (two-replica) part, out[2] = the ordinary
+ * part. alpha_up and alpha_down are the double values of ALPHA_UP and
+ * ALPHA_DOWN; the shifts are formed from them in double as the reference does.
+ * Returns 1 (and writes nothing) when U == 0, which the reference rejects. */
+int oracle_diagonal_order1(const oracle_scalars* s, const oracle_tables* t, double alpha_up,
+                           double alpha_down, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,8 +26,11 @@
 //   ref_green_replica      -> ReplicaGreenCalculator::green_replica_matrix
 //                             (replica_free_greens.h:314-331), the direct kernel
 //                             solve the Chebyshev accuracy audit compares with.
+//   ref_diagonal_order1    -> normalized_log_partition_first_order_density_dd and its
+//                             twisted / ordinary parts (diagonal_green_observable.h:237-327)
 
 #include "cdet/cdet_integrand_evaluator.h"
+#include "cdet/diagonal_green_observable.h"
 #include "cdet/load_data.h"
 #include "cdet/mcmcmc_sampler.h"
 
@@ -291,5 +294,19 @@ void ref_sample_vertices(unsigned long long seed, int count, double* out) {
 unsigned long long ref_fpm_fallbacks() { return snapshot_cdet_runtime_counters().fpm_fallbacks; }
 
 void ref_reset_counters() { reset_cdet_runtime_counters(); }
+
+int ref_diagonal_order1(double* out) {
+    return guarded([&] {
+        const auto& tu = std::get<PiecewiseChebyshevTable<double>>(g_table_up);
+        const auto& td = std::get<PiecewiseChebyshevTable<double>>(g_table_down);
+        const auto& ou = std::get<PiecewiseChebyshevTable<double>>(g_table_ordinary_up);
+        const auto& od = std::get<PiecewiseChebyshevTable<double>>(g_table_ordinary_down);
+        out[1] = replica_log_partition_first_order_density_typed<double>(tu, td);
+        out[2] = ordinary_log_partition_first_order_density_typed<double>(ou, od);
+        const DoubleDouble normalized = normalized_log_partition_first_order_density_dd();
+        out[0] = normalized.hi;
+        out[3] = normalized.lo;
+    });
+}
 
 }  // extern "C"
