@@ -39,6 +39,9 @@ WORKLOAD = {
 }
 BATCH = 65536
 SPLIT_SLICE_PAIRS = 29  # tcgen05.mma per K step of the split assembly
+# DRAM bytes (read + write) of one split_assembly launch of the default
+# workload, from one ncu capture (profiles/split_assembly_8x8_d128_n10.md)
+SPLIT_ASSEMBLY_DRAM_BYTES = 12.481185e9 + 0.900138e9
 ORDER = 10
 L2_FLUSH_BYTES = 512 << 20
 PRESET = "8x8-d128"
@@ -296,7 +299,9 @@ def run_gpu(args):
                     "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                     "frac": achieved / bf16_peak,
                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json bf16_tflops, burst; fp16 dense rate is the same)",
-                    "traffic": None,
+                    "traffic": SPLIT_ASSEMBLY_DRAM_BYTES if PRESET == "8x8-d128" and BATCH == 65536 else None,
+                    "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                    "profiles/split_assembly_8x8_d128_n10.md)",
                     "algorithmic": f"lookups x {SPLIT_SLICE_PAIRS} slice pairs x 2 x nu x nv"}
     else:
         per_launch_ms = stage_ms[1] / args.steps
