@@ -12,7 +12,8 @@ LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libcdet_gb300.so")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 
-SOURCES = ["cdet_kernels.cu", "cdet_split.cu", "cdet_capi.cu", "cdet_noalloc.cu", "cdet_diagonal.cu"]
+SOURCES = ["cdet_kernels.cu", "cdet_split.cu", "cdet_capi.cu", "cdet_noalloc.cu", "cdet_diagonal.cu",
+           "cdet_mcmcmc.cu"]
 HEADERS = ["cdet_device.cuh", "cdet_kernels.cuh"]
 
 NVCC_FLAGS = [

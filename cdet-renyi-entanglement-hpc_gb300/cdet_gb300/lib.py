@@ -31,6 +31,8 @@ EXPORTED = (
     "cdet_last_launch_count", "cdet_profile_enable", "cdet_profile_read",
     "cdet_set_assembly", "cdet_prepare_split", "cdet_assemble_device",
     "cdet_integrand_device_noalloc", "cdet_diagonal_order1_density",
+    "cdet_mcmcmc_create", "cdet_mcmcmc_run", "cdet_mcmcmc_end_warmup", "cdet_mcmcmc_state",
+    "cdet_mcmcmc_destroy",
 )
 
 ASSEMBLY_FP64 = 0
@@ -38,6 +40,12 @@ ASSEMBLY_SPLIT_BF16 = 1
 
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int32)
+
+
+class McmcmcConfig(C.Structure):
+    """cdet_mcmcmc_config (include/cdet_gb300.h)."""
+    _fields_ = [("order_min", C.c_int32), ("order_max", C.c_int32), ("envelope_order", C.c_int32),
+                ("lambda_adapt_interval", C.c_int32), ("lambda_adapt_rate", C.c_double)]
 
 
 class RuntimeScalars(C.Structure):
@@ -81,6 +89,12 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_all_subsets_host.argtypes = [vp, vp, i32, i64, vp, vp]
     lib.cdet_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.cdet_diagonal_order1_density.argtypes = [vp, C.c_double, C.c_double, _DP]
+    _UP = C.POINTER(C.c_uint64)
+    lib.cdet_mcmcmc_create.argtypes = [vp, C.POINTER(McmcmcConfig), C.c_int64, _UP, _DP, C.POINTER(vp)]
+    lib.cdet_mcmcmc_run.argtypes = [vp, C.c_int, C.c_int64, _UP, _DP, _DP]
+    lib.cdet_mcmcmc_end_warmup.argtypes = [vp]
+    lib.cdet_mcmcmc_state.argtypes = [vp, _DP, _DP, _UP]
+    lib.cdet_mcmcmc_destroy.argtypes = [vp]
     lib.cdet_last_error.restype = C.c_char_p
     lib.cdet_last_launch_count.argtypes = [vp]
     lib.cdet_integrand_device_noalloc.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp]

@@ -718,3 +718,261 @@ int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------- MCMCMC chains ----
+struct cdet_mcmcmc {
+    cdet_context* ctx = nullptr;
+    cdet_mcmcmc_config cfg{};
+    int64_t chains = 0;
+    double inv_binom[cdet::kMcmcmcMaxEnvelope + 1] = {};
+    void* block = nullptr;
+    double* vert[2] = {nullptr, nullptr};
+    int cur = 0;
+    double* values = nullptr;
+    int32_t* istatus = nullptr;
+    double* lambdas = nullptr;
+    uint64_t* mt = nullptr;
+    int32_t* mt_index = nullptr;
+    uint64_t* counts = nullptr;
+    int32_t* error = nullptr;
+    int64_t warmup_done = 0;
+};
+
+namespace {
+
+// adapt_mcmcmc_lambdas (mcmcmc_sampler.h:579-600) for every chain with a
+// nonzero block (only_pending: the partial last block, :1050-1054), then the
+// counts are cleared.
+int mcmcmc_adapt(cdet_mcmcmc* m, bool only_pending) {
+    const int env = m->cfg.envelope_order;
+    const size_t n = static_cast<size_t>(m->chains) * (env + 1);
+    std::vector<uint64_t> counts(n);
+    std::vector<double> lambdas(n);
+    cudaError_t err = cudaMemcpy(counts.data(), m->counts, n * sizeof(uint64_t), cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(lambdas.data(), m->lambdas, n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC lambda adaptation");
+    const int omin = m->cfg.order_min, omax = m->cfg.order_max;
+    const int order_count = omax - omin + 1;
+    const double target = 1.0 / static_cast<double>(order_count);
+    for (int64_t c = 0; c < m->chains; ++c) {
+        uint64_t* cc = counts.data() + c * (env + 1);
+        double* lam = lambdas.data() + c * (env + 1);
+        bool pending = false;
+        for (int o = 0; o <= env; ++o) pending |= cc[o] != 0;
+        if (only_pending && !pending) continue;
+        uint64_t total = 0;
+        for (int o = omin; o <= omax; ++o) total += cc[o];
+        if (total != 0) {
+            for (int o = omin; o <= omax; ++o) {
+                const double actual = (static_cast<double>(cc[o]) + 1.0) /
+                                      (static_cast<double>(total) + static_cast<double>(order_count));
+                lam[o] *= std::exp(m->cfg.lambda_adapt_rate * std::log(target / actual));
+            }
+        }
+        for (int o = 0; o <= env; ++o) cc[o] = 0;
+    }
+    err = cudaMemcpy(m->counts, counts.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(m->lambdas, lambdas.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC lambda adaptation");
+    return CDET_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cdet_mcmcmc_create(cdet_context* ctx, const cdet_mcmcmc_config* config, int64_t chains, const uint64_t* seeds,
+                       const double* lambdas, cdet_mcmcmc** out) {
+    if (!ctx || !config || !seeds || !lambdas || !out) return fail(CDET_ERR_INVALID, "null argument");
+    const cdet_mcmcmc_config& c = *config;
+    // validate_mcmcmc_config (mcmcmc_sampler.h:432-493)
+    if (c.order_min < 1) return fail(CDET_ERR_INVALID, "MCMCMC_ORDER_MIN must be at least 1 for the replica integrand");
+    if (c.order_max < c.order_min) return fail(CDET_ERR_INVALID, "MCMCMC_ORDER_MAX must be >= MCMCMC_ORDER_MIN");
+    if (c.envelope_order <= c.order_max)
+        return fail(CDET_ERR_INVALID, "MCMCMC_ENVELOPE_ORDER must be larger than MCMCMC_ORDER_MAX");
+    if (c.envelope_order > cdet::kMcmcmcMaxEnvelope)
+        return fail(CDET_ERR_INVALID, "MCMCMC_ENVELOPE_ORDER must be <= 24 for the GPU chains");
+    if (chains <= 0) return fail(CDET_ERR_INVALID, "MCMCMC_CHAIN_COUNT must be positive");
+    if (c.lambda_adapt_interval <= 0) return fail(CDET_ERR_INVALID, "MCMCMC_LAMBDA_ADAPT_INTERVAL must be positive");
+    for (int o = c.order_min; o <= c.order_max; ++o)
+        if (!(lambdas[o] > 0.0) || !std::isfinite(lambdas[o]))
+            return fail(CDET_ERR_INVALID, "MCMCMC_LAMBDAS entries must be positive finite numbers");
+    for (int k = 0; k < 4; ++k)
+        if (!resolve(ctx, k)) return fail(CDET_ERR_STATE, "Green-function tables have not been uploaded");
+    DeviceGuard guard(ctx->device);
+    auto* m = new cdet_mcmcmc;
+    m->ctx = ctx;
+    m->cfg = c;
+    m->chains = chains;
+    const int env = c.envelope_order;
+    for (int o = c.order_min; o <= c.order_max; ++o) {
+        // 1 / binomial_as_double(envelope, order) (:174-185); the binomial is an exact integer here
+        uint64_t b = 1;
+        const int k = o < env - o ? o : env - o;
+        for (int i = 1; i <= k; ++i) b = b * static_cast<uint64_t>(env - k + i) / static_cast<uint64_t>(i);
+        m->inv_binom[o] = 1.0 / static_cast<double>(b);
+    }
+    const size_t nv = static_cast<size_t>(chains) * env * 4;
+    const size_t nvals = static_cast<size_t>(chains) << env;
+    const size_t nl = static_cast<size_t>(chains) * (env + 1);
+    const size_t nmt = static_cast<size_t>(chains) * 312;
+    auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
+    const size_t bytes = 2 * up(nv * 8) + up(nvals * 8) + up(chains * 4) + up(nl * 8) + up(nmt * 8) +
+                         up(chains * 4) + up(nl * 8) + up(chains * 4) + up(chains * 8);
+    cudaError_t err = cudaMalloc(&m->block, bytes);
+    if (err != cudaSuccess) {
+        delete m;
+        return cuda_fail(err, "cudaMalloc(MCMCMC chains)");
+    }
+    char* p = static_cast<char*>(m->block);
+    auto take = [&](size_t b) {
+        void* r = p;
+        p += up(b);
+        return r;
+    };
+    m->vert[0] = static_cast<double*>(take(nv * 8));
+    m->vert[1] = static_cast<double*>(take(nv * 8));
+    m->values = static_cast<double*>(take(nvals * 8));
+    m->istatus = static_cast<int32_t*>(take(chains * 4));
+    m->lambdas = static_cast<double*>(take(nl * 8));
+    m->mt = static_cast<uint64_t*>(take(nmt * 8));
+    m->mt_index = static_cast<int32_t*>(take(chains * 4));
+    m->counts = static_cast<uint64_t*>(take(nl * 8));
+    m->error = static_cast<int32_t*>(take(chains * 4));
+    uint64_t* dseeds = static_cast<uint64_t*>(take(chains * 8));
+    std::vector<double> lam(nl);
+    for (int64_t ch = 0; ch < chains; ++ch)
+        for (int o = 0; o <= env; ++o) lam[ch * (env + 1) + o] = lambdas[o];
+    err = cudaMemcpy(dseeds, seeds, chains * 8, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(m->lambdas, lam.data(), nl * 8, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemset(m->counts, 0, nl * 8);
+    if (err == cudaSuccess) err = cudaMemset(m->error, 0, chains * 4);
+    if (err == cudaSuccess) err = cdet::launch_mcmcmc_init(chains, env, dseeds, m->mt, m->mt_index, m->vert[0], nullptr);
+    if (err == cudaSuccess) err = cudaDeviceSynchronize();
+    if (err != cudaSuccess) {
+        cudaFree(m->block);
+        delete m;
+        return cuda_fail(err, "MCMCMC chain initialisation");
+    }
+    *out = m;
+    return CDET_OK;
+}
+
+int cdet_mcmcmc_run(cdet_mcmcmc* m, int warmup, int64_t steps, uint64_t* chosen, double* norms, double* signal) {
+    if (!m || steps < 0) return fail(CDET_ERR_INVALID, "bad argument");
+    if (steps == 0) return CDET_OK;
+    DeviceGuard guard(m->ctx->device);
+    const int env = m->cfg.envelope_order;
+    const int64_t chains = m->chains;
+    uint64_t* d_chosen = nullptr;
+    double* d_norms = nullptr;
+    double* d_signal = nullptr;
+    cudaError_t err = cudaSuccess;
+    if (chosen) err = cudaMalloc(&d_chosen, static_cast<size_t>(steps) * chains * 8);
+    if (err == cudaSuccess && norms) err = cudaMalloc(&d_norms, static_cast<size_t>(steps) * chains * 8);
+    if (err == cudaSuccess && signal)
+        err = cudaMalloc(&d_signal, static_cast<size_t>(steps) * chains * (env + 1) * 8);
+    int rc = err == cudaSuccess ? CDET_OK : cuda_fail(err, "cudaMalloc(MCMCMC step outputs)");
+    for (int64_t s = 0; rc == CDET_OK && s < steps; ++s) {
+        rc = run(m->ctx, m->vert[m->cur], nullptr, chains, env, 1, m->values, m->istatus, nullptr);
+        if (rc != CDET_OK) break;
+        cdet::McmcmcStepArgs a{};
+        a.chains = chains;
+        a.envelope = env;
+        a.order_min = m->cfg.order_min;
+        a.order_max = m->cfg.order_max;
+        a.warmup = warmup ? 1 : 0;
+        for (int o = 0; o <= env; ++o) a.inv_binom[o] = m->inv_binom[o];
+        a.values = m->values;
+        a.integrand_status = m->istatus;
+        a.vertices = m->vert[m->cur];
+        a.next_vertices = m->vert[m->cur ^ 1];
+        a.lambdas = m->lambdas;
+        a.mt = m->mt;
+        a.mt_index = m->mt_index;
+        a.counts = m->counts;
+        a.error = m->error;
+        a.chosen_out = d_chosen ? d_chosen + s * chains : nullptr;
+        a.norm_out = d_norms ? d_norms + s * chains : nullptr;
+        a.signal_out = d_signal ? d_signal + s * chains * (env + 1) : nullptr;
+        err = cdet::launch_mcmcmc_step(a, nullptr);
+        if (err != cudaSuccess) {
+            rc = cuda_fail(err, "MCMCMC step launch");
+            break;
+        }
+        m->cur ^= 1;
+        if (warmup) {
+            ++m->warmup_done;
+            if (m->warmup_done % m->cfg.lambda_adapt_interval == 0) rc = mcmcmc_adapt(m, false);
+        }
+    }
+    if (rc == CDET_OK) {
+        err = cudaDeviceSynchronize();
+        if (err == cudaSuccess && chosen)
+            err = cudaMemcpy(chosen, d_chosen, static_cast<size_t>(steps) * chains * 8, cudaMemcpyDeviceToHost);
+        if (err == cudaSuccess && norms)
+            err = cudaMemcpy(norms, d_norms, static_cast<size_t>(steps) * chains * 8, cudaMemcpyDeviceToHost);
+        if (err == cudaSuccess && signal)
+            err = cudaMemcpy(signal, d_signal, static_cast<size_t>(steps) * chains * (env + 1) * 8,
+                             cudaMemcpyDeviceToHost);
+        if (err != cudaSuccess) rc = cuda_fail(err, "MCMCMC step outputs");
+    }
+    if (d_chosen) cudaFree(d_chosen);
+    if (d_norms) cudaFree(d_norms);
+    if (d_signal) cudaFree(d_signal);
+    if (rc != CDET_OK) return rc;
+    std::vector<int32_t> errors(static_cast<size_t>(chains));
+    err = cudaMemcpy(errors.data(), m->error, chains * 4, cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC status");
+    for (int64_t c = 0; c < chains; ++c) {
+        if (errors[c] == 1)
+            return fail(CDET_ERR_VALUE, "Error (all-subset integrand): Value is not finite (chain " +
+                                            std::to_string(c) + ")");
+        if (errors[c] == 2)
+            return fail(CDET_ERR_VALUE,
+                        "MCMCMC local normalization is zero or non-finite (chain " + std::to_string(c) + ")");
+    }
+    return CDET_OK;
+}
+
+int cdet_mcmcmc_end_warmup(cdet_mcmcmc* m) {
+    if (!m) return fail(CDET_ERR_INVALID, "bad argument");
+    DeviceGuard guard(m->ctx->device);
+    if (m->warmup_done % m->cfg.lambda_adapt_interval == 0) return CDET_OK;
+    return mcmcmc_adapt(m, true);
+}
+
+int cdet_mcmcmc_state(const cdet_mcmcmc* m, double* vertices, double* lambdas, uint64_t* rng_state) {
+    if (!m) return fail(CDET_ERR_INVALID, "bad argument");
+    DeviceGuard guard(m->ctx->device);
+    const int env = m->cfg.envelope_order;
+    const int64_t chains = m->chains;
+    cudaError_t err = cudaDeviceSynchronize();
+    if (err == cudaSuccess && vertices)
+        err = cudaMemcpy(vertices, m->vert[m->cur], static_cast<size_t>(chains) * env * 4 * 8, cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess && lambdas)
+        err = cudaMemcpy(lambdas, m->lambdas, static_cast<size_t>(chains) * (env + 1) * 8, cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess && rng_state) {
+        std::vector<uint64_t> words(static_cast<size_t>(chains) * 312);
+        std::vector<int32_t> index(static_cast<size_t>(chains));
+        err = cudaMemcpy(words.data(), m->mt, words.size() * 8, cudaMemcpyDeviceToHost);
+        if (err == cudaSuccess) err = cudaMemcpy(index.data(), m->mt_index, chains * 4, cudaMemcpyDeviceToHost);
+        if (err == cudaSuccess)
+            for (int64_t c = 0; c < chains; ++c) {
+                for (int i = 0; i < 312; ++i) rng_state[c * 313 + i] = words[static_cast<size_t>(i) * chains + c];
+                rng_state[c * 313 + 312] = static_cast<uint64_t>(index[c]);
+            }
+    }
+    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC state");
+    return CDET_OK;
+}
+
+int cdet_mcmcmc_destroy(cdet_mcmcmc* m) {
+    if (!m) return CDET_OK;
+    DeviceGuard guard(m->ctx->device);
+    cudaFree(m->block);
+    delete m;
+    return CDET_OK;
+}
+
+}  // extern "C"

@@ -101,6 +101,31 @@ size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps);
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out);
 // assembly = true launches the FP64 Green-matrix assembly first; false
 // expects the Green matrices already in scratch (split-precision assembly).
+// One MCMCMC step for a batch of chains (uniform seed kernel), after the
+// all-subset integrand of every chain's envelope.
+constexpr int kMcmcmcMaxEnvelope = 24;
+struct McmcmcStepArgs {
+    int64_t chains;
+    int envelope, order_min, order_max;
+    int warmup;                     // 1: count the chosen order for the lambda adaptation
+    double inv_binom[kMcmcmcMaxEnvelope + 1];
+    const double* values;           // [chains][2^envelope] all-subset integrands
+    const int32_t* integrand_status;
+    const double* vertices;         // [chains][envelope][4]
+    double* next_vertices;
+    const double* lambdas;          // [chains][envelope + 1]
+    uint64_t* mt;                   // [312][chains]
+    int32_t* mt_index;              // [chains]
+    uint64_t* counts;               // [chains][envelope + 1] warmup block counts
+    int32_t* error;                 // [chains]: 0, 1 (integrand not finite), 2 (normalisation)
+    uint64_t* chosen_out;           // [chains] or null
+    double* norm_out;               // [chains] or null
+    double* signal_out;             // [chains][envelope + 1] or null
+};
+cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* seeds, uint64_t* mt, int32_t* mt_index,
+                               double* vertices, cudaStream_t stream);
+cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream);
+
 // Order-1 diagonal observable: items[3 * N1 * N2] scratch, out[3] = {twisted -
 // 2 ordinary, twisted, ordinary}; tables in kind order (twisted up, twisted
 // down, ordinary up, ordinary down).

@@ -166,6 +166,55 @@ int cdet_all_subsets_host(cdet_context* ctx, const double* vertices, int envelop
  * throws "The diagonal observable is undefined for U = 0"). */
 int cdet_diagonal_order1_density(cdet_context* ctx, double alpha_up, double alpha_down, double* out);
 
+/* ------------------------------------------------- MCMCMC chains on the GPU
+ * A batch of MCMCMC chains (run_single_mcmcmc_chain, mcmcmc_sampler.h:994-1088)
+ * resident on the GPU, with the uniform seed kernel (MCMCMC_SEED_MODE=uniform,
+ * mcmcmc_seed.h:41-61). Every step evaluates the all-subset integrand of each
+ * chain's envelope with the context's assembly and runs run_mcmcmc_step
+ * (:524-577) in one thread per chain. Each chain keeps the reference's
+ * std::mt19937_64 stream and draws from it as libstdc++'s distributions do,
+ * so with the FP64 assembly the chains follow the reference's chains step for
+ * step. The lambda adaptation (adapt_mcmcmc_lambdas, :579-600) runs on the
+ * host after every adapt interval of warmup steps. Checkpoint files and the
+ * histogram seed kernel are not part of this interface. */
+typedef struct cdet_mcmcmc cdet_mcmcmc;
+
+typedef struct cdet_mcmcmc_config {
+    int32_t order_min;             /* MCMCMC_ORDER_MIN (>= 1) */
+    int32_t order_max;             /* MCMCMC_ORDER_MAX (>= order_min) */
+    int32_t envelope_order;        /* MCMCMC_ENVELOPE_ORDER (> order_max, <= 24 here) */
+    int32_t lambda_adapt_interval; /* MCMCMC_LAMBDA_ADAPT_INTERVAL (> 0) */
+    double lambda_adapt_rate;      /* MCMCMC_LAMBDA_ADAPT_RATE */
+} cdet_mcmcmc_config;
+
+/* Creates `chains` chains: chain k is make_initial_mcmcmc_chain_state with
+ * seed seeds[k] (std::mt19937_64(seed), then envelope_order uniform vertices)
+ * and lambdas[0..envelope_order] (MCMCMC_LAMBDAS). validate_mcmcmc_config's
+ * checks apply, with its messages. The context's tables must be uploaded. */
+int cdet_mcmcmc_create(cdet_context* ctx, const cdet_mcmcmc_config* config, int64_t chains, const uint64_t* seeds,
+                       const double* lambdas, cdet_mcmcmc** out);
+
+/* Advances every chain `steps` steps. warmup = 1: warmup steps (the chosen
+ * orders are counted and lambdas adapted every lambda_adapt_interval warmup
+ * steps); warmup = 0: production steps. Optional host outputs (null to skip):
+ * chosen[step][chain] masks, norms[step][chain] local normalisations,
+ * signal[step][chain][envelope + 1] the raw order signals (the reference's
+ * workspace.order_signal). A chain whose integrand is not finite or whose
+ * local normalisation is not positive stops (the reference throws); the call
+ * then returns CDET_ERR_VALUE naming the chain. Blocking. */
+int cdet_mcmcmc_run(cdet_mcmcmc* m, int warmup, int64_t steps, uint64_t* chosen, double* norms, double* signal);
+
+/* The adaptation for a partial last warmup block (run_single_mcmcmc_chain,
+ * :1050-1054): chains with pending counts adapt once more. */
+int cdet_mcmcmc_end_warmup(cdet_mcmcmc* m);
+
+/* Current state (null to skip): vertices[chain][envelope][4],
+ * lambdas[chain][envelope + 1], rng_state[chain][313] = the 312 words of the
+ * mt19937_64 state and its position, in the order std::mt19937_64 writes them. */
+int cdet_mcmcmc_state(const cdet_mcmcmc* m, double* vertices, double* lambdas, uint64_t* rng_state);
+
+int cdet_mcmcmc_destroy(cdet_mcmcmc* m);
+
 /* Counters of the host entry points: integrand calls and whole-matrix
  * principal-minor fallbacks (runtime_counters.h:14-51). */
 int cdet_counters(const cdet_context* ctx, uint64_t* integrand_calls, uint64_t* fpm_fallbacks);

@@ -94,6 +94,10 @@ class Oracle:
         lib.oracle_prefactor_ld.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
         lib.oracle_prefactor_ld.restype = C.c_double
         lib.oracle_diagonal_order1.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, _DP]
+        _UP = C.POINTER(C.c_uint64)
+        lib.oracle_mcmcmc_chain.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, _DP, C.c_int,
+                                            C.c_int, C.c_double, C.c_int, C.c_uint64, _UP, _DP, _DP, _DP, _DP,
+                                            _UP]
         self.scalars = OracleScalars(**{k: scalars[k] for k, _ in OracleScalars._fields_})
         self._keep = {k: _as_numpy_table(tables[k]) for k in KINDS}
         tabs = {}
@@ -161,6 +165,27 @@ class Oracle:
         if rc != 0:
             raise RuntimeError("The diagonal observable is undefined for U = 0")
         return out
+
+    def mcmcmc_chain(self, order_min, order_max, envelope, lambdas, warmup, adapt_interval,
+                     adapt_rate, production, seed):
+        """One chain with the uniform seed kernel; the same outputs as
+        Reference.mcmcmc_chain."""
+        steps = warmup + production
+        chosen = np.zeros(steps, dtype=np.uint64)
+        norms = np.zeros(steps)
+        signal = np.zeros((production, envelope + 1))
+        verts = np.zeros((envelope, 4))
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        lam_out = np.zeros(envelope + 1)
+        rng = np.zeros(8, dtype=np.uint64)
+        up = C.POINTER(C.c_uint64)
+        rc = self.lib.oracle_mcmcmc_chain(C.byref(self.scalars), C.byref(self.tables), order_min, order_max,
+                                          envelope, _ptr(lam), warmup, adapt_interval, adapt_rate, production,
+                                          seed, chosen.ctypes.data_as(up), _ptr(norms), _ptr(signal),
+                                          _ptr(verts), _ptr(lam_out), rng.ctypes.data_as(up))
+        if rc != 0:
+            raise RuntimeError(f"oracle chain failed ({rc})")
+        return dict(chosen=chosen, norms=norms, signal=signal, vertices=verts, lambdas=lam_out, rng=rng)
 
     @staticmethod
     def _lib():
@@ -253,6 +278,9 @@ class Reference:
         lib.ref_fpm_fallbacks.restype = C.c_ulonglong
         lib.ref_sample_vertices.argtypes = [C.c_ulonglong, C.c_int, _DP]
         lib.ref_diagonal_order1.argtypes = [_DP]
+        _UP = C.POINTER(C.c_ulonglong)
+        lib.ref_mcmcmc_chain.argtypes = [C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_double,
+                                         C.c_int, C.c_ulonglong, _UP, _DP, _DP, _DP, _DP, _UP]
 
     def _check(self, rc):
         if rc != 0:
@@ -308,6 +336,26 @@ class Reference:
         out = np.zeros(1 << v.shape[0])
         self._check(self.lib.ref_eval_all_subsets(_ptr(v), v.shape[0], _ptr(out)))
         return out
+
+    def mcmcmc_chain(self, order_min, order_max, envelope, lambdas, warmup, adapt_interval,
+                     adapt_rate, production, seed):
+        """One reference chain (uniform seed): per-step chosen masks and local
+        normalisations, production order signals, final vertices, lambdas and
+        the next 8 raw generator outputs."""
+        steps = warmup + production
+        chosen = np.zeros(steps, dtype=np.uint64)
+        norms = np.zeros(steps)
+        signal = np.zeros((production, envelope + 1))
+        verts = np.zeros((envelope, 4))
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        lam_out = np.zeros(envelope + 1)
+        rng = np.zeros(8, dtype=np.uint64)
+        up = C.POINTER(C.c_ulonglong)
+        self._check(self.lib.ref_mcmcmc_chain(order_min, order_max, envelope, _ptr(lam), warmup,
+                                              adapt_interval, adapt_rate, production, seed,
+                                              chosen.ctypes.data_as(up), _ptr(norms), _ptr(signal),
+                                              _ptr(verts), _ptr(lam_out), rng.ctypes.data_as(up)))
+        return dict(chosen=chosen, norms=norms, signal=signal, vertices=verts, lambdas=lam_out, rng=rng)
 
     def diagonal_order1(self) -> np.ndarray:
         """[normalised hi, twisted, ordinary, normalised lo] from the reference."""

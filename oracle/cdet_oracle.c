@@ -796,3 +796,192 @@ int oracle_diagonal_order1(const oracle_scalars* s, const oracle_tables* t, doub
     out[2] = ordinary;
     return 0;
 }
+
+/* ------------------------------------------------------- MCMCMC chain --- */
+
+#define MT64_N 312
+#define MT64_M 156
+
+void oracle_mt64_seed(oracle_mt64* g, uint64_t seed) {
+    g->mt[0] = seed;
+    for (int i = 1; i < MT64_N; ++i) {
+        const uint64_t x = g->mt[i - 1];
+        g->mt[i] = 6364136223846793005ULL * (x ^ (x >> 62)) + (uint64_t)i;
+    }
+    g->index = MT64_N;
+}
+
+uint64_t oracle_mt64_next(oracle_mt64* g) {
+    const uint64_t upper = 0xFFFFFFFF80000000ULL, lower = 0x7FFFFFFFULL, matrix = 0xB5026F5AA96619E9ULL;
+    if (g->index >= MT64_N) {
+        for (int i = 0; i < MT64_N; ++i) {
+            const uint64_t x = (g->mt[i] & upper) | (g->mt[(i + 1) % MT64_N] & lower);
+            g->mt[i] = g->mt[(i + MT64_M) % MT64_N] ^ (x >> 1) ^ ((x & 1ULL) ? matrix : 0ULL);
+        }
+        g->index = 0;
+    }
+    uint64_t y = g->mt[g->index++];
+    y ^= (y >> 29) & 0x5555555555555555ULL;
+    y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+    y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+    y ^= y >> 43;
+    return y;
+}
+
+double oracle_canonical(oracle_mt64* g) {
+    const double r = (double)oracle_mt64_next(g) / 18446744073709551616.0;
+    return r >= 1.0 ? nextafter(1.0, 0.0) : r;
+}
+
+int oracle_uniform_int(oracle_mt64* g, int n) {
+    const uint64_t range = (uint64_t)n;
+    unsigned __int128 product = (unsigned __int128)oracle_mt64_next(g) * range;
+    uint64_t low = (uint64_t)product;
+    if (low < range) {
+        const uint64_t threshold = (0 - range) % range;
+        while (low < threshold) {
+            product = (unsigned __int128)oracle_mt64_next(g) * range;
+            low = (uint64_t)product;
+        }
+    }
+    return (int)(product >> 64);
+}
+
+/* binomial_as_double (mcmcmc_sampler.h:174-185): exact for the orders used. */
+static double binomial_double(int n, int k) {
+    if (k < 0 || k > n) return 0.0;
+    if (k > n - k) k = n - k;
+    uint64_t r = 1;
+    for (int i = 1; i <= k; ++i) r = r * (uint64_t)(n - k + i) / (uint64_t)i;
+    return (double)r;
+}
+
+/* adapt_mcmcmc_lambdas (mcmcmc_sampler.h:579-600) */
+static void adapt_lambdas(double* lambdas, int order_min, int order_max, double rate, uint64_t* counts) {
+    uint64_t total = 0;
+    for (int o = order_min; o <= order_max; ++o) total += counts[o];
+    if (total == 0) return;
+    const int order_count = order_max - order_min + 1;
+    const double target = 1.0 / (double)order_count;
+    for (int o = order_min; o <= order_max; ++o) {
+        const double actual = ((double)counts[o] + 1.0) / ((double)total + (double)order_count);
+        lambdas[o] *= exp(rate * log(target / actual));
+    }
+}
+
+/* run_mcmcmc_step (mcmcmc_sampler.h:524-577) with the uniform seed kernel. */
+static int mcmcmc_step(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max, int envelope,
+                       const double* lambdas, const double* inv_binom, double* vertices, oracle_mt64* rng,
+                       double* values, double* fluxes, double* weights, uint64_t* chosen_out, double* norm_out,
+                       double* signal) {
+    if (oracle_all_subsets(s, t, vertices, envelope, values) & ORACLE_NONFINITE) return 1;
+    const uint64_t subsets = (uint64_t)1 << envelope;
+    double norm = 0.0;
+    int idx = 0;
+    for (uint64_t mask = 1; mask < subsets; ++mask) {
+        const int o = __builtin_popcountll(mask);
+        if (o < order_min || o > order_max) continue;
+        const double flux = lambdas[o] * values[mask] * 1.0;
+        const double w = fabs(flux) * inv_binom[o];
+        fluxes[idx] = flux;
+        weights[idx] = w;
+        norm += w;
+        ++idx;
+    }
+    /* sample_weighted_candidate_mask (:225-250) */
+    if (!(norm > 0.0) || !isfinite(norm)) return 2;
+    const double threshold = oracle_canonical(rng) * (norm - 0.0) + 0.0;
+    double cumulative = 0.0;
+    uint64_t chosen = 0, last_positive = 0;
+    int found = 0;
+    idx = 0;
+    for (uint64_t mask = 1; mask < subsets && !found; ++mask) {
+        const int o = __builtin_popcountll(mask);
+        if (o < order_min || o > order_max) continue;
+        const double w = weights[idx++];
+        if (!(w > 0.0)) continue;
+        if (isfinite(w)) last_positive = mask;
+        cumulative += w;
+        if (cumulative > threshold) {
+            chosen = mask;
+            found = 1;
+        }
+    }
+    if (!found) chosen = last_positive;
+    for (int o = 0; o <= envelope; ++o) signal[o] = 0.0;
+    idx = 0;
+    for (uint64_t mask = 1; mask < subsets; ++mask) {
+        const int o = __builtin_popcountll(mask);
+        if (o < order_min || o > order_max) continue;
+        const double time = fluxes[idx++] / norm;
+        signal[o] += time * inv_binom[o];
+    }
+    /* create_next_vertices_from_seed_into (:380-400), uniform seed (mcmcmc_seed.h:51-55) */
+    double next[64 * 4];
+    int size = 0;
+    for (int i = 0; i < envelope; ++i)
+        if (chosen & ((uint64_t)1 << i)) {
+            for (int k = 0; k < 4; ++k) next[4 * size + k] = vertices[4 * i + k];
+            ++size;
+        }
+    while (size < envelope) {
+        (void)oracle_uniform_int(rng, size); /* the parent; the uniform kernel ignores it */
+        for (int k = 0; k < 4; ++k) next[4 * size + k] = oracle_canonical(rng);
+        ++size;
+    }
+    memcpy(vertices, next, sizeof(double) * 4 * (size_t)envelope);
+    *chosen_out = chosen;
+    *norm_out = norm;
+    return 0;
+}
+
+int oracle_mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
+                        int envelope, const double* lambdas_in, int warmup, int adapt_interval, double adapt_rate,
+                        int production, uint64_t seed, uint64_t* chosen, double* norms, double* signal,
+                        double* vertices_out, double* lambdas_out, uint64_t* rng_out) {
+    oracle_mt64 rng;
+    oracle_mt64_seed(&rng, seed);
+    double vertices[64 * 4];
+    for (int i = 0; i < envelope * 4; ++i) vertices[i] = oracle_canonical(&rng); /* sample_uniform_vertex_set */
+    double lambdas[65], inv_binom[65];
+    uint64_t counts[65];
+    for (int o = 0; o <= envelope; ++o) {
+        lambdas[o] = lambdas_in[o];
+        counts[o] = 0;
+        inv_binom[o] = (o >= order_min && o <= order_max) ? 1.0 / binomial_double(envelope, o) : 0.0;
+    }
+    const size_t subsets = (size_t)1 << envelope;
+    double* values = (double*)malloc(sizeof(double) * subsets);
+    double* fluxes = (double*)malloc(sizeof(double) * subsets);
+    double* weights = (double*)malloc(sizeof(double) * subsets);
+    double step_signal[65];
+    int rc = (values && fluxes && weights) ? 0 : 3;
+    int k = 0;
+    for (int step = 0; rc == 0 && step < warmup; ++step, ++k) {
+        rc = mcmcmc_step(s, t, order_min, order_max, envelope, lambdas, inv_binom, vertices, &rng, values, fluxes,
+                         weights, &chosen[k], &norms[k], step_signal);
+        if (rc) break;
+        ++counts[__builtin_popcountll(chosen[k])];
+        if ((step + 1) % adapt_interval == 0) {
+            adapt_lambdas(lambdas, order_min, order_max, adapt_rate, counts);
+            for (int o = 0; o <= envelope; ++o) counts[o] = 0;
+        }
+    }
+    if (rc == 0 && warmup % adapt_interval != 0) {
+        int pending = 0;
+        for (int o = 0; o <= envelope; ++o) pending |= counts[o] != 0;
+        if (pending) adapt_lambdas(lambdas, order_min, order_max, adapt_rate, counts);
+    }
+    for (int step = 0; rc == 0 && step < production; ++step, ++k) {
+        rc = mcmcmc_step(s, t, order_min, order_max, envelope, lambdas, inv_binom, vertices, &rng, values, fluxes,
+                         weights, &chosen[k], &norms[k], signal + (size_t)step * (envelope + 1));
+    }
+    free(values);
+    free(fluxes);
+    free(weights);
+    if (rc) return rc;
+    memcpy(vertices_out, vertices, sizeof(double) * 4 * (size_t)envelope);
+    for (int o = 0; o <= envelope; ++o) lambdas_out[o] = lambdas[o];
+    for (int i = 0; i < 8; ++i) rng_out[i] = oracle_mt64_next(&rng);
+    return 0;
+}

@@ -109,6 +109,34 @@ int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
 int oracle_diagonal_order1(const oracle_scalars* s, const oracle_tables* t, double alpha_up,
                            double alpha_down, double* out);
 
+/* std::mt19937_64 (the published MT19937-64 generator, libstdc++'s
+ * mersenne_twister_engine parameters and seeding). */
+typedef struct oracle_mt64 {
+    uint64_t mt[312];
+    int index;
+} oracle_mt64;
+void oracle_mt64_seed(oracle_mt64* g, uint64_t seed);
+uint64_t oracle_mt64_next(oracle_mt64* g);
+/* std::generate_canonical<double, 53>(mt19937_64) as libstdc++ computes it. */
+double oracle_canonical(oracle_mt64* g);
+/* std::uniform_int_distribution<int>(0, n - 1)(mt19937_64) (libstdc++'s
+ * 128-bit nearly-divisionless downscaling). */
+int oracle_uniform_int(oracle_mt64* g, int n);
+
+/* One MCMCMC chain with the uniform seed kernel: make_initial_mcmcmc_chain_state,
+ * warmup steps with lambda adaptation every adapt_interval steps (and once more
+ * for a partial last block), production steps (run_single_mcmcmc_chain,
+ * mcmcmc_sampler.h:994-1088, without checkpoints). Outputs as
+ * ref_mcmcmc_chain in oracle/ref_harness.cpp: chosen[k], norms[k] per step
+ * (warmup first), signal[p * (envelope + 1) + order] per production step,
+ * vertices_out [envelope][4], lambdas_out [envelope + 1], rng_out the next 8
+ * raw generator outputs. Returns 0, or 1 when the integrand is not finite, 2
+ * when a local normalisation is zero or not finite (the reference throws). */
+int oracle_mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
+                        int envelope, const double* lambdas, int warmup, int adapt_interval, double adapt_rate,
+                        int production, uint64_t seed, uint64_t* chosen, double* norms, double* signal,
+                        double* vertices_out, double* lambdas_out, uint64_t* rng_out);
+
 #ifdef __cplusplus
 }
 #endif

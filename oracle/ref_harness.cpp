@@ -28,6 +28,9 @@
 //                             solve the Chebyshev accuracy audit compares with.
 //   ref_diagonal_order1    -> normalized_log_partition_first_order_density_dd and its
 //                             twisted / ordinary parts (diagonal_green_observable.h:237-327)
+//   ref_mcmcmc_chain       -> the step loop of run_single_mcmcmc_chain
+//                             (mcmcmc_sampler.h:994-1088) with the uniform seed, no
+//                             checkpoints, recording every step
 
 #include "cdet/cdet_integrand_evaluator.h"
 #include "cdet/diagonal_green_observable.h"
@@ -294,6 +297,73 @@ void ref_sample_vertices(unsigned long long seed, int count, double* out) {
 unsigned long long ref_fpm_fallbacks() { return snapshot_cdet_runtime_counters().fpm_fallbacks; }
 
 void ref_reset_counters() { reset_cdet_runtime_counters(); }
+
+// One chain: make_initial_mcmcmc_chain_state, then warmup steps with lambda
+// adaptation every adapt_interval steps (and once more for a partial last
+// block), then production steps, exactly as run_single_mcmcmc_chain does.
+// chosen[k], norms[k]: chosen mask and local normalisation of step k (warmup
+// first); signal[p * (envelope + 1) + order]: the raw order signal of
+// production step p; vertices_out [envelope][4], lambdas_out [envelope + 1];
+// rng_out: the next 8 raw outputs of the chain's generator after the run.
+int ref_mcmcmc_chain(int order_min, int order_max, int envelope_order, const double* lambdas_in,
+                     int warmup_steps, int adapt_interval, double adapt_rate, int production_steps,
+                     unsigned long long seed, unsigned long long* chosen, double* norms, double* signal,
+                     double* vertices_out, double* lambdas_out, unsigned long long* rng_out) {
+    return guarded([&] {
+        MCMCMCConfig config;
+        config.order_min = order_min;
+        config.order_max = order_max;
+        config.envelope_order = envelope_order;
+        config.normalization_order = order_min;
+        config.lambdas.assign(lambdas_in, lambdas_in + envelope_order + 1);
+        config.lambda_warmup_steps = warmup_steps;
+        config.lambda_adapt_interval = adapt_interval;
+        config.lambda_adapt_rate = adapt_rate;
+        config.production_steps = production_steps;
+        config.chain_count = 1;
+        config.seed_mode = "uniform";
+        validate_mcmcmc_config(config);
+        MCMCMCChainState state = make_initial_mcmcmc_chain_state(config, 0, seed);
+        const MCMCMCMaskPlan plan = make_mcmcmc_mask_plan(config);
+        const UniformMCMCMCSeed seed_kernel;
+        MCMCMCStepWorkspace workspace;
+        int k = 0;
+        for (int step = 0; step < warmup_steps; ++step, ++k) {
+            const MCMCMCStepResult r =
+                run_mcmcmc_step(state.vertices, config, plan, state.lambdas, seed_kernel, state.rng, workspace);
+            state.vertices.swap(workspace.next_vertices);
+            chosen[k] = r.chosen_mask;
+            norms[k] = r.local_normalization;
+            ++state.warmup_block_counts[static_cast<std::size_t>(r.chosen_order)];
+            if ((step + 1) % adapt_interval == 0) {
+                adapt_mcmcmc_lambdas(state.lambdas, config, state.warmup_block_counts);
+                std::fill(state.warmup_block_counts.begin(), state.warmup_block_counts.end(), 0);
+            }
+        }
+        if (warmup_steps % adapt_interval != 0 && mcmcmc_has_pending_warmup_block(state.warmup_block_counts)) {
+            adapt_mcmcmc_lambdas(state.lambdas, config, state.warmup_block_counts);
+            std::fill(state.warmup_block_counts.begin(), state.warmup_block_counts.end(), 0);
+        }
+        for (int step = 0; step < production_steps; ++step, ++k) {
+            const MCMCMCStepResult r =
+                run_mcmcmc_step(state.vertices, config, plan, state.lambdas, seed_kernel, state.rng, workspace);
+            state.vertices.swap(workspace.next_vertices);
+            chosen[k] = r.chosen_mask;
+            norms[k] = r.local_normalization;
+            for (int order = 0; order <= envelope_order; ++order)
+                signal[static_cast<std::size_t>(step) * (envelope_order + 1) + order] =
+                    workspace.order_signal[static_cast<std::size_t>(order)];
+        }
+        for (int i = 0; i < envelope_order; ++i) {
+            vertices_out[4 * i + 0] = state.vertices[static_cast<std::size_t>(i)].tau;
+            vertices_out[4 * i + 1] = state.vertices[static_cast<std::size_t>(i)].x;
+            vertices_out[4 * i + 2] = state.vertices[static_cast<std::size_t>(i)].y;
+            vertices_out[4 * i + 3] = state.vertices[static_cast<std::size_t>(i)].replica;
+        }
+        for (int order = 0; order <= envelope_order; ++order) lambdas_out[order] = state.lambdas[static_cast<std::size_t>(order)];
+        for (int i = 0; i < 8; ++i) rng_out[i] = state.rng();
+    });
+}
 
 int ref_diagonal_order1(double* out) {
     return guarded([&] {

@@ -1,0 +1,85 @@
+"""Reference MCMCMC chain trajectories (uniform seed kernel) for the device
+chain step, from the reference itself.
+
+Run from the repository root in a checkout that has the reference at
+REFERENCE (default /root/reference), after make_golden.py:
+
+    python tests/golden/make_mcmcmc_golden.py
+
+For each golden parameter set it loads the reference-built tables stored in
+<name>.npz into the reference build and runs, per chain, the step loop of
+run_single_mcmcmc_chain (mcmcmc_sampler.h:994-1088): make_initial_mcmcmc_chain_state
+from the chain's seed (derive_mcmcmc_seed, :159-172, with the parallel driver's
+stream tag), warmup steps with lambda adaptation, production steps. It records
+every step's chosen mask and local normalisation, the production order
+signals, the final vertices and lambdas and the next 8 raw generator outputs,
+in mcmcmc_chains.npz.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, HERE)
+
+import bindings  # noqa: E402
+from make_golden import CASES, REFERENCE  # noqa: E402
+
+KINDS = ("twisted_up", "twisted_down", "ordinary_up", "ordinary_down")
+KEYS = ("upper", "lower", "upper_corners", "lower_corners")
+STREAM_TAG = 0x4D434D434D435348  # run_mcmcmc_chains_parallel (mcmcmc_sampler.h:1102)
+M64 = (1 << 64) - 1
+
+# name -> chain settings
+RUNS = {
+    "physical_2x2": dict(order_min=1, order_max=3, envelope=5, lambdas=[0.0, 1.0, 0.6, 0.3, 0.0, 0.0],
+                         warmup=24, adapt_interval=5, adapt_rate=0.25, production=20, base_seed=20261203),
+    "column_3x3": dict(order_min=2, order_max=4, envelope=6, lambdas=[0.0, 0.0, 1.0, 0.5, 0.25, 0.0, 0.0],
+                       warmup=16, adapt_interval=4, adapt_rate=0.25, production=24, base_seed=7),
+}
+CHAINS = 8
+
+
+def splitmix64(x):
+    x = (x + 0x9E3779B97F4A7C15) & M64
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & M64
+    return x ^ (x >> 31)
+
+
+def derive_seed(base, tag, index):
+    mixed = splitmix64(base ^ tag)
+    mixed ^= (0x9E3779B97F4A7C15 * (index + 1)) & M64
+    return splitmix64(mixed)
+
+
+def main():
+    bindings.build(REFERENCE)
+    ref = bindings.Reference()
+    out, meta = {}, {}
+    for name, run in RUNS.items():
+        data = np.load(os.path.join(HERE, f"{name}.npz"))
+        ref.configure(**CASES[name])
+        ref.set_tables({k: {key: data[f"table.{k}.{key}"] for key in KEYS} for k in KINDS})
+        seeds = [derive_seed(run["base_seed"], STREAM_TAG, i) for i in range(CHAINS)]
+        per = [ref.mcmcmc_chain(run["order_min"], run["order_max"], run["envelope"], run["lambdas"],
+                                run["warmup"], run["adapt_interval"], run["adapt_rate"], run["production"],
+                                s) for s in seeds]
+        out[f"{name}.seeds"] = np.array(seeds, dtype=np.uint64)
+        for key in ("chosen", "norms", "signal", "vertices", "lambdas", "rng"):
+            out[f"{name}.{key}"] = np.stack([p[key] for p in per])
+        meta[name] = run
+    np.savez_compressed(os.path.join(HERE, "mcmcmc_chains.npz"), **out)
+    with open(os.path.join(HERE, "mcmcmc_chains.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print({k: v.shape for k, v in out.items()})
+
+
+if __name__ == "__main__":
+    main()
