@@ -385,6 +385,55 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_mcmcmc(args):
+    """--mcmcmc: throughput of the device MCMCMC chains (a separate line, not
+    the headline): chain-steps/s of run_mcmcmc_step with the uniform seed on
+    the 6x6 / U=2 / beta=6 / half-lattice / degree-96 set, envelope 9, orders
+    1..8, with the oracle's single-threaded chain beside it."""
+    import torch
+    from cdet_gb300.integrand import CdetIntegrand
+    from cdet_gb300.mcmcmc import STREAM_TAG, McmcmcChains
+    from cdet_gb300.params import CdetParams, half_lattice_mask
+    from cdet_gb300.synthetic import derive_seed
+    from cdet_gb300.tables import build_tables
+    params = CdetParams(n1=6, n2=6, beta="6", mu="0", u="2", alpha_up="0", alpha_down="0",
+                        mask_sites=half_lattice_mask(6, 6), cheb_nu=96, cheb_nv=96)
+    env, omin, omax = 9, 1, 8
+    lambdas = [0.0] + [1.0] * 8 + [0.0]
+    chains_n = args.chains
+    tables = build_tables(params, device="cuda")
+    gpu = CdetIntegrand(params, tables)
+    out = {"metric": "MCMCMC chain-steps/s (uniform seed, envelope 9, orders 1..8)", "unit": "chain-steps/s",
+           "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "config": {"workload": "6x6 Hubbard U=2 beta=6 half lattice, degree 96, envelope 9, orders 1..8",
+                      "chains": chains_n}, "data": "synthetic (seeded chains, tables from the in-tree precompute)"}
+    for path in ("fp64", "split"):
+        gpu.set_assembly(path)
+        seeds = [derive_seed(20261203, STREAM_TAG, i) for i in range(chains_n)]
+        chains = McmcmcChains(gpu, omin, omax, env, seeds, lambdas, adapt_interval=1000)
+        chains.run(args.warmup, warmup=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        chains.run(args.steps, warmup=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[path] = {"value": chains_n * args.steps / dt, "ms_per_step": 1e3 * dt / args.steps}
+        chains.close()
+    out["value"] = out["split"]["value"]
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from bindings import Oracle
+        host = {k: {kk: vv.cpu().numpy() for kk, vv in t.items()} for k, t in tables.items()}
+        orc = Oracle(params.runtime_scalars(), host)
+        t0 = time.perf_counter()
+        n = 6
+        orc.mcmcmc_chain(omin, omax, env, lambdas, 0, 1000, 0.25, n, derive_seed(20261203, STREAM_TAG, 0))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "chain-steps/s", "cores": 1, "kind": "port",
+                               "sample": f"one chain, {n} production steps (C restatement of the reference chain)"}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -399,11 +448,16 @@ def main():
     ap.add_argument("--batch", type=int, default=65536, help="configurations per step per GPU")
     ap.add_argument("--path", choices=["both", "split", "fp64"], default="both",
                     help="both: time the FP64 form and the split form, report the split form")
+    ap.add_argument("--mcmcmc", action="store_true",
+                    help="time the device MCMCMC chains instead (a separate line, not the headline)")
+    ap.add_argument("--chains", type=int, default=8192, help="chains for --mcmcmc")
     args = ap.parse_args()
     global PRESET, BATCH
     PRESET, BATCH = args.preset, args.batch
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
-    if args.impl == "reference":
+    if args.mcmcmc:
+        run_mcmcmc(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
