@@ -16,6 +16,7 @@ proposals per step calls instead of one configuration at a time.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from collections import namedtuple
 from typing import Dict, Iterable, List, Optional, Sequence
 
@@ -55,7 +56,7 @@ class CdetIntegrand:
     the reference does when ALPHA_UP == ALPHA_DOWN.
     """
 
-    def __init__(self, params: CdetParams, tables: Dict[str, Dict], device: int = 0):
+    def __init__(self, params: CdetParams, tables: Optional[Dict[str, Dict]], device: int = 0):
         self.params = params
         self.scalars = params.runtime_scalars()
         self._lib = L.load()
@@ -67,7 +68,7 @@ class CdetIntegrand:
         self.coeff_count = 4 * sites * sites * params.cheb_nu * params.cheb_nv
         self.corner_count = 4 * sites * sites
         seen = {}
-        for kind, name in enumerate(L.KIND_NAMES):
+        for kind, name in enumerate(L.KIND_NAMES if tables is not None else ()):
             t = tables[name]
             if id(t) in seen:
                 L.check(self._lib.cdet_alias_table(self._ctx, kind, seen[id(t)]))
@@ -92,6 +93,18 @@ class CdetIntegrand:
             view = L.TableView(*[h.ctypes.data for h in host])
             L.check(self._lib.cdet_upload_table(self._ctx, kind, C.byref(view),
                                                 self.coeff_count, self.corner_count))
+
+    def load_chunks(self, directory: str) -> Optional[tuple]:
+        """Loads the four tables from a chunked load-data directory of the
+        reference's chunk workflow straight into HBM
+        (load_chunked_data_into_resident_tables, chunked_load_data.h:1467-1479).
+        Returns the directory's precomputed diagonal order-1 value (hi, lo),
+        or None when it has none."""
+        out = np.zeros(2)
+        L.check(self._lib.cdet_load_chunks(self._ctx, os.fsencode(directory),
+                                           out.ctypes.data_as(C.POINTER(C.c_double))))
+        self._keep = []
+        return None if np.isnan(out[0]) else (float(out[0]), float(out[1]))
 
     def close(self) -> None:
         if self._ctx:

@@ -32,7 +32,7 @@ EXPORTED = (
     "cdet_set_assembly", "cdet_prepare_split", "cdet_assemble_device",
     "cdet_integrand_device_noalloc", "cdet_diagonal_order1_density",
     "cdet_mcmcmc_create", "cdet_mcmcmc_run", "cdet_mcmcmc_end_warmup", "cdet_mcmcmc_state",
-    "cdet_mcmcmc_destroy",
+    "cdet_mcmcmc_destroy", "cdet_load_chunks",
 )
 
 ASSEMBLY_FP64 = 0
@@ -95,6 +95,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_mcmcmc_end_warmup.argtypes = [vp]
     lib.cdet_mcmcmc_state.argtypes = [vp, _DP, _DP, _UP]
     lib.cdet_mcmcmc_destroy.argtypes = [vp]
+    lib.cdet_load_chunks.argtypes = [vp, C.c_char_p, _DP]
     lib.cdet_last_error.restype = C.c_char_p
     lib.cdet_last_launch_count.argtypes = [vp]
     lib.cdet_integrand_device_noalloc.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp]

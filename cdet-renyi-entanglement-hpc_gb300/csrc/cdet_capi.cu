@@ -10,6 +10,8 @@
 
 #include <cmath>
 #include <cstdio>
+#include <filesystem>
+#include <fstream>
 #include <cstring>
 #include <map>
 #include <string>
@@ -180,6 +182,20 @@ size_t expected_corners(const cdet_runtime_scalars& s) {
 void release_slot(TableSlot& slot) {
     if (slot.owned) cudaFree(slot.owned);
     slot = TableSlot{};
+}
+
+// Drops the cached split slices of a slot's coefficients before the slot is
+// replaced: a new table may be allocated at the same device address.
+void forget_slices(cdet_context* ctx, const TableSlot& slot) {
+    if (!slot.ready) return;
+    for (auto it = ctx->sliced.begin(); it != ctx->sliced.end();) {
+        if (it->first.first == slot.dev.upper || it->first.first == slot.dev.lower) {
+            cudaFree(it->second.mem);
+            it = ctx->sliced.erase(it);
+        } else {
+            ++it;
+        }
+    }
 }
 
 int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
@@ -524,6 +540,7 @@ int cdet_upload_table(cdet_context* ctx, int kind, const cdet_table_view* t, siz
         return fail(CDET_ERR_INVALID, "null table array");
     DeviceGuard guard(ctx->device);
     TableSlot& slot = ctx->tables[kind];
+    forget_slices(ctx, slot);
     release_slot(slot);
     const size_t cb = coeff_count * sizeof(double), kb = corner_count * sizeof(double);
     void* mem = nullptr;
@@ -556,6 +573,7 @@ int cdet_bind_device_table(cdet_context* ctx, int kind, const cdet_table_view* t
     if (!t->upper_coeffs || !t->lower_coeffs || !t->upper_corners || !t->lower_corners)
         return fail(CDET_ERR_INVALID, "null table array");
     TableSlot& slot = ctx->tables[kind];
+    forget_slices(ctx, slot);
     release_slot(slot);
     slot.dev = cdet::TableDev{t->upper_coeffs, t->lower_coeffs, t->upper_corners, t->lower_corners};
     slot.ready = true;
@@ -976,3 +994,216 @@ int cdet_mcmcmc_destroy(cdet_mcmcmc* m) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ chunked table directory --
+namespace {
+
+bool read_key_values(const std::filesystem::path& path, std::map<std::string, std::string>& out) {
+    std::ifstream in(path);
+    if (!in.is_open()) return false;
+    std::string line;
+    while (std::getline(in, line)) {
+        if (line.empty() || line[0] == '#') continue;
+        const size_t pos = line.find('=');
+        if (pos == std::string::npos) continue;
+        out[line.substr(0, pos)] = line.substr(pos + 1);
+    }
+    return true;
+}
+
+struct TransformJob {
+    int kind, branch;  // branch 0 = upper, 1 = lower
+    size_t begin, end;
+};
+
+int kind_index(const std::string& name) {
+    static const char* names[4] = {"twisted_up", "twisted_down", "ordinary_up", "ordinary_down"};
+    for (int k = 0; k < 4; ++k)
+        if (name == names[k]) return k;
+    return -1;
+}
+
+const char* kind_name(int k) {
+    static const char* names[4] = {"twisted_up", "twisted_down", "ordinary_up", "ordinary_down"};
+    return names[k];
+}
+
+std::string range_token(size_t begin, size_t end) {
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%010zu_%010zu", begin, end);
+    return buf;
+}
+
+}  // namespace
+
+extern "C" int cdet_load_chunks(cdet_context* ctx, const char* dir, double* order1) {
+    namespace fs = std::filesystem;
+    if (!ctx || !dir) return fail(CDET_ERR_INVALID, "bad argument");
+    const fs::path root(dir);
+    // ensure_manifest_matches_for_real (chunked_load_data.h:884-906) for the
+    // entries this context can check
+    std::map<std::string, std::string> manifest;
+    if (!read_key_values(root / "manifest.txt", manifest))
+        return fail(CDET_ERR_INVALID, "Could not open " + (root / "manifest.txt").string());
+    const cdet_runtime_scalars& s = ctx->scalars;
+    const size_t sitepairs = ctx->corner_count;
+    const size_t nodes = static_cast<size_t>(s.cheb_nu) * s.cheb_nv;
+    const std::pair<const char*, std::string> expected[] = {
+        {"layout_version", "1"},
+        {"N1", std::to_string(s.n1)},
+        {"N2", std::to_string(s.n2)},
+        {"CHEB_NU", std::to_string(s.cheb_nu)},
+        {"CHEB_NV", std::to_string(s.cheb_nv)},
+        {"node_count", std::to_string(nodes)},
+        {"replica_sitepair_count", std::to_string(sitepairs)},
+        {"LOAD_DATA_REAL", "double"},
+        {"VECTOR_REAL", "double"},
+    };
+    for (const auto& [key, value] : expected) {
+        auto it = manifest.find(key);
+        if (it == manifest.end() || it->second != value)
+            return fail(CDET_ERR_INVALID, std::string("Chunk manifest mismatch for ") + key + ": expected " + value +
+                                              " but found " + (it == manifest.end() ? "(missing)" : it->second));
+    }
+    {
+        auto it = manifest.find("BETA");
+        if (it == manifest.end() || std::strtod(it->second.c_str(), nullptr) != s.beta)
+            return fail(CDET_ERR_INVALID, "Chunk manifest mismatch for BETA");
+    }
+    if (!fs::exists(root / "READY"))
+        return fail(CDET_ERR_INVALID, "Chunked load-data directory is missing READY: " + (root / "READY").string());
+    // read_chunked_transform_jobs (:510-534)
+    std::vector<TransformJob> jobs;
+    {
+        std::ifstream in(root / "transform_jobs.tsv");
+        if (!in.is_open()) return fail(CDET_ERR_INVALID, "Could not open " + (root / "transform_jobs.tsv").string());
+        std::string line;
+        while (std::getline(in, line)) {
+            if (line.empty() || line[0] == '#') continue;
+            std::vector<std::string> tok;
+            size_t start = 0;
+            while (true) {
+                const size_t tab = line.find('\t', start);
+                tok.push_back(line.substr(start, tab == std::string::npos ? std::string::npos : tab - start));
+                if (tab == std::string::npos) break;
+                start = tab + 1;
+            }
+            if (tok.size() < 5) return fail(CDET_ERR_INVALID, "Malformed transform job line: " + line);
+            TransformJob j{kind_index(tok[1]), tok[2] == "upper" ? 0 : (tok[2] == "lower" ? 1 : -1),
+                           static_cast<size_t>(std::stoull(tok[3])), static_cast<size_t>(std::stoull(tok[4]))};
+            if (j.kind < 0 || j.branch < 0 || j.end < j.begin || j.end > sitepairs)
+                return fail(CDET_ERR_INVALID, "Malformed transform job line: " + line);
+            jobs.push_back(j);
+        }
+    }
+    DeviceGuard guard(ctx->device);
+    const size_t cb = ctx->coeff_count * sizeof(double), kb = sitepairs * sizeof(double);
+    void* mem[4] = {nullptr, nullptr, nullptr, nullptr};
+    char* pinned[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    cudaStream_t stream = nullptr;
+    constexpr size_t kStage = size_t{32} << 20;
+    int rc = CDET_OK;
+    auto cleanup = [&](bool free_tables) {
+        if (stream) cudaStreamSynchronize(stream);
+        for (int i = 0; i < 2; ++i) {
+            if (pinned[i]) cudaFreeHost(pinned[i]);
+            if (done[i]) cudaEventDestroy(done[i]);
+        }
+        if (stream) cudaStreamDestroy(stream);
+        if (free_tables)
+            for (void* m : mem)
+                if (m) cudaFree(m);
+    };
+    cudaError_t err = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    for (int i = 0; err == cudaSuccess && i < 2; ++i) {
+        err = cudaHostAlloc(reinterpret_cast<void**>(&pinned[i]), kStage, cudaHostAllocDefault);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+    }
+    for (int k = 0; err == cudaSuccess && k < 4; ++k) {
+        err = cudaMalloc(&mem[k], 2 * cb + 2 * kb);
+        if (err == cudaSuccess) err = cudaMemsetAsync(mem[k], 0, 2 * cb + 2 * kb, stream);  // uncovered ranges stay 0
+    }
+    if (err != cudaSuccess) {
+        cleanup(true);
+        return cuda_fail(err, "allocating the chunked tables");
+    }
+    int slot_i = 0;
+    // one file into device memory through the two pinned buffers
+    auto stream_file = [&](const fs::path& path, size_t bytes, char* dst) -> int {
+        std::error_code ec;
+        const auto size = fs::file_size(path, ec);
+        if (ec) return fail(CDET_ERR_INVALID, "Could not stat " + path.string());
+        if (static_cast<size_t>(size) != bytes)
+            return fail(CDET_ERR_INVALID, "Unexpected file size for " + path.string() + ": expected " +
+                                              std::to_string(bytes) + " bytes, got " + std::to_string(size));
+        FILE* f = std::fopen(path.string().c_str(), "rb");
+        if (!f) return fail(CDET_ERR_INVALID, "Could not open " + path.string());
+        while (bytes > 0) {
+            const size_t n = bytes < kStage ? bytes : kStage;
+            cudaError_t e = cudaEventSynchronize(done[slot_i]);
+            if (e != cudaSuccess || std::fread(pinned[slot_i], 1, n, f) != n) {
+                std::fclose(f);
+                return e != cudaSuccess ? cuda_fail(e, "chunk copy") : fail(CDET_ERR_INVALID, "Short read from " + path.string());
+            }
+            e = cudaMemcpyAsync(dst, pinned[slot_i], n, cudaMemcpyHostToDevice, stream);
+            if (e == cudaSuccess) e = cudaEventRecord(done[slot_i], stream);
+            if (e != cudaSuccess) {
+                std::fclose(f);
+                return cuda_fail(e, "chunk copy");
+            }
+            dst += n;
+            bytes -= n;
+            slot_i ^= 1;
+        }
+        std::fclose(f);
+        return CDET_OK;
+    };
+    // load_coeff_chunks_for_branch (:1372-1392)
+    for (const TransformJob& j : jobs) {
+        const fs::path path = root / "coeffs" / kind_name(j.kind) / (j.branch == 0 ? "upper" : "lower") /
+                              ("sitepairs_" + range_token(j.begin, j.end) + ".bin");
+        char* dst = static_cast<char*>(mem[j.kind]) + (j.branch == 0 ? 0 : cb) + j.begin * nodes * sizeof(double);
+        rc = stream_file(path, (j.end - j.begin) * nodes * sizeof(double), dst);
+        if (rc != CDET_OK) break;
+    }
+    // load_corner_chunk_for_branch (:1394-1406)
+    for (int k = 0; rc == CDET_OK && k < 4; ++k)
+        for (int b = 0; rc == CDET_OK && b < 2; ++b) {
+            const fs::path path = root / "corners" / kind_name(k) / (b == 0 ? "upper.bin" : "lower.bin");
+            rc = stream_file(path, kb, static_cast<char*>(mem[k]) + 2 * cb + b * kb);
+        }
+    if (rc == CDET_OK) {
+        err = cudaStreamSynchronize(stream);
+        if (err != cudaSuccess) rc = cuda_fail(err, "chunk copy");
+    }
+    if (rc != CDET_OK) {
+        cleanup(true);
+        return rc;
+    }
+    cleanup(false);
+    for (int k = 0; k < 4; ++k) {
+        TableSlot& slot = ctx->tables[k];
+        forget_slices(ctx, slot);
+        release_slot(slot);
+        char* base = static_cast<char*>(mem[k]);
+        slot.owned = mem[k];
+        slot.dev = cdet::TableDev{reinterpret_cast<const double*>(base), reinterpret_cast<const double*>(base + cb),
+                                  reinterpret_cast<const double*>(base + 2 * cb),
+                                  reinterpret_cast<const double*>(base + 2 * cb + kb)};
+        slot.ready = true;
+    }
+    // read_chunked_diagonal_observable_value (:1320-1329), when present
+    if (order1) {
+        order1[0] = order1[1] = std::nan("");
+        std::map<std::string, std::string> diag;
+        if (read_key_values(root / "diagonal_observable.txt", diag)) {
+            auto hi = diag.find("order1_hi"), lo = diag.find("order1_lo");
+            if (hi == diag.end() || lo == diag.end())
+                return fail(CDET_ERR_INVALID, "Malformed " + (root / "diagonal_observable.txt").string());
+            order1[0] = std::stod(hi->second);
+            order1[1] = std::stod(lo->second);
+        }
+    }
+    return CDET_OK;
+}

@@ -166,6 +166,18 @@ int cdet_all_subsets_host(cdet_context* ctx, const double* vertices, int envelop
  * throws "The diagonal observable is undefined for U = 0"). */
 int cdet_diagonal_order1_density(cdet_context* ctx, double alpha_up, double alpha_down, double* out);
 
+/* Loads the four tables from a chunked load-data directory written by the
+ * reference's chunk workflow (chunked_load_data.h: manifest.txt, READY,
+ * transform_jobs.tsv, coeffs/<kind>/<branch>/sitepairs_<begin>_<end>.bin,
+ * corners/<kind>/<branch>.bin), replacing load_chunked_data_into_resident_tables
+ * (:1467-1479) and the disk-LRU backend (:1481-1515): every coefficient chunk is
+ * streamed from disk through pinned buffers straight into HBM, once. The
+ * manifest must match the context (layout_version, N1, N2, CHEB_NU, CHEB_NV,
+ * node and sitepair counts, BETA, double tables). order1 (optional, [2]): the
+ * precomputed diagonal order-1 value (diagonal_observable.txt, hi and lo), NaN
+ * when the directory has none. */
+int cdet_load_chunks(cdet_context* ctx, const char* dir, double* order1);
+
 /* ------------------------------------------------- MCMCMC chains on the GPU
  * A batch of MCMCMC chains (run_single_mcmcmc_chain, mcmcmc_sampler.h:994-1088)
  * resident on the GPU, with the uniform seed kernel (MCMCMC_SEED_MODE=uniform,

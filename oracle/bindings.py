@@ -278,6 +278,8 @@ class Reference:
         lib.ref_fpm_fallbacks.restype = C.c_ulonglong
         lib.ref_sample_vertices.argtypes = [C.c_ulonglong, C.c_int, _DP]
         lib.ref_diagonal_order1.argtypes = [_DP]
+        lib.ref_chunk_workflow.argtypes = [C.c_char_p, C.c_int, C.c_int]
+        lib.ref_load_chunks.argtypes = [C.c_char_p]
         _UP = C.POINTER(C.c_ulonglong)
         lib.ref_mcmcmc_chain.argtypes = [C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_double,
                                          C.c_int, C.c_ulonglong, _UP, _DP, _DP, _DP, _DP, _UP]
@@ -356,6 +358,15 @@ class Reference:
                                               chosen.ctypes.data_as(up), _ptr(norms), _ptr(signal),
                                               _ptr(verts), _ptr(lam_out), rng.ctypes.data_as(up)))
         return dict(chosen=chosen, norms=norms, signal=signal, vertices=verts, lambdas=lam_out, rng=rng)
+
+    def chunk_workflow(self, directory: str, node_chunk_size: int, sitepair_chunk_size: int) -> None:
+        """Runs every stage of the reference's chunked load-data workflow into
+        `directory` for the configured parameter set."""
+        self._check(self.lib.ref_chunk_workflow(directory.encode(), node_chunk_size, sitepair_chunk_size))
+
+    def load_chunks(self, directory: str) -> None:
+        """load_chunked_data_into_resident_tables from `directory`."""
+        self._check(self.lib.ref_load_chunks(directory.encode()))
 
     def diagonal_order1(self) -> np.ndarray:
         """[normalised hi, twisted, ordinary, normalised lo] from the reference."""

@@ -28,11 +28,17 @@
 //                             solve the Chebyshev accuracy audit compares with.
 //   ref_diagonal_order1    -> normalized_log_partition_first_order_density_dd and its
 //                             twisted / ordinary parts (diagonal_green_observable.h:237-327)
+//   ref_chunk_workflow     -> the chunked load-data stages main.cpp runs one job at a
+//                             time (chunked_load_data.h:1530-1570): plan, node
+//                             samples, corners, sitepair transforms, diagonal
+//                             reduce, validate
+//   ref_load_chunks        -> load_chunked_data_into_resident_tables (:1467-1479)
 //   ref_mcmcmc_chain       -> the step loop of run_single_mcmcmc_chain
 //                             (mcmcmc_sampler.h:994-1088) with the uniform seed, no
 //                             checkpoints, recording every step
 
 #include "cdet/cdet_integrand_evaluator.h"
+#include "cdet/chunked_load_data.h"
 #include "cdet/diagonal_green_observable.h"
 #include "cdet/load_data.h"
 #include "cdet/mcmcmc_sampler.h"
@@ -362,6 +368,36 @@ int ref_mcmcmc_chain(int order_min, int order_max, int envelope_order, const dou
         }
         for (int order = 0; order <= envelope_order; ++order) lambdas_out[order] = state.lambdas[static_cast<std::size_t>(order)];
         for (int i = 0; i < 8; ++i) rng_out[i] = state.rng();
+    });
+}
+
+int ref_chunk_workflow(const char* dir, int node_chunk_size, int sitepair_chunk_size) {
+    return guarded([&] {
+        load_data_chunk_dir = dir;
+        load_data_node_chunk_size = node_chunk_size;
+        load_data_sitepair_chunk_size = sitepair_chunk_size;
+        run_chunked_load_data_planner();
+        for (const ChunkedNodeJob& job : read_chunked_node_jobs()) {
+            setenv("CDET_LOAD_DATA_JOB_INDEX", std::to_string(job.index).c_str(), 1);
+            run_chunked_load_data_sample_node_job();
+        }
+        for (const ChunkedCornerJob& job : read_chunked_corner_jobs()) {
+            setenv("CDET_LOAD_DATA_JOB_INDEX", std::to_string(job.index).c_str(), 1);
+            run_chunked_load_data_corner_job();
+        }
+        for (const ChunkedSitepairJob& job : read_chunked_transform_jobs()) {
+            setenv("CDET_LOAD_DATA_JOB_INDEX", std::to_string(job.index).c_str(), 1);
+            run_chunked_load_data_transform_sitepair_job();
+        }
+        run_chunked_load_data_diagonal_reduce();
+        validate_chunked_load_data_outputs();
+    });
+}
+
+int ref_load_chunks(const char* dir) {
+    return guarded([&] {
+        load_data_chunk_dir = dir;
+        load_chunked_data_into_resident_tables();
     });
 }
 
