@@ -98,6 +98,11 @@ class Oracle:
         lib.oracle_mcmcmc_chain.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, _DP, C.c_int,
                                             C.c_int, C.c_double, C.c_int, C.c_uint64, _UP, _DP, _DP, _DP, _DP,
                                             _UP]
+        lib.oracle_mcmcmc_chain_hist.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, _DP, C.c_int,
+                                                 C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int, _DP, _DP, _DP,
+                                                 _UP, _DP, _DP, _DP, _DP, _UP]
+        lib.oracle_learn_histogram.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                               C.c_int, C.c_double, C.c_double, C.c_uint64, _DP, _DP, _DP, _DP]
         self.scalars = OracleScalars(**{k: scalars[k] for k, _ in OracleScalars._fields_})
         self._keep = {k: _as_numpy_table(tables[k]) for k in KINDS}
         tabs = {}
@@ -167,8 +172,9 @@ class Oracle:
         return out
 
     def mcmcmc_chain(self, order_min, order_max, envelope, lambdas, warmup, adapt_interval,
-                     adapt_rate, production, seed):
-        """One chain with the uniform seed kernel; the same outputs as
+                     adapt_rate, production, seed, histogram=None):
+        """One chain with the uniform seed kernel, or the histogram seed of
+        histogram = (tau_bins, tau, space, replica); the same outputs as
         Reference.mcmcmc_chain."""
         steps = warmup + production
         chosen = np.zeros(steps, dtype=np.uint64)
@@ -179,13 +185,36 @@ class Oracle:
         lam_out = np.zeros(envelope + 1)
         rng = np.zeros(8, dtype=np.uint64)
         up = C.POINTER(C.c_uint64)
-        rc = self.lib.oracle_mcmcmc_chain(C.byref(self.scalars), C.byref(self.tables), order_min, order_max,
-                                          envelope, _ptr(lam), warmup, adapt_interval, adapt_rate, production,
-                                          seed, chosen.ctypes.data_as(up), _ptr(norms), _ptr(signal),
-                                          _ptr(verts), _ptr(lam_out), rng.ctypes.data_as(up))
+        if histogram is None:
+            rc = self.lib.oracle_mcmcmc_chain(C.byref(self.scalars), C.byref(self.tables), order_min, order_max,
+                                              envelope, _ptr(lam), warmup, adapt_interval, adapt_rate, production,
+                                              seed, chosen.ctypes.data_as(up), _ptr(norms), _ptr(signal),
+                                              _ptr(verts), _ptr(lam_out), rng.ctypes.data_as(up))
+        else:
+            bins, ht, hs, hr = histogram
+            ht, hs, hr = (np.ascontiguousarray(x, dtype=np.float64) for x in (ht, hs, hr))
+            rc = self.lib.oracle_mcmcmc_chain_hist(C.byref(self.scalars), C.byref(self.tables), order_min,
+                                                   order_max, envelope, _ptr(lam), warmup, adapt_interval,
+                                                   adapt_rate, production, seed, bins, _ptr(ht), _ptr(hs),
+                                                   _ptr(hr), chosen.ctypes.data_as(up), _ptr(norms),
+                                                   _ptr(signal), _ptr(verts), _ptr(lam_out),
+                                                   rng.ctypes.data_as(up))
         if rc != 0:
             raise RuntimeError(f"oracle chain failed ({rc})")
         return dict(chosen=chosen, norms=norms, signal=signal, vertices=verts, lambdas=lam_out, rng=rng)
+
+    def learn_histogram(self, order_min, order_max, envelope, learning_steps, tau_bins, uniform_mix,
+                        pseudo_count, base_seed):
+        """learn_factorized_histogram_seed: (tau, space, replica, total pair weight)."""
+        sites = self.scalars.n1 * self.scalars.n2
+        tau, space, rep = np.zeros(tau_bins * tau_bins), np.zeros(sites * sites), np.zeros(4)
+        total = C.c_double()
+        rc = self.lib.oracle_learn_histogram(C.byref(self.scalars), C.byref(self.tables), order_min, order_max,
+                                             envelope, learning_steps, tau_bins, uniform_mix, pseudo_count,
+                                             base_seed, _ptr(tau), _ptr(space), _ptr(rep), C.byref(total))
+        if rc != 0:
+            raise RuntimeError(f"oracle histogram learning failed ({rc})")
+        return tau, space, rep, total.value
 
     @staticmethod
     def _lib():
@@ -282,7 +311,10 @@ class Reference:
         lib.ref_load_chunks.argtypes = [C.c_char_p]
         _UP = C.POINTER(C.c_ulonglong)
         lib.ref_mcmcmc_chain.argtypes = [C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_double,
-                                         C.c_int, C.c_ulonglong, _UP, _DP, _DP, _DP, _DP, _UP]
+                                         C.c_int, C.c_ulonglong, C.c_int, _DP, _DP, _DP, _UP, _DP, _DP, _DP,
+                                         _DP, _UP]
+        lib.ref_learn_histogram.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                            C.c_double, C.c_ulonglong, _DP, _DP, _DP, _DP]
 
     def _check(self, rc):
         if rc != 0:
@@ -340,10 +372,11 @@ class Reference:
         return out
 
     def mcmcmc_chain(self, order_min, order_max, envelope, lambdas, warmup, adapt_interval,
-                     adapt_rate, production, seed):
-        """One reference chain (uniform seed): per-step chosen masks and local
-        normalisations, production order signals, final vertices, lambdas and
-        the next 8 raw generator outputs."""
+                     adapt_rate, production, seed, histogram=None):
+        """One reference chain (uniform seed, or the FactorizedHistogramSeed of
+        histogram = (tau_bins, tau, space, replica)): per-step chosen masks and
+        local normalisations, production order signals, final vertices,
+        lambdas and the next 8 raw generator outputs."""
         steps = warmup + production
         chosen = np.zeros(steps, dtype=np.uint64)
         norms = np.zeros(steps)
@@ -353,11 +386,26 @@ class Reference:
         lam_out = np.zeros(envelope + 1)
         rng = np.zeros(8, dtype=np.uint64)
         up = C.POINTER(C.c_ulonglong)
+        bins, ht, hs, hr = (0, np.zeros(1), np.zeros(1), np.zeros(1)) if histogram is None else histogram
+        ht, hs, hr = (np.ascontiguousarray(x, dtype=np.float64) for x in (ht, hs, hr))
         self._check(self.lib.ref_mcmcmc_chain(order_min, order_max, envelope, _ptr(lam), warmup,
-                                              adapt_interval, adapt_rate, production, seed,
-                                              chosen.ctypes.data_as(up), _ptr(norms), _ptr(signal),
-                                              _ptr(verts), _ptr(lam_out), rng.ctypes.data_as(up)))
+                                              adapt_interval, adapt_rate, production, seed, bins, _ptr(ht),
+                                              _ptr(hs), _ptr(hr), chosen.ctypes.data_as(up), _ptr(norms),
+                                              _ptr(signal), _ptr(verts), _ptr(lam_out), rng.ctypes.data_as(up)))
         return dict(chosen=chosen, norms=norms, signal=signal, vertices=verts, lambdas=lam_out, rng=rng)
+
+    def learn_histogram(self, order_min, order_max, envelope, learning_steps, tau_bins, uniform_mix,
+                        pseudo_count, base_seed, sites):
+        """learn_factorized_histogram_seed: (tau, space, replica) row
+        probabilities and the total pair weight."""
+        tau = np.zeros(tau_bins * tau_bins)
+        space = np.zeros(sites * sites)
+        rep = np.zeros(4)
+        total = C.c_double()
+        self._check(self.lib.ref_learn_histogram(order_min, order_max, envelope, learning_steps, tau_bins,
+                                                 uniform_mix, pseudo_count, base_seed, _ptr(tau), _ptr(space),
+                                                 _ptr(rep), C.byref(total)))
+        return tau, space, rep, total.value
 
     def chunk_workflow(self, directory: str, node_chunk_size: int, sitepair_chunk_size: int) -> None:
         """Runs every stage of the reference's chunked load-data workflow into

@@ -869,19 +869,131 @@ static void adapt_lambdas(double* lambdas, int order_min, int order_max, double 
     }
 }
 
-/* run_mcmcmc_step (mcmcmc_sampler.h:524-577) with the uniform seed kernel. */
+/* FactorizedHistogramSeed (mcmcmc_seed.h:71-229); bins == 0: the uniform seed. */
+typedef struct hist_seed {
+    int bins, n1, n2, sites;
+    const double *tau_prob, *space_prob, *rep_prob;
+    double *tau_cdf, *space_cdf, *rep_cdf;
+} hist_seed;
+
+/* unit_coordinate_to_index (mcmcmc_seed.h:30-39) */
+static int unit_index(double value, int extent) {
+    const int index = (int)floor(value * (double)extent);
+    if (index < 0) return 0;
+    if (index >= extent) return extent - 1;
+    return index;
+}
+
+/* build_cdfs (:190-203) */
+static void build_cdf(const double* prob, int columns, int rows, double* cdf) {
+    for (int r = 0; r < rows; ++r) {
+        double cumulative = 0.0;
+        for (int c = 0; c < columns; ++c) {
+            cumulative += prob[r * columns + c];
+            cdf[r * columns + c] = cumulative;
+        }
+        cdf[r * columns + columns - 1] = 1.0;
+    }
+}
+
+/* sample_from_row (:205-218): std::lower_bound of a canonical draw */
+static int sample_row(const double* cdf, int columns, int row, oracle_mt64* rng) {
+    const double threshold = oracle_canonical(rng);
+    const double* b = cdf + (size_t)row * columns;
+    for (int c = 0; c < columns; ++c)
+        if (!(b[c] < threshold)) return c;
+    return columns - 1;
+}
+
+/* sample_child_from_parent (:106-128) */
+static void hist_child(const hist_seed* h, const double* parent, oracle_mt64* rng, double* child) {
+    const int child_tau = sample_row(h->tau_cdf, h->bins, unit_index(parent[0], h->bins), rng);
+    const int parent_site = unit_index(parent[1], h->n1) * h->n2 + unit_index(parent[2], h->n2);
+    const int child_site = sample_row(h->space_cdf, h->sites, parent_site, rng);
+    const int child_x = child_site / h->n2;
+    const int child_y = child_site - child_x * h->n2;
+    const int child_rep = sample_row(h->rep_cdf, 2, unit_index(parent[3], 2), rng);
+    child[0] = ((double)child_tau + oracle_canonical(rng)) / (double)h->bins;
+    child[1] = ((double)child_x + oracle_canonical(rng)) / (double)h->n1;
+    child[2] = ((double)child_y + oracle_canonical(rng)) / (double)h->n2;
+    child[3] = ((double)child_rep + oracle_canonical(rng)) / 2.0;
+}
+
+/* density_child_given_parent (:130-150) */
+static double hist_density(const hist_seed* h, const double* child, const double* parent) {
+    const double tau_d = h->tau_prob[unit_index(parent[0], h->bins) * h->bins + unit_index(child[0], h->bins)] *
+                         (double)h->bins;
+    const int ps = unit_index(parent[1], h->n1) * h->n2 + unit_index(parent[2], h->n2);
+    const int cs = unit_index(child[1], h->n1) * h->n2 + unit_index(child[2], h->n2);
+    const double space_d = h->space_prob[ps * h->sites + cs] * (double)h->sites;
+    const double rep_d = h->rep_prob[unit_index(parent[3], 2) * 2 + unit_index(child[3], 2)] * 2.0;
+    return tau_d * space_d * rep_d;
+}
+
+/* compute_conditional_generation_probabilities_typed_into<double>
+ * (mcmcmc_sampler.h:252-335); cd is [2^n][n] scratch. Returns 4 on a
+ * negative or non-finite seed density. */
+static int conditional_probabilities(const hist_seed* h, const double* v, int n, double* prob, double* cd) {
+    double sd[64 * 64];
+    for (int c = 0; c < n; ++c)
+        for (int p = 0; p < n; ++p) {
+            if (c == p) {
+                sd[c * n + p] = 0.0;
+                continue;
+            }
+            const double d = hist_density(h, v + 4 * c, v + 4 * p);
+            if (d < 0.0 || !isfinite(d)) return 4;
+            sd[c * n + p] = d;
+        }
+    const uint64_t count = (uint64_t)1 << n, full = count - 1;
+    for (int c = 0; c < n; ++c) {
+        double sum = 0.0;
+        for (int p = 0; p < n; ++p) sum += sd[c * n + p];
+        cd[c] = sum;
+    }
+    for (uint64_t m = 0; m < count; ++m) prob[m] = 0.0;
+    prob[0] = 1.0;
+    for (uint64_t gm = 1; gm < full; ++gm) {
+        const uint64_t low = gm & (~gm + 1);
+        const int removed = __builtin_ctzll(low);
+        const uint64_t prev = gm ^ low;
+        for (int c = 0; c < n; ++c) {
+            double d = cd[prev * n + c] - sd[c * n + removed];
+            if (d < 0.0 && d > -1.0e-12) d = 0.0;
+            cd[gm * n + c] = d;
+        }
+        const int gc = __builtin_popcountll(gm), pc = n - gc;
+        double sum = 0.0;
+        for (int c = 0; c < n; ++c) {
+            const uint64_t cb = (uint64_t)1 << c;
+            if (!(gm & cb)) continue;
+            sum += prob[gm ^ cb] * cd[gm * n + c];
+        }
+        prob[gm] = sum / ((double)gc * (double)pc);
+    }
+    prob[full] = 0.0;
+    return 0;
+}
+
+/* run_mcmcmc_step (mcmcmc_sampler.h:524-577) with the uniform seed kernel, or
+ * the histogram seed when h->bins > 0. */
 static int mcmcmc_step(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max, int envelope,
                        const double* lambdas, const double* inv_binom, double* vertices, oracle_mt64* rng,
                        double* values, double* fluxes, double* weights, uint64_t* chosen_out, double* norm_out,
-                       double* signal) {
+                       double* signal, const hist_seed* h, double* cprob, double* cd) {
     if (oracle_all_subsets(s, t, vertices, envelope, values) & ORACLE_NONFINITE) return 1;
+    const uint64_t full_mask = ((uint64_t)1 << envelope) - 1;
+    if (h->bins > 0) {
+        const int rc = conditional_probabilities(h, vertices, envelope, cprob, cd);
+        if (rc) return rc;
+    }
     const uint64_t subsets = (uint64_t)1 << envelope;
     double norm = 0.0;
     int idx = 0;
     for (uint64_t mask = 1; mask < subsets; ++mask) {
         const int o = __builtin_popcountll(mask);
         if (o < order_min || o > order_max) continue;
-        const double flux = lambdas[o] * values[mask] * 1.0;
+        const double flux = lambdas[o] * values[mask] * (h->bins > 0 ? cprob[full_mask ^ mask] : 1.0);
         const double w = fabs(flux) * inv_binom[o];
         fluxes[idx] = flux;
         weights[idx] = w;
@@ -925,8 +1037,12 @@ static int mcmcmc_step(const oracle_scalars* s, const oracle_tables* t, int orde
             ++size;
         }
     while (size < envelope) {
-        (void)oracle_uniform_int(rng, size); /* the parent; the uniform kernel ignores it */
-        for (int k = 0; k < 4; ++k) next[4 * size + k] = oracle_canonical(rng);
+        const int parent = oracle_uniform_int(rng, size);
+        if (h->bins > 0) {
+            hist_child(h, next + 4 * parent, rng, next + 4 * size);
+        } else {
+            for (int k = 0; k < 4; ++k) next[4 * size + k] = oracle_canonical(rng); /* uniform: parent ignored */
+        }
         ++size;
     }
     memcpy(vertices, next, sizeof(double) * 4 * (size_t)envelope);
@@ -935,9 +1051,9 @@ static int mcmcmc_step(const oracle_scalars* s, const oracle_tables* t, int orde
     return 0;
 }
 
-int oracle_mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
-                        int envelope, const double* lambdas_in, int warmup, int adapt_interval, double adapt_rate,
-                        int production, uint64_t seed, uint64_t* chosen, double* norms, double* signal,
+static int mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max, int envelope,
+                        const double* lambdas_in, int warmup, int adapt_interval, double adapt_rate, int production,
+                        uint64_t seed, const hist_seed* h, uint64_t* chosen, double* norms, double* signal,
                         double* vertices_out, double* lambdas_out, uint64_t* rng_out) {
     oracle_mt64 rng;
     oracle_mt64_seed(&rng, seed);
@@ -954,12 +1070,14 @@ int oracle_mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int ord
     double* values = (double*)malloc(sizeof(double) * subsets);
     double* fluxes = (double*)malloc(sizeof(double) * subsets);
     double* weights = (double*)malloc(sizeof(double) * subsets);
+    double* cprob = (double*)malloc(sizeof(double) * subsets);
+    double* cd = (double*)malloc(sizeof(double) * subsets * (size_t)envelope);
     double step_signal[65];
-    int rc = (values && fluxes && weights) ? 0 : 3;
+    int rc = (values && fluxes && weights && cprob && cd) ? 0 : 3;
     int k = 0;
     for (int step = 0; rc == 0 && step < warmup; ++step, ++k) {
         rc = mcmcmc_step(s, t, order_min, order_max, envelope, lambdas, inv_binom, vertices, &rng, values, fluxes,
-                         weights, &chosen[k], &norms[k], step_signal);
+                         weights, &chosen[k], &norms[k], step_signal, h, cprob, cd);
         if (rc) break;
         ++counts[__builtin_popcountll(chosen[k])];
         if ((step + 1) % adapt_interval == 0) {
@@ -974,14 +1092,150 @@ int oracle_mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int ord
     }
     for (int step = 0; rc == 0 && step < production; ++step, ++k) {
         rc = mcmcmc_step(s, t, order_min, order_max, envelope, lambdas, inv_binom, vertices, &rng, values, fluxes,
-                         weights, &chosen[k], &norms[k], signal + (size_t)step * (envelope + 1));
+                         weights, &chosen[k], &norms[k], signal + (size_t)step * (envelope + 1), h, cprob, cd);
     }
     free(values);
     free(fluxes);
     free(weights);
+    free(cprob);
+    free(cd);
     if (rc) return rc;
     memcpy(vertices_out, vertices, sizeof(double) * 4 * (size_t)envelope);
     for (int o = 0; o <= envelope; ++o) lambdas_out[o] = lambdas[o];
     for (int i = 0; i < 8; ++i) rng_out[i] = oracle_mt64_next(&rng);
+    return 0;
+}
+
+int oracle_mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
+                        int envelope, const double* lambdas_in, int warmup, int adapt_interval, double adapt_rate,
+                        int production, uint64_t seed, uint64_t* chosen, double* norms, double* signal,
+                        double* vertices_out, double* lambdas_out, uint64_t* rng_out) {
+    const hist_seed none = {0, 0, 0, 0, NULL, NULL, NULL, NULL, NULL, NULL};
+    return mcmcmc_chain(s, t, order_min, order_max, envelope, lambdas_in, warmup, adapt_interval, adapt_rate,
+                        production, seed, &none, chosen, norms, signal, vertices_out, lambdas_out, rng_out);
+}
+
+int oracle_mcmcmc_chain_hist(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
+                             int envelope, const double* lambdas_in, int warmup, int adapt_interval, double adapt_rate,
+                             int production, uint64_t seed, int tau_bins, const double* tau_prob,
+                             const double* space_prob, const double* replica_prob, uint64_t* chosen, double* norms,
+                             double* signal, double* vertices_out, double* lambdas_out, uint64_t* rng_out) {
+    hist_seed h;
+    h.bins = tau_bins;
+    h.n1 = s->n1;
+    h.n2 = s->n2;
+    h.sites = s->n1 * s->n2;
+    h.tau_prob = tau_prob;
+    h.space_prob = space_prob;
+    h.rep_prob = replica_prob;
+    h.tau_cdf = (double*)malloc(sizeof(double) * (size_t)tau_bins * tau_bins);
+    h.space_cdf = (double*)malloc(sizeof(double) * (size_t)h.sites * h.sites);
+    h.rep_cdf = (double*)malloc(sizeof(double) * 4);
+    int rc = 3;
+    if (h.tau_cdf && h.space_cdf && h.rep_cdf) {
+        build_cdf(tau_prob, tau_bins, tau_bins, h.tau_cdf);
+        build_cdf(space_prob, h.sites, h.sites, h.space_cdf);
+        build_cdf(replica_prob, 2, 2, h.rep_cdf);
+        rc = mcmcmc_chain(s, t, order_min, order_max, envelope, lambdas_in, warmup, adapt_interval, adapt_rate,
+                          production, seed, &h, chosen, norms, signal, vertices_out, lambdas_out, rng_out);
+    }
+    free(h.tau_cdf);
+    free(h.space_cdf);
+    free(h.rep_cdf);
+    return rc;
+}
+
+/* splitmix64_mcmcmc / derive_mcmcmc_seed (mcmcmc_sampler.h:159-172) */
+static uint64_t splitmix64(uint64_t x) {
+    x += 0x9e3779b97f4a7c15ULL;
+    x = (x ^ (x >> 30U)) * 0xbf58476d1ce4e5b9ULL;
+    x = (x ^ (x >> 27U)) * 0x94d049bb133111ebULL;
+    return x ^ (x >> 31U);
+}
+
+static uint64_t derive_seed(uint64_t base, uint64_t tag, uint64_t index) {
+    uint64_t mixed = splitmix64(base ^ tag);
+    mixed ^= 0x9e3779b97f4a7c15ULL * (index + 1ULL);
+    return splitmix64(mixed);
+}
+
+/* FactorizedHistogramSeedAccumulator::normalize_rows (mcmcmc_seed.h:288-327) */
+static void normalize_rows(const long double* counts, int columns, int rows, double mix_d, double pseudo_d,
+                           double* out) {
+    const long double uniform = 1.0L / (long double)columns;
+    const long double mix = (long double)mix_d, pseudo = (long double)pseudo_d;
+    for (int r = 0; r < rows; ++r) {
+        long double row_sum = 0.0L;
+        for (int c = 0; c < columns; ++c) row_sum += counts[r * columns + c];
+        const long double denominator = row_sum + pseudo * (long double)columns;
+        for (int c = 0; c < columns; ++c) {
+            long double learned = uniform;
+            if (denominator > 0.0L) learned = (counts[r * columns + c] + pseudo) / denominator;
+            const long double probability = (1.0L - mix) * learned + mix * uniform;
+            out[r * columns + c] = (double)probability;
+        }
+        double row_total = 0.0;
+        for (int c = 0; c < columns; ++c) row_total += out[r * columns + c];
+        if (row_total > 0.0 && isfinite(row_total))
+            for (int c = 0; c < columns; ++c) out[r * columns + c] /= row_total;
+    }
+}
+
+int oracle_learn_histogram(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
+                           int envelope, int learning_steps, int tau_bins, double uniform_mix, double pseudo_count,
+                           uint64_t base_seed, double* tau_out, double* space_out, double* replica_out,
+                           double* total_weight_out) {
+    const int sites = s->n1 * s->n2;
+    long double* tau_c = (long double*)calloc((size_t)tau_bins * tau_bins, sizeof(long double));
+    long double* space_c = (long double*)calloc((size_t)sites * sites, sizeof(long double));
+    long double rep_c[4] = {0.0L, 0.0L, 0.0L, 0.0L};
+    long double total = 0.0L;
+    const size_t subsets = (size_t)1 << envelope;
+    double* values = (double*)malloc(sizeof(double) * subsets);
+    if (!tau_c || !space_c || !values) {
+        free(tau_c);
+        free(space_c);
+        free(values);
+        return 3;
+    }
+    oracle_mt64 rng;
+    oracle_mt64_seed(&rng, derive_seed(base_seed, 0x484953544F534545ULL, 0));
+    double v[64 * 4];
+    for (int step = 0; step < learning_steps; ++step) {
+        for (int i = 0; i < envelope * 4; ++i) v[i] = oracle_canonical(&rng); /* sample_uniform_vertex_set */
+        (void)oracle_all_subsets(s, t, v, envelope, values);
+        for (uint64_t mask = 1; mask < subsets; ++mask) {
+            const int order = __builtin_popcountll(mask);
+            if (order < order_min || order > order_max || order < 2) continue;
+            const double value = values[mask];
+            if (!isfinite(value)) continue;
+            const long double subset_weight = (long double)fabs(value) / (long double)binomial_double(envelope, order);
+            const long double pair_weight = subset_weight / (long double)(order * (order - 1));
+            if (!(pair_weight > 0.0L)) continue;
+            for (int p = 0; p < envelope; ++p) {
+                if (!(mask & ((uint64_t)1 << p))) continue;
+                for (int c = 0; c < envelope; ++c) {
+                    if (c == p || !(mask & ((uint64_t)1 << c))) continue;
+                    /* add_pair (mcmcmc_seed.h:249-258) */
+                    if (!(pair_weight > 0.0L) || !isfinite((double)pair_weight)) continue;
+                    const double* pv = v + 4 * p;
+                    const double* cv = v + 4 * c;
+                    tau_c[unit_index(pv[0], tau_bins) * tau_bins + unit_index(cv[0], tau_bins)] += pair_weight;
+                    const int ps = unit_index(pv[1], s->n1) * s->n2 + unit_index(pv[2], s->n2);
+                    const int cs = unit_index(cv[1], s->n1) * s->n2 + unit_index(cv[2], s->n2);
+                    space_c[ps * sites + cs] += pair_weight;
+                    rep_c[unit_index(pv[3], 2) * 2 + unit_index(cv[3], 2)] += pair_weight;
+                    total += pair_weight;
+                }
+            }
+        }
+    }
+    normalize_rows(tau_c, tau_bins, tau_bins, uniform_mix, pseudo_count, tau_out);
+    normalize_rows(space_c, sites, sites, uniform_mix, pseudo_count, space_out);
+    normalize_rows(rep_c, 2, 2, uniform_mix, pseudo_count, replica_out);
+    *total_weight_out = (double)total;
+    free(tau_c);
+    free(space_c);
+    free(values);
     return 0;
 }

@@ -137,6 +137,25 @@ int oracle_mcmcmc_chain(const oracle_scalars* s, const oracle_tables* t, int ord
                         int production, uint64_t seed, uint64_t* chosen, double* norms, double* signal,
                         double* vertices_out, double* lambdas_out, uint64_t* rng_out);
 
+/* The same with the FactorizedHistogramSeed (mcmcmc_seed.h:71-229) of the
+ * given row probabilities: tau [tau_bins][tau_bins], space [S][S] (S = N1 N2),
+ * replica [2][2]; the conditional generation probabilities
+ * (mcmcmc_sampler.h:252-335) weight the fluxes. Returns 4 when a seed density
+ * is negative or not finite. */
+int oracle_mcmcmc_chain_hist(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
+                             int envelope, const double* lambdas, int warmup, int adapt_interval, double adapt_rate,
+                             int production, uint64_t seed, int tau_bins, const double* tau_prob,
+                             const double* space_prob, const double* replica_prob, uint64_t* chosen, double* norms,
+                             double* signal, double* vertices_out, double* lambdas_out, uint64_t* rng_out);
+
+/* learn_factorized_histogram_seed (mcmcmc_sampler.h:602-664): the learned row
+ * probabilities (long double accumulation, as the reference) and the total
+ * pair weight. */
+int oracle_learn_histogram(const oracle_scalars* s, const oracle_tables* t, int order_min, int order_max,
+                           int envelope, int learning_steps, int tau_bins, double uniform_mix, double pseudo_count,
+                           uint64_t base_seed, double* tau_out, double* space_out, double* replica_out,
+                           double* total_weight_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,8 +34,10 @@
 //                             reduce, validate
 //   ref_load_chunks        -> load_chunked_data_into_resident_tables (:1467-1479)
 //   ref_mcmcmc_chain       -> the step loop of run_single_mcmcmc_chain
-//                             (mcmcmc_sampler.h:994-1088) with the uniform seed, no
-//                             checkpoints, recording every step
+//                             (mcmcmc_sampler.h:994-1088) with the uniform seed or a
+//                             FactorizedHistogramSeed of given probabilities
+//                             (mcmcmc_seed.h:71-229), no checkpoints, recording every step
+//   ref_learn_histogram    -> learn_factorized_histogram_seed (mcmcmc_sampler.h:602-664)
 
 #include "cdet/cdet_integrand_evaluator.h"
 #include "cdet/chunked_load_data.h"
@@ -311,9 +313,13 @@ void ref_reset_counters() { reset_cdet_runtime_counters(); }
 // first); signal[p * (envelope + 1) + order]: the raw order signal of
 // production step p; vertices_out [envelope][4], lambdas_out [envelope + 1];
 // rng_out: the next 8 raw outputs of the chain's generator after the run.
+// hist_tau_bins > 0 selects a FactorizedHistogramSeed with the given row
+// probabilities (tau [bins][bins], space [S][S], replica [2][2]) instead of the
+// uniform seed.
 int ref_mcmcmc_chain(int order_min, int order_max, int envelope_order, const double* lambdas_in,
                      int warmup_steps, int adapt_interval, double adapt_rate, int production_steps,
-                     unsigned long long seed, unsigned long long* chosen, double* norms, double* signal,
+                     unsigned long long seed, int hist_tau_bins, const double* hist_tau, const double* hist_space,
+                     const double* hist_replica, unsigned long long* chosen, double* norms, double* signal,
                      double* vertices_out, double* lambdas_out, unsigned long long* rng_out) {
     return guarded([&] {
         MCMCMCConfig config;
@@ -331,7 +337,23 @@ int ref_mcmcmc_chain(int order_min, int order_max, int envelope_order, const dou
         validate_mcmcmc_config(config);
         MCMCMCChainState state = make_initial_mcmcmc_chain_state(config, 0, seed);
         const MCMCMCMaskPlan plan = make_mcmcmc_mask_plan(config);
-        const UniformMCMCMCSeed seed_kernel;
+        std::shared_ptr<const MCMCMCSeedKernel> kernel;
+        if (hist_tau_bins > 0) {
+            FactorizedHistogramSeedSettings settings;
+            settings.tau_bins = hist_tau_bins;
+            settings.N1 = N1;
+            settings.N2 = N2;
+            const int sites = N1 * N2;
+            kernel = std::make_shared<FactorizedHistogramSeed>(
+                settings, std::vector<double>(hist_tau, hist_tau + hist_tau_bins * hist_tau_bins),
+                std::vector<double>(hist_space, hist_space + sites * sites),
+                std::vector<double>(hist_replica, hist_replica + 4));
+            config.seed_mode = "histogram";
+            config.histogram_learning_steps = 1;
+        } else {
+            kernel = make_uniform_mcmcmc_seed();
+        }
+        const MCMCMCSeedKernel& seed_kernel = *kernel;
         MCMCMCStepWorkspace workspace;
         int k = 0;
         for (int step = 0; step < warmup_steps; ++step, ++k) {
@@ -398,6 +420,32 @@ int ref_load_chunks(const char* dir) {
     return guarded([&] {
         load_data_chunk_dir = dir;
         load_chunked_data_into_resident_tables();
+    });
+}
+
+// learn_factorized_histogram_seed with these settings; writes the row
+// probabilities of the learned seed (tau [bins][bins], space [S][S],
+// replica [2][2]) and the total pair weight.
+int ref_learn_histogram(int order_min, int order_max, int envelope_order, int learning_steps, int tau_bins,
+                        double uniform_mix, double pseudo_count, unsigned long long base_seed, double* tau_out,
+                        double* space_out, double* replica_out, double* total_weight_out) {
+    return guarded([&] {
+        MCMCMCConfig config;
+        config.order_min = order_min;
+        config.order_max = order_max;
+        config.envelope_order = envelope_order;
+        config.histogram_learning_steps = learning_steps;
+        config.histogram_tau_bins = tau_bins;
+        config.histogram_uniform_mix = uniform_mix;
+        config.histogram_pseudo_count = pseudo_count;
+        config.base_seed = base_seed;
+        long double total = 0.0L;
+        const auto kernel = learn_factorized_histogram_seed(config, &total);
+        const auto& h = dynamic_cast<const FactorizedHistogramSeed&>(*kernel);
+        std::copy(h.tau_probabilities().begin(), h.tau_probabilities().end(), tau_out);
+        std::copy(h.space_probabilities().begin(), h.space_probabilities().end(), space_out);
+        std::copy(h.replica_probabilities().begin(), h.replica_probabilities().end(), replica_out);
+        *total_weight_out = static_cast<double>(total);
     });
 }
 

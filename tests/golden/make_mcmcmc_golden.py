@@ -13,7 +13,11 @@ from the chain's seed (derive_mcmcmc_seed, :159-172, with the parallel driver's
 stream tag), warmup steps with lambda adaptation, production steps. It records
 every step's chosen mask and local normalisation, the production order
 signals, the final vertices and lambdas and the next 8 raw generator outputs,
-in mcmcmc_chains.npz.
+in mcmcmc_chains.npz. A second set of chains per parameter set runs with the
+FactorizedHistogramSeed (mcmcmc_seed.h:71-229) that
+learn_factorized_histogram_seed (mcmcmc_sampler.h:602-664) learns for the
+recorded settings; its row probabilities and total pair weight are stored too
+(<name>.hist.*).
 """
 from __future__ import annotations
 
@@ -44,6 +48,8 @@ RUNS = {
                        warmup=16, adapt_interval=4, adapt_rate=0.25, production=24, base_seed=7),
 }
 CHAINS = 8
+HIST = dict(learning_steps=30, tau_bins=4, uniform_mix=0.05, pseudo_count=0.5, learn_seed=99,
+            base_seed=424242)
 
 
 def splitmix64(x):
@@ -74,7 +80,21 @@ def main():
         out[f"{name}.seeds"] = np.array(seeds, dtype=np.uint64)
         for key in ("chosen", "norms", "signal", "vertices", "lambdas", "rng"):
             out[f"{name}.{key}"] = np.stack([p[key] for p in per])
-        meta[name] = run
+        sites = CASES[name]["n1"] * CASES[name]["n2"]
+        tau, space, rep, total = ref.learn_histogram(run["order_min"], run["order_max"], run["envelope"],
+                                                     HIST["learning_steps"], HIST["tau_bins"],
+                                                     HIST["uniform_mix"], HIST["pseudo_count"],
+                                                     HIST["learn_seed"], sites)
+        out[f"{name}.hist.tau"], out[f"{name}.hist.space"], out[f"{name}.hist.replica"] = tau, space, rep
+        out[f"{name}.hist.total"] = np.array([total])
+        hseeds = [derive_seed(HIST["base_seed"], STREAM_TAG, i) for i in range(CHAINS)]
+        hper = [ref.mcmcmc_chain(run["order_min"], run["order_max"], run["envelope"], run["lambdas"],
+                                 run["warmup"], run["adapt_interval"], run["adapt_rate"], run["production"], s,
+                                 histogram=(HIST["tau_bins"], tau, space, rep)) for s in hseeds]
+        out[f"{name}.hist.seeds"] = np.array(hseeds, dtype=np.uint64)
+        for key in ("chosen", "norms", "signal", "vertices", "lambdas", "rng"):
+            out[f"{name}.hist.{key}"] = np.stack([p[key] for p in hper])
+        meta[name] = dict(run, histogram=HIST)
     np.savez_compressed(os.path.join(HERE, "mcmcmc_chains.npz"), **out)
     with open(os.path.join(HERE, "mcmcmc_chains.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
