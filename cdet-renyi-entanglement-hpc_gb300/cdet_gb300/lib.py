@@ -32,7 +32,7 @@ EXPORTED = (
     "cdet_set_assembly", "cdet_prepare_split", "cdet_assemble_device",
     "cdet_integrand_device_noalloc", "cdet_diagonal_order1_density",
     "cdet_mcmcmc_create", "cdet_mcmcmc_run", "cdet_mcmcmc_end_warmup", "cdet_mcmcmc_state",
-    "cdet_mcmcmc_destroy", "cdet_load_chunks",
+    "cdet_mcmcmc_destroy", "cdet_mcmcmc_set_histogram", "cdet_mcmcmc_learn_histogram", "cdet_load_chunks",
 )
 
 ASSEMBLY_FP64 = 0
@@ -46,6 +46,12 @@ class McmcmcConfig(C.Structure):
     """cdet_mcmcmc_config (include/cdet_gb300.h)."""
     _fields_ = [("order_min", C.c_int32), ("order_max", C.c_int32), ("envelope_order", C.c_int32),
                 ("lambda_adapt_interval", C.c_int32), ("lambda_adapt_rate", C.c_double)]
+
+
+class HistogramConfig(C.Structure):
+    """cdet_histogram_config (include/cdet_gb300.h)."""
+    _fields_ = [("learning_steps", C.c_int32), ("tau_bins", C.c_int32), ("uniform_mix", C.c_double),
+                ("pseudo_count", C.c_double)]
 
 
 class RuntimeScalars(C.Structure):
@@ -95,6 +101,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_mcmcmc_end_warmup.argtypes = [vp]
     lib.cdet_mcmcmc_state.argtypes = [vp, _DP, _DP, _UP]
     lib.cdet_mcmcmc_destroy.argtypes = [vp]
+    lib.cdet_mcmcmc_set_histogram.argtypes = [vp, C.c_int32, _DP, _DP, _DP]
+    lib.cdet_mcmcmc_learn_histogram.argtypes = [vp, C.POINTER(McmcmcConfig), C.POINTER(HistogramConfig), C.c_uint64,
+                                                _DP, _DP, _DP, _DP]
     lib.cdet_load_chunks.argtypes = [vp, C.c_char_p, _DP]
     lib.cdet_last_error.restype = C.c_char_p
     lib.cdet_last_launch_count.argtypes = [vp]

@@ -1,10 +1,13 @@
-"""MCMCMC chains resident on the GPU (uniform seed kernel).
+"""MCMCMC chains resident on the GPU (uniform or factorized histogram seed).
 
 The batch counterpart of run_single_mcmcmc_chain (mcmcmc_sampler.h:994-1088):
 every step evaluates the all-subset integrand of each chain's envelope on the
 GPU and runs run_mcmcmc_step (:524-577) in one thread per chain, with each
 chain's std::mt19937_64 stream reproduced on the device. With the FP64
 assembly the chains are the reference's chains, step for step.
+`learn_histogram` is learn_factorized_histogram_seed (:607-664) and
+`McmcmcChains.set_histogram` switches the chains to that seed kernel
+(MCMCMC_SEED_MODE=histogram).
 """
 from __future__ import annotations
 
@@ -52,6 +55,19 @@ class McmcmcChains:
         L.check(self._lib.cdet_mcmcmc_run(self._h, int(warmup), steps, None, None, None))
         return None
 
+    def set_histogram(self, tau_bins: int, tau, space, replica) -> None:
+        """Seed later steps with the FactorizedHistogramSeed of these row
+        probabilities: tau [bins][bins], space [N1 N2][N1 N2], replica [2][2]."""
+        sites = self._integrand.params.n1 * self._integrand.params.n2
+        arrs = []
+        for x, n in ((tau, tau_bins * tau_bins), (space, sites * sites), (replica, 4)):
+            a = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+            if a.size != n:
+                raise ValueError("histogram probabilities have the wrong size")
+            arrs.append(a)
+        dp = C.POINTER(C.c_double)
+        L.check(self._lib.cdet_mcmcmc_set_histogram(self._h, int(tau_bins), *(a.ctypes.data_as(dp) for a in arrs)))
+
     def end_warmup(self) -> None:
         L.check(self._lib.cdet_mcmcmc_end_warmup(self._h))
 
@@ -76,6 +92,24 @@ class McmcmcChains:
             self.close()
         except Exception:
             pass
+
+
+def learn_histogram(integrand: CdetIntegrand, order_min: int, order_max: int, envelope: int, learning_steps: int,
+                    tau_bins: int = 16, uniform_mix: float = 0.05, pseudo_count: float = 0.0,
+                    base_seed: int = 0):
+    """learn_factorized_histogram_seed on the integrand's tables: (tau, space,
+    replica, total pair weight), the probabilities as flat rows."""
+    sites = integrand.params.n1 * integrand.params.n2
+    tau, space, rep = np.zeros(tau_bins * tau_bins), np.zeros(sites * sites), np.zeros(4)
+    total = C.c_double()
+    cfg = L.McmcmcConfig(order_min, order_max, envelope, 1, 0.0)
+    hcfg = L.HistogramConfig(learning_steps, tau_bins, uniform_mix, pseudo_count)
+    dp = C.POINTER(C.c_double)
+    L.check(integrand._lib.cdet_mcmcmc_learn_histogram(integrand._ctx, C.byref(cfg), C.byref(hcfg),
+                                                        int(base_seed), tau.ctypes.data_as(dp),
+                                                        space.ctypes.data_as(dp), rep.ctypes.data_as(dp),
+                                                        C.byref(total)))
+    return tau, space, rep, total.value
 
 
 def mt64_outputs(state: np.ndarray, count: int) -> np.ndarray:

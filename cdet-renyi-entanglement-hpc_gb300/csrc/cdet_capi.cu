@@ -8,12 +8,14 @@
 #include "cdet_gb300.h"
 #include "cdet_kernels.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <filesystem>
 #include <fstream>
 #include <cstring>
 #include <map>
+#include <random>
 #include <string>
 #include <utility>
 #include <vector>
@@ -754,6 +756,13 @@ struct cdet_mcmcmc {
     uint64_t* counts = nullptr;
     int32_t* error = nullptr;
     int64_t warmup_done = 0;
+    // histogram seed kernel (tau_bins > 0): probabilities, CDFs and the
+    // conditional generation probabilities scratch in one allocation
+    int tau_bins = 0;
+    void* hist_block = nullptr;
+    double *tau_prob = nullptr, *space_prob = nullptr, *replica_prob = nullptr;
+    double *tau_cdf = nullptr, *space_cdf = nullptr, *replica_cdf = nullptr;
+    double* cprob = nullptr;
 };
 
 namespace {
@@ -913,6 +922,18 @@ int cdet_mcmcmc_run(cdet_mcmcmc* m, int warmup, int64_t steps, uint64_t* chosen,
         a.chosen_out = d_chosen ? d_chosen + s * chains : nullptr;
         a.norm_out = d_norms ? d_norms + s * chains : nullptr;
         a.signal_out = d_signal ? d_signal + s * chains * (env + 1) : nullptr;
+        if (m->tau_bins > 0) {
+            a.tau_bins = m->tau_bins;
+            a.n1 = m->ctx->scalars.n1;
+            a.n2 = m->ctx->scalars.n2;
+            a.tau_prob = m->tau_prob;
+            a.space_prob = m->space_prob;
+            a.replica_prob = m->replica_prob;
+            a.tau_cdf = m->tau_cdf;
+            a.space_cdf = m->space_cdf;
+            a.replica_cdf = m->replica_cdf;
+            a.cprob = m->cprob;
+        }
         err = cdet::launch_mcmcmc_step(a, nullptr);
         if (err != cudaSuccess) {
             rc = cuda_fail(err, "MCMCMC step launch");
@@ -949,6 +970,9 @@ int cdet_mcmcmc_run(cdet_mcmcmc* m, int warmup, int64_t steps, uint64_t* chosen,
         if (errors[c] == 2)
             return fail(CDET_ERR_VALUE,
                         "MCMCMC local normalization is zero or non-finite (chain " + std::to_string(c) + ")");
+        if (errors[c] == 3)
+            return fail(CDET_ERR_VALUE,
+                        "MCMCMC seed density is negative or non-finite (chain " + std::to_string(c) + ")");
     }
     return CDET_OK;
 }
@@ -989,7 +1013,229 @@ int cdet_mcmcmc_destroy(cdet_mcmcmc* m) {
     if (!m) return CDET_OK;
     DeviceGuard guard(m->ctx->device);
     cudaFree(m->block);
+    if (m->hist_block) cudaFree(m->hist_block);
     delete m;
+    return CDET_OK;
+}
+
+int cdet_mcmcmc_set_histogram(cdet_mcmcmc* m, int32_t tau_bins, const double* tau_prob, const double* space_prob,
+                              const double* replica_prob) {
+    if (!m || !tau_prob || !space_prob || !replica_prob) return fail(CDET_ERR_INVALID, "null argument");
+    const int n1 = m->ctx->scalars.n1, n2 = m->ctx->scalars.n2;
+    if (tau_bins <= 0 || n1 <= 0 || n2 <= 0) return fail(CDET_ERR_INVALID, "Histogram seed dimensions must be positive");
+    const size_t sites = static_cast<size_t>(n1) * n2;
+    const size_t nt = static_cast<size_t>(tau_bins) * tau_bins, ns = sites * sites;
+    // build_cdfs (mcmcmc_seed.h:190-203): running row sums, the last column set to 1
+    auto cdf = [](const double* prob, size_t columns, size_t rows) {
+        std::vector<double> out(columns * rows);
+        for (size_t r = 0; r < rows; ++r) {
+            double cumulative = 0.0;
+            for (size_t c = 0; c < columns; ++c) {
+                cumulative += prob[r * columns + c];
+                out[r * columns + c] = cumulative;
+            }
+            out[r * columns + columns - 1] = 1.0;
+        }
+        return out;
+    };
+    const std::vector<double> tc = cdf(tau_prob, tau_bins, tau_bins), sc = cdf(space_prob, sites, sites),
+                              rc = cdf(replica_prob, 2, 2);
+    DeviceGuard guard(m->ctx->device);
+    auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
+    const size_t nprob = static_cast<size_t>(m->chains) << m->cfg.envelope_order;
+    const size_t bytes = 2 * (up(nt * 8) + up(ns * 8) + up(32)) + up(nprob * 8);
+    void* block = nullptr;
+    cudaError_t err = cudaMalloc(&block, bytes);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(MCMCMC histogram seed)");
+    char* p = static_cast<char*>(block);
+    auto take = [&](size_t b) {
+        double* r = reinterpret_cast<double*>(p);
+        p += up(b);
+        return r;
+    };
+    double* tp = take(nt * 8);
+    double* sp = take(ns * 8);
+    double* rp = take(32);
+    double* tcd = take(nt * 8);
+    double* scd = take(ns * 8);
+    double* rcd = take(32);
+    double* cprob = take(nprob * 8);
+    err = cudaMemcpy(tp, tau_prob, nt * 8, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(sp, space_prob, ns * 8, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(rp, replica_prob, 32, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(tcd, tc.data(), nt * 8, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(scd, sc.data(), ns * 8, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(rcd, rc.data(), 32, cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+        cudaFree(block);
+        return cuda_fail(err, "MCMCMC histogram seed upload");
+    }
+    if (m->hist_block) {
+        cudaDeviceSynchronize();
+        cudaFree(m->hist_block);
+    }
+    m->hist_block = block;
+    m->tau_bins = tau_bins;
+    m->tau_prob = tp;
+    m->space_prob = sp;
+    m->replica_prob = rp;
+    m->tau_cdf = tcd;
+    m->space_cdf = scd;
+    m->replica_cdf = rcd;
+    m->cprob = cprob;
+    return CDET_OK;
+}
+
+int cdet_mcmcmc_learn_histogram(cdet_context* ctx, const cdet_mcmcmc_config* config,
+                                const cdet_histogram_config* histogram, uint64_t base_seed, double* tau_prob,
+                                double* space_prob, double* replica_prob, double* total_pair_weight) {
+    if (!ctx || !config || !histogram || !tau_prob || !space_prob || !replica_prob)
+        return fail(CDET_ERR_INVALID, "null argument");
+    const cdet_mcmcmc_config& c = *config;
+    const cdet_histogram_config& h = *histogram;
+    const int env = c.envelope_order;
+    if (c.order_min < 1 || c.order_max < c.order_min || env <= c.order_max || env > cdet::kMcmcmcMaxEnvelope)
+        return fail(CDET_ERR_INVALID, "invalid MCMCMC order range or envelope");
+    if (h.learning_steps <= 0)
+        return fail(CDET_ERR_INVALID, "MCMCMC_SEED_HISTOGRAM_LEARNING_STEPS must be positive for histogram seed");
+    const int n1 = ctx->scalars.n1, n2 = ctx->scalars.n2;
+    if (h.tau_bins <= 0 || n1 <= 0 || n2 <= 0) return fail(CDET_ERR_INVALID, "Histogram seed dimensions must be positive");
+    if (!(h.uniform_mix >= 0.0 && h.uniform_mix <= 1.0))
+        return fail(CDET_ERR_INVALID, "MCMCMC_SEED_HISTOGRAM_UNIFORM_MIX must lie in [0, 1]");
+    if (h.pseudo_count < 0.0 || !std::isfinite(h.pseudo_count))
+        return fail(CDET_ERR_INVALID, "MCMCMC_SEED_HISTOGRAM_PSEUDO_COUNT must be nonnegative and finite");
+    for (int k = 0; k < 4; ++k)
+        if (!resolve(ctx, k)) return fail(CDET_ERR_STATE, "Green-function tables have not been uploaded");
+    DeviceGuard guard(ctx->device);
+    // learn_factorized_histogram_seed (mcmcmc_sampler.h:607-664): uniform
+    // envelopes from the std::mt19937_64 stream derive_mcmcmc_seed(base,
+    // "HISTOSEE"), their all-subset integrands, pair weights accumulated in
+    // long double (FactorizedHistogramSeedAccumulator, mcmcmc_seed.h:232-330).
+    // The envelopes only consume the generator, so they are drawn first and
+    // the integrands evaluated on the GPU in batches.
+    auto splitmix = [](uint64_t x) {
+        x += 0x9e3779b97f4a7c15ULL;
+        x = (x ^ (x >> 30U)) * 0xbf58476d1ce4e5b9ULL;
+        x = (x ^ (x >> 27U)) * 0x94d049bb133111ebULL;
+        return x ^ (x >> 31U);
+    };
+    uint64_t mixed = splitmix(base_seed ^ 0x484953544F534545ULL);
+    mixed ^= 0x9e3779b97f4a7c15ULL * 1ULL;
+    std::mt19937_64 rng(splitmix(mixed));
+    std::uniform_real_distribution<double> uniform01(0.0, 1.0);
+    const int64_t steps = h.learning_steps;
+    std::vector<double> vertices(static_cast<size_t>(steps) * env * 4);
+    for (double& x : vertices) x = uniform01(rng);
+
+    const int sites = n1 * n2;
+    const int bins = h.tau_bins;
+    std::vector<long double> tau_c(static_cast<size_t>(bins) * bins, 0.0L);
+    std::vector<long double> space_c(static_cast<size_t>(sites) * sites, 0.0L);
+    std::vector<long double> rep_c(4, 0.0L);
+    long double total = 0.0L;
+    auto index = [](double value, int extent) {
+        const int i = static_cast<int>(std::floor(value * static_cast<double>(extent)));
+        return i < 0 ? 0 : (i >= extent ? extent - 1 : i);
+    };
+    double binom[cdet::kMcmcmcMaxEnvelope + 1];
+    for (int o = 0; o <= env; ++o) {
+        uint64_t b = 1;
+        const int k = o < env - o ? o : env - o;
+        for (int i = 1; i <= k; ++i) b = b * static_cast<uint64_t>(env - k + i) / static_cast<uint64_t>(i);
+        binom[o] = static_cast<double>(b);
+    }
+    const uint64_t subsets = uint64_t{1} << env;
+    // batches of envelopes whose integrands fit 256 MiB
+    const int64_t batch = std::max<int64_t>(1, std::min<int64_t>(steps, (int64_t{256} << 20) / (subsets * 8)));
+    double* dverts = nullptr;
+    double* dvals = nullptr;
+    int32_t* dstatus = nullptr;
+    cudaError_t err = cudaMalloc(&dverts, static_cast<size_t>(batch) * env * 4 * 8);
+    if (err == cudaSuccess) err = cudaMalloc(&dvals, static_cast<size_t>(batch) * subsets * 8);
+    if (err == cudaSuccess) err = cudaMalloc(&dstatus, static_cast<size_t>(batch) * 4);
+    int rc = err == cudaSuccess ? CDET_OK : cuda_fail(err, "cudaMalloc(histogram learning)");
+    std::vector<double> values;
+    std::vector<int32_t> status;
+    for (int64_t first = 0; rc == CDET_OK && first < steps; first += batch) {
+        const int64_t n = std::min<int64_t>(batch, steps - first);
+        const double* hv = vertices.data() + static_cast<size_t>(first) * env * 4;
+        err = cudaMemcpy(dverts, hv, static_cast<size_t>(n) * env * 4 * 8, cudaMemcpyHostToDevice);
+        if (err != cudaSuccess) {
+            rc = cuda_fail(err, "histogram learning upload");
+            break;
+        }
+        rc = run(ctx, dverts, nullptr, n, env, 1, dvals, dstatus, nullptr);
+        if (rc != CDET_OK) break;
+        values.resize(static_cast<size_t>(n) * subsets);
+        status.resize(static_cast<size_t>(n));
+        err = cudaMemcpy(values.data(), dvals, values.size() * 8, cudaMemcpyDeviceToHost);
+        if (err == cudaSuccess) err = cudaMemcpy(status.data(), dstatus, status.size() * 4, cudaMemcpyDeviceToHost);
+        if (err != cudaSuccess) {
+            rc = cuda_fail(err, "histogram learning values");
+            break;
+        }
+        for (int64_t e = 0; e < n && rc == CDET_OK; ++e) {
+            if (status[e] & cdet::kStatusNonFinite) {
+                rc = fail(CDET_ERR_VALUE, "Error (all-subset integrand): Value is not finite");
+                break;
+            }
+            const double* v = hv + static_cast<size_t>(e) * env * 4;
+            const double* val = values.data() + static_cast<size_t>(e) * subsets;
+            for (uint64_t mask = 1; mask < subsets; ++mask) {
+                const int order = __builtin_popcountll(mask);
+                if (order < c.order_min || order > c.order_max || order < 2) continue;
+                const double value = val[mask];
+                if (!std::isfinite(value)) continue;
+                const long double subset_weight =
+                    static_cast<long double>(std::abs(value)) / static_cast<long double>(binom[order]);
+                const long double pair_weight = subset_weight / static_cast<long double>(order * (order - 1));
+                if (!(pair_weight > 0.0L) || !std::isfinite(static_cast<double>(pair_weight))) continue;
+                for (int parent = 0; parent < env; ++parent) {
+                    if (!(mask & (uint64_t{1} << parent))) continue;
+                    const double* pv = v + 4 * parent;
+                    for (int child = 0; child < env; ++child) {
+                        if (child == parent || !(mask & (uint64_t{1} << child))) continue;
+                        const double* cv = v + 4 * child;
+                        tau_c[static_cast<size_t>(index(pv[0], bins)) * bins + index(cv[0], bins)] += pair_weight;
+                        const int ps = index(pv[1], n1) * n2 + index(pv[2], n2);
+                        const int cs = index(cv[1], n1) * n2 + index(cv[2], n2);
+                        space_c[static_cast<size_t>(ps) * sites + cs] += pair_weight;
+                        rep_c[index(pv[3], 2) * 2 + index(cv[3], 2)] += pair_weight;
+                        total += pair_weight;
+                    }
+                }
+            }
+        }
+    }
+    if (dverts) cudaFree(dverts);
+    if (dvals) cudaFree(dvals);
+    if (dstatus) cudaFree(dstatus);
+    if (rc != CDET_OK) return rc;
+    // normalize_rows (mcmcmc_seed.h:288-327)
+    auto normalize = [&](const std::vector<long double>& counts, int columns, double* out) {
+        const int rows = static_cast<int>(counts.size()) / columns;
+        const long double uniform = 1.0L / static_cast<long double>(columns);
+        const long double mix = static_cast<long double>(h.uniform_mix);
+        const long double pseudo = static_cast<long double>(h.pseudo_count);
+        for (int r = 0; r < rows; ++r) {
+            long double row_sum = 0.0L;
+            for (int k = 0; k < columns; ++k) row_sum += counts[static_cast<size_t>(r) * columns + k];
+            const long double denominator = row_sum + pseudo * static_cast<long double>(columns);
+            for (int k = 0; k < columns; ++k) {
+                long double learned = uniform;
+                if (denominator > 0.0L) learned = (counts[static_cast<size_t>(r) * columns + k] + pseudo) / denominator;
+                out[static_cast<size_t>(r) * columns + k] = static_cast<double>((1.0L - mix) * learned + mix * uniform);
+            }
+            double row_total = 0.0;
+            for (int k = 0; k < columns; ++k) row_total += out[static_cast<size_t>(r) * columns + k];
+            if (row_total > 0.0 && std::isfinite(row_total))
+                for (int k = 0; k < columns; ++k) out[static_cast<size_t>(r) * columns + k] /= row_total;
+        }
+    };
+    normalize(tau_c, bins, tau_prob);
+    normalize(space_c, sites, space_prob);
+    normalize(rep_c, 2, replica_prob);
+    if (total_pair_weight) *total_pair_weight = static_cast<double>(total);
     return CDET_OK;
 }
 

@@ -101,8 +101,8 @@ size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps);
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out);
 // assembly = true launches the FP64 Green-matrix assembly first; false
 // expects the Green matrices already in scratch (split-precision assembly).
-// One MCMCMC step for a batch of chains (uniform seed kernel), after the
-// all-subset integrand of every chain's envelope.
+// One MCMCMC step for a batch of chains (uniform or histogram seed kernel),
+// after the all-subset integrand of every chain's envelope.
 constexpr int kMcmcmcMaxEnvelope = 24;
 struct McmcmcStepArgs {
     int64_t chains;
@@ -117,10 +117,17 @@ struct McmcmcStepArgs {
     uint64_t* mt;                   // [312][chains]
     int32_t* mt_index;              // [chains]
     uint64_t* counts;               // [chains][envelope + 1] warmup block counts
-    int32_t* error;                 // [chains]: 0, 1 (integrand not finite), 2 (normalisation)
+    int32_t* error;                 // [chains]: 0, 1 (integrand not finite), 2 (normalisation), 3 (seed density)
     uint64_t* chosen_out;           // [chains] or null
     double* norm_out;               // [chains] or null
     double* signal_out;             // [chains][envelope + 1] or null
+    // histogram seed kernel when tau_bins > 0: row probabilities and their
+    // CDFs (tau [bins][bins], space [N1 N2][N1 N2], replica [2][2]) and the
+    // conditional generation probabilities scratch [chains][2^envelope]
+    int tau_bins, n1, n2;
+    const double *tau_prob, *space_prob, *replica_prob;
+    const double *tau_cdf, *space_cdf, *replica_cdf;
+    double* cprob;
 };
 cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* seeds, uint64_t* mt, int32_t* mt_index,
                                double* vertices, cudaStream_t stream);

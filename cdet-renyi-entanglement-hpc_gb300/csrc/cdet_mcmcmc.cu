@@ -1,7 +1,10 @@
-// Device-resident MCMCMC chains with the uniform seed kernel: one thread per
-// chain runs run_mcmcmc_step (mcmcmc_sampler.h:524-577) on the all-subset
-// integrand values of its envelope, so a batch of chains advances one step
-// per launch pair (integrand, step) with no host round trip.
+// Device-resident MCMCMC chains: one thread per chain runs run_mcmcmc_step
+// (mcmcmc_sampler.h:524-577) on the all-subset integrand values of its
+// envelope, so a batch of chains advances one step per launch pair
+// (integrand, step) with no host round trip. The seed kernel is the uniform
+// one (mcmcmc_seed.h:41-61) or the factorized histogram (:71-229), whose
+// conditional generation probabilities (mcmcmc_sampler.h:252-335) weight the
+// fluxes.
 //
 // Each chain keeps the reference's std::mt19937_64 stream (the published
 // MT19937-64 generator with libstdc++'s seeding) and draws from it exactly as
@@ -70,6 +73,107 @@ struct Mt64 {
     }
 };
 
+// unit_coordinate_to_index (mcmcmc_seed.h:30-39)
+__device__ __forceinline__ int unit_index(double value, int extent) {
+    const int index = static_cast<int>(floor(dmul(value, static_cast<double>(extent))));
+    if (index < 0) return 0;
+    if (index >= extent) return extent - 1;
+    return index;
+}
+
+// sample_from_row (mcmcmc_seed.h:205-218): std::lower_bound (the binary search
+// for the first entry not below the draw) in one CDF row; past the end, the
+// last column
+__device__ int sample_row(const double* __restrict__ cdf, int columns, int row, const Mt64& g) {
+    const double threshold = g.canonical();
+    const double* b = cdf + static_cast<int64_t>(row) * columns;
+    int first = 0, len = columns;
+    while (len > 0) {
+        const int half = len >> 1;
+        if (b[first + half] < threshold) {
+            first += half + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    return first == columns ? columns - 1 : first;
+}
+
+// density_child_given_parent (mcmcmc_seed.h:130-150)
+__device__ double hist_density(const McmcmcStepArgs& a, const double* child, const double* parent) {
+    const int sites = a.n1 * a.n2;
+    const double tau_d = dmul(a.tau_prob[unit_index(parent[0], a.tau_bins) * a.tau_bins +
+                                         unit_index(child[0], a.tau_bins)],
+                              static_cast<double>(a.tau_bins));
+    const int ps = unit_index(parent[1], a.n1) * a.n2 + unit_index(parent[2], a.n2);
+    const int cs = unit_index(child[1], a.n1) * a.n2 + unit_index(child[2], a.n2);
+    const double space_d = dmul(a.space_prob[static_cast<int64_t>(ps) * sites + cs], static_cast<double>(sites));
+    const double rep_d = dmul(a.replica_prob[unit_index(parent[3], 2) * 2 + unit_index(child[3], 2)], 2.0);
+    return dmul(dmul(tau_d, space_d), rep_d);
+}
+
+// sample_child_from_parent (mcmcmc_seed.h:106-128): three row draws, then the
+// four in-cell offsets in vertex order
+__device__ void hist_child(const McmcmcStepArgs& a, const Mt64& g, const double* parent, double* child) {
+    const int child_tau = sample_row(a.tau_cdf, a.tau_bins, unit_index(parent[0], a.tau_bins), g);
+    const int parent_site = unit_index(parent[1], a.n1) * a.n2 + unit_index(parent[2], a.n2);
+    const int child_site = sample_row(a.space_cdf, a.n1 * a.n2, parent_site, g);
+    const int child_x = child_site / a.n2;
+    const int child_y = child_site - child_x * a.n2;
+    const int child_rep = sample_row(a.replica_cdf, 2, unit_index(parent[3], 2), g);
+    child[0] = ddiv(dadd(static_cast<double>(child_tau), g.canonical()), static_cast<double>(a.tau_bins));
+    child[1] = ddiv(dadd(static_cast<double>(child_x), g.canonical()), static_cast<double>(a.n1));
+    child[2] = ddiv(dadd(static_cast<double>(child_y), g.canonical()), static_cast<double>(a.n2));
+    child[3] = ddiv(dadd(static_cast<double>(child_rep), g.canonical()), 2.0);
+}
+
+// compute_conditional_generation_probabilities_typed_into<double>
+// (mcmcmc_sampler.h:252-335). The reference tabulates the remaining child
+// densities cd[gm][c] by peeling the lowest bit of gm; here each one is formed
+// on the spot with the same subtractions in the same order (the highest bit of
+// gm first), each result clamped as the table's is, so only the 2^n
+// probabilities are stored. false: a seed density is negative or not finite.
+__device__ bool conditional_probabilities(const McmcmcStepArgs& a, const double* v, int n, double* prob) {
+    double sd[kMcmcmcMaxEnvelope * kMcmcmcMaxEnvelope];
+    double cd0[kMcmcmcMaxEnvelope];
+    for (int c = 0; c < n; ++c)
+        for (int p = 0; p < n; ++p) {
+            double d = 0.0;
+            if (c != p) {
+                d = hist_density(a, v + 4 * c, v + 4 * p);
+                if (d < 0.0 || !isfinite(d)) return false;
+            }
+            sd[c * n + p] = d;
+        }
+    for (int c = 0; c < n; ++c) {
+        double sum = 0.0;
+        for (int p = 0; p < n; ++p) sum = dadd(sum, sd[c * n + p]);
+        cd0[c] = sum;
+    }
+    const uint64_t full = (uint64_t{1} << n) - 1;
+    prob[0] = 1.0;
+    for (uint64_t gm = 1; gm < full; ++gm) {
+        const int gc = __popcll(gm), pc = n - gc;
+        double sum = 0.0;
+        for (int c = 0; c < n; ++c) {
+            const uint64_t cb = uint64_t{1} << c;
+            if (!(gm & cb)) continue;
+            double d = cd0[c];
+            for (uint64_t rest = gm; rest;) {
+                const int b = 63 - __clzll(static_cast<long long>(rest));
+                rest ^= uint64_t{1} << b;
+                d = dsub(d, sd[c * n + b]);
+                if (d < 0.0 && d > -1.0e-12) d = 0.0;
+            }
+            sum = dadd(sum, dmul(prob[gm ^ cb], d));
+        }
+        prob[gm] = ddiv(sum, dmul(static_cast<double>(gc), static_cast<double>(pc)));
+    }
+    prob[full] = 0.0;
+    return true;
+}
+
 // std::mt19937_64(seed) and sample_uniform_vertex_set (mcmcmc_sampler.h:187-198)
 __global__ void mcmcmc_init(int64_t chains, int envelope, const uint64_t* __restrict__ seeds, uint64_t* mt,
                             int32_t* mt_index, double* vertices) {
@@ -87,7 +191,8 @@ __global__ void mcmcmc_init(int64_t chains, int envelope, const uint64_t* __rest
     for (int k = 0; k < envelope * 4; ++k) v[k] = g.canonical();
 }
 
-__global__ void __launch_bounds__(128) mcmcmc_step_uniform(const __grid_constant__ McmcmcStepArgs a) {
+template <bool Hist>
+__global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ McmcmcStepArgs a) {
     const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= a.chains) return;
     if (a.error[c]) return;  // a chain that failed stays where it stopped
@@ -100,13 +205,27 @@ __global__ void __launch_bounds__(128) mcmcmc_step_uniform(const __grid_constant
     const double* values = a.values + c * static_cast<int64_t>(subsets);
     const double* lam = a.lambdas + c * (env + 1);
     const Mt64 g{a.mt + c, a.chains, a.mt_index + c};
+    const double* v = a.vertices + c * env * 4;
+    const uint64_t full = subsets - 1;
+    double* cprob = nullptr;
+    if constexpr (Hist) {
+        cprob = a.cprob + c * static_cast<int64_t>(subsets);
+        if (!conditional_probabilities(a, v, env, cprob)) {
+            a.error[c] = 3;  // "MCMCMC seed density is negative or non-finite"
+            return;
+        }
+    }
+    // flux = lambda * value * conditional probability of the complement
+    // (1 for the uniform kernel)
+    auto flux_of = [&](uint64_t mask, int o) {
+        return dmul(dmul(lam[o], values[mask]), Hist ? cprob[full ^ mask] : 1.0);
+    };
     // fluxes and selection weights in the mask plan's order (:411-430, :540-560)
     double norm = 0.0;
     for (uint64_t mask = 1; mask < subsets; ++mask) {
         const int o = __popcll(mask);
         if (o < a.order_min || o > a.order_max) continue;
-        const double flux = dmul(dmul(lam[o], values[mask]), 1.0);
-        norm = dadd(norm, dmul(fabs(flux), a.inv_binom[o]));
+        norm = dadd(norm, dmul(fabs(flux_of(mask, o)), a.inv_binom[o]));
     }
     // sample_weighted_candidate_mask (:225-250)
     if (!(norm > 0.0) || !isfinite(norm)) {
@@ -120,7 +239,7 @@ __global__ void __launch_bounds__(128) mcmcmc_step_uniform(const __grid_constant
     for (uint64_t mask = 1; mask < subsets && !found; ++mask) {
         const int o = __popcll(mask);
         if (o < a.order_min || o > a.order_max) continue;
-        const double w = dmul(fabs(dmul(dmul(lam[o], values[mask]), 1.0)), a.inv_binom[o]);
+        const double w = dmul(fabs(flux_of(mask, o)), a.inv_binom[o]);
         if (!(w > 0.0)) continue;
         if (isfinite(w)) last_positive = mask;
         cumulative = dadd(cumulative, w);
@@ -137,14 +256,13 @@ __global__ void __launch_bounds__(128) mcmcmc_step_uniform(const __grid_constant
         for (uint64_t mask = 1; mask < subsets; ++mask) {
             const int o = __popcll(mask);
             if (o < a.order_min || o > a.order_max) continue;
-            const double time = ddiv(dmul(dmul(lam[o], values[mask]), 1.0), norm);
+            const double time = ddiv(flux_of(mask, o), norm);
             sig[o] = dadd(sig[o], dmul(time, a.inv_binom[o]));
         }
     }
-    // create_next_vertices_from_seed_into (:380-400) with the uniform seed
-    // kernel (mcmcmc_seed.h:51-55): the retained vertices in order, then
-    // children from uniformly chosen parents (the uniform kernel ignores them)
-    const double* v = a.vertices + c * env * 4;
+    // create_next_vertices_from_seed_into (:380-400): the retained vertices in
+    // order, then children of uniformly chosen parents among the vertices so
+    // far (the uniform kernel, mcmcmc_seed.h:51-55, ignores the parent)
     double* nv = a.next_vertices + c * env * 4;
     int size = 0;
     for (int i = 0; i < env; ++i)
@@ -153,8 +271,13 @@ __global__ void __launch_bounds__(128) mcmcmc_step_uniform(const __grid_constant
             ++size;
         }
     while (size < env) {
-        (void)g.uniform_int(size);
-        for (int k = 0; k < 4; ++k) nv[4 * size + k] = g.canonical();
+        const int parent = g.uniform_int(size);
+        if constexpr (Hist) {
+            hist_child(a, g, nv + 4 * parent, nv + 4 * size);
+        } else {
+            (void)parent;
+            for (int k = 0; k < 4; ++k) nv[4 * size + k] = g.canonical();
+        }
         ++size;
     }
     const int order = __popcll(chosen);
@@ -175,7 +298,11 @@ cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* see
 
 cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream) {
     if (args.chains <= 0) return cudaSuccess;
-    mcmcmc_step_uniform<<<static_cast<unsigned>((args.chains + 127) / 128), 128, 0, stream>>>(args);
+    const unsigned grid = static_cast<unsigned>((args.chains + 127) / 128);
+    if (args.tau_bins > 0)
+        mcmcmc_step<true><<<grid, 128, 0, stream>>>(args);
+    else
+        mcmcmc_step<false><<<grid, 128, 0, stream>>>(args);
     return cudaGetLastError();
 }
 

@@ -187,8 +187,11 @@ int cdet_load_chunks(cdet_context* ctx, const char* dir, double* order1);
  * std::mt19937_64 stream and draws from it as libstdc++'s distributions do,
  * so with the FP64 assembly the chains follow the reference's chains step for
  * step. The lambda adaptation (adapt_mcmcmc_lambdas, :579-600) runs on the
- * host after every adapt interval of warmup steps. Checkpoint files and the
- * histogram seed kernel are not part of this interface. */
+ * host after every adapt interval of warmup steps. cdet_mcmcmc_set_histogram
+ * switches the chains to the factorized histogram seed kernel
+ * (MCMCMC_SEED_MODE=histogram, mcmcmc_seed.h:71-229); the chains are then the
+ * reference's histogram-seeded chains step for step. Checkpoint files are not
+ * part of this interface. */
 typedef struct cdet_mcmcmc cdet_mcmcmc;
 
 typedef struct cdet_mcmcmc_config {
@@ -226,6 +229,35 @@ int cdet_mcmcmc_end_warmup(cdet_mcmcmc* m);
 int cdet_mcmcmc_state(const cdet_mcmcmc* m, double* vertices, double* lambdas, uint64_t* rng_state);
 
 int cdet_mcmcmc_destroy(cdet_mcmcmc* m);
+
+/* Settings of the factorized histogram seed (MCMCMCConfig's histogram_*
+ * fields, mcmcmc_sampler.h:92-95). */
+typedef struct cdet_histogram_config {
+    int32_t learning_steps; /* MCMCMC_SEED_HISTOGRAM_LEARNING_STEPS (> 0) */
+    int32_t tau_bins;       /* MCMCMC_SEED_HISTOGRAM_TAU_BINS (> 0) */
+    double uniform_mix;     /* MCMCMC_SEED_HISTOGRAM_UNIFORM_MIX, in [0, 1] */
+    double pseudo_count;    /* MCMCMC_SEED_HISTOGRAM_PSEUDO_COUNT (>= 0, finite) */
+} cdet_histogram_config;
+
+/* learn_factorized_histogram_seed (mcmcmc_sampler.h:607-664) on the context's
+ * tables: learning_steps uniform envelopes from std::mt19937_64 seeded with
+ * derive_mcmcmc_seed(base_seed, 0x484953544F534545), their all-subset
+ * integrands on the GPU (the context's assembly), the pair weights
+ * accumulated on the host in long double as the reference does. Outputs the
+ * row probabilities tau_prob[tau_bins][tau_bins], space_prob[N1 N2][N1 N2]
+ * (site x * N2 + y), replica_prob[2][2] and (if not null) the total pair
+ * weight. */
+int cdet_mcmcmc_learn_histogram(cdet_context* ctx, const cdet_mcmcmc_config* config,
+                                const cdet_histogram_config* histogram, uint64_t base_seed, double* tau_prob,
+                                double* space_prob, double* replica_prob, double* total_pair_weight);
+
+/* Seeds every later step of the chains with the FactorizedHistogramSeed of
+ * these row probabilities (layouts as above; its CDFs are built here as
+ * build_cdfs does). Allocates 2^envelope_order doubles per chain for the
+ * conditional generation probabilities. A step whose seed density is negative
+ * or not finite fails with "MCMCMC seed density is negative or non-finite". */
+int cdet_mcmcmc_set_histogram(cdet_mcmcmc* m, int32_t tau_bins, const double* tau_prob, const double* space_prob,
+                              const double* replica_prob);
 
 /* Counters of the host entry points: integrand calls and whole-matrix
  * principal-minor fallbacks (runtime_counters.h:14-51). */

@@ -896,13 +896,22 @@ static void build_cdf(const double* prob, int columns, int rows, double* cdf) {
     }
 }
 
-/* sample_from_row (:205-218): std::lower_bound of a canonical draw */
+/* sample_from_row (:205-218): std::lower_bound (binary search for the first
+ * entry not below the draw) of a canonical draw; past the end: the last column */
 static int sample_row(const double* cdf, int columns, int row, oracle_mt64* rng) {
     const double threshold = oracle_canonical(rng);
     const double* b = cdf + (size_t)row * columns;
-    for (int c = 0; c < columns; ++c)
-        if (!(b[c] < threshold)) return c;
-    return columns - 1;
+    int first = 0, len = columns;
+    while (len > 0) {
+        const int half = len >> 1;
+        if (b[first + half] < threshold) {
+            first += half + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    return first == columns ? columns - 1 : first;
 }
 
 /* sample_child_from_parent (:106-128) */
@@ -1203,7 +1212,12 @@ int oracle_learn_histogram(const oracle_scalars* s, const oracle_tables* t, int 
     double v[64 * 4];
     for (int step = 0; step < learning_steps; ++step) {
         for (int i = 0; i < envelope * 4; ++i) v[i] = oracle_canonical(&rng); /* sample_uniform_vertex_set */
-        (void)oracle_all_subsets(s, t, v, envelope, values);
+        if (oracle_all_subsets(s, t, v, envelope, values) & ORACLE_NONFINITE) {
+            free(tau_c);
+            free(space_c);
+            free(values);
+            return 1; /* the all-subset evaluation throws on a non-finite value */
+        }
         for (uint64_t mask = 1; mask < subsets; ++mask) {
             const int order = __builtin_popcountll(mask);
             if (order < order_min || order > order_max || order < 2) continue;
