@@ -32,7 +32,9 @@ EXPORTED = (
     "cdet_set_assembly", "cdet_prepare_split", "cdet_assemble_device",
     "cdet_integrand_device_noalloc", "cdet_diagonal_order1_density",
     "cdet_mcmcmc_create", "cdet_mcmcmc_run", "cdet_mcmcmc_end_warmup", "cdet_mcmcmc_state",
-    "cdet_mcmcmc_destroy", "cdet_mcmcmc_set_histogram", "cdet_mcmcmc_learn_histogram", "cdet_load_chunks",
+    "cdet_mcmcmc_destroy", "cdet_mcmcmc_set_histogram", "cdet_mcmcmc_learn_histogram", "cdet_mcmcmc_result",
+    "cdet_mcmcmc_summary", "cdet_mcmcmc_estimates", "cdet_write_mcmcmc_checkpoint", "cdet_read_mcmcmc_checkpoint",
+    "cdet_mcmcmc_save_checkpoints", "cdet_mcmcmc_load_checkpoints", "cdet_mcmcmc_launch_count", "cdet_load_chunks",
 )
 
 ASSEMBLY_FP64 = 0
@@ -52,6 +54,42 @@ class HistogramConfig(C.Structure):
     """cdet_histogram_config (include/cdet_gb300.h)."""
     _fields_ = [("learning_steps", C.c_int32), ("tau_bins", C.c_int32), ("uniform_mix", C.c_double),
                 ("pseudo_count", C.c_double)]
+
+
+MAX_ENVELOPE = 24  # CDET_MCMCMC_MAX_ENVELOPE
+
+
+class RunningStats(C.Structure):
+    """cdet_running_stats: RunningStatsLongDouble in the host's long double."""
+    _fields_ = [("count", C.c_uint64), ("mean", C.c_longdouble), ("m2", C.c_longdouble)]
+
+
+class ChainResult(C.Structure):
+    """cdet_mcmcmc_chain_result (MCMCMCChainResult)."""
+    _fields_ = [("seed", C.c_uint64), ("warmup_proposed_steps", C.c_uint64),
+                ("warmup_accepted_steps", C.c_uint64), ("production_proposed_steps", C.c_uint64),
+                ("production_accepted_steps", C.c_uint64),
+                ("warmup_chosen_counts", C.c_uint64 * (MAX_ENVELOPE + 1)),
+                ("production_chosen_counts", C.c_uint64 * (MAX_ENVELOPE + 1)),
+                ("warmup_retained_fraction_stats", RunningStats),
+                ("production_retained_fraction_stats", RunningStats),
+                ("order_signal_stats", RunningStats * (MAX_ENVELOPE + 1))]
+
+
+class Checkpoint(C.Structure):
+    """cdet_mcmcmc_checkpoint: one CDET_MCMCMC_CHAIN_CHECKPOINT_V1 file."""
+    _fields_ = [("chain_index", C.c_uint64), ("seed", C.c_uint64), ("order_min", C.c_int32),
+                ("order_max", C.c_int32), ("envelope_order", C.c_int32), ("normalization_order", C.c_int32),
+                ("lambda_warmup_steps", C.c_int32), ("production_steps", C.c_int32), ("seed_mode", C.c_char * 16),
+                ("rng_state", C.c_uint64 * 313), ("lambdas", C.c_double * (MAX_ENVELOPE + 1)),
+                ("warmup_block_counts", C.c_uint64 * (MAX_ENVELOPE + 1)),
+                ("vertices", (C.c_double * 4) * MAX_ENVELOPE), ("result", ChainResult)]
+
+
+class RunInfo(C.Structure):
+    """cdet_mcmcmc_run_info."""
+    _fields_ = [("normalization_order", C.c_int32), ("lambda_warmup_steps", C.c_int32),
+                ("production_steps", C.c_int32)]
 
 
 class RuntimeScalars(C.Structure):
@@ -102,6 +140,16 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_mcmcmc_state.argtypes = [vp, _DP, _DP, _UP]
     lib.cdet_mcmcmc_destroy.argtypes = [vp]
     lib.cdet_mcmcmc_set_histogram.argtypes = [vp, C.c_int32, _DP, _DP, _DP]
+    _LDP = C.POINTER(C.c_longdouble)
+    lib.cdet_mcmcmc_result.argtypes = [vp, C.c_int64, C.POINTER(ChainResult)]
+    lib.cdet_mcmcmc_summary.argtypes = [vp, C.c_int32, C.POINTER(RunningStats), _LDP]
+    lib.cdet_mcmcmc_estimates.argtypes = [vp, C.c_double, C.c_double, _LDP, _LDP, _LDP, _LDP]
+    lib.cdet_write_mcmcmc_checkpoint.argtypes = [C.c_char_p, C.POINTER(Checkpoint)]
+    lib.cdet_read_mcmcmc_checkpoint.argtypes = [C.c_char_p, C.POINTER(Checkpoint)]
+    lib.cdet_mcmcmc_save_checkpoints.argtypes = [vp, C.c_char_p, C.POINTER(RunInfo)]
+    lib.cdet_mcmcmc_load_checkpoints.argtypes = [vp, C.c_char_p, C.POINTER(RunInfo), C.c_int,
+                                                 C.POINTER(C.c_int64)]
+    lib.cdet_mcmcmc_launch_count.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.cdet_mcmcmc_learn_histogram.argtypes = [vp, C.POINTER(McmcmcConfig), C.POINTER(HistogramConfig), C.c_uint64,
                                                 _DP, _DP, _DP, _DP]
     lib.cdet_load_chunks.argtypes = [vp, C.c_char_p, _DP]

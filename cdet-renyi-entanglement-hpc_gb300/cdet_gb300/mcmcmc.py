@@ -7,11 +7,17 @@ chain's std::mt19937_64 stream reproduced on the device. With the FP64
 assembly the chains are the reference's chains, step for step.
 `learn_histogram` is learn_factorized_histogram_seed (:607-664) and
 `McmcmcChains.set_histogram` switches the chains to that seed kernel
-(MCMCMC_SEED_MODE=histogram).
+(MCMCMC_SEED_MODE=histogram). Every step also updates each chain's
+MCMCMCChainResult (`results`); `summary` and `estimates` are the reference's
+cross-chain aggregation (:1118-1146) and absolute estimates (main.cpp:831-870);
+`save_checkpoints` / `load_checkpoints` read and write the reference's V1
+checkpoint files, and `run_to` is run_single_mcmcmc_chain's loop (:994-1088)
+for the whole batch.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Optional, Sequence
 
 import numpy as np
@@ -68,6 +74,87 @@ class McmcmcChains:
         dp = C.POINTER(C.c_double)
         L.check(self._lib.cdet_mcmcmc_set_histogram(self._h, int(tau_bins), *(a.ctypes.data_as(dp) for a in arrs)))
 
+    def results(self) -> np.ndarray:
+        """Every chain's MCMCMCChainResult as a structured array (fields as in
+        cdet_mcmcmc_chain_result; running statistics with count, mean, m2 in
+        the host's long double)."""
+        arr = (L.ChainResult * self.chains)()
+        for c in range(self.chains):
+            L.check(self._lib.cdet_mcmcmc_result(self._h, c, C.byref(arr[c])))
+        return np.frombuffer(arr, dtype=result_dtype()).copy()
+
+    def summary(self, normalization_order: int):
+        """(cross-chain running statistics [envelope + 1], ratios to the
+        normalisation order [envelope + 1] as np.longdouble)."""
+        e1 = self.envelope + 1
+        cross = (L.RunningStats * e1)()
+        ratios = (C.c_longdouble * e1)()
+        L.check(self._lib.cdet_mcmcmc_summary(self._h, int(normalization_order), cross, ratios))
+        return (np.frombuffer(cross, dtype=stats_dtype()).copy(),
+                np.frombuffer(ratios, dtype=np.longdouble).copy())
+
+    def estimates(self, order1_hi: float, order1_lo: float = 0.0) -> dict:
+        """Absolute estimates normalised by the deterministic order-1 value."""
+        e1 = self.envelope + 1
+        const, const_err = C.c_longdouble(), C.c_longdouble()
+        est, err = (C.c_longdouble * e1)(), (C.c_longdouble * e1)()
+        L.check(self._lib.cdet_mcmcmc_estimates(self._h, float(order1_hi), float(order1_lo), C.byref(const),
+                                                C.byref(const_err), est, err))
+        return dict(normalization=_ld(const), normalization_stderr=_ld(const_err),
+                    estimate=np.frombuffer(est, dtype=np.longdouble).copy(),
+                    stderr=np.frombuffer(err, dtype=np.longdouble).copy())
+
+    def save_checkpoints(self, directory: str, normalization_order: int, lambda_warmup_steps: int,
+                         production_steps: int) -> None:
+        info = L.RunInfo(normalization_order, lambda_warmup_steps, production_steps)
+        L.check(self._lib.cdet_mcmcmc_save_checkpoints(self._h, os.fsencode(directory), C.byref(info)))
+
+    def load_checkpoints(self, directory: str, normalization_order: int, lambda_warmup_steps: int,
+                         production_steps: int, require: bool = False) -> int:
+        """Restores the chains that have a checkpoint in `directory`; returns
+        how many did."""
+        info = L.RunInfo(normalization_order, lambda_warmup_steps, production_steps)
+        restored = C.c_int64()
+        L.check(self._lib.cdet_mcmcmc_load_checkpoints(self._h, os.fsencode(directory), C.byref(info),
+                                                       int(require), C.byref(restored)))
+        return restored.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        L.check(self._lib.cdet_mcmcmc_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    def run_to(self, lambda_warmup_steps: int, production_steps: int, normalization_order: int,
+               checkpoint_dir: Optional[str] = None, checkpoint_interval: int = 0) -> None:
+        """run_single_mcmcmc_chain's loop for the batch: the remaining warmup
+        steps, the adaptation of a partial last block, the remaining
+        production steps; with checkpoint_dir, checkpoints whenever the
+        completed steps reach a multiple of checkpoint_interval (if > 0) and at
+        the end."""
+        res = self.results()
+        done = int(res["warmup_proposed_steps"][0] + res["production_proposed_steps"][0])
+
+        def save():
+            if checkpoint_dir:
+                self.save_checkpoints(checkpoint_dir, normalization_order, lambda_warmup_steps, production_steps)
+
+        def advance(steps: int, warmup: bool) -> None:
+            nonlocal done
+            while steps > 0:
+                chunk = steps
+                if checkpoint_dir and checkpoint_interval > 0:
+                    chunk = min(chunk, checkpoint_interval - done % checkpoint_interval)
+                self.run(chunk, warmup=warmup)
+                done += chunk
+                steps -= chunk
+                if checkpoint_dir and checkpoint_interval > 0 and done % checkpoint_interval == 0:
+                    save()
+
+        advance(max(0, lambda_warmup_steps - int(res["warmup_proposed_steps"][0])), True)
+        self.end_warmup()
+        advance(max(0, production_steps - int(res["production_proposed_steps"][0])), False)
+        save()
+
     def end_warmup(self) -> None:
         L.check(self._lib.cdet_mcmcmc_end_warmup(self._h))
 
@@ -92,6 +179,44 @@ class McmcmcChains:
             self.close()
         except Exception:
             pass
+
+
+def _ld(x: C.c_longdouble) -> np.longdouble:
+    """A ctypes long double as np.longdouble, every bit kept."""
+    return np.frombuffer(bytes(x), dtype=np.longdouble)[0]
+
+
+def stats_dtype() -> np.dtype:
+    """cdet_running_stats as a numpy structured type."""
+    if np.dtype(np.longdouble).itemsize != C.sizeof(C.c_longdouble):
+        raise RuntimeError("numpy's long double does not match the C long double")
+    R = L.RunningStats
+    return np.dtype({"names": ["count", "mean", "m2"], "formats": [np.uint64, np.longdouble, np.longdouble],
+                     "offsets": [R.count.offset, R.mean.offset, R.m2.offset], "itemsize": C.sizeof(R)})
+
+
+def result_dtype() -> np.dtype:
+    """cdet_mcmcmc_chain_result as a numpy structured type."""
+    R, st, e = L.ChainResult, stats_dtype(), L.MAX_ENVELOPE + 1
+    names = ["seed", "warmup_proposed_steps", "warmup_accepted_steps", "production_proposed_steps",
+             "production_accepted_steps", "warmup_chosen_counts", "production_chosen_counts",
+             "warmup_retained_fraction_stats", "production_retained_fraction_stats", "order_signal_stats"]
+    formats = [np.uint64] * 5 + [(np.uint64, (e,)), (np.uint64, (e,)), st, st, (st, (e,))]
+    return np.dtype({"names": names, "formats": formats, "offsets": [getattr(R, n).offset for n in names],
+                     "itemsize": C.sizeof(R)})
+
+
+def read_checkpoint(path: str, lib=None) -> L.Checkpoint:
+    """One CDET_MCMCMC_CHAIN_CHECKPOINT_V1 file (host only)."""
+    lib = lib or L.load()
+    ck = L.Checkpoint()
+    L.check(lib.cdet_read_mcmcmc_checkpoint(os.fsencode(path), C.byref(ck)))
+    return ck
+
+
+def write_checkpoint(path: str, ck: L.Checkpoint, lib=None) -> None:
+    lib = lib or L.load()
+    L.check(lib.cdet_write_mcmcmc_checkpoint(os.fsencode(path), C.byref(ck)))
 
 
 def learn_histogram(integrand: CdetIntegrand, order_min: int, order_max: int, envelope: int, learning_steps: int,

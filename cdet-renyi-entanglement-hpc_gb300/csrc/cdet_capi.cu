@@ -5,8 +5,7 @@
 // the FP64 kernels in cdet_kernels.cu. The host compiler runs with
 // -ffp-contract=off so the double-double prefactor arithmetic below rounds
 // every operation separately, as the reference's DoubleDouble does.
-#include "cdet_gb300.h"
-#include "cdet_kernels.cuh"
+#include "cdet_capi_internal.h"
 
 #include <algorithm>
 #include <cmath>
@@ -24,6 +23,10 @@ namespace {
 
 thread_local std::string g_last_error;
 
+}  // namespace
+
+namespace capi {
+
 int fail(int code, const std::string& message) {
     g_last_error = message;
     return code;
@@ -32,6 +35,17 @@ int fail(int code, const std::string& message) {
 int cuda_fail(cudaError_t err, const char* what) {
     return fail(CDET_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
 }
+
+}  // namespace capi
+
+using capi::cuda_fail;
+using capi::DeviceGuard;
+using capi::fail;
+using capi::SlicedBranch;
+using capi::TableSlot;
+
+namespace {
+
 
 // DoubleDouble (utility/types.h:30-182), host side.
 struct HostDD {
@@ -100,69 +114,10 @@ double prefactor_ld(int order, int n1, int n2, int r) {
     return static_cast<double>(num / den);
 }
 
-struct TableSlot {
-    cdet::TableDev dev{};
-    void* owned = nullptr;  // device allocation made by cdet_upload_table
-    int alias_of = -1;      // kind this slot shares, or -1
-    bool ready = false;
-};
-
-// bf16 slices of one branch of one table (split assembly)
-struct SlicedBranch {
-    void* mem = nullptr;  // slices followed by exponents
-    const uint16_t* slices = nullptr;
-    const int32_t* exponents = nullptr;
-    size_t blocks = 0;
-};
-
 }  // namespace
 
-struct cdet_context {
-    int device = 0;
-    int sm_count = 0;
-    cdet_runtime_scalars scalars{};
-    size_t coeff_count = 0, corner_count = 0;
-    TableSlot tables[4];
-    // scratch
-    void* scratch = nullptr;
-    size_t scratch_bytes = 0;
-    int64_t scratch_batch = 0;
-    int scratch_order = 0;
-    size_t ws_warps = 0;
-    // staging for the host-buffer entry points
-    void* staging = nullptr;
-    size_t staging_bytes = 0;
-    uint64_t calls = 0, fallbacks = 0;
-    int last_launches = 0;
-    // split assembly
-    int assembly = CDET_ASSEMBLY_FP64;
-    std::map<std::pair<const double*, size_t>, SlicedBranch> sliced;  // (coeffs, blocks) -> slices
-    void* split_scratch = nullptr;
-    size_t split_scratch_bytes = 0;
-    int32_t* split_error = nullptr;  // device flag of the last split evaluation
-    // measurement hooks
-    bool profiling = false;
-    std::vector<cdet::KernelEvents> pending;  // recorded, not yet read
-    std::vector<cdet::KernelEvents> spare;    // read, reusable
-    int64_t pending_launches = 0;
-};
 
 namespace {
-
-class DeviceGuard {
-public:
-    explicit DeviceGuard(int device) {
-        cudaGetDevice(&previous_);
-        if (previous_ != device) cudaSetDevice(device);
-        device_ = device;
-    }
-    ~DeviceGuard() {
-        if (previous_ != device_) cudaSetDevice(previous_);
-    }
-
-private:
-    int previous_ = 0, device_ = 0;
-};
 
 const cdet::TableDev* resolve(const cdet_context* ctx, int kind) {
     const TableSlot& slot = ctx->tables[kind];
@@ -189,6 +144,7 @@ void release_slot(TableSlot& slot) {
 // Drops the cached split slices of a slot's coefficients before the slot is
 // replaced: a new table may be allocated at the same device address.
 void forget_slices(cdet_context* ctx, const TableSlot& slot) {
+    ++ctx->generation;  // the slot is about to be replaced
     if (!slot.ready) return;
     for (auto it = ctx->sliced.begin(); it != ctx->sliced.end();) {
         if (it->first.first == slot.dev.upper || it->first.first == slot.dev.lower) {
@@ -217,6 +173,7 @@ int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
         ctx->scratch_order = 0;
         return cuda_fail(err, "cudaMalloc(scratch)");
     }
+    ++ctx->generation;
     ctx->scratch_bytes = bytes;
     ctx->scratch_batch = new_batch;
     ctx->scratch_order = new_order;
@@ -287,6 +244,7 @@ int slice_branch(cdet_context* ctx, const double* coeffs, size_t blocks, SlicedB
         cudaFree(b.mem);
         return cuda_fail(err, "slicing the tables");
     }
+    ++ctx->generation;
     auto res = ctx->sliced.emplace(key, b);
     *out = &res.first->second;
     return CDET_OK;
@@ -377,6 +335,7 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
             ctx->split_scratch = nullptr;
             ctx->split_scratch_bytes = 0;
             err = cudaMalloc(&ctx->split_scratch, need);
+            ++ctx->generation;
             if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(split scratch)");
             ctx->split_scratch_bytes = need;
         }
@@ -460,6 +419,17 @@ int run_host(cdet_context* ctx, const double* vertices, const int32_t* orders, i
 }
 
 }  // namespace
+
+namespace capi {
+
+const cdet::TableDev* resolve(const cdet_context* ctx, int kind) { return ::resolve(ctx, kind); }
+
+int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch, int max_order,
+        int all_subsets, double* values, int32_t* status, cudaStream_t stream, bool assembly_only) {
+    return ::run(ctx, vertices, orders, batch, max_order, all_subsets, values, status, stream, assembly_only);
+}
+
+}  // namespace capi
 
 namespace cdet {
 
@@ -588,6 +558,7 @@ int cdet_alias_table(cdet_context* ctx, int kind, int source_kind) {
     for (int k = source_kind; k >= 0; k = ctx->tables[k].alias_of)
         if (k == kind) return fail(CDET_ERR_INVALID, "alias cycle");
     TableSlot& slot = ctx->tables[kind];
+    forget_slices(ctx, slot);
     release_slot(slot);
     slot.alias_of = source_kind;
     return CDET_OK;
@@ -656,6 +627,7 @@ int cdet_set_assembly(cdet_context* ctx, int mode) {
         return fail(CDET_ERR_INVALID, "unknown assembly mode");
     if (mode == CDET_ASSEMBLY_SPLIT_BF16 && (ctx->scalars.cheb_nu > 128 || ctx->scalars.cheb_nv > 128))
         return fail(CDET_ERR_INVALID, "split assembly needs CHEB_NU and CHEB_NV <= 128");
+    if (ctx->assembly != mode) ++ctx->generation;
     ctx->assembly = mode;
     return CDET_OK;
 }
@@ -734,508 +706,6 @@ int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches) {
     ctx->pending.clear();
     if (launches) *launches += ctx->pending_launches;
     ctx->pending_launches = 0;
-    return CDET_OK;
-}
-
-}  // extern "C"
-
-// ------------------------------------------------------- MCMCMC chains ----
-struct cdet_mcmcmc {
-    cdet_context* ctx = nullptr;
-    cdet_mcmcmc_config cfg{};
-    int64_t chains = 0;
-    double inv_binom[cdet::kMcmcmcMaxEnvelope + 1] = {};
-    void* block = nullptr;
-    double* vert[2] = {nullptr, nullptr};
-    int cur = 0;
-    double* values = nullptr;
-    int32_t* istatus = nullptr;
-    double* lambdas = nullptr;
-    uint64_t* mt = nullptr;
-    int32_t* mt_index = nullptr;
-    uint64_t* counts = nullptr;
-    int32_t* error = nullptr;
-    int64_t warmup_done = 0;
-    // histogram seed kernel (tau_bins > 0): probabilities, CDFs and the
-    // conditional generation probabilities scratch in one allocation
-    int tau_bins = 0;
-    void* hist_block = nullptr;
-    double *tau_prob = nullptr, *space_prob = nullptr, *replica_prob = nullptr;
-    double *tau_cdf = nullptr, *space_cdf = nullptr, *replica_cdf = nullptr;
-    double* cprob = nullptr;
-};
-
-namespace {
-
-// adapt_mcmcmc_lambdas (mcmcmc_sampler.h:579-600) for every chain with a
-// nonzero block (only_pending: the partial last block, :1050-1054), then the
-// counts are cleared.
-int mcmcmc_adapt(cdet_mcmcmc* m, bool only_pending) {
-    const int env = m->cfg.envelope_order;
-    const size_t n = static_cast<size_t>(m->chains) * (env + 1);
-    std::vector<uint64_t> counts(n);
-    std::vector<double> lambdas(n);
-    cudaError_t err = cudaMemcpy(counts.data(), m->counts, n * sizeof(uint64_t), cudaMemcpyDeviceToHost);
-    if (err == cudaSuccess) err = cudaMemcpy(lambdas.data(), m->lambdas, n * sizeof(double), cudaMemcpyDeviceToHost);
-    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC lambda adaptation");
-    const int omin = m->cfg.order_min, omax = m->cfg.order_max;
-    const int order_count = omax - omin + 1;
-    const double target = 1.0 / static_cast<double>(order_count);
-    for (int64_t c = 0; c < m->chains; ++c) {
-        uint64_t* cc = counts.data() + c * (env + 1);
-        double* lam = lambdas.data() + c * (env + 1);
-        bool pending = false;
-        for (int o = 0; o <= env; ++o) pending |= cc[o] != 0;
-        if (only_pending && !pending) continue;
-        uint64_t total = 0;
-        for (int o = omin; o <= omax; ++o) total += cc[o];
-        if (total != 0) {
-            for (int o = omin; o <= omax; ++o) {
-                const double actual = (static_cast<double>(cc[o]) + 1.0) /
-                                      (static_cast<double>(total) + static_cast<double>(order_count));
-                lam[o] *= std::exp(m->cfg.lambda_adapt_rate * std::log(target / actual));
-            }
-        }
-        for (int o = 0; o <= env; ++o) cc[o] = 0;
-    }
-    err = cudaMemcpy(m->counts, counts.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(m->lambdas, lambdas.data(), n * sizeof(double), cudaMemcpyHostToDevice);
-    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC lambda adaptation");
-    return CDET_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int cdet_mcmcmc_create(cdet_context* ctx, const cdet_mcmcmc_config* config, int64_t chains, const uint64_t* seeds,
-                       const double* lambdas, cdet_mcmcmc** out) {
-    if (!ctx || !config || !seeds || !lambdas || !out) return fail(CDET_ERR_INVALID, "null argument");
-    const cdet_mcmcmc_config& c = *config;
-    // validate_mcmcmc_config (mcmcmc_sampler.h:432-493)
-    if (c.order_min < 1) return fail(CDET_ERR_INVALID, "MCMCMC_ORDER_MIN must be at least 1 for the replica integrand");
-    if (c.order_max < c.order_min) return fail(CDET_ERR_INVALID, "MCMCMC_ORDER_MAX must be >= MCMCMC_ORDER_MIN");
-    if (c.envelope_order <= c.order_max)
-        return fail(CDET_ERR_INVALID, "MCMCMC_ENVELOPE_ORDER must be larger than MCMCMC_ORDER_MAX");
-    if (c.envelope_order > cdet::kMcmcmcMaxEnvelope)
-        return fail(CDET_ERR_INVALID, "MCMCMC_ENVELOPE_ORDER must be <= 24 for the GPU chains");
-    if (chains <= 0) return fail(CDET_ERR_INVALID, "MCMCMC_CHAIN_COUNT must be positive");
-    if (c.lambda_adapt_interval <= 0) return fail(CDET_ERR_INVALID, "MCMCMC_LAMBDA_ADAPT_INTERVAL must be positive");
-    for (int o = c.order_min; o <= c.order_max; ++o)
-        if (!(lambdas[o] > 0.0) || !std::isfinite(lambdas[o]))
-            return fail(CDET_ERR_INVALID, "MCMCMC_LAMBDAS entries must be positive finite numbers");
-    for (int k = 0; k < 4; ++k)
-        if (!resolve(ctx, k)) return fail(CDET_ERR_STATE, "Green-function tables have not been uploaded");
-    DeviceGuard guard(ctx->device);
-    auto* m = new cdet_mcmcmc;
-    m->ctx = ctx;
-    m->cfg = c;
-    m->chains = chains;
-    const int env = c.envelope_order;
-    for (int o = c.order_min; o <= c.order_max; ++o) {
-        // 1 / binomial_as_double(envelope, order) (:174-185); the binomial is an exact integer here
-        uint64_t b = 1;
-        const int k = o < env - o ? o : env - o;
-        for (int i = 1; i <= k; ++i) b = b * static_cast<uint64_t>(env - k + i) / static_cast<uint64_t>(i);
-        m->inv_binom[o] = 1.0 / static_cast<double>(b);
-    }
-    const size_t nv = static_cast<size_t>(chains) * env * 4;
-    const size_t nvals = static_cast<size_t>(chains) << env;
-    const size_t nl = static_cast<size_t>(chains) * (env + 1);
-    const size_t nmt = static_cast<size_t>(chains) * 312;
-    auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
-    const size_t bytes = 2 * up(nv * 8) + up(nvals * 8) + up(chains * 4) + up(nl * 8) + up(nmt * 8) +
-                         up(chains * 4) + up(nl * 8) + up(chains * 4) + up(chains * 8);
-    cudaError_t err = cudaMalloc(&m->block, bytes);
-    if (err != cudaSuccess) {
-        delete m;
-        return cuda_fail(err, "cudaMalloc(MCMCMC chains)");
-    }
-    char* p = static_cast<char*>(m->block);
-    auto take = [&](size_t b) {
-        void* r = p;
-        p += up(b);
-        return r;
-    };
-    m->vert[0] = static_cast<double*>(take(nv * 8));
-    m->vert[1] = static_cast<double*>(take(nv * 8));
-    m->values = static_cast<double*>(take(nvals * 8));
-    m->istatus = static_cast<int32_t*>(take(chains * 4));
-    m->lambdas = static_cast<double*>(take(nl * 8));
-    m->mt = static_cast<uint64_t*>(take(nmt * 8));
-    m->mt_index = static_cast<int32_t*>(take(chains * 4));
-    m->counts = static_cast<uint64_t*>(take(nl * 8));
-    m->error = static_cast<int32_t*>(take(chains * 4));
-    uint64_t* dseeds = static_cast<uint64_t*>(take(chains * 8));
-    std::vector<double> lam(nl);
-    for (int64_t ch = 0; ch < chains; ++ch)
-        for (int o = 0; o <= env; ++o) lam[ch * (env + 1) + o] = lambdas[o];
-    err = cudaMemcpy(dseeds, seeds, chains * 8, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(m->lambdas, lam.data(), nl * 8, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemset(m->counts, 0, nl * 8);
-    if (err == cudaSuccess) err = cudaMemset(m->error, 0, chains * 4);
-    if (err == cudaSuccess) err = cdet::launch_mcmcmc_init(chains, env, dseeds, m->mt, m->mt_index, m->vert[0], nullptr);
-    if (err == cudaSuccess) err = cudaDeviceSynchronize();
-    if (err != cudaSuccess) {
-        cudaFree(m->block);
-        delete m;
-        return cuda_fail(err, "MCMCMC chain initialisation");
-    }
-    *out = m;
-    return CDET_OK;
-}
-
-int cdet_mcmcmc_run(cdet_mcmcmc* m, int warmup, int64_t steps, uint64_t* chosen, double* norms, double* signal) {
-    if (!m || steps < 0) return fail(CDET_ERR_INVALID, "bad argument");
-    if (steps == 0) return CDET_OK;
-    DeviceGuard guard(m->ctx->device);
-    const int env = m->cfg.envelope_order;
-    const int64_t chains = m->chains;
-    uint64_t* d_chosen = nullptr;
-    double* d_norms = nullptr;
-    double* d_signal = nullptr;
-    cudaError_t err = cudaSuccess;
-    if (chosen) err = cudaMalloc(&d_chosen, static_cast<size_t>(steps) * chains * 8);
-    if (err == cudaSuccess && norms) err = cudaMalloc(&d_norms, static_cast<size_t>(steps) * chains * 8);
-    if (err == cudaSuccess && signal)
-        err = cudaMalloc(&d_signal, static_cast<size_t>(steps) * chains * (env + 1) * 8);
-    int rc = err == cudaSuccess ? CDET_OK : cuda_fail(err, "cudaMalloc(MCMCMC step outputs)");
-    for (int64_t s = 0; rc == CDET_OK && s < steps; ++s) {
-        rc = run(m->ctx, m->vert[m->cur], nullptr, chains, env, 1, m->values, m->istatus, nullptr);
-        if (rc != CDET_OK) break;
-        cdet::McmcmcStepArgs a{};
-        a.chains = chains;
-        a.envelope = env;
-        a.order_min = m->cfg.order_min;
-        a.order_max = m->cfg.order_max;
-        a.warmup = warmup ? 1 : 0;
-        for (int o = 0; o <= env; ++o) a.inv_binom[o] = m->inv_binom[o];
-        a.values = m->values;
-        a.integrand_status = m->istatus;
-        a.vertices = m->vert[m->cur];
-        a.next_vertices = m->vert[m->cur ^ 1];
-        a.lambdas = m->lambdas;
-        a.mt = m->mt;
-        a.mt_index = m->mt_index;
-        a.counts = m->counts;
-        a.error = m->error;
-        a.chosen_out = d_chosen ? d_chosen + s * chains : nullptr;
-        a.norm_out = d_norms ? d_norms + s * chains : nullptr;
-        a.signal_out = d_signal ? d_signal + s * chains * (env + 1) : nullptr;
-        if (m->tau_bins > 0) {
-            a.tau_bins = m->tau_bins;
-            a.n1 = m->ctx->scalars.n1;
-            a.n2 = m->ctx->scalars.n2;
-            a.tau_prob = m->tau_prob;
-            a.space_prob = m->space_prob;
-            a.replica_prob = m->replica_prob;
-            a.tau_cdf = m->tau_cdf;
-            a.space_cdf = m->space_cdf;
-            a.replica_cdf = m->replica_cdf;
-            a.cprob = m->cprob;
-        }
-        err = cdet::launch_mcmcmc_step(a, nullptr);
-        if (err != cudaSuccess) {
-            rc = cuda_fail(err, "MCMCMC step launch");
-            break;
-        }
-        m->cur ^= 1;
-        if (warmup) {
-            ++m->warmup_done;
-            if (m->warmup_done % m->cfg.lambda_adapt_interval == 0) rc = mcmcmc_adapt(m, false);
-        }
-    }
-    if (rc == CDET_OK) {
-        err = cudaDeviceSynchronize();
-        if (err == cudaSuccess && chosen)
-            err = cudaMemcpy(chosen, d_chosen, static_cast<size_t>(steps) * chains * 8, cudaMemcpyDeviceToHost);
-        if (err == cudaSuccess && norms)
-            err = cudaMemcpy(norms, d_norms, static_cast<size_t>(steps) * chains * 8, cudaMemcpyDeviceToHost);
-        if (err == cudaSuccess && signal)
-            err = cudaMemcpy(signal, d_signal, static_cast<size_t>(steps) * chains * (env + 1) * 8,
-                             cudaMemcpyDeviceToHost);
-        if (err != cudaSuccess) rc = cuda_fail(err, "MCMCMC step outputs");
-    }
-    if (d_chosen) cudaFree(d_chosen);
-    if (d_norms) cudaFree(d_norms);
-    if (d_signal) cudaFree(d_signal);
-    if (rc != CDET_OK) return rc;
-    std::vector<int32_t> errors(static_cast<size_t>(chains));
-    err = cudaMemcpy(errors.data(), m->error, chains * 4, cudaMemcpyDeviceToHost);
-    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC status");
-    for (int64_t c = 0; c < chains; ++c) {
-        if (errors[c] == 1)
-            return fail(CDET_ERR_VALUE, "Error (all-subset integrand): Value is not finite (chain " +
-                                            std::to_string(c) + ")");
-        if (errors[c] == 2)
-            return fail(CDET_ERR_VALUE,
-                        "MCMCMC local normalization is zero or non-finite (chain " + std::to_string(c) + ")");
-        if (errors[c] == 3)
-            return fail(CDET_ERR_VALUE,
-                        "MCMCMC seed density is negative or non-finite (chain " + std::to_string(c) + ")");
-    }
-    return CDET_OK;
-}
-
-int cdet_mcmcmc_end_warmup(cdet_mcmcmc* m) {
-    if (!m) return fail(CDET_ERR_INVALID, "bad argument");
-    DeviceGuard guard(m->ctx->device);
-    if (m->warmup_done % m->cfg.lambda_adapt_interval == 0) return CDET_OK;
-    return mcmcmc_adapt(m, true);
-}
-
-int cdet_mcmcmc_state(const cdet_mcmcmc* m, double* vertices, double* lambdas, uint64_t* rng_state) {
-    if (!m) return fail(CDET_ERR_INVALID, "bad argument");
-    DeviceGuard guard(m->ctx->device);
-    const int env = m->cfg.envelope_order;
-    const int64_t chains = m->chains;
-    cudaError_t err = cudaDeviceSynchronize();
-    if (err == cudaSuccess && vertices)
-        err = cudaMemcpy(vertices, m->vert[m->cur], static_cast<size_t>(chains) * env * 4 * 8, cudaMemcpyDeviceToHost);
-    if (err == cudaSuccess && lambdas)
-        err = cudaMemcpy(lambdas, m->lambdas, static_cast<size_t>(chains) * (env + 1) * 8, cudaMemcpyDeviceToHost);
-    if (err == cudaSuccess && rng_state) {
-        std::vector<uint64_t> words(static_cast<size_t>(chains) * 312);
-        std::vector<int32_t> index(static_cast<size_t>(chains));
-        err = cudaMemcpy(words.data(), m->mt, words.size() * 8, cudaMemcpyDeviceToHost);
-        if (err == cudaSuccess) err = cudaMemcpy(index.data(), m->mt_index, chains * 4, cudaMemcpyDeviceToHost);
-        if (err == cudaSuccess)
-            for (int64_t c = 0; c < chains; ++c) {
-                for (int i = 0; i < 312; ++i) rng_state[c * 313 + i] = words[static_cast<size_t>(i) * chains + c];
-                rng_state[c * 313 + 312] = static_cast<uint64_t>(index[c]);
-            }
-    }
-    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC state");
-    return CDET_OK;
-}
-
-int cdet_mcmcmc_destroy(cdet_mcmcmc* m) {
-    if (!m) return CDET_OK;
-    DeviceGuard guard(m->ctx->device);
-    cudaFree(m->block);
-    if (m->hist_block) cudaFree(m->hist_block);
-    delete m;
-    return CDET_OK;
-}
-
-int cdet_mcmcmc_set_histogram(cdet_mcmcmc* m, int32_t tau_bins, const double* tau_prob, const double* space_prob,
-                              const double* replica_prob) {
-    if (!m || !tau_prob || !space_prob || !replica_prob) return fail(CDET_ERR_INVALID, "null argument");
-    const int n1 = m->ctx->scalars.n1, n2 = m->ctx->scalars.n2;
-    if (tau_bins <= 0 || n1 <= 0 || n2 <= 0) return fail(CDET_ERR_INVALID, "Histogram seed dimensions must be positive");
-    const size_t sites = static_cast<size_t>(n1) * n2;
-    const size_t nt = static_cast<size_t>(tau_bins) * tau_bins, ns = sites * sites;
-    // build_cdfs (mcmcmc_seed.h:190-203): running row sums, the last column set to 1
-    auto cdf = [](const double* prob, size_t columns, size_t rows) {
-        std::vector<double> out(columns * rows);
-        for (size_t r = 0; r < rows; ++r) {
-            double cumulative = 0.0;
-            for (size_t c = 0; c < columns; ++c) {
-                cumulative += prob[r * columns + c];
-                out[r * columns + c] = cumulative;
-            }
-            out[r * columns + columns - 1] = 1.0;
-        }
-        return out;
-    };
-    const std::vector<double> tc = cdf(tau_prob, tau_bins, tau_bins), sc = cdf(space_prob, sites, sites),
-                              rc = cdf(replica_prob, 2, 2);
-    DeviceGuard guard(m->ctx->device);
-    auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
-    const size_t nprob = static_cast<size_t>(m->chains) << m->cfg.envelope_order;
-    const size_t bytes = 2 * (up(nt * 8) + up(ns * 8) + up(32)) + up(nprob * 8);
-    void* block = nullptr;
-    cudaError_t err = cudaMalloc(&block, bytes);
-    if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(MCMCMC histogram seed)");
-    char* p = static_cast<char*>(block);
-    auto take = [&](size_t b) {
-        double* r = reinterpret_cast<double*>(p);
-        p += up(b);
-        return r;
-    };
-    double* tp = take(nt * 8);
-    double* sp = take(ns * 8);
-    double* rp = take(32);
-    double* tcd = take(nt * 8);
-    double* scd = take(ns * 8);
-    double* rcd = take(32);
-    double* cprob = take(nprob * 8);
-    err = cudaMemcpy(tp, tau_prob, nt * 8, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(sp, space_prob, ns * 8, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(rp, replica_prob, 32, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(tcd, tc.data(), nt * 8, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(scd, sc.data(), ns * 8, cudaMemcpyHostToDevice);
-    if (err == cudaSuccess) err = cudaMemcpy(rcd, rc.data(), 32, cudaMemcpyHostToDevice);
-    if (err != cudaSuccess) {
-        cudaFree(block);
-        return cuda_fail(err, "MCMCMC histogram seed upload");
-    }
-    if (m->hist_block) {
-        cudaDeviceSynchronize();
-        cudaFree(m->hist_block);
-    }
-    m->hist_block = block;
-    m->tau_bins = tau_bins;
-    m->tau_prob = tp;
-    m->space_prob = sp;
-    m->replica_prob = rp;
-    m->tau_cdf = tcd;
-    m->space_cdf = scd;
-    m->replica_cdf = rcd;
-    m->cprob = cprob;
-    return CDET_OK;
-}
-
-int cdet_mcmcmc_learn_histogram(cdet_context* ctx, const cdet_mcmcmc_config* config,
-                                const cdet_histogram_config* histogram, uint64_t base_seed, double* tau_prob,
-                                double* space_prob, double* replica_prob, double* total_pair_weight) {
-    if (!ctx || !config || !histogram || !tau_prob || !space_prob || !replica_prob)
-        return fail(CDET_ERR_INVALID, "null argument");
-    const cdet_mcmcmc_config& c = *config;
-    const cdet_histogram_config& h = *histogram;
-    const int env = c.envelope_order;
-    if (c.order_min < 1 || c.order_max < c.order_min || env <= c.order_max || env > cdet::kMcmcmcMaxEnvelope)
-        return fail(CDET_ERR_INVALID, "invalid MCMCMC order range or envelope");
-    if (h.learning_steps <= 0)
-        return fail(CDET_ERR_INVALID, "MCMCMC_SEED_HISTOGRAM_LEARNING_STEPS must be positive for histogram seed");
-    const int n1 = ctx->scalars.n1, n2 = ctx->scalars.n2;
-    if (h.tau_bins <= 0 || n1 <= 0 || n2 <= 0) return fail(CDET_ERR_INVALID, "Histogram seed dimensions must be positive");
-    if (!(h.uniform_mix >= 0.0 && h.uniform_mix <= 1.0))
-        return fail(CDET_ERR_INVALID, "MCMCMC_SEED_HISTOGRAM_UNIFORM_MIX must lie in [0, 1]");
-    if (h.pseudo_count < 0.0 || !std::isfinite(h.pseudo_count))
-        return fail(CDET_ERR_INVALID, "MCMCMC_SEED_HISTOGRAM_PSEUDO_COUNT must be nonnegative and finite");
-    for (int k = 0; k < 4; ++k)
-        if (!resolve(ctx, k)) return fail(CDET_ERR_STATE, "Green-function tables have not been uploaded");
-    DeviceGuard guard(ctx->device);
-    // learn_factorized_histogram_seed (mcmcmc_sampler.h:607-664): uniform
-    // envelopes from the std::mt19937_64 stream derive_mcmcmc_seed(base,
-    // "HISTOSEE"), their all-subset integrands, pair weights accumulated in
-    // long double (FactorizedHistogramSeedAccumulator, mcmcmc_seed.h:232-330).
-    // The envelopes only consume the generator, so they are drawn first and
-    // the integrands evaluated on the GPU in batches.
-    auto splitmix = [](uint64_t x) {
-        x += 0x9e3779b97f4a7c15ULL;
-        x = (x ^ (x >> 30U)) * 0xbf58476d1ce4e5b9ULL;
-        x = (x ^ (x >> 27U)) * 0x94d049bb133111ebULL;
-        return x ^ (x >> 31U);
-    };
-    uint64_t mixed = splitmix(base_seed ^ 0x484953544F534545ULL);
-    mixed ^= 0x9e3779b97f4a7c15ULL * 1ULL;
-    std::mt19937_64 rng(splitmix(mixed));
-    std::uniform_real_distribution<double> uniform01(0.0, 1.0);
-    const int64_t steps = h.learning_steps;
-    std::vector<double> vertices(static_cast<size_t>(steps) * env * 4);
-    for (double& x : vertices) x = uniform01(rng);
-
-    const int sites = n1 * n2;
-    const int bins = h.tau_bins;
-    std::vector<long double> tau_c(static_cast<size_t>(bins) * bins, 0.0L);
-    std::vector<long double> space_c(static_cast<size_t>(sites) * sites, 0.0L);
-    std::vector<long double> rep_c(4, 0.0L);
-    long double total = 0.0L;
-    auto index = [](double value, int extent) {
-        const int i = static_cast<int>(std::floor(value * static_cast<double>(extent)));
-        return i < 0 ? 0 : (i >= extent ? extent - 1 : i);
-    };
-    double binom[cdet::kMcmcmcMaxEnvelope + 1];
-    for (int o = 0; o <= env; ++o) {
-        uint64_t b = 1;
-        const int k = o < env - o ? o : env - o;
-        for (int i = 1; i <= k; ++i) b = b * static_cast<uint64_t>(env - k + i) / static_cast<uint64_t>(i);
-        binom[o] = static_cast<double>(b);
-    }
-    const uint64_t subsets = uint64_t{1} << env;
-    // batches of envelopes whose integrands fit 256 MiB
-    const int64_t batch = std::max<int64_t>(1, std::min<int64_t>(steps, (int64_t{256} << 20) / (subsets * 8)));
-    double* dverts = nullptr;
-    double* dvals = nullptr;
-    int32_t* dstatus = nullptr;
-    cudaError_t err = cudaMalloc(&dverts, static_cast<size_t>(batch) * env * 4 * 8);
-    if (err == cudaSuccess) err = cudaMalloc(&dvals, static_cast<size_t>(batch) * subsets * 8);
-    if (err == cudaSuccess) err = cudaMalloc(&dstatus, static_cast<size_t>(batch) * 4);
-    int rc = err == cudaSuccess ? CDET_OK : cuda_fail(err, "cudaMalloc(histogram learning)");
-    std::vector<double> values;
-    std::vector<int32_t> status;
-    for (int64_t first = 0; rc == CDET_OK && first < steps; first += batch) {
-        const int64_t n = std::min<int64_t>(batch, steps - first);
-        const double* hv = vertices.data() + static_cast<size_t>(first) * env * 4;
-        err = cudaMemcpy(dverts, hv, static_cast<size_t>(n) * env * 4 * 8, cudaMemcpyHostToDevice);
-        if (err != cudaSuccess) {
-            rc = cuda_fail(err, "histogram learning upload");
-            break;
-        }
-        rc = run(ctx, dverts, nullptr, n, env, 1, dvals, dstatus, nullptr);
-        if (rc != CDET_OK) break;
-        values.resize(static_cast<size_t>(n) * subsets);
-        status.resize(static_cast<size_t>(n));
-        err = cudaMemcpy(values.data(), dvals, values.size() * 8, cudaMemcpyDeviceToHost);
-        if (err == cudaSuccess) err = cudaMemcpy(status.data(), dstatus, status.size() * 4, cudaMemcpyDeviceToHost);
-        if (err != cudaSuccess) {
-            rc = cuda_fail(err, "histogram learning values");
-            break;
-        }
-        for (int64_t e = 0; e < n && rc == CDET_OK; ++e) {
-            if (status[e] & cdet::kStatusNonFinite) {
-                rc = fail(CDET_ERR_VALUE, "Error (all-subset integrand): Value is not finite");
-                break;
-            }
-            const double* v = hv + static_cast<size_t>(e) * env * 4;
-            const double* val = values.data() + static_cast<size_t>(e) * subsets;
-            for (uint64_t mask = 1; mask < subsets; ++mask) {
-                const int order = __builtin_popcountll(mask);
-                if (order < c.order_min || order > c.order_max || order < 2) continue;
-                const double value = val[mask];
-                if (!std::isfinite(value)) continue;
-                const long double subset_weight =
-                    static_cast<long double>(std::abs(value)) / static_cast<long double>(binom[order]);
-                const long double pair_weight = subset_weight / static_cast<long double>(order * (order - 1));
-                if (!(pair_weight > 0.0L) || !std::isfinite(static_cast<double>(pair_weight))) continue;
-                for (int parent = 0; parent < env; ++parent) {
-                    if (!(mask & (uint64_t{1} << parent))) continue;
-                    const double* pv = v + 4 * parent;
-                    for (int child = 0; child < env; ++child) {
-                        if (child == parent || !(mask & (uint64_t{1} << child))) continue;
-                        const double* cv = v + 4 * child;
-                        tau_c[static_cast<size_t>(index(pv[0], bins)) * bins + index(cv[0], bins)] += pair_weight;
-                        const int ps = index(pv[1], n1) * n2 + index(pv[2], n2);
-                        const int cs = index(cv[1], n1) * n2 + index(cv[2], n2);
-                        space_c[static_cast<size_t>(ps) * sites + cs] += pair_weight;
-                        rep_c[index(pv[3], 2) * 2 + index(cv[3], 2)] += pair_weight;
-                        total += pair_weight;
-                    }
-                }
-            }
-        }
-    }
-    if (dverts) cudaFree(dverts);
-    if (dvals) cudaFree(dvals);
-    if (dstatus) cudaFree(dstatus);
-    if (rc != CDET_OK) return rc;
-    // normalize_rows (mcmcmc_seed.h:288-327)
-    auto normalize = [&](const std::vector<long double>& counts, int columns, double* out) {
-        const int rows = static_cast<int>(counts.size()) / columns;
-        const long double uniform = 1.0L / static_cast<long double>(columns);
-        const long double mix = static_cast<long double>(h.uniform_mix);
-        const long double pseudo = static_cast<long double>(h.pseudo_count);
-        for (int r = 0; r < rows; ++r) {
-            long double row_sum = 0.0L;
-            for (int k = 0; k < columns; ++k) row_sum += counts[static_cast<size_t>(r) * columns + k];
-            const long double denominator = row_sum + pseudo * static_cast<long double>(columns);
-            for (int k = 0; k < columns; ++k) {
-                long double learned = uniform;
-                if (denominator > 0.0L) learned = (counts[static_cast<size_t>(r) * columns + k] + pseudo) / denominator;
-                out[static_cast<size_t>(r) * columns + k] = static_cast<double>((1.0L - mix) * learned + mix * uniform);
-            }
-            double row_total = 0.0;
-            for (int k = 0; k < columns; ++k) row_total += out[static_cast<size_t>(r) * columns + k];
-            if (row_total > 0.0 && std::isfinite(row_total))
-                for (int k = 0; k < columns; ++k) out[static_cast<size_t>(r) * columns + k] /= row_total;
-        }
-    };
-    normalize(tau_c, bins, tau_prob);
-    normalize(space_c, sites, space_prob);
-    normalize(rep_c, 2, replica_prob);
-    if (total_pair_weight) *total_pair_weight = static_cast<double>(total);
     return CDET_OK;
 }
 

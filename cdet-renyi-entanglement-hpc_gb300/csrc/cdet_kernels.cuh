@@ -118,9 +118,12 @@ struct McmcmcStepArgs {
     int32_t* mt_index;              // [chains]
     uint64_t* counts;               // [chains][envelope + 1] warmup block counts
     int32_t* error;                 // [chains]: 0, 1 (integrand not finite), 2 (normalisation), 3 (seed density)
-    uint64_t* chosen_out;           // [chains] or null
-    double* norm_out;               // [chains] or null
-    double* signal_out;             // [chains][envelope + 1] or null
+    // per-step outputs at ring row r = *ring_row (0 when ring_row is null):
+    // chosen_out[r][chains], norm_out[r][chains], signal_out[r][chains][envelope + 1]
+    const int64_t* ring_row;
+    uint64_t* chosen_out;           // or null
+    double* norm_out;               // or null
+    double* signal_out;             // or null
     // histogram seed kernel when tau_bins > 0: row probabilities and their
     // CDFs (tau [bins][bins], space [N1 N2][N1 N2], replica [2][2]) and the
     // conditional generation probabilities scratch [chains][2^envelope]
@@ -132,6 +135,8 @@ struct McmcmcStepArgs {
 cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* seeds, uint64_t* mt, int32_t* mt_index,
                                double* vertices, cudaStream_t stream);
 cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream);
+// *row = (*row + 1) % rows, after a step (one thread)
+cudaError_t launch_mcmcmc_advance_row(int64_t* row, int64_t rows, cudaStream_t stream);
 
 // Order-1 diagonal observable: items[3 * N1 * N2] scratch, out[3] = {twisted -
 // 2 ordinary, twisted, ordinary}; tables in kind order (twisted up, twisted

@@ -195,6 +195,8 @@ template <bool Hist>
 __global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ McmcmcStepArgs a) {
     const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= a.chains) return;
+    const int64_t row = a.ring_row ? *a.ring_row : 0;
+    if (a.chosen_out) a.chosen_out[row * a.chains + c] = 0;  // 0: no step (a failed chain)
     if (a.error[c]) return;  // a chain that failed stays where it stopped
     if (a.integrand_status[c] & kStatusNonFinite) {
         a.error[c] = 1;  // "Error (all-subset integrand): Value is not finite"
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ Mcmcm
     if (!found) chosen = last_positive;
     // order signal: time = flux / local_normalization, weighted by 1/binomial (:566-571)
     if (a.signal_out) {
-        double* sig = a.signal_out + c * (env + 1);
+        double* sig = a.signal_out + (row * a.chains + c) * (env + 1);
         for (int o = 0; o <= env; ++o) sig[o] = 0.0;
         for (uint64_t mask = 1; mask < subsets; ++mask) {
             const int o = __popcll(mask);
@@ -281,12 +283,21 @@ __global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ Mcmcm
         ++size;
     }
     const int order = __popcll(chosen);
-    if (a.chosen_out) a.chosen_out[c] = chosen;
-    if (a.norm_out) a.norm_out[c] = norm;
+    if (a.chosen_out) a.chosen_out[row * a.chains + c] = chosen;
+    if (a.norm_out) a.norm_out[row * a.chains + c] = norm;
     if (a.warmup) ++a.counts[c * (env + 1) + order];
 }
 
+__global__ void mcmcmc_advance_row(int64_t* row, int64_t rows) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *row = (*row + 1) % rows;
+}
+
 }  // namespace
+
+cudaError_t launch_mcmcmc_advance_row(int64_t* row, int64_t rows, cudaStream_t stream) {
+    mcmcmc_advance_row<<<1, 32, 0, stream>>>(row, rows);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* seeds, uint64_t* mt, int32_t* mt_index,
                                double* vertices, cudaStream_t stream) {

@@ -211,13 +211,108 @@ int cdet_mcmcmc_create(cdet_context* ctx, const cdet_mcmcmc_config* config, int6
 
 /* Advances every chain `steps` steps. warmup = 1: warmup steps (the chosen
  * orders are counted and lambdas adapted every lambda_adapt_interval warmup
- * steps); warmup = 0: production steps. Optional host outputs (null to skip):
- * chosen[step][chain] masks, norms[step][chain] local normalisations,
- * signal[step][chain][envelope + 1] the raw order signals (the reference's
- * workspace.order_signal). A chain whose integrand is not finite or whose
- * local normalisation is not positive stops (the reference throws); the call
- * then returns CDET_ERR_VALUE naming the chain. Blocking. */
+ * steps); warmup = 0: production steps. Each step also updates the chain's
+ * MCMCMCChainResult (below) as run_single_mcmcmc_chain does (:1036-1084).
+ * Optional host outputs (null to skip): chosen[step][chain] masks,
+ * norms[step][chain] local normalisations, signal[step][chain][envelope + 1]
+ * the raw order signals (the reference's workspace.order_signal). A chain
+ * whose integrand is not finite or whose local normalisation is not positive
+ * stops (the reference throws); the call then returns CDET_ERR_VALUE naming
+ * the chain, and the results of that call are not defined. Steps after the
+ * first are replayed from a CUDA graph of one step. Blocking. */
 int cdet_mcmcmc_run(cdet_mcmcmc* m, int warmup, int64_t steps, uint64_t* chosen, double* norms, double* signal);
+
+#define CDET_MCMCMC_MAX_ENVELOPE 24
+
+/* RunningStatsLongDouble (mcmcmc_sampler.h:31-77): Welford's running mean
+ * and sum of squared deviations, in the host's long double. */
+typedef struct cdet_running_stats {
+    uint64_t count;
+    long double mean;
+    long double m2;
+} cdet_running_stats;
+
+/* MCMCMCChainResult (mcmcmc_sampler.h:126-139) of one chain; arrays are
+ * indexed by order (0..envelope_order used). The order signal statistics
+ * collect order_signal[order] / lambdas[order] of every production step. */
+typedef struct cdet_mcmcmc_chain_result {
+    uint64_t seed;
+    uint64_t warmup_proposed_steps;
+    uint64_t warmup_accepted_steps;
+    uint64_t production_proposed_steps;
+    uint64_t production_accepted_steps;
+    uint64_t warmup_chosen_counts[CDET_MCMCMC_MAX_ENVELOPE + 1];
+    uint64_t production_chosen_counts[CDET_MCMCMC_MAX_ENVELOPE + 1];
+    cdet_running_stats warmup_retained_fraction_stats;
+    cdet_running_stats production_retained_fraction_stats;
+    cdet_running_stats order_signal_stats[CDET_MCMCMC_MAX_ENVELOPE + 1];
+} cdet_mcmcmc_chain_result;
+
+int cdet_mcmcmc_result(const cdet_mcmcmc* m, int64_t chain, cdet_mcmcmc_chain_result* out);
+
+/* The aggregation of run_mcmcmc_chains_parallel (mcmcmc_sampler.h:1118-1146):
+ * cross_chain[order] = running statistics of the chain means (each chain with
+ * samples is one sample, in chain order) and ratios[order] = its mean over the
+ * mean at normalization_order (NaN when that is 0), for order_min..order_max;
+ * other orders are zero statistics and NaN ratios. Arrays of envelope + 1. */
+int cdet_mcmcmc_summary(const cdet_mcmcmc* m, int32_t normalization_order, cdet_running_stats* cross_chain,
+                        long double* ratios);
+
+/* The absolute estimates of print_mcmcmc_summary (main.cpp:831-870): with
+ * the deterministic order-1 value (a double-double, hi + lo) and the order-1
+ * cross-chain statistics, the normalisation constant and its error, and per
+ * order (envelope + 1 entries; order_min..order_max filled, order 1 = the
+ * deterministic value) the estimate and its propagated error. Needs
+ * order_min <= 1 <= order_max; CDET_ERR_VALUE when the order-1 mean is zero
+ * or not finite (the reference skips the estimates). */
+int cdet_mcmcmc_estimates(const cdet_mcmcmc* m, double order1_hi, double order1_lo, long double* normalization,
+                          long double* normalization_stderr, long double* estimate, long double* estimate_stderr);
+
+/* One CDET_MCMCMC_CHAIN_CHECKPOINT_V1 file (save_mcmcmc_chain_checkpoint /
+ * load_mcmcmc_chain_checkpoint, mcmcmc_sampler.h:807-992): the chain's
+ * state, the run settings it was written under, and its result. Arrays are
+ * indexed by order (envelope_order + 1 used) or vertex. */
+typedef struct cdet_mcmcmc_checkpoint {
+    uint64_t chain_index;
+    uint64_t seed;
+    int32_t order_min, order_max, envelope_order, normalization_order;
+    int32_t lambda_warmup_steps, production_steps;
+    char seed_mode[16]; /* "uniform" or "histogram" */
+    uint64_t rng_state[313]; /* the 312 mt19937_64 words, then the position */
+    double lambdas[CDET_MCMCMC_MAX_ENVELOPE + 1];
+    uint64_t warmup_block_counts[CDET_MCMCMC_MAX_ENVELOPE + 1];
+    double vertices[CDET_MCMCMC_MAX_ENVELOPE][4];
+    cdet_mcmcmc_chain_result result;
+} cdet_mcmcmc_checkpoint;
+
+/* Writes / reads one checkpoint file, in the reference's text format (host
+ * only; no GPU needed). The writer goes through "<path>.tmp" and a rename,
+ * as the reference does. The reader applies the reference's label and size
+ * checks, with its messages. */
+int cdet_write_mcmcmc_checkpoint(const char* path, const cdet_mcmcmc_checkpoint* checkpoint);
+int cdet_read_mcmcmc_checkpoint(const char* path, cdet_mcmcmc_checkpoint* checkpoint);
+
+/* Run settings recorded in checkpoints (MCMCMCConfig fields). */
+typedef struct cdet_mcmcmc_run_info {
+    int32_t normalization_order; /* MCMCMC_NORMALIZATION_ORDER */
+    int32_t lambda_warmup_steps; /* MCMCMC_LAMBDA_WARMUP_STEPS */
+    int32_t production_steps;    /* MCMCMC_PRODUCTION_STEPS */
+} cdet_mcmcmc_run_info;
+
+/* Writes dir/chain_NNNNNN.chk for every chain (chain index = position in the
+ * batch), creating dir: the checkpoint the reference writes for the same
+ * chain state. seed_mode is "histogram" after cdet_mcmcmc_set_histogram. */
+int cdet_mcmcmc_save_checkpoints(const cdet_mcmcmc* m, const char* dir, const cdet_mcmcmc_run_info* info);
+
+/* Restores chains from dir/chain_NNNNNN.chk (MCMCMC_RESUME): each file must
+ * match the batch's settings and seed (the reference's "does not match"
+ * check) and all restored chains must have completed the same numbers of
+ * warmup and production steps, since the batch advances in lockstep. A chain
+ * without a file keeps its fresh state, unless require = 1 (the reference's
+ * MCMCMC_RESUME=require message). Returns the number of chains restored in
+ * *restored (may be null). */
+int cdet_mcmcmc_load_checkpoints(cdet_mcmcmc* m, const char* dir, const cdet_mcmcmc_run_info* info, int require,
+                                 int64_t* restored);
 
 /* The adaptation for a partial last warmup block (run_single_mcmcmc_chain,
  * :1050-1054): chains with pending counts adapt once more. */
@@ -229,6 +324,10 @@ int cdet_mcmcmc_end_warmup(cdet_mcmcmc* m);
 int cdet_mcmcmc_state(const cdet_mcmcmc* m, double* vertices, double* lambdas, uint64_t* rng_state);
 
 int cdet_mcmcmc_destroy(cdet_mcmcmc* m);
+
+/* Kernels of this library the batch's runs have launched so far (graph
+ * replays count every kernel node). */
+int cdet_mcmcmc_launch_count(const cdet_mcmcmc* m, int64_t* launches);
 
 /* Settings of the factorized histogram seed (MCMCMCConfig's histogram_*
  * fields, mcmcmc_sampler.h:92-95). */

@@ -315,6 +315,9 @@ class Reference:
                                          _DP, _UP]
         lib.ref_learn_histogram.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                             C.c_double, C.c_ulonglong, _DP, _DP, _DP, _DP]
+        lib.ref_mcmcmc_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _DP, C.c_int, C.c_int, C.c_double,
+                                       C.c_int, C.c_int, C.c_ulonglong, C.c_int, _DP, _DP, _DP, C.c_char_p,
+                                       C.c_ulonglong, C.c_char_p, _UP, _DP, _DP, _DP, _DP]
 
     def _check(self, rc):
         if rc != 0:
@@ -406,6 +409,29 @@ class Reference:
                                                  uniform_mix, pseudo_count, base_seed, _ptr(tau), _ptr(space),
                                                  _ptr(rep), C.byref(total)))
         return tau, space, rep, total.value
+
+    def mcmcmc_run(self, order_min, order_max, envelope, normalization_order, lambdas, warmup, adapt_interval,
+                   adapt_rate, production, chains, base_seed, histogram=None, checkpoint_dir="",
+                   checkpoint_interval=10_000_000, resume_mode="off"):
+        """run_mcmcmc_chains_parallel: per-chain results (u64 [chains][5 + 2(env+1)],
+        stats [chains][3 + env][5] as (count, mean hi, lo, m2 hi, lo)), final
+        lambdas, cross-chain stats [env+1][5] and ratios [env+1][2] (hi, lo)."""
+        e1 = envelope + 1
+        u64 = np.zeros((chains, 5 + 2 * e1), dtype=np.uint64)
+        stats = np.zeros((chains, 2 + e1, 5))
+        lam_out = np.zeros((chains, e1))
+        cross = np.zeros((e1, 5))
+        ratios = np.zeros((e1, 2))
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        bins, ht, hs, hr = (0, np.zeros(1), np.zeros(1), np.zeros(1)) if histogram is None else histogram
+        ht, hs, hr = (np.ascontiguousarray(x, dtype=np.float64) for x in (ht, hs, hr))
+        self._check(self.lib.ref_mcmcmc_run(order_min, order_max, envelope, normalization_order, _ptr(lam), warmup,
+                                            adapt_interval, adapt_rate, production, chains, base_seed, bins,
+                                            _ptr(ht), _ptr(hs), _ptr(hr), checkpoint_dir.encode(),
+                                            checkpoint_interval, resume_mode.encode(),
+                                            u64.ctypes.data_as(C.POINTER(C.c_ulonglong)), _ptr(stats),
+                                            _ptr(lam_out), _ptr(cross), _ptr(ratios)))
+        return dict(u64=u64, stats=stats, lambdas=lam_out, cross=cross, ratios=ratios)
 
     def chunk_workflow(self, directory: str, node_chunk_size: int, sitepair_chunk_size: int) -> None:
         """Runs every stage of the reference's chunked load-data workflow into

@@ -38,6 +38,9 @@
 //                             FactorizedHistogramSeed of given probabilities
 //                             (mcmcmc_seed.h:71-229), no checkpoints, recording every step
 //   ref_learn_histogram    -> learn_factorized_histogram_seed (mcmcmc_sampler.h:602-664)
+//   ref_mcmcmc_run         -> run_mcmcmc_chains_parallel (mcmcmc_sampler.h:1090-1150):
+//                             per-chain MCMCMCChainResult, the cross-chain summary,
+//                             optional checkpoint files and resume
 
 #include "cdet/cdet_integrand_evaluator.h"
 #include "cdet/chunked_load_data.h"
@@ -47,6 +50,8 @@
 
 #include <cstdint>
 #include <cstring>
+#include <cmath>
+#include <limits>
 #include <exception>
 #include <string>
 #include <thread>
@@ -390,6 +395,102 @@ int ref_mcmcmc_chain(int order_min, int order_max, int envelope_order, const dou
         }
         for (int order = 0; order <= envelope_order; ++order) lambdas_out[order] = state.lambdas[static_cast<std::size_t>(order)];
         for (int i = 0; i < 8; ++i) rng_out[i] = state.rng();
+    });
+}
+
+// long double as an exact (hi, lo) pair of doubles (exact for the x87 80-bit format)
+static void split_ld(long double x, double* out) {
+    const double hi = static_cast<double>(x);
+    out[0] = hi;
+    out[1] = std::isfinite(hi) ? static_cast<double>(x - static_cast<long double>(hi)) : 0.0;
+}
+
+static void put_stats(const RunningStatsLongDouble& st, double* out) {
+    out[0] = static_cast<double>(st.count);
+    split_ld(st.mean, out + 1);
+    split_ld(st.m2, out + 3);
+}
+
+// u64_out [chains][5 + 2 (env + 1)]: seed, warmup proposed / accepted,
+// production proposed / accepted, warmup then production chosen counts;
+// stats_out [chains][3 + env][5]: warmup retained fraction, production
+// retained fraction, order signal 0..env as (count, mean hi, lo, m2 hi, lo);
+// lambdas_out [chains][env + 1]; cross_out [env + 1][5]; ratios_out [env + 1][2]
+// (NaN outside order_min..order_max).
+int ref_mcmcmc_run(int order_min, int order_max, int envelope_order, int normalization_order,
+                   const double* lambdas_in, int warmup_steps, int adapt_interval, double adapt_rate,
+                   int production_steps, int chain_count, unsigned long long base_seed, int hist_tau_bins,
+                   const double* hist_tau, const double* hist_space, const double* hist_replica,
+                   const char* checkpoint_dir, unsigned long long checkpoint_interval, const char* resume_mode,
+                   unsigned long long* u64_out, double* stats_out, double* lambdas_out, double* cross_out,
+                   double* ratios_out) {
+    return guarded([&] {
+        MCMCMCConfig config;
+        config.order_min = order_min;
+        config.order_max = order_max;
+        config.envelope_order = envelope_order;
+        config.normalization_order = normalization_order;
+        config.lambdas.assign(lambdas_in, lambdas_in + envelope_order + 1);
+        config.lambda_warmup_steps = warmup_steps;
+        config.lambda_adapt_interval = adapt_interval;
+        config.lambda_adapt_rate = adapt_rate;
+        config.production_steps = production_steps;
+        config.chain_count = chain_count;
+        config.base_seed = base_seed;
+        config.seed_mode = "uniform";
+        std::shared_ptr<const MCMCMCSeedKernel> kernel;
+        if (hist_tau_bins > 0) {
+            FactorizedHistogramSeedSettings settings;
+            settings.tau_bins = hist_tau_bins;
+            settings.N1 = N1;
+            settings.N2 = N2;
+            const int sites = N1 * N2;
+            kernel = std::make_shared<FactorizedHistogramSeed>(
+                settings, std::vector<double>(hist_tau, hist_tau + hist_tau_bins * hist_tau_bins),
+                std::vector<double>(hist_space, hist_space + sites * sites),
+                std::vector<double>(hist_replica, hist_replica + 4));
+            config.seed_mode = "histogram";
+            config.histogram_learning_steps = 1;
+            config.histogram_tau_bins = hist_tau_bins;
+        } else {
+            kernel = make_uniform_mcmcmc_seed();
+        }
+        if (checkpoint_dir && checkpoint_dir[0]) {
+            config.checkpoint_enabled = true;
+            config.checkpoint_dir = checkpoint_dir;
+            config.checkpoint_interval_steps = checkpoint_interval;
+            config.resume_mode = resume_mode;
+        }
+        const MCMCMCSummary summary = run_mcmcmc_chains_parallel(config, kernel);
+        const int e1 = envelope_order + 1;
+        for (int c = 0; c < chain_count; ++c) {
+            const MCMCMCChainResult& r = summary.chains[static_cast<std::size_t>(c)];
+            unsigned long long* u = u64_out + static_cast<std::size_t>(c) * (5 + 2 * e1);
+            u[0] = r.seed;
+            u[1] = r.warmup_proposed_steps;
+            u[2] = r.warmup_accepted_steps;
+            u[3] = r.production_proposed_steps;
+            u[4] = r.production_accepted_steps;
+            for (int o = 0; o < e1; ++o) {
+                u[5 + o] = r.warmup_chosen_counts[static_cast<std::size_t>(o)];
+                u[5 + e1 + o] = r.production_chosen_counts[static_cast<std::size_t>(o)];
+            }
+            double* st = stats_out + static_cast<std::size_t>(c) * (2 + e1) * 5;
+            put_stats(r.warmup_retained_fraction_stats, st);
+            put_stats(r.production_retained_fraction_stats, st + 5);
+            for (int o = 0; o < e1; ++o) put_stats(r.order_signal_stats[static_cast<std::size_t>(o)], st + 10 + 5 * o);
+            for (int o = 0; o < e1; ++o)
+                lambdas_out[static_cast<std::size_t>(c) * e1 + o] = r.final_lambdas[static_cast<std::size_t>(o)];
+        }
+        for (int o = 0; o < e1; ++o) {
+            put_stats(summary.cross_chain_order_signal_stats[static_cast<std::size_t>(o)], cross_out + 5 * o);
+            const auto it = summary.ratios_to_normalization.find(o);
+            if (it == summary.ratios_to_normalization.end()) {
+                ratios_out[2 * o] = ratios_out[2 * o + 1] = std::numeric_limits<double>::quiet_NaN();
+            } else {
+                split_ld(it->second, ratios_out + 2 * o);
+            }
+        }
     });
 }
 

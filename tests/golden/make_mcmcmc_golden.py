@@ -18,12 +18,22 @@ FactorizedHistogramSeed (mcmcmc_seed.h:71-229) that
 learn_factorized_histogram_seed (mcmcmc_sampler.h:602-664) learns for the
 recorded settings; its row probabilities and total pair weight are stored too
 (<name>.hist.*).
+
+Finally, run_mcmcmc_chains_parallel (mcmcmc_sampler.h:1090-1150) itself runs
+the same histogram-seeded chains (normalization order = order_min) and its
+per-chain MCMCMCChainResult, cross-chain statistics and ratios are stored
+(<name>.run.*; long doubles as exact hi/lo pairs of the x86-64 80-bit values).
+A run of half the production length writes the reference's V1 checkpoint files
+into mcmcmc_checkpoints/<name>/, and a resumed run (MCMCMC_RESUME=require) to
+the full length is checked to reproduce the uninterrupted run.
 """
 from __future__ import annotations
 
 import json
 import os
+import shutil
 import sys
+import tempfile
 
 import numpy as np
 
@@ -94,7 +104,28 @@ def main():
         out[f"{name}.hist.seeds"] = np.array(hseeds, dtype=np.uint64)
         for key in ("chosen", "norms", "signal", "vertices", "lambdas", "rng"):
             out[f"{name}.hist.{key}"] = np.stack([p[key] for p in hper])
-        meta[name] = dict(run, histogram=HIST)
+        hist = (HIST["tau_bins"], tau, space, rep)
+        full = ref.mcmcmc_run(run["order_min"], run["order_max"], run["envelope"], run["order_min"],
+                              run["lambdas"], run["warmup"], run["adapt_interval"], run["adapt_rate"],
+                              run["production"], CHAINS, HIST["base_seed"], histogram=hist)
+        for key, val in full.items():
+            out[f"{name}.run.{key}"] = val
+        ck_dir = os.path.join(HERE, "mcmcmc_checkpoints", name)
+        shutil.rmtree(ck_dir, ignore_errors=True)
+        half = run["production"] // 2
+        ref.mcmcmc_run(run["order_min"], run["order_max"], run["envelope"], run["order_min"], run["lambdas"],
+                       run["warmup"], run["adapt_interval"], run["adapt_rate"], half, CHAINS, HIST["base_seed"],
+                       histogram=hist, checkpoint_dir=ck_dir)
+        with tempfile.TemporaryDirectory() as tmp:
+            resume_dir = os.path.join(tmp, name)
+            shutil.copytree(ck_dir, resume_dir)
+            resumed = ref.mcmcmc_run(run["order_min"], run["order_max"], run["envelope"], run["order_min"],
+                                     run["lambdas"], run["warmup"], run["adapt_interval"], run["adapt_rate"],
+                                     run["production"], CHAINS, HIST["base_seed"], histogram=hist,
+                                     checkpoint_dir=resume_dir, resume_mode="require")
+        for key in full:
+            assert np.array_equal(np.asarray(full[key]).view(np.uint64), np.asarray(resumed[key]).view(np.uint64)), key
+        meta[name] = dict(run, histogram=HIST, checkpoint_production=half, chains=CHAINS)
     np.savez_compressed(os.path.join(HERE, "mcmcmc_chains.npz"), **out)
     with open(os.path.join(HERE, "mcmcmc_chains.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)

@@ -143,3 +143,190 @@ def test_histogram_seed_density_error():
     chains.close()
     with pytest.raises(RuntimeError, match="UNIFORM_MIX must lie in"):
         learn_histogram(gpu, 1, 2, 4, 2, 4, 1.5, 0.0, 1)
+
+
+X87 = np.finfo(np.longdouble).nmant == 63  # the fixtures' long double format
+CKPT = os.path.join(GOLDEN, "mcmcmc_checkpoints")
+
+
+def _ld(pair):
+    return np.longdouble(pair[..., 0]) + np.longdouble(pair[..., 1])
+
+
+def _same_ld(a, b, rtol=1e-15):
+    """Exact where this host's long double is the fixtures' x87 format; else
+    to rtol (the reference's aarch64 build rounds its long doubles in quad)."""
+    a, b = np.asarray(a, dtype=np.longdouble), np.asarray(b, dtype=np.longdouble)
+    if X87:
+        return np.array_equal(a, b)
+    return bool(np.all(np.abs(a - b) <= rtol * np.maximum(np.abs(a), np.abs(b))))
+
+
+def _welford(values):
+    count, mean, m2 = 0, np.longdouble(0), np.longdouble(0)
+    for v in values:
+        count += 1
+        delta = np.longdouble(v) - mean
+        mean += delta / np.longdouble(count)
+        m2 += delta * (np.longdouble(v) - mean)
+    return count, mean, m2
+
+
+def _hist_chains(name, gpu):
+    run = RUNS[name]
+    chains = McmcmcChains(gpu, run["order_min"], run["order_max"], run["envelope"], GOLD[f"{name}.hist.seeds"],
+                          run["lambdas"], run["adapt_interval"], run["adapt_rate"])
+    chains.set_histogram(run["histogram"]["tau_bins"], GOLD[f"{name}.hist.tau"], GOLD[f"{name}.hist.space"],
+                         GOLD[f"{name}.hist.replica"])
+    return chains
+
+
+def _check_results(name, res):
+    run = RUNS[name]
+    env = run["envelope"]
+    u64, stats = GOLD[f"{name}.run.u64"], GOLD[f"{name}.run.stats"]
+    assert np.array_equal(res["seed"], u64[:, 0])
+    for k, field in enumerate(("warmup_proposed_steps", "warmup_accepted_steps", "production_proposed_steps",
+                               "production_accepted_steps")):
+        assert np.array_equal(res[field], u64[:, 1 + k]), field
+    assert np.array_equal(res["warmup_chosen_counts"][:, :env + 1], u64[:, 5:6 + env])
+    assert np.array_equal(res["production_chosen_counts"][:, :env + 1], u64[:, 6 + env:])
+    for k, field in enumerate(("warmup_retained_fraction_stats", "production_retained_fraction_stats")):
+        assert np.array_equal(res[field]["count"], stats[:, k, 0])
+        assert _same_ld(res[field]["mean"], _ld(stats[:, k, 1:3])), field
+        assert _same_ld(res[field]["m2"], _ld(stats[:, k, 3:5])), field
+    sig = res["order_signal_stats"][:, :env + 1]
+    assert np.array_equal(sig["count"], stats[:, 2:, 0])
+    assert _same_ld(sig["mean"], _ld(stats[:, 2:, 1:3]))
+    assert _same_ld(sig["m2"], _ld(stats[:, 2:, 3:5]))
+
+
+@pytest.mark.parametrize("name", sorted(RUNS))
+def test_chain_results_match_reference(name):
+    """MCMCMCChainResult of every chain, the cross-chain summary and the
+    absolute estimates, against run_mcmcmc_chains_parallel's, and bit for bit
+    against np.longdouble on this host from the chains' own order signals."""
+    run = RUNS[name]
+    omin, omax, env = run["order_min"], run["order_max"], run["envelope"]
+    params, tables, _ = load_case(name)
+    gpu = CdetIntegrand(params, tables)
+    chains = _hist_chains(name, gpu)
+    chains.run(run["warmup"], warmup=True)
+    chains.end_warmup()
+    p = chains.run(run["production"], warmup=False, record=True)
+    _, lams, _ = chains.state()
+    res = chains.results()
+    _check_results(name, res)
+    means = {}
+    for o in range(omin, omax + 1):
+        means[o] = []
+        for c in range(chains.chains):
+            count, mean, m2 = _welford(p["signal"][:, c, o] / lams[c, o])
+            st = res["order_signal_stats"][c, o]
+            assert st["count"] == count and st["mean"] == mean and st["m2"] == m2, (c, o)
+            means[o].append(mean)
+    cross, ratios = chains.summary(omin)
+    for o in range(omin, omax + 1):
+        count, mean, m2 = _welford(means[o])
+        assert cross[o]["count"] == count and cross[o]["mean"] == mean and cross[o]["m2"] == m2
+        assert ratios[o] == mean / _welford(means[omin])[1]
+        assert _same_ld(cross[o]["mean"], _ld(GOLD[f"{name}.run.cross"][o, 1:3]))
+        assert _same_ld(ratios[o], _ld(GOLD[f"{name}.run.ratios"][o]))
+    if omin <= 1:
+        est = chains.estimates(0.0625, 0.0)
+        c1 = cross[1]
+        se1 = np.sqrt(c1["m2"] / np.longdouble(c1["count"] - 1) / np.longdouble(c1["count"]))
+        const = np.longdouble(0.0625) / c1["mean"]
+        assert est["normalization"] == const
+        assert est["normalization_stderr"] == abs(np.longdouble(0.0625) * se1 / (c1["mean"] * c1["mean"]))
+        assert est["estimate"][1] == np.longdouble(0.0625)
+        for o in range(2, omax + 1):
+            assert est["estimate"][o] == const * cross[o]["mean"]
+    else:
+        with pytest.raises(RuntimeError, match="order 1"):
+            chains.estimates(0.0625)
+    assert chains.launch_count() > 0
+    chains.close()
+
+
+@pytest.mark.parametrize("name", sorted(RUNS))
+def test_checkpoints_match_reference(name, tmp_path):
+    """After half the production steps the chains' checkpoints hold what the
+    reference's do (exact state; long double statistics as above)."""
+    from cdet_gb300.mcmcmc import read_checkpoint
+    run = RUNS[name]
+    params, tables, _ = load_case(name)
+    gpu = CdetIntegrand(params, tables)
+    chains = _hist_chains(name, gpu)
+    half = run["checkpoint_production"]
+    chains.run_to(run["warmup"], half, run["order_min"], checkpoint_dir=str(tmp_path))
+    for fname in sorted(os.listdir(os.path.join(CKPT, name))):
+        ref = read_checkpoint(os.path.join(CKPT, name, fname))
+        got = read_checkpoint(str(tmp_path / fname))
+        for field in ("chain_index", "seed", "order_min", "order_max", "envelope_order", "normalization_order",
+                      "lambda_warmup_steps", "production_steps", "seed_mode"):
+            assert getattr(got, field) == getattr(ref, field), (fname, field)
+        for field in ("rng_state", "lambdas", "warmup_block_counts", "vertices"):
+            assert bytes(getattr(got, field)) == bytes(getattr(ref, field)), (fname, field)
+        if X87:
+            assert bytes(got.result) == bytes(ref.result)
+    chains.close()
+
+
+@pytest.mark.parametrize("name", sorted(RUNS))
+def test_resume_from_reference_checkpoints(name):
+    """Chains restored from the reference's checkpoint files and run to the
+    full length end where the reference's uninterrupted run ends."""
+    run = RUNS[name]
+    params, tables, _ = load_case(name)
+    gpu = CdetIntegrand(params, tables)
+    chains = _hist_chains(name, gpu)
+    n = chains.load_checkpoints(os.path.join(CKPT, name), run["order_min"], run["warmup"], run["production"],
+                                require=True)
+    assert n == chains.chains
+    chains.run_to(run["warmup"], run["production"], run["order_min"])
+    verts, lams, rng = chains.state()
+    assert np.array_equal(verts.view(np.uint64), GOLD[f"{name}.hist.vertices"].view(np.uint64))
+    for c in range(chains.chains):
+        assert np.array_equal(mt64_outputs(rng[c], 8), GOLD[f"{name}.hist.rng"][c]), c
+    assert np.array_equal(lams.view(np.uint64), GOLD[f"{name}.run.lambdas"].view(np.uint64))
+    _check_results(name, chains.results())
+    chains.close()
+
+
+def test_resume_checks():
+    run = RUNS["column_3x3"]
+    params, tables, _ = load_case("column_3x3")
+    gpu = CdetIntegrand(params, tables)
+    chains = _hist_chains("column_3x3", gpu)
+    with pytest.raises(RuntimeError, match="does not match current run settings"):
+        chains.load_checkpoints(os.path.join(CKPT, "column_3x3"), run["order_min"], run["warmup"] + 1,
+                                run["production"])
+    with pytest.raises(RuntimeError, match="MCMCMC_RESUME=require but checkpoint is missing for chain 0"):
+        chains.load_checkpoints(os.path.join(CKPT, "physical_2x2", "none"), run["order_min"], run["warmup"],
+                                run["production"], require=True)
+    chains.close()
+
+
+def test_graphs_follow_context_changes():
+    """The step graphs are dropped and captured again when the context's
+    buffers change between steps (a larger evaluation on the same context
+    reallocates its scratch); the chains still follow the reference's."""
+    name = "column_3x3"
+    run = RUNS[name]
+    params, tables, _ = load_case(name)
+    gpu = CdetIntegrand(params, tables)
+    seeds = GOLD[f"{name}.seeds"]
+    chains = McmcmcChains(gpu, run["order_min"], run["order_max"], run["envelope"], seeds, run["lambdas"],
+                          run["adapt_interval"], run["adapt_rate"])
+    first = chains.run(7, warmup=True, record=True)
+    rng = np.random.default_rng(3)
+    gpu.integrand_batch(rng.random((3000, 8, 4)), [8] * 3000)
+    rest = chains.run(run["warmup"] - 7, warmup=True, record=True)
+    chains.end_warmup()
+    p = chains.run(run["production"], warmup=False, record=True)
+    chosen = np.concatenate([first["chosen"], rest["chosen"], p["chosen"]]).T
+    assert np.array_equal(chosen, GOLD[f"{name}.chosen"])
+    verts, _, _ = chains.state()
+    assert np.array_equal(verts.view(np.uint64), GOLD[f"{name}.vertices"].view(np.uint64))
+    chains.close()
