@@ -386,13 +386,15 @@ def run_gpu(args):
 
 
 def run_mcmcmc(args):
-    """--mcmcmc: throughput of the device MCMCMC chains (a separate line, not
-    the headline): chain-steps/s of run_mcmcmc_step with the uniform seed on
-    the 6x6 / U=2 / beta=6 / half-lattice / degree-96 set, envelope 9, orders
-    1..8, with the oracle's single-threaded chain beside it."""
+    """--mcmcmc: the device-resident MCMCMC run (a separate line, not the
+    headline): 6x6 / U=2 / beta=6 / half lattice / degree 96, orders 1..8
+    (envelope 9), --chains chains (128 by default) on a factorized histogram
+    seed learned on the GPU, lambda adaptation during warmup, then timed
+    production steps (each updating every chain's long-double statistics), for
+    both assemblies; the oracle's single-threaded histogram chain beside it."""
     import torch
     from cdet_gb300.integrand import CdetIntegrand
-    from cdet_gb300.mcmcmc import STREAM_TAG, McmcmcChains
+    from cdet_gb300.mcmcmc import STREAM_TAG, McmcmcChains, learn_histogram
     from cdet_gb300.params import CdetParams, half_lattice_mask
     from cdet_gb300.synthetic import derive_seed
     from cdet_gb300.tables import build_tables
@@ -401,36 +403,55 @@ def run_mcmcmc(args):
     env, omin, omax = 9, 1, 8
     lambdas = [0.0] + [1.0] * 8 + [0.0]
     chains_n = args.chains
+    steps = args.mcmcmc_steps
+    warmup = max(args.warmup, 100)
+    hist = dict(learning_steps=64, tau_bins=16, uniform_mix=0.05, pseudo_count=0.0)
     tables = build_tables(params, device="cuda")
     gpu = CdetIntegrand(params, tables)
-    out = {"metric": "MCMCMC chain-steps/s (uniform seed, envelope 9, orders 1..8)", "unit": "chain-steps/s",
-           "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "config": {"workload": "6x6 Hubbard U=2 beta=6 half lattice, degree 96, envelope 9, orders 1..8",
-                      "chains": chains_n}, "data": "synthetic (seeded chains, tables from the in-tree precompute)"}
+    out = {"metric": "MCMCMC chain-steps/s (histogram seed, envelope 9, orders 1..8)", "unit": "chain-steps/s",
+           "higher_is_better": True, "n_gpus": 1, "steps": steps, "warmup": warmup,
+           "config": {"workload": "6x6 Hubbard U=2 beta=6 half lattice, degree 96, envelope 9, orders 1..8, "
+                                  "factorized histogram seed, lambda adaptation every 50 warmup steps",
+                      "chains": chains_n, "histogram": hist},
+           "data": "synthetic (seeded chains, tables from the in-tree precompute)"}
     for path in ("fp64", "split"):
         gpu.set_assembly(path)
-        seeds = [derive_seed(20261203, STREAM_TAG, i) for i in range(chains_n)]
-        chains = McmcmcChains(gpu, omin, omax, env, seeds, lambdas, adapt_interval=1000)
-        chains.run(args.warmup, warmup=True)
-        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        chains.run(args.steps, warmup=False)
+        tau, space, rep, _ = learn_histogram(gpu, omin, omax, env, hist["learning_steps"], hist["tau_bins"],
+                                             hist["uniform_mix"], hist["pseudo_count"], 20261203)
+        learn_s = time.perf_counter() - t0
+        seeds = [derive_seed(20261203, STREAM_TAG, i) for i in range(chains_n)]
+        chains = McmcmcChains(gpu, omin, omax, env, seeds, lambdas, adapt_interval=50)
+        chains.set_histogram(hist["tau_bins"], tau, space, rep)
+        chains.run(warmup, warmup=True)
+        chains.end_warmup()
         torch.cuda.synchronize()
+        l0, g0 = chains.launch_count()
+        t0 = time.perf_counter()
+        chains.run(steps, warmup=False)
         dt = time.perf_counter() - t0
-        out[path] = {"value": chains_n * args.steps / dt, "ms_per_step": 1e3 * dt / args.steps}
+        l1, g1 = chains.launch_count()
+        out[path] = {"value": chains_n * steps / dt, "ms_per_step": 1e3 * dt / steps,
+                     "hours_for_1e5_steps": dt / steps * 1e5 / 3600, "histogram_learning_s": learn_s,
+                     "gpu_launches": l1 - l0, "graph_steps": g1 - g0}
         chains.close()
     out["value"] = out["split"]["value"]
+    out["gpu_launches"] = out["split"]["gpu_launches"]
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         from bindings import Oracle
         host = {k: {kk: vv.cpu().numpy() for kk, vv in t.items()} for k, t in tables.items()}
         orc = Oracle(params.runtime_scalars(), host)
+        tau, space, rep, _ = orc.learn_histogram(omin, omax, env, 4, hist["tau_bins"], hist["uniform_mix"],
+                                                 hist["pseudo_count"], 20261203)
         t0 = time.perf_counter()
         n = 6
-        orc.mcmcmc_chain(omin, omax, env, lambdas, 0, 1000, 0.25, n, derive_seed(20261203, STREAM_TAG, 0))
+        orc.mcmcmc_chain(omin, omax, env, lambdas, 0, 1000, 0.25, n, derive_seed(20261203, STREAM_TAG, 0),
+                         histogram=(hist["tau_bins"], tau, space, rep))
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": n / dt, "unit": "chain-steps/s", "cores": 1, "kind": "port",
-                               "sample": f"one chain, {n} production steps (C restatement of the reference chain)"}
+                               "sample": f"one histogram-seeded chain, {n} production steps (C restatement of "
+                                         "the reference chain)"}
     print(json.dumps(out))
 
 
@@ -450,7 +471,8 @@ def main():
                     help="both: time the FP64 form and the split form, report the split form")
     ap.add_argument("--mcmcmc", action="store_true",
                     help="time the device MCMCMC chains instead (a separate line, not the headline)")
-    ap.add_argument("--chains", type=int, default=8192, help="chains for --mcmcmc")
+    ap.add_argument("--chains", type=int, default=128, help="chains for --mcmcmc")
+    ap.add_argument("--mcmcmc-steps", type=int, default=2000, help="timed production steps for --mcmcmc")
     args = ap.parse_args()
     global PRESET, BATCH
     PRESET, BATCH = args.preset, args.batch

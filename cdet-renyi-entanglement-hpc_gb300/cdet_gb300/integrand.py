@@ -58,6 +58,7 @@ class CdetIntegrand:
 
     def __init__(self, params: CdetParams, tables: Optional[Dict[str, Dict]], device: int = 0):
         self.params = params
+        self._assembly = "fp64"
         self.scalars = params.runtime_scalars()
         self._lib = L.load()
         self._ctx = C.c_void_p()
@@ -190,11 +191,26 @@ class CdetIntegrand:
     def last_launch_count(self) -> int:
         return int(self._lib.cdet_last_launch_count(self._ctx))
 
+    def set_all_subsets_form(self, form: str) -> None:
+        """'auto', 'lane' or 'warp': the work layout of the all-subsets CDet
+        recursion (same values bit for bit, different speed)."""
+        code = {"auto": 0, "lane": 1, "warp": 2}[form]
+        L.check(self._lib.cdet_set_all_subsets_form(self._ctx, code))
+
+    def all_subsets_form_tuned(self, max_order: int, batch: int) -> str:
+        """The all-subsets form the autotuner kept for this order and batch
+        size class under the current assembly ('auto' before a measurement)."""
+        form = C.c_int()
+        L.check(self._lib.cdet_all_subsets_form_tuned(self._ctx, int(max_order), int(self._assembly == "split"),
+                                                      int(batch), C.byref(form)))
+        return {0: "auto", 1: "lane", 2: "warp"}[form.value]
+
     def set_assembly(self, mode: str) -> None:
         """"fp64": the reference's Clenshaw in FP64, bit-identical (default);
         "split": batched split-bf16 tcgen05 assembly, FP64-level accuracy."""
         code = {"fp64": L.ASSEMBLY_FP64, "split": L.ASSEMBLY_SPLIT_BF16}[mode]
         L.check(self._lib.cdet_set_assembly(self._ctx, code))
+        self._assembly = mode
 
     def prepare_split(self) -> None:
         """Slice the tables for the split assembly now (device memory)."""

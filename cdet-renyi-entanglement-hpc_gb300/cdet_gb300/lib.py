@@ -34,7 +34,7 @@ EXPORTED = (
     "cdet_mcmcmc_create", "cdet_mcmcmc_run", "cdet_mcmcmc_end_warmup", "cdet_mcmcmc_state",
     "cdet_mcmcmc_destroy", "cdet_mcmcmc_set_histogram", "cdet_mcmcmc_learn_histogram", "cdet_mcmcmc_result",
     "cdet_mcmcmc_summary", "cdet_mcmcmc_estimates", "cdet_write_mcmcmc_checkpoint", "cdet_read_mcmcmc_checkpoint",
-    "cdet_mcmcmc_save_checkpoints", "cdet_mcmcmc_load_checkpoints", "cdet_mcmcmc_launch_count", "cdet_load_chunks",
+    "cdet_mcmcmc_save_checkpoints", "cdet_mcmcmc_load_checkpoints", "cdet_mcmcmc_launch_count", "cdet_set_all_subsets_form", "cdet_all_subsets_form_tuned", "cdet_load_chunks",
 )
 
 ASSEMBLY_FP64 = 0
@@ -149,7 +149,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_mcmcmc_save_checkpoints.argtypes = [vp, C.c_char_p, C.POINTER(RunInfo)]
     lib.cdet_mcmcmc_load_checkpoints.argtypes = [vp, C.c_char_p, C.POINTER(RunInfo), C.c_int,
                                                  C.POINTER(C.c_int64)]
-    lib.cdet_mcmcmc_launch_count.argtypes = [vp, C.POINTER(C.c_int64)]
+    lib.cdet_set_all_subsets_form.argtypes = [vp, i32]
+    lib.cdet_all_subsets_form_tuned.argtypes = [vp, i32, i32, i64, C.POINTER(C.c_int)]
+    lib.cdet_mcmcmc_launch_count.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.cdet_mcmcmc_learn_histogram.argtypes = [vp, C.POINTER(McmcmcConfig), C.POINTER(HistogramConfig), C.c_uint64,
                                                 _DP, _DP, _DP, _DP]
     lib.cdet_load_chunks.argtypes = [vp, C.c_char_p, _DP]

@@ -119,10 +119,11 @@ class McmcmcChains:
                                                        int(require), C.byref(restored)))
         return restored.value
 
-    def launch_count(self) -> int:
-        n = C.c_int64()
-        L.check(self._lib.cdet_mcmcmc_launch_count(self._h, C.byref(n)))
-        return n.value
+    def launch_count(self) -> tuple:
+        """(kernels launched by the runs so far, steps replayed from a CUDA graph)."""
+        n, g = C.c_int64(), C.c_int64()
+        L.check(self._lib.cdet_mcmcmc_launch_count(self._h, C.byref(n), C.byref(g)))
+        return n.value, g.value
 
     def run_to(self, lambda_warmup_steps: int, production_steps: int, normalization_order: int,
                checkpoint_dir: Optional[str] = None, checkpoint_interval: int = 0) -> None:

@@ -209,6 +209,7 @@ int build_problem(cdet_context* ctx, const double* vertices, const int32_t* orde
     p->max_order = max_order;
     p->all_subsets = all_subsets;
     p->fused_cdet = ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16 ? 1 : 0;
+    p->all_subsets_form = ctx->all_subsets_form;
     for (int set = 0; set < 2; ++set) {
         const int r = set == 0 ? 2 : 1;
         for (int n = 0; n <= cdet::kMaxOrder; ++n) {
@@ -291,6 +292,64 @@ int build_split_plan(cdet_context* ctx, cdet::SplitPlan* plan) {
     return CDET_OK;
 }
 
+// Times the whole evaluation with each all-subsets form (twice each, so that
+// neither pays the kernels' first-launch costs alone) and returns the faster.
+// Both forms write the same values, so the evaluation's outputs stand.
+int tune_all_subsets_form(cdet_context* ctx, cdet::Problem p, const cdet::Scratch& w, cudaStream_t stream,
+                          int* best) {
+    int rc = CDET_OK;
+    if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16) {
+        // the split path needs its plan and scratch first: run it once in the automatic form
+        cdet::SplitPlan plan;
+        rc = build_split_plan(ctx, &plan);
+        if (rc != CDET_OK) return rc;
+        const size_t need = cdet::split_scratch_bytes(p.batch, p.max_order, plan.nblocks);
+        if (need > ctx->split_scratch_bytes) {
+            cudaDeviceSynchronize();
+            if (ctx->split_scratch) cudaFree(ctx->split_scratch);
+            ctx->split_scratch = nullptr;
+            ctx->split_scratch_bytes = 0;
+            const cudaError_t err = cudaMalloc(&ctx->split_scratch, need);
+            ++ctx->generation;
+            if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(split scratch)");
+            ctx->split_scratch_bytes = need;
+        }
+    }
+    auto launch = [&](int form) -> cudaError_t {
+        p.all_subsets_form = form;
+        if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16) {
+            cdet::SplitPlan plan;
+            if (build_split_plan(ctx, &plan) != CDET_OK) return cudaErrorUnknown;
+            cudaError_t err = cdet::launch_split_assembly(p, w, plan, ctx->split_scratch, ctx->split_scratch_bytes,
+                                                          ctx->sm_count, &ctx->split_error, stream, nullptr);
+            if (err != cudaSuccess) return err;
+            return cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, nullptr, false);
+        }
+        return cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, nullptr);
+    };
+    cudaEvent_t ev[3];
+    for (cudaEvent_t& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+    float ms[2] = {0.0f, 0.0f};
+    cudaError_t err = cudaSuccess;
+    for (int round = 0; round < 2 && err == cudaSuccess; ++round) {
+        err = cudaEventRecord(ev[0], stream);
+        if (err == cudaSuccess) err = launch(cdet::kFormLane);
+        if (err == cudaSuccess) err = cudaEventRecord(ev[1], stream);
+        if (err == cudaSuccess) err = launch(cdet::kFormWarp);
+        if (err == cudaSuccess) err = cudaEventRecord(ev[2], stream);
+        if (err == cudaSuccess) err = cudaEventSynchronize(ev[2]);
+        if (err == cudaSuccess && round == 1) {
+            err = cudaEventElapsedTime(&ms[0], ev[0], ev[1]);
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
+        }
+    }
+    for (cudaEvent_t& e : ev) cudaEventDestroy(e);
+    if (err != cudaSuccess) return cuda_fail(err, "timing the all-subsets forms");
+    *best = ms[1] < ms[0] ? cdet::kFormWarp : cdet::kFormLane;
+    return CDET_OK;
+}
+
 int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
         int max_order, int all_subsets, double* values, int32_t* status, cudaStream_t stream,
         bool assembly_only = false) {
@@ -324,6 +383,26 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         events = &ctx->pending.back();
     }
     int launches = 3;
+    // The all-subsets CDet has two work layouts with identical values; under
+    // CDET_FORM_AUTO the first evaluation of each (order, fused, batch size
+    // class) outside a stream capture times both and keeps the faster.
+    if (p.all_subsets && ctx->all_subsets_form == CDET_FORM_AUTO && !assembly_only && !ctx->profiling &&
+        max_order <= cdet::kAllWarpMaxOrder) {
+        int log2b = 0;
+        while ((int64_t{2} << log2b) <= batch) ++log2b;
+        const auto key = std::make_tuple(max_order, p.fused_cdet, log2b);
+        auto it = ctx->form_tuned.find(key);
+        if (it == ctx->form_tuned.end()) {
+            cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(stream, &capture) == cudaSuccess && capture == cudaStreamCaptureStatusNone) {
+                int best = cdet::kFormAuto;
+                rc = tune_all_subsets_form(ctx, p, w, stream, &best);
+                if (rc != CDET_OK) return rc;
+                it = ctx->form_tuned.emplace(key, best).first;
+            }
+        }
+        if (it != ctx->form_tuned.end()) p.all_subsets_form = it->second;
+    }
     if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16) {
         cdet::SplitPlan plan;
         rc = build_split_plan(ctx, &plan);
@@ -620,6 +699,26 @@ int cdet_counters(const cdet_context* ctx, uint64_t* integrand_calls, uint64_t* 
 }
 
 int cdet_last_launch_count(const cdet_context* ctx) { return ctx ? ctx->last_launches : 0; }
+
+int cdet_all_subsets_form_tuned(const cdet_context* ctx, int max_order, int fused, int64_t batch, int* form) {
+    if (!ctx || !form) return fail(CDET_ERR_INVALID, "null argument");
+    int log2b = 0;
+    while ((int64_t{2} << log2b) <= batch) ++log2b;
+    const auto it = ctx->form_tuned.find(std::make_tuple(max_order, fused ? 1 : 0, log2b));
+    *form = it == ctx->form_tuned.end() ? CDET_FORM_AUTO : it->second;
+    return CDET_OK;
+}
+
+int cdet_set_all_subsets_form(cdet_context* ctx, int form) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (form != CDET_FORM_AUTO && form != CDET_FORM_LANE && form != CDET_FORM_WARP)
+        return fail(CDET_ERR_INVALID, "unknown all-subsets form");
+    static_assert(CDET_FORM_AUTO == cdet::kFormAuto && CDET_FORM_LANE == cdet::kFormLane &&
+                      CDET_FORM_WARP == cdet::kFormWarp,
+                  "form codes");
+    ctx->all_subsets_form = form;
+    return CDET_OK;
+}
 
 int cdet_set_assembly(cdet_context* ctx, int mode) {
     if (!ctx) return fail(CDET_ERR_INVALID, "null context");

@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -52,6 +53,9 @@ struct cdet_context {
     int last_launches = 0;
     // split assembly
     int assembly = CDET_ASSEMBLY_FP64;
+    int all_subsets_form = CDET_FORM_AUTO;
+    // all-subsets CDet form measured fastest, per (order, fused, floor(log2 batch))
+    std::map<std::tuple<int, int, int>, int> form_tuned;
     std::map<std::pair<const double*, size_t>, capi::SlicedBranch> sliced;  // (coeffs, blocks) -> slices
     void* split_scratch = nullptr;
     size_t split_scratch_bytes = 0;

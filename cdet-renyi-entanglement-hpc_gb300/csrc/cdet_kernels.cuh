@@ -48,6 +48,10 @@ struct Scratch {
     size_t ws_warps;    // warps the global workspace holds
 };
 
+// all-subsets CDet work layouts, the values of the C ABI's CDET_FORM_*
+constexpr int kFormAuto = 0, kFormLane = 1, kFormWarp = 2;
+constexpr int kAllWarpMaxOrder = 11;  // the warp form holds a and dp of one set in shared memory
+
 struct Problem {
     Scalars s;
     TableDev up[2], down[2];  // set 0 = twisted (r=2), set 1 = ordinary (r=1)
@@ -59,6 +63,7 @@ struct Problem {
     int all_subsets;          // 0: one value per configuration; 1: 2^max_order values
     int fused_cdet;           // 1: CDet pair updates as FMAs (split assembly); 0: the reference's
                               // separately rounded multiply, subtract and add
+    int all_subsets_form;     // kFormAuto / kFormLane / kFormWarp (CDET_FORM_*, cdet_set_all_subsets_form)
     DDPair pref_dd[2][kMaxOrder + 1];   // cdet_order_prefactor<DoubleDouble>, [set][order]
     double pref_ld[2][kMaxOrder + 1];   // cdet_order_prefactor<double> (host long double)
     double* values;
@@ -134,7 +139,12 @@ struct McmcmcStepArgs {
 };
 cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* seeds, uint64_t* mt, int32_t* mt_index,
                                double* vertices, cudaStream_t stream);
+// Launches the step: one kernel for the uniform seed kernel, two (the
+// conditional probabilities, then the step) for the histogram seed kernel.
 cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream);
+// Smallest all-subsets batch for which the FP64 CDet runs one lane per
+// configuration; smaller batches run one warp per configuration.
+int all_subsets_lane_form_min_batch(int sm_count);
 // *row = (*row + 1) % rows, after a step (one thread)
 cudaError_t launch_mcmcmc_advance_row(int64_t* row, int64_t rows, cudaStream_t stream);
 

@@ -129,48 +129,62 @@ __device__ void hist_child(const McmcmcStepArgs& a, const Mt64& g, const double*
 }
 
 // compute_conditional_generation_probabilities_typed_into<double>
-// (mcmcmc_sampler.h:252-335). The reference tabulates the remaining child
-// densities cd[gm][c] by peeling the lowest bit of gm; here each one is formed
-// on the spot with the same subtractions in the same order (the highest bit of
-// gm first), each result clamped as the table's is, so only the 2^n
-// probabilities are stored. false: a seed density is negative or not finite.
-__device__ bool conditional_probabilities(const McmcmcStepArgs& a, const double* v, int n, double* prob) {
-    double sd[kMcmcmcMaxEnvelope * kMcmcmcMaxEnvelope];
-    double cd0[kMcmcmcMaxEnvelope];
-    for (int c = 0; c < n; ++c)
-        for (int p = 0; p < n; ++p) {
-            double d = 0.0;
-            if (c != p) {
-                d = hist_density(a, v + 4 * c, v + 4 * p);
-                if (d < 0.0 || !isfinite(d)) return false;
-            }
-            sd[c * n + p] = d;
+// (mcmcmc_sampler.h:252-335), one warp per chain. The reference tabulates the
+// remaining child densities cd[gm][c] by peeling the lowest bit of gm; here
+// each one is formed on the spot from the row sum with the same subtractions
+// in the same order (the highest bit of gm first), each result clamped as the
+// table's is, so only the 2^n probabilities are stored. The subsets of one
+// popcount level depend only on the level below, so the lanes share each
+// level; every subset's sum runs on one lane in the reference's order, so the
+// values are the reference's bit for bit. sd: this warp's n x n densities in
+// shared memory. false (on every lane): a density is negative or not finite.
+__device__ bool conditional_probabilities_warp(const McmcmcStepArgs& a, const double* v, int n, double* prob,
+                                               double* sd, double* cd0, int lane) {
+    bool bad = false;
+    for (int idx = lane; idx < n * n; idx += 32) {
+        const int c = idx / n, p = idx - (idx / n) * n;
+        double d = 0.0;
+        if (c != p) {
+            d = hist_density(a, v + 4 * c, v + 4 * p);
+            bad |= d < 0.0 || !isfinite(d);
         }
-    for (int c = 0; c < n; ++c) {
+        sd[idx] = d;
+    }
+    if (__any_sync(0xffffffffu, bad)) return false;
+    __syncwarp();
+    if (lane < n) {
         double sum = 0.0;
-        for (int p = 0; p < n; ++p) sum = dadd(sum, sd[c * n + p]);
-        cd0[c] = sum;
+        for (int p = 0; p < n; ++p) sum = dadd(sum, sd[lane * n + p]);
+        cd0[lane] = sum;
     }
     const uint64_t full = (uint64_t{1} << n) - 1;
-    prob[0] = 1.0;
-    for (uint64_t gm = 1; gm < full; ++gm) {
-        const int gc = __popcll(gm), pc = n - gc;
-        double sum = 0.0;
-        for (int c = 0; c < n; ++c) {
-            const uint64_t cb = uint64_t{1} << c;
-            if (!(gm & cb)) continue;
-            double d = cd0[c];
-            for (uint64_t rest = gm; rest;) {
-                const int b = 63 - __clzll(static_cast<long long>(rest));
-                rest ^= uint64_t{1} << b;
-                d = dsub(d, sd[c * n + b]);
-                if (d < 0.0 && d > -1.0e-12) d = 0.0;
-            }
-            sum = dadd(sum, dmul(prob[gm ^ cb], d));
-        }
-        prob[gm] = ddiv(sum, dmul(static_cast<double>(gc), static_cast<double>(pc)));
+    if (lane == 0) {
+        prob[0] = 1.0;
+        prob[full] = 0.0;
     }
-    prob[full] = 0.0;
+    __syncwarp();
+    for (int level = 1; level < n; ++level) {
+        const int pc = n - level;
+        const double denom = dmul(static_cast<double>(level), static_cast<double>(pc));
+        for (uint64_t gm = 1 + static_cast<uint64_t>(lane); gm < full; gm += 32) {
+            if (__popcll(gm) != level) continue;
+            double sum = 0.0;
+            for (int c = 0; c < n; ++c) {
+                const uint64_t cb = uint64_t{1} << c;
+                if (!(gm & cb)) continue;
+                double d = cd0[c];
+                for (uint64_t rest = gm; rest;) {
+                    const int b = 63 - __clzll(static_cast<long long>(rest));
+                    rest ^= uint64_t{1} << b;
+                    d = dsub(d, sd[c * n + b]);
+                    if (d < 0.0 && d > -1.0e-12) d = 0.0;
+                }
+                sum = dadd(sum, dmul(prob[gm ^ cb], d));
+            }
+            prob[gm] = ddiv(sum, denom);
+        }
+        __syncwarp();  // the next level reads this one
+    }
     return true;
 }
 
@@ -191,17 +205,10 @@ __global__ void mcmcmc_init(int64_t chains, int envelope, const uint64_t* __rest
     for (int k = 0; k < envelope * 4; ++k) v[k] = g.canonical();
 }
 
+// The serial part of run_mcmcmc_step (:540-577) for chain c, after the seed
+// kernel's conditional probabilities (cprob; null for the uniform kernel).
 template <bool Hist>
-__global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ McmcmcStepArgs a) {
-    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c >= a.chains) return;
-    const int64_t row = a.ring_row ? *a.ring_row : 0;
-    if (a.chosen_out) a.chosen_out[row * a.chains + c] = 0;  // 0: no step (a failed chain)
-    if (a.error[c]) return;  // a chain that failed stays where it stopped
-    if (a.integrand_status[c] & kStatusNonFinite) {
-        a.error[c] = 1;  // "Error (all-subset integrand): Value is not finite"
-        return;
-    }
+__device__ void finish_step(const McmcmcStepArgs& a, int64_t c, int64_t row, const double* cprob) {
     const int env = a.envelope;
     const uint64_t subsets = uint64_t{1} << env;
     const double* values = a.values + c * static_cast<int64_t>(subsets);
@@ -209,14 +216,6 @@ __global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ Mcmcm
     const Mt64 g{a.mt + c, a.chains, a.mt_index + c};
     const double* v = a.vertices + c * env * 4;
     const uint64_t full = subsets - 1;
-    double* cprob = nullptr;
-    if constexpr (Hist) {
-        cprob = a.cprob + c * static_cast<int64_t>(subsets);
-        if (!conditional_probabilities(a, v, env, cprob)) {
-            a.error[c] = 3;  // "MCMCMC seed density is negative or non-finite"
-            return;
-        }
-    }
     // flux = lambda * value * conditional probability of the complement
     // (1 for the uniform kernel)
     auto flux_of = [&](uint64_t mask, int o) {
@@ -288,6 +287,41 @@ __global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ Mcmcm
     if (a.warmup) ++a.counts[c * (env + 1) + order];
 }
 
+// The step, one thread per chain (after mcmcmc_hist_probs for the histogram
+// seed kernel).
+template <bool Hist>
+__global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ McmcmcStepArgs a) {
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= a.chains) return;
+    const int64_t row = a.ring_row ? *a.ring_row : 0;
+    if (a.chosen_out) a.chosen_out[row * a.chains + c] = 0;  // 0: no step (a failed chain)
+    if (a.error[c]) return;  // a chain that failed stays where it stopped
+    if (a.integrand_status[c] & kStatusNonFinite) {
+        a.error[c] = 1;  // "Error (all-subset integrand): Value is not finite"
+        return;
+    }
+    finish_step<Hist>(a, c, row, Hist ? a.cprob + c * (int64_t{1} << a.envelope) : nullptr);
+}
+
+// The histogram seed kernel's conditional generation probabilities, one warp
+// per chain, into a.cprob; a negative or non-finite seed density stops the
+// chain (error 3), which the step kernel then skips.
+constexpr int kHistWarps = 4;
+__global__ void __launch_bounds__(kHistWarps * 32) mcmcmc_hist_probs(const __grid_constant__ McmcmcStepArgs a) {
+    __shared__ double sd_all[kHistWarps][kMcmcmcMaxEnvelope * kMcmcmcMaxEnvelope];
+    __shared__ double cd0_all[kHistWarps][kMcmcmcMaxEnvelope];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * kHistWarps + warp;
+    if (c >= a.chains) return;  // whole warps
+    // both read the same value on every lane; the step kernel reports a non-finite integrand
+    if (a.error[c] || (a.integrand_status[c] & kStatusNonFinite)) return;
+    const int env = a.envelope;
+    double* cprob = a.cprob + c * (int64_t{1} << env);
+    const double* v = a.vertices + c * env * 4;
+    if (!conditional_probabilities_warp(a, v, env, cprob, sd_all[warp], cd0_all[warp], lane) && lane == 0)
+        a.error[c] = 3;  // "MCMCMC seed density is negative or non-finite"
+}
+
 __global__ void mcmcmc_advance_row(int64_t* row, int64_t rows) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *row = (*row + 1) % rows;
 }
@@ -310,10 +344,15 @@ cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* see
 cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream) {
     if (args.chains <= 0) return cudaSuccess;
     const unsigned grid = static_cast<unsigned>((args.chains + 127) / 128);
-    if (args.tau_bins > 0)
+    if (args.tau_bins > 0) {
+        mcmcmc_hist_probs<<<static_cast<unsigned>((args.chains + kHistWarps - 1) / kHistWarps), kHistWarps * 32, 0,
+                            stream>>>(args);
+        const cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
         mcmcmc_step<true><<<grid, 128, 0, stream>>>(args);
-    else
+    } else {
         mcmcmc_step<false><<<grid, 128, 0, stream>>>(args);
+    }
     return cudaGetLastError();
 }
 

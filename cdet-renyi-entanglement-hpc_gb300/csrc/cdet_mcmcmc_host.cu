@@ -81,6 +81,7 @@ struct cdet_mcmcmc {
     bool use_graphs = true;
     int launches_per_step = 0;
     int64_t kernel_launches = 0;
+    int64_t graph_steps = 0;
 };
 
 namespace {
@@ -186,7 +187,7 @@ int enqueue_step(cdet_mcmcmc* m, int warmup, int* launches) {
     cudaError_t err = cdet::launch_mcmcmc_step(step_args(m, warmup), m->stream);
     if (err == cudaSuccess) err = cdet::launch_mcmcmc_advance_row(m->d_row, ring_rows(m), m->stream);
     if (err != cudaSuccess) return cuda_fail(err, "MCMCMC step launch");
-    *launches = m->ctx->last_launches + 2;
+    *launches = m->ctx->last_launches + (m->tau_bins > 0 ? 3 : 2);
     return CDET_OK;
 }
 
@@ -234,6 +235,7 @@ int launch_step(cdet_mcmcmc* m, int warmup) {
         const cudaError_t err = cudaGraphLaunch(g, m->stream);
         if (err != cudaSuccess) return cuda_fail(err, "MCMCMC step graph launch");
         m->kernel_launches += m->launches_per_step;
+        ++m->graph_steps;
     } else {
         int launches = 0;
         const int rc = enqueue_step(m, warmup, &launches);
@@ -547,9 +549,10 @@ int cdet_mcmcmc_destroy(cdet_mcmcmc* m) {
     return CDET_OK;
 }
 
-int cdet_mcmcmc_launch_count(const cdet_mcmcmc* m, int64_t* launches) {
-    if (!m || !launches) return fail(CDET_ERR_INVALID, "null argument");
-    *launches = m->kernel_launches;
+int cdet_mcmcmc_launch_count(const cdet_mcmcmc* m, int64_t* launches, int64_t* graph_steps) {
+    if (!m) return fail(CDET_ERR_INVALID, "null argument");
+    if (launches) *launches = m->kernel_launches;
+    if (graph_steps) *graph_steps = m->graph_steps;
     return CDET_OK;
 }
 

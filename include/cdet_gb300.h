@@ -326,8 +326,9 @@ int cdet_mcmcmc_state(const cdet_mcmcmc* m, double* vertices, double* lambdas, u
 int cdet_mcmcmc_destroy(cdet_mcmcmc* m);
 
 /* Kernels of this library the batch's runs have launched so far (graph
- * replays count every kernel node). */
-int cdet_mcmcmc_launch_count(const cdet_mcmcmc* m, int64_t* launches);
+ * replays count every kernel node), and how many steps were graph replays
+ * (either may be null). */
+int cdet_mcmcmc_launch_count(const cdet_mcmcmc* m, int64_t* launches, int64_t* graph_steps);
 
 /* Settings of the factorized histogram seed (MCMCMCConfig's histogram_*
  * fields, mcmcmc_sampler.h:92-95). */
@@ -385,6 +386,24 @@ enum cdet_assembly_mode {
  * INTEGRAND_REAL precision switch (cdet_integrand_evaluator.h:431-465) with
  * the two GB300 assembly forms above. */
 int cdet_set_assembly(cdet_context* ctx, int mode);
+
+/* Work layout of the all-subsets CDet recursion (cdet_set_all_subsets_form).
+ * Both forms compute every mask with the same operations in the same order,
+ * so they give the same values bit for bit; they differ only in speed. */
+enum cdet_all_subsets_form {
+    CDET_FORM_AUTO = 0, /* the warp form below 8 warps' worth of configurations per SM, else the lane form */
+    CDET_FORM_LANE = 1, /* one lane per configuration (full FP64 warps; for large batches) */
+    CDET_FORM_WARP = 2  /* one warp per configuration (small batches; orders <= 11, else the lane form) */
+};
+
+int cdet_set_all_subsets_form(cdet_context* ctx, int form);
+
+/* Under CDET_FORM_AUTO the first all-subsets evaluation of each (order,
+ * assembly, batch size class = floor(log2 batch)) outside a CUDA-graph
+ * capture times both forms and keeps the faster for later evaluations; this
+ * reports the kept form (CDET_FORM_AUTO before any measurement). fused = 1
+ * for the split assembly. */
+int cdet_all_subsets_form_tuned(const cdet_context* ctx, int max_order, int fused, int64_t batch, int* form);
 
 /* Builds the bf16 slices of every uploaded table for the split assembly
  * (otherwise done by the first split evaluation). Allocates about twice the

@@ -245,7 +245,10 @@ def test_chain_results_match_reference(name):
     else:
         with pytest.raises(RuntimeError, match="order 1"):
             chains.estimates(0.0625)
-    assert chains.launch_count() > 0
+    launches, graph_steps = chains.launch_count()
+    # the first step of each (vertex buffer, warmup) kind is direct, the rest are graph replays
+    assert graph_steps >= run["warmup"] + run["production"] - 4
+    assert launches >= 3 * (run["warmup"] + run["production"])
     chains.close()
 
 

@@ -189,3 +189,31 @@ def test_all_subsets_against_single_order():
     combined = allv[:, 1:].reshape(-1)
     scale = np.maximum(1.0, np.maximum(np.abs(single), np.abs(combined)))
     assert np.all(np.abs(single - combined) <= 2e-9 + 2e-9 * scale)
+
+
+@pytest.mark.parametrize("assembly", ["fp64", "split"])
+def test_all_subsets_forms_identical(assembly):
+    """The lane and warp forms of the all-subsets CDet recursion give the same
+    values bit for bit (orders 2..11, batches not a multiple of the warp or
+    block), and the automatic choice is one of them."""
+    params = _column_3x3(64)
+    tables = build_tables(params, device="cuda")
+    gpu = CdetIntegrand(params, tables)
+    gpu.set_assembly(assembly)
+    for n, count in ((2, 37), (5, 70), (9, 129), (11, 45)):
+        v = uniform_configurations(500 + n, count, n)
+        out = {}
+        for form in ("lane", "warp", "auto"):
+            gpu.set_all_subsets_form(form)
+            out[form] = gpu.all_subsets_batch(v)
+        assert bits_equal(out["lane"][0], out["warp"][0]), n
+        assert np.array_equal(out["lane"][1], out["warp"][1]), n
+        assert bits_equal(out["auto"][0], out["warp"][0]), n
+        assert gpu.all_subsets_form_tuned(n, count) in ("lane", "warp")  # measured by the "auto" call
+    if assembly == "fp64":
+        orc = Oracle(params.runtime_scalars(), tables)
+        v = uniform_configurations(611, 40, 11)
+        gpu.set_all_subsets_form("warp")
+        got, _ = gpu.all_subsets_batch(v)
+        want, _ = orc.all_subsets_batch(v, threads=THREADS)
+        assert bits_equal(got, want)
