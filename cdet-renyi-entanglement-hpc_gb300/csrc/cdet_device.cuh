@@ -146,4 +146,33 @@ __device__ __forceinline__ uint32_t next_same_popcount(uint32_t v) {
     return (t + 1u) | (((~t & (t + 1u)) - 1u) >> (__ffs(v)));
 }
 
+// ------------------------------------------------- subsets by colex rank ---
+// Binomial coefficients C(n, k) for n, k <= 24, built at compile time.
+struct BinomialTable {
+    uint32_t c[25][25];
+};
+constexpr BinomialTable make_binomial_table() {
+    BinomialTable t{};
+    for (int n = 0; n <= 24; ++n)
+        for (int k = 0; k <= n; ++k) t.c[n][k] = (k == 0 || k == n) ? 1u : t.c[n - 1][k - 1] + t.c[n - 1][k];
+    return t;
+}
+static __constant__ BinomialTable kBinomial = make_binomial_table();
+
+// The m-subset of {0, ..., n-1} with colex rank r (r < C(n, m)), as a mask:
+// its largest element is the largest c with C(c, m) <= r, and so on down.
+// Work over the subsets of one size is spread evenly over lanes by rank.
+__device__ __forceinline__ uint32_t colex_subset(uint32_t r, int m, int n) {
+    uint32_t set = 0;
+    int hi = n - 1;
+    for (int i = m; i >= 1; --i) {
+        int c = hi;
+        while (c >= i && kBinomial.c[c][i] > r) --c;
+        set |= 1u << c;
+        r -= kBinomial.c[c][i];
+        hi = c - 1;
+    }
+    return set;
+}
+
 }  // namespace cdet

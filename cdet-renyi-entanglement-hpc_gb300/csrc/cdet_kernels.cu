@@ -528,12 +528,14 @@ __global__ void __launch_bounds__(128) cdet_fp64(const __grid_constant__ Problem
 
 // ------------------------------------- 3a'. all-subsets CDet, warp form ----
 // compute_dp_ztransform_all_subsets for small batches (a few MCMCMC chains):
-// one warp per configuration, the two sets in turn, a and dp in shared
-// memory. The masks of one popcount level are independent; the lanes share
-// them, and each mask's submask sum runs on one lane in the reference's
-// descending order with the same operations as cdet_all, so the values are
-// those of cdet_fp64 bit for bit. The lane form keeps the FP64 pipe full on
-// large batches; this form gives a small batch 32 lanes per configuration.
+// one warp per configuration, both sets at once, a and dp of each set in
+// shared memory. The masks of one popcount level are independent; the lanes
+// share the level's masks of both sets, dealt out by colex rank so that no
+// lane holds more than its share, and each mask's submask sum runs on one
+// lane in the reference's descending order with the same operations as
+// cdet_all, so the values are those of cdet_fp64 bit for bit. The lane form
+// keeps the FP64 pipe full on large batches; this form gives a small batch 32
+// lanes per configuration.
 template <bool Fused>
 __global__ void __launch_bounds__(128) cdet_all_warp(const __grid_constant__ Problem p,
                                                     const __grid_constant__ Scratch w) {
@@ -543,59 +545,66 @@ __global__ void __launch_bounds__(128) cdet_all_warp(const __grid_constant__ Pro
     if (c >= p.batch) return;  // whole warps
     const int n = p.max_order;
     const uint32_t count = 1u << n;
-    double* a_s = all_smem + static_cast<size_t>(warp) * 2 * count;
-    double* dp = a_s + count;
+    double* base = all_smem + static_cast<size_t>(warp) * 4 * count;  // [set][a, dp][count]
     const Scalars& s = p.s;
     const double threshold = dmul(s.z_eps0, s.z_safety);
     const bool filter = threshold > 0.0;
     const int64_t g = c >> 5;
     const int cl = static_cast<int>(c & 31);
+    for (int set = 0; set < 2; ++set) {
+        const double* a = w.a_int + (g * 2 + set) * static_cast<int64_t>(count) * kWarp + cl;
+        double* a_s = base + set * 2 * count;
+        for (uint32_t m = lane; m < count; m += 32) a_s[m] = a[static_cast<int64_t>(m) * kWarp];
+    }
+    __syncwarp();
+    for (int item = lane; item < 2 * n; item += 32) {
+        const int set = item >= n ? 1 : 0, i = item - set * n;
+        double* a_s = base + set * 2 * count;
+        a_s[count + (1u << i)] = a_s[1u << i];  // dp of a singleton
+    }
+    __syncwarp();
+    for (int bits = 2; bits <= n; ++bits) {
+        const uint32_t per = kBinomial.c[n][bits];
+        for (uint32_t item = lane; item < 2 * per; item += 32) {
+            const int set = item >= per ? 1 : 0;
+            const uint32_t mask = colex_subset(item - set * per, bits, n);
+            const double* a_s = base + set * 2 * count;
+            double* dp = base + set * 2 * count + count;
+            const uint32_t anchor = mask & (~mask + 1u);
+            const uint32_t rest = mask ^ anchor;
+            double acc = a_s[mask];
+            double rhs = fabs(acc);
+            for (uint32_t sm = (rest - 1u) & rest;; sm = (sm - 1u) & rest) {
+                const uint32_t sub = sm | anchor;
+                pair_update<Fused>(dp[sub], a_s[mask ^ sub], acc, rhs);
+                if (sm == 0) break;
+            }
+            if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
+            dp[mask] = acc;
+        }
+        __syncwarp();  // the next level reads this one
+    }
+    // integrand_all_subset_values_typed_into (:826-877) per set, then
+    // twisted - 2 * ordinary (cdet_integrand_evaluator.h:346-350)
     const double* diag = w.diag + c * 2 * 2 * n;
     double* out = p.values + c * static_cast<int64_t>(count);
     bool bad = false;
-    for (int set = 0; set < 2; ++set) {
-        const int r = set == 0 ? 2 : 1;
-        const double* a = w.a_int + (g * 2 + set) * static_cast<int64_t>(count) * kWarp + cl;
-        for (uint32_t m = lane; m < count; m += 32) a_s[m] = a[static_cast<int64_t>(m) * kWarp];
-        __syncwarp();
-        if (lane == 0) dp[0] = 0.0;
-        for (int i = lane; i < n; i += 32) dp[1u << i] = a_s[1u << i];
-        __syncwarp();
-        for (int bits = 2; bits <= n; ++bits) {
-            for (uint32_t mask = 3 + lane; mask < count; mask += 32) {
-                if (__popc(mask) != bits) continue;
-                const uint32_t anchor = mask & (~mask + 1u);
-                const uint32_t rest = mask ^ anchor;
-                double acc = a_s[mask];
-                double rhs = fabs(acc);
-                for (uint32_t sm = (rest - 1u) & rest;; sm = (sm - 1u) & rest) {
-                    const uint32_t sub = sm | anchor;
-                    pair_update<Fused>(dp[sub], a_s[mask ^ sub], acc, rhs);
-                    if (sm == 0) break;
-                }
-                if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
-                dp[mask] = acc;
-            }
-            __syncwarp();  // the next level reads this one
-        }
-        // integrand_all_subset_values_typed_into (:826-877); each lane owns the
-        // same masks in both sets
-        for (uint32_t mask = lane; mask < count; mask += 32) {
-            const int k = __popc(mask);
-            double v;
+    for (uint32_t mask = lane; mask < count; mask += 32) {
+        const int k = __popc(mask);
+        double v[2];
+        for (int set = 0; set < 2; ++set) {
+            const int r = set == 0 ? 2 : 1;
             if (k == 0) {
-                v = 0.0;
+                v[set] = 0.0;
             } else if (k == 1) {
                 const int i = __ffs(mask) - 1;
-                v = order1_value(s, diag[(set * 2) * n + i], diag[(set * 2 + 1) * n + i], r);
+                v[set] = order1_value(s, diag[(set * 2) * n + i], diag[(set * 2 + 1) * n + i], r);
             } else {
-                v = dmul(p.pref_ld[set][k], dp[mask]);
+                v[set] = dmul(p.pref_ld[set][k], base[set * 2 * count + count + mask]);
             }
-            if (!isfinite(v)) bad = true;
-            if (set == 0) out[mask] = v;
-            else out[mask] = dsub(out[mask], dmul(2.0, v));
+            if (!isfinite(v[set])) bad = true;
         }
-        __syncwarp();  // a_s and dp are reused by the next set
+        out[mask] = dsub(v[0], dmul(2.0, v[1]));
     }
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(p.status + c, kStatusNonFinite);
 }
@@ -873,9 +882,12 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
     } else if (p.all_subsets && p.max_order <= kAllWarpMaxOrder && p.all_subsets_form != kFormLane &&
                (p.all_subsets_form == kFormWarp ||
                 p.batch < static_cast<int64_t>(all_subsets_lane_form_min_batch(sm_count)))) {
-        // a small batch of all-subset envelopes: one warp per configuration
-        const size_t per_warp = 2 * (size_t{1} << p.max_order) * sizeof(double);
-        const int warps = static_cast<int>(std::min<size_t>(4, (200 * 1024) / per_warp));
+        // a small batch of all-subset envelopes: one warp per configuration,
+        // one warp per block while that spreads the batch over more SMs
+        const size_t per_warp = 4 * (size_t{1} << p.max_order) * sizeof(double);
+        const int warps = p.batch < 4 * static_cast<int64_t>(sm_count > 0 ? sm_count : 152)
+                              ? 1
+                              : static_cast<int>(std::min<size_t>(4, (200 * 1024) / per_warp));
         const size_t csmem = per_warp * warps;
         if (p.fused_cdet) {
             err = cudaFuncSetAttribute(cdet_all_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -139,9 +139,10 @@ struct McmcmcStepArgs {
 };
 cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* seeds, uint64_t* mt, int32_t* mt_index,
                                double* vertices, cudaStream_t stream);
-// Launches the step: one kernel for the uniform seed kernel, two (the
-// conditional probabilities, then the step) for the histogram seed kernel.
-cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream);
+// Launches the step: for small batches one warp-per-chain kernel; otherwise
+// one thread-per-chain kernel, preceded for the histogram seed kernel by the
+// warp-per-chain conditional probabilities. *kernels = the kernels launched.
+cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream, int* kernels);
 // Smallest all-subsets batch for which the FP64 CDet runs one lane per
 // configuration; smaller batches run one warp per configuration.
 int all_subsets_lane_form_min_batch(int sm_count);

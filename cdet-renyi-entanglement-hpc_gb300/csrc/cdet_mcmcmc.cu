@@ -166,8 +166,9 @@ __device__ bool conditional_probabilities_warp(const McmcmcStepArgs& a, const do
     for (int level = 1; level < n; ++level) {
         const int pc = n - level;
         const double denom = dmul(static_cast<double>(level), static_cast<double>(pc));
-        for (uint64_t gm = 1 + static_cast<uint64_t>(lane); gm < full; gm += 32) {
-            if (__popcll(gm) != level) continue;
+        const uint32_t per = kBinomial.c[n][level];
+        for (uint32_t r = lane; r < per; r += 32) {
+            const uint64_t gm = colex_subset(r, level, n);  // the level's subsets dealt out evenly
             double sum = 0.0;
             for (int c = 0; c < n; ++c) {
                 const uint64_t cb = uint64_t{1} << c;
@@ -303,6 +304,122 @@ __global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ Mcmcm
     finish_step<Hist>(a, c, row, Hist ? a.cprob + c * (int64_t{1} << a.envelope) : nullptr);
 }
 
+// The serial part of the step with one warp per chain (small batches): the
+// fluxes elementwise on all lanes, the local normalisation and the weighted
+// draw on lane 0 (both are running sums in mask order), each order's signal
+// sum on its own lane (its masks in increasing order, as the reference adds
+// them), then the next vertices on lane 0. Same values as finish_step.
+template <bool Hist>
+__device__ void finish_step_warp(const McmcmcStepArgs& a, int64_t c, int64_t row, const double* cprob, double* flux,
+                                 int lane) {
+    const int env = a.envelope;
+    const uint32_t subsets = 1u << env, full = subsets - 1;
+    const double* values = a.values + c * static_cast<int64_t>(subsets);
+    const double* lam = a.lambdas + c * (env + 1);
+    for (uint32_t mask = lane; mask < subsets; mask += 32) {
+        const int o = __popc(mask);
+        flux[mask] = (mask == 0 || o < a.order_min || o > a.order_max)
+                         ? 0.0
+                         : dmul(dmul(lam[o], values[mask]), Hist ? cprob[full ^ mask] : 1.0);
+    }
+    __syncwarp();
+    double norm = 0.0;
+    if (lane == 0)
+        for (uint32_t mask = 1; mask < subsets; ++mask) {
+            const int o = __popc(mask);
+            if (o < a.order_min || o > a.order_max) continue;
+            norm = dadd(norm, dmul(fabs(flux[mask]), a.inv_binom[o]));
+        }
+    norm = __shfl_sync(0xffffffffu, norm, 0);
+    if (!(norm > 0.0) || !isfinite(norm)) {
+        if (lane == 0) a.error[c] = 2;  // "MCMCMC local normalization is zero or non-finite"
+        return;
+    }
+    if (a.signal_out && lane <= env) {
+        double sig = 0.0;
+        if (lane >= 1 && lane >= a.order_min && lane <= a.order_max) {
+            const uint32_t masks = kBinomial.c[env][lane];
+            uint32_t m = (1u << lane) - 1u;
+            for (uint32_t r = 0; r < masks; ++r, m = next_same_popcount(m))
+                sig = dadd(sig, dmul(ddiv(flux[m], norm), a.inv_binom[lane]));
+        }
+        a.signal_out[(row * a.chains + c) * (env + 1) + lane] = sig;
+    }
+    if (lane != 0) return;
+    const Mt64 g{a.mt + c, a.chains, a.mt_index + c};
+    const double threshold = dadd(dmul(g.canonical(), dsub(norm, 0.0)), 0.0);
+    double cumulative = 0.0;
+    uint64_t chosen = 0, last_positive = 0;
+    bool found = false;
+    for (uint32_t mask = 1; mask < subsets && !found; ++mask) {
+        const int o = __popc(mask);
+        if (o < a.order_min || o > a.order_max) continue;
+        const double w = dmul(fabs(flux[mask]), a.inv_binom[o]);
+        if (!(w > 0.0)) continue;
+        if (isfinite(w)) last_positive = mask;
+        cumulative = dadd(cumulative, w);
+        if (cumulative > threshold) {
+            chosen = mask;
+            found = true;
+        }
+    }
+    if (!found) chosen = last_positive;
+    const double* v = a.vertices + c * env * 4;
+    double* nv = a.next_vertices + c * env * 4;
+    int size = 0;
+    for (int i = 0; i < env; ++i)
+        if (chosen & (uint64_t{1} << i)) {
+            for (int k = 0; k < 4; ++k) nv[4 * size + k] = v[4 * i + k];
+            ++size;
+        }
+    while (size < env) {
+        const int parent = g.uniform_int(size);
+        if constexpr (Hist) {
+            hist_child(a, g, nv + 4 * parent, nv + 4 * size);
+        } else {
+            (void)parent;
+            for (int k = 0; k < 4; ++k) nv[4 * size + k] = g.canonical();
+        }
+        ++size;
+    }
+    if (a.chosen_out) a.chosen_out[row * a.chains + c] = chosen;
+    if (a.norm_out) a.norm_out[row * a.chains + c] = norm;
+    if (a.warmup) ++a.counts[c * (env + 1) + __popcll(chosen)];
+}
+
+// The whole step for a small batch: one warp (and block) per chain, its
+// fluxes, and for the histogram seed kernel its densities and conditional
+// probabilities, in shared memory.
+constexpr int kStepWarpMaxEnvelope = 12;
+constexpr int64_t kStepWarpMaxChains = 2048;
+template <bool Hist>
+__global__ void __launch_bounds__(32) mcmcmc_step_warp(const __grid_constant__ McmcmcStepArgs a) {
+    extern __shared__ double step_smem[];
+    const int lane = threadIdx.x;
+    const int64_t c = blockIdx.x;
+    const int env = a.envelope;
+    const uint32_t subsets = 1u << env;
+    double* flux = step_smem;
+    double* prob = flux + subsets;
+    double* sd = prob + subsets;
+    double* cd0 = sd + env * env;
+    const int64_t row = a.ring_row ? *a.ring_row : 0;
+    if (lane == 0 && a.chosen_out) a.chosen_out[row * a.chains + c] = 0;  // 0: no step (a failed chain)
+    if (a.error[c]) return;  // the same value on every lane
+    if (a.integrand_status[c] & kStatusNonFinite) {
+        if (lane == 0) a.error[c] = 1;  // "Error (all-subset integrand): Value is not finite"
+        return;
+    }
+    if constexpr (Hist) {
+        if (!conditional_probabilities_warp(a, a.vertices + c * env * 4, env, prob, sd, cd0, lane)) {
+            if (lane == 0) a.error[c] = 3;  // "MCMCMC seed density is negative or non-finite"
+            return;
+        }
+        __syncwarp();
+    }
+    finish_step_warp<Hist>(a, c, row, prob, flux, lane);
+}
+
 // The histogram seed kernel's conditional generation probabilities, one warp
 // per chain, into a.cprob; a negative or non-finite seed density stops the
 // chain (error 3), which the step kernel then skips.
@@ -341,10 +458,29 @@ cudaError_t launch_mcmcmc_init(int64_t chains, int envelope, const uint64_t* see
     return cudaGetLastError();
 }
 
-cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream) {
+cudaError_t launch_mcmcmc_step(const McmcmcStepArgs& args, cudaStream_t stream, int* kernels) {
+    *kernels = 0;
     if (args.chains <= 0) return cudaSuccess;
+    const bool hist = args.tau_bins > 0;
+    if (args.chains < kStepWarpMaxChains && args.envelope <= kStepWarpMaxEnvelope) {
+        const size_t subsets = size_t{1} << args.envelope;
+        const size_t smem =
+            (subsets + (hist ? subsets + static_cast<size_t>(args.envelope) * (args.envelope + 1) : 0)) *
+            sizeof(double);
+        const void* fn = hist ? reinterpret_cast<const void*>(mcmcmc_step_warp<true>)
+                              : reinterpret_cast<const void*>(mcmcmc_step_warp<false>);
+        cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (err != cudaSuccess) return err;
+        if (hist)
+            mcmcmc_step_warp<true><<<static_cast<unsigned>(args.chains), 32, smem, stream>>>(args);
+        else
+            mcmcmc_step_warp<false><<<static_cast<unsigned>(args.chains), 32, smem, stream>>>(args);
+        *kernels = 1;
+        return cudaGetLastError();
+    }
     const unsigned grid = static_cast<unsigned>((args.chains + 127) / 128);
-    if (args.tau_bins > 0) {
+    *kernels = hist ? 2 : 1;
+    if (hist) {
         mcmcmc_hist_probs<<<static_cast<unsigned>((args.chains + kHistWarps - 1) / kHistWarps), kHistWarps * 32, 0,
                             stream>>>(args);
         const cudaError_t err = cudaGetLastError();

@@ -184,10 +184,11 @@ int enqueue_step(cdet_mcmcmc* m, int warmup, int* launches) {
     int rc = run(m->ctx, m->vert[m->cur], nullptr, m->chains, m->cfg.envelope_order, 1, m->values, m->istatus,
                  m->stream);
     if (rc != CDET_OK) return rc;
-    cudaError_t err = cdet::launch_mcmcmc_step(step_args(m, warmup), m->stream);
+    int step_kernels = 0;
+    cudaError_t err = cdet::launch_mcmcmc_step(step_args(m, warmup), m->stream, &step_kernels);
     if (err == cudaSuccess) err = cdet::launch_mcmcmc_advance_row(m->d_row, ring_rows(m), m->stream);
     if (err != cudaSuccess) return cuda_fail(err, "MCMCMC step launch");
-    *launches = m->ctx->last_launches + (m->tau_bins > 0 ? 3 : 2);
+    *launches = m->ctx->last_launches + step_kernels + 1;
     return CDET_OK;
 }
 

@@ -333,3 +333,33 @@ def test_graphs_follow_context_changes():
     verts, _, _ = chains.state()
     assert np.array_equal(verts.view(np.uint64), GOLD[f"{name}.vertices"].view(np.uint64))
     chains.close()
+
+
+@pytest.mark.parametrize("hist", [False, True])
+def test_large_batch_step_path(hist):
+    """From 2048 chains the step runs one thread per chain (after the
+    warp-per-chain conditional probabilities for the histogram seed); chains
+    are independent, so the first 8 chains of a 2048-chain batch seeded like
+    the reference's must still be the reference's chains."""
+    name = "column_3x3"
+    run = RUNS[name]
+    params, tables, _ = load_case(name)
+    gpu = CdetIntegrand(params, tables)
+    key = f"{name}.hist" if hist else name
+    seeds = np.concatenate([GOLD[f"{key}.seeds"], np.arange(1, 2041, dtype=np.uint64) * np.uint64(7919)])
+    chains = McmcmcChains(gpu, run["order_min"], run["order_max"], run["envelope"], seeds, run["lambdas"],
+                          run["adapt_interval"], run["adapt_rate"])
+    if hist:
+        chains.set_histogram(run["histogram"]["tau_bins"], GOLD[f"{key}.tau"], GOLD[f"{key}.space"],
+                             GOLD[f"{key}.replica"])
+    w = chains.run(run["warmup"], warmup=True, record=True)
+    chains.end_warmup()
+    p = chains.run(run["production"], warmup=False, record=True)
+    verts, _, rng = chains.state()
+    chosen = np.concatenate([w["chosen"], p["chosen"]]).T[:8]
+    assert np.array_equal(chosen, GOLD[f"{key}.chosen"])
+    assert np.array_equal(verts[:8].view(np.uint64), GOLD[f"{key}.vertices"].view(np.uint64))
+    for c in range(8):
+        assert np.array_equal(mt64_outputs(rng[c], 8), GOLD[f"{key}.rng"][c]), c
+    assert _close(p["signal"].transpose(1, 0, 2)[:8], GOLD[f"{key}.signal"])
+    chains.close()
