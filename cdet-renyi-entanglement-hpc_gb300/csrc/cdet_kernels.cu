@@ -160,7 +160,9 @@ struct WsLayout {
     size_t a, old_list, new_list, aux, shifted_up, shifted_down, total;
 };
 
-__host__ __device__ inline WsLayout ws_layout(int nmax) {
+// two_spins = false when both sets evaluate one spin only (up and down tables
+// and shifts identical): the spin-down minors then need no space.
+__host__ __device__ inline WsLayout ws_layout(int nmax, bool two_spins = true) {
     WsLayout l;
     size_t list = static_cast<size_t>(nmax) * nmax;
     for (int level = 0; level < nmax - 1; ++level) {
@@ -177,7 +179,7 @@ __host__ __device__ inline WsLayout ws_layout(int nmax) {
     l.aux = l.new_list + even(list);
     l.shifted_up = l.aux + even(subsets / 2 + 2);
     l.shifted_down = l.shifted_up + subsets;
-    l.total = l.shifted_down + subsets;
+    l.total = two_spins ? l.shifted_down + subsets : l.shifted_down;
     return l;
 }
 
@@ -336,7 +338,7 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
     return false;
 }
 
-__global__ void __launch_bounds__(128) principal_minors_fp64(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_constant__ Problem p,
                                                             const __grid_constant__ Scratch w,
                                                             int use_smem) {
     extern __shared__ double smem[];
@@ -346,7 +348,8 @@ __global__ void __launch_bounds__(128) principal_minors_fp64(const __grid_consta
     const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
     const int64_t total_warps = static_cast<int64_t>(gridDim.x) * warps_per_block;
     const int nmax = p.max_order;
-    const WsLayout lay = ws_layout(nmax);
+    // the global workspace is laid out for two spins; shared memory for what the sets need
+    const WsLayout lay = ws_layout(nmax, !use_smem || !(p.same_spin[0] && p.same_spin[1]));
     double* ws = use_smem ? smem + static_cast<size_t>(warp_in_block) * lay.total
                           : w.ws_global + static_cast<size_t>(global_warp) * lay.total;
     double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
@@ -848,16 +851,21 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
         mark(2);
     }
 
-    // Minors: the per-warp workspace goes to shared memory when four warps'
-    // worth fits a block, otherwise to the global workspace.
-    const size_t ws_bytes = minors_workspace_doubles(p.max_order) * sizeof(double);
-    const size_t smem_budget = 200 * 1024;
-    const int warps_per_block = 4;
-    const bool use_smem = ws_bytes * warps_per_block <= smem_budget;
+    // Minors: the per-warp workspace goes to shared memory when at least four
+    // warps' worth fits a block (one block per SM, as many warps as fit, at
+    // most 8; without the spin-down minors when both sets have one spin),
+    // otherwise to the global workspace (4 warps per block).
+    const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
+    const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(double);
+    const size_t smem_budget = 227 * 1024;
+    const int fit = static_cast<int>(std::min<size_t>(8, smem_budget / ws_bytes));
+    const bool use_smem = fit >= 4;
+    const int warps_per_block = use_smem ? fit : 4;
     const int64_t items = p.batch * 2;
     int64_t blocks = (items + warps_per_block - 1) / warps_per_block;
     const int64_t max_blocks = static_cast<int64_t>(w.ws_warps) / warps_per_block;
     blocks = std::min<int64_t>(blocks, std::max<int64_t>(1, max_blocks));
+    if (use_smem) blocks = std::min<int64_t>(blocks, sm_count > 0 ? sm_count : 152);  // one wave
     const size_t smem = use_smem ? ws_bytes * warps_per_block : 0;
     if (smem > 48 * 1024) {
         err = cudaFuncSetAttribute(principal_minors_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
