@@ -758,11 +758,20 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t count = meta.count;
             const int exponent = meta.exponent;
+            // Drain: every accumulator of this thread's row and the group's 32
+            // lookups into 64-bit fixed point, W * 2^55 = sum_tau P_tau
+            // 2^(55 - 8 tau), tau = 2..8 (levels 2..6 exact integers, 7 and 8
+            // folded in FP32), in registers; then the tensor memory is free
+            // and the next tile's MMAs run while the products and row sums below
+            // are formed. Two loads per chunk (levels 2-5, then 6-8) bound the
+            // registers in flight.
+            int64_t wfix[kGroupLookups];
+#pragma unroll
             for (int c0 = 0; c0 < kGroupLookups; c0 += kRedChunk) {
                 const int l0 = group * kGroupLookups + c0;
-                uint32_t acc[kLevels][8];
+                uint32_t acc[4][8];
 #pragma unroll
-                for (int lev = 0; lev < kLevels; ++lev) {
+                for (int lev = 0; lev < 4; ++lev) {
                     const uint32_t addr = lane_base + lev * kTileN + l0;
                     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                                  : "=r"(acc[lev][0]), "=r"(acc[lev][1]), "=r"(acc[lev][2]), "=r"(acc[lev][3]),
@@ -770,25 +779,40 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                                  : "r"(addr));
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
-                if (c0 + kRedChunk == kGroupLookups) {  // accumulators read: the next tile's MMAs may start
-                    asm volatile("tcgen05.fence::before_thread_sync;");
-                    mbar_arrive(&sh.acc_empty);
+#pragma unroll
+                for (int j = 0; j < kRedChunk; ++j)
+                    wfix[c0 + j] = static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[0][j]))) * (int64_t{1} << 39) +
+                                   static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[1][j]))) * (int64_t{1} << 31) +
+                                   static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[2][j]))) * (int64_t{1} << 23) +
+                                   static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[3][j]))) * (int64_t{1} << 15);
+#pragma unroll
+                for (int lev = 4; lev < kLevels; ++lev) {
+                    const uint32_t addr = lane_base + lev * kTileN + l0;
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                 : "=r"(acc[lev - 4][0]), "=r"(acc[lev - 4][1]), "=r"(acc[lev - 4][2]),
+                                   "=r"(acc[lev - 4][3]), "=r"(acc[lev - 4][4]), "=r"(acc[lev - 4][5]),
+                                   "=r"(acc[lev - 4][6]), "=r"(acc[lev - 4][7])
+                                 : "r"(addr));
                 }
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                for (int j = 0; j < kRedChunk; ++j) {
+                    const float p78 = fmaf(__uint_as_float(acc[2][j]), 0.001953125f, __uint_as_float(acc[1][j]) * 0.5f);
+                    wfix[c0 + j] += static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[0][j]))) * 128 +
+                                    __float2int_rn(p78);
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(&sh.acc_empty);  // accumulators read: the next tile's MMAs may start
+#pragma unroll
+            for (int c0 = 0; c0 < kGroupLookups; c0 += kRedChunk) {
+                const int l0 = group * kGroupLookups + c0;
 #pragma unroll
                 for (int j = 0; j < kRedChunk; ++j) {
                     const int l = l0 + j;
-                    // W * 2^55 = sum_tau P_tau 2^(55 - 8 tau), tau = 2..8; levels
-                    // 2..6 are exact integers, 7 and 8 are folded in FP32
-                    int64_t pl[5];
-#pragma unroll
-                    for (int lev = 0; lev < 5; ++lev) pl[lev] = __float2int_rn(__uint_as_float(acc[lev][j]));
-                    const float p78 = fmaf(__uint_as_float(acc[6][j]), 0.001953125f, __uint_as_float(acc[5][j]) * 0.5f);
-                    const int64_t wfix = pl[0] * (int64_t{1} << 39) + pl[1] * (int64_t{1} << 31) +
-                                         pl[2] * (int64_t{1} << 23) + pl[3] * (int64_t{1} << 15) + pl[4] * 128 +
-                                         __float2int_rn(p78);
                     const int64_t tf = sh.ubasis[l * kRows + (row ^ (l & 31))];
-                    const uint64_t lo = static_cast<uint64_t>(wfix) * static_cast<uint64_t>(tf);
-                    int64_t hi = __mul64hi(wfix, tf);
+                    const uint64_t lo = static_cast<uint64_t>(wfix[c0 + j]) * static_cast<uint64_t>(tf);
+                    int64_t hi = __mul64hi(wfix[c0 + j], tf);
                     const uint64_t lo2 = lo + (uint64_t{1} << 61);
                     hi += lo2 < lo ? 1 : 0;
                     red[j * kRows + row] = static_cast<int64_t>((static_cast<uint64_t>(hi) << 2) | (lo2 >> 62));
