@@ -619,10 +619,12 @@ __global__ void __launch_bounds__(128) cdet_all_warp(const __grid_constant__ Pro
 // submasks on the L highest set bits and add their partial sums with
 // shuffles, so the FP64 pipe sees few idle lanes even at the top levels.
 // Each pair update is one FP64 FMA. The round-off filter's magnitude sum
-// runs in FP32 on shadow copies scaled by 2^(-e |m|) (e: binary exponent of
-// the first singleton), which keeps all terms of a mask near 1 whatever the
-// order; a shadow is clamped to the FP32 range, so an overflow can only keep a
-// value, never zero it.
+// runs in FP32 on the terms' magnitudes scaled by 2^(-e |m|) (e: binary
+// exponent of the first singleton), which keeps all terms of a mask near 1
+// whatever the order; each magnitude is formed from the two factors' exponent
+// and mantissa bits (product_magnitude), so a pair update loads only its two
+// doubles from shared memory. Magnitudes are clamped to the FP32 range, and a
+// non-finite accumulator is never zeroed.
 constexpr int kWarpCdetMaxOrder = 10;
 constexpr int kWarpCdetWarps = 8;
 
@@ -653,23 +655,35 @@ __device__ __forceinline__ uint32_t colex_unrank(uint32_t r, int m, int N) {
     return set;
 }
 
+// |x y| 2^(-s) as a float, from the exponent fields and the leading 20
+// mantissa bits of x and y (integer work only; the filter's magnitude sums
+// need about 2^-20 relative accuracy). field_bias = 127 - 2046 - s. Zeros and
+// subnormals give 0; the exponent is clamped so the result stays finite.
+__device__ __forceinline__ float product_magnitude(double x, double y, int field_bias) {
+    const int hx = __double2hiint(x), hy = __double2hiint(y);
+    const float mx = __int_as_float(0x3F800000 | ((hx & 0xFFFFF) << 3));
+    const float my = __int_as_float(0x3F800000 | ((hy & 0xFFFFF) << 3));
+    const int ex = ((hx >> 20) & 0x7FF), ey = ((hy >> 20) & 0x7FF);
+    int field = ex + ey + field_bias;
+    field = (ex == 0 || ey == 0) ? 0 : min(max(field, 0), 252);
+    return mx * my * __int_as_float(field << 23);
+}
+
 // |v| * 2^k as a float, clamped to the finite range (|k| <= 1000).
 __device__ __forceinline__ float scaled_magnitude(double v, int k) {
     const double p2 = __longlong_as_double(static_cast<long long>(1023 + k) << 52);
     return fminf(static_cast<float>(fabs(dmul(v, p2))), 3.0e38f);
 }
 
-__global__ void __launch_bounds__(kWarpCdetWarps * 32) cdet_split_warp(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(kWarpCdetWarps * 32, 2) cdet_split_warp(const __grid_constant__ Problem p,
                                                                        const __grid_constant__ Scratch w) {
     extern __shared__ __align__(16) unsigned char cdet_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nmax = p.max_order;
     const int full_n = 1 << nmax;
-    double* a_s = reinterpret_cast<double*>(cdet_smem) + warp * 2 * full_n;
+    // a of every mask; dp only of the masks holding vertex 0 (odd), at mask >> 1
+    double* a_s = reinterpret_cast<double*>(cdet_smem) + warp * (full_n + full_n / 2);
     double* dp_s = a_s + full_n;
-    float* af_s = reinterpret_cast<float*>(reinterpret_cast<double*>(cdet_smem) + kWarpCdetWarps * 2 * full_n) +
-                  warp * 2 * full_n;
-    float* dpf_s = af_s + full_n;
     const Scalars& s = p.s;
     const double threshold = dmul(s.z_eps0, s.z_safety);
     const bool filter = threshold > 0.0;
@@ -700,16 +714,9 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32) cdet_split_warp(const __g
                 if (field != 0 && field != 0x7FF) e = field - 1023;
                 e = e > 90 ? 90 : (e < -90 ? -90 : e);  // |e| * nmax stays within 1000
             }
-            for (int m = lane; m < count; m += kWarp) {
-                const double v = ag[static_cast<int64_t>(m) * kWarp];
-                a_s[m] = v;
-                af_s[m] = scaled_magnitude(v, -e * __popc(m));
-            }
+            for (int m = lane; m < count; m += kWarp) a_s[m] = ag[static_cast<int64_t>(m) * kWarp];
             __syncwarp();
-            if (lane == 0) {
-                dp_s[1] = a_s[1];
-                dpf_s[1] = af_s[1];
-            }
+            if (lane == 0) dp_s[0] = a_s[1];
             __syncwarp();
             const int nbits = n - 1;
             for (int k = 2; k <= n; ++k) {
@@ -734,6 +741,7 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32) cdet_split_warp(const __g
                     double part = 0.0;
                     float rpart = 0.0f;
                     uint32_t mask = 0;
+                    const int field_bias = 127 - 2046 - e * k;
                     if (active) {
                         const uint32_t rest = colex_unrank(static_cast<uint32_t>(idx), kk, nbits);
                         mask = (rest << 1) | 1u;
@@ -754,8 +762,9 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32) cdet_split_warp(const __g
                             if (sm != rest) {
                                 const uint32_t sub = (sm << 1) | 1u;
                                 const uint32_t other = mask ^ sub;
-                                part = __fma_rn(dp_s[sub], a_s[other], part);
-                                rpart = fmaf(dpf_s[sub], af_s[other], rpart);
+                                const double x = dp_s[sub >> 1], y = a_s[other];
+                                part = __fma_rn(x, y, part);
+                                rpart += product_magnitude(x, y, field_bias);
                             }
                             if (sl == 0) break;
                         }
@@ -766,17 +775,16 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32) cdet_split_warp(const __g
                     }
                     if (active && j == 0) {
                         double acc = dsub(a_s[mask], part);
-                        const float rhs = af_s[mask] + rpart;
+                        const float rhs = scaled_magnitude(a_s[mask], -e * k) + rpart;
                         if (filter && scaled_magnitude(acc, -e * k) < thresholdf * rhs) acc = 0.0;
-                        dp_s[mask] = acc;
-                        dpf_s[mask] = scaled_magnitude(acc, -e * k);
+                        dp_s[mask >> 1] = acc;
                     }
                     base += take;
                 }
                 __syncwarp();
             }
             const DDPair pf = p.pref_dd[set][n];
-            value = dd_mul(DD{pf.hi, pf.lo}, DD{dp_s[count - 1], 0.0});
+            value = dd_mul(DD{pf.hi, pf.lo}, DD{dp_s[(count - 1) >> 1], 0.0});
             if (!dd_finite(value)) status |= kStatusNonFinite;
             __syncwarp();  // the next set reuses the arrays
         }
@@ -880,8 +888,8 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
 
     if (p.fused_cdet && !p.all_subsets && p.max_order <= kWarpCdetMaxOrder) {
         // split assembly: warp-per-configuration recursion in shared memory
-        const size_t csmem = static_cast<size_t>(kWarpCdetWarps) * (2 * sizeof(double) + 2 * sizeof(float)) *
-                             (size_t{1} << p.max_order);
+        const size_t csmem =
+            static_cast<size_t>(kWarpCdetWarps) * sizeof(double) * ((size_t{3} << p.max_order) / 2);
         err = cudaFuncSetAttribute(cdet_split_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(csmem));
         if (err != cudaSuccess) return err;
