@@ -675,15 +675,17 @@ __device__ __forceinline__ float scaled_magnitude(double v, int k) {
     return fminf(static_cast<float>(fabs(dmul(v, p2))), 3.0e38f);
 }
 
-__global__ void __launch_bounds__(kWarpCdetWarps * 32, 2) cdet_split_warp(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const __grid_constant__ Problem p,
                                                                        const __grid_constant__ Scratch w) {
     extern __shared__ __align__(16) unsigned char cdet_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nmax = p.max_order;
     const int full_n = 1 << nmax;
-    // a of every mask; dp only of the masks holding vertex 0 (odd), at mask >> 1
-    double* a_s = reinterpret_cast<double*>(cdet_smem) + warp * (full_n + full_n / 2);
-    double* dp_s = a_s + full_n;
+    // a of the masks without vertex 0 (even; the pair updates' second factor)
+    // and dp of the masks with it (odd), both at mask >> 1; a of an odd mask
+    // is read once per mask from global memory
+    double* a_s = reinterpret_cast<double*>(cdet_smem) + warp * full_n;
+    double* dp_s = a_s + full_n / 2;
     const Scalars& s = p.s;
     const double threshold = dmul(s.z_eps0, s.z_safety);
     const bool filter = threshold > 0.0;
@@ -714,9 +716,9 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 2) cdet_split_warp(const 
                 if (field != 0 && field != 0x7FF) e = field - 1023;
                 e = e > 90 ? 90 : (e < -90 ? -90 : e);  // |e| * nmax stays within 1000
             }
-            for (int m = lane; m < count; m += kWarp) a_s[m] = ag[static_cast<int64_t>(m) * kWarp];
+            for (int m2 = lane; m2 < count / 2; m2 += kWarp) a_s[m2] = ag[static_cast<int64_t>(2 * m2) * kWarp];
             __syncwarp();
-            if (lane == 0) dp_s[0] = a_s[1];
+            if (lane == 0) dp_s[0] = ag[1 * kWarp];
             __syncwarp();
             const int nbits = n - 1;
             for (int k = 2; k <= n; ++k) {
@@ -762,7 +764,7 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 2) cdet_split_warp(const 
                             if (sm != rest) {
                                 const uint32_t sub = (sm << 1) | 1u;
                                 const uint32_t other = mask ^ sub;
-                                const double x = dp_s[sub >> 1], y = a_s[other];
+                                const double x = dp_s[sub >> 1], y = a_s[other >> 1];
                                 part = __fma_rn(x, y, part);
                                 rpart += product_magnitude(x, y, field_bias);
                             }
@@ -774,8 +776,9 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 2) cdet_split_warp(const 
                         rpart += __shfl_xor_sync(0xffffffffu, rpart, off);
                     }
                     if (active && j == 0) {
-                        double acc = dsub(a_s[mask], part);
-                        const float rhs = scaled_magnitude(a_s[mask], -e * k) + rpart;
+                        const double am = ag[static_cast<int64_t>(mask) * kWarp];
+                        double acc = dsub(am, part);
+                        const float rhs = scaled_magnitude(am, -e * k) + rpart;
                         if (filter && scaled_magnitude(acc, -e * k) < thresholdf * rhs) acc = 0.0;
                         dp_s[mask >> 1] = acc;
                     }
@@ -888,8 +891,7 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
 
     if (p.fused_cdet && !p.all_subsets && p.max_order <= kWarpCdetMaxOrder) {
         // split assembly: warp-per-configuration recursion in shared memory
-        const size_t csmem =
-            static_cast<size_t>(kWarpCdetWarps) * sizeof(double) * ((size_t{3} << p.max_order) / 2);
+        const size_t csmem = static_cast<size_t>(kWarpCdetWarps) * sizeof(double) * (size_t{1} << p.max_order);
         err = cudaFuncSetAttribute(cdet_split_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(csmem));
         if (err != cudaSuccess) return err;
