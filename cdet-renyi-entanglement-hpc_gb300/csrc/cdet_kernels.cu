@@ -277,7 +277,7 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
             const double pivot = dadd(old_list[set * old_msize], p);
             const double pa = fabs(pivot);
             if (pa == 0.0 || (fallback_eps > 0.0 && pa <= fallback_eps)) bad_pivot = true;
-            inv[set] = ddiv(1.0, pivot);
+            inv[set] = __drcp_rn(pivot);  // 1.0 / pivot, correctly rounded (IEEE): the same value
         }
         if (__any_sync(0xffffffffu, bad_pivot)) {
             fell_back = true;

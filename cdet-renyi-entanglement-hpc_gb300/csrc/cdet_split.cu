@@ -526,7 +526,8 @@ struct SplitShared {
     uint64_t a_full[kAStages], a_empty[kAStages];
     uint64_t b_full[kBStages], b_empty[kBStages];
     uint64_t meta_full[kMetaBufs], meta_empty[kMetaBufs];
-    uint64_t acc_full, acc_empty;
+    uint64_t acc_full;
+    uint64_t acc_empty[kLevels];  // per accumulator level: drained, the next tile may write it
     uint64_t drain;  // last commit of the MMA thread, waited on before dealloc
     uint32_t tmem_base;
     uint32_t error;
@@ -644,7 +645,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
             mbar_init(&sh.meta_empty[i], kEpilogueWarps * 32);
         }
         mbar_init(&sh.acc_full, 1);
-        mbar_init(&sh.acc_empty, kEpilogueWarps * 32);
+        for (int i = 0; i < kLevels; ++i) mbar_init(&sh.acc_empty[i], kEpilogueWarps * 32);
         mbar_init(&sh.drain, 1);
         sh.error = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
@@ -761,49 +762,55 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
             // Drain: every accumulator of this thread's row and the group's 32
             // lookups into 64-bit fixed point, W * 2^55 = sum_tau P_tau
             // 2^(55 - 8 tau), tau = 2..8 (levels 2..6 exact integers, 7 and 8
-            // folded in FP32), in registers; then the tensor memory is free
-            // and the next tile's MMAs run while the products and row sums below
-            // are formed. Two loads per chunk (levels 2-5, then 6-8) bound the
-            // registers in flight.
+            // folded in FP32), in registers. Each level is released as soon as
+            // it is read, so the next tile's MMAs into it (issued level by
+            // level in the same order) start while the rest drains: levels 7
+            // and 8 first (folded together), then 2..6. The products and row
+            // sums below then run alongside the next tile's MMAs.
             int64_t wfix[kGroupLookups];
 #pragma unroll
             for (int c0 = 0; c0 < kGroupLookups; c0 += kRedChunk) {
                 const int l0 = group * kGroupLookups + c0;
-                uint32_t acc[4][8];
-#pragma unroll
-                for (int lev = 0; lev < 4; ++lev) {
-                    const uint32_t addr = lane_base + lev * kTileN + l0;
-                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                                 : "=r"(acc[lev][0]), "=r"(acc[lev][1]), "=r"(acc[lev][2]), "=r"(acc[lev][3]),
-                                   "=r"(acc[lev][4]), "=r"(acc[lev][5]), "=r"(acc[lev][6]), "=r"(acc[lev][7])
-                                 : "r"(addr));
-                }
+                uint32_t p7[8], p8[8];
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                             : "=r"(p7[0]), "=r"(p7[1]), "=r"(p7[2]), "=r"(p7[3]), "=r"(p7[4]), "=r"(p7[5]),
+                               "=r"(p7[6]), "=r"(p7[7])
+                             : "r"(lane_base + 5 * kTileN + l0));
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                             : "=r"(p8[0]), "=r"(p8[1]), "=r"(p8[2]), "=r"(p8[3]), "=r"(p8[4]), "=r"(p8[5]),
+                               "=r"(p8[6]), "=r"(p8[7])
+                             : "r"(lane_base + 6 * kTileN + l0));
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
                 for (int j = 0; j < kRedChunk; ++j)
-                    wfix[c0 + j] = static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[0][j]))) * (int64_t{1} << 39) +
-                                   static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[1][j]))) * (int64_t{1} << 31) +
-                                   static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[2][j]))) * (int64_t{1} << 23) +
-                                   static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[3][j]))) * (int64_t{1} << 15);
+                    wfix[c0 + j] = __float2int_rn(
+                        fmaf(__uint_as_float(p8[j]), 0.001953125f, __uint_as_float(p7[j]) * 0.5f));
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(&sh.acc_empty[5]);
+            mbar_arrive(&sh.acc_empty[6]);
 #pragma unroll
-                for (int lev = 4; lev < kLevels; ++lev) {
-                    const uint32_t addr = lane_base + lev * kTileN + l0;
+            for (int lev = 0; lev < 5; ++lev) {
+                uint32_t v[kGroupLookups / kRedChunk][8];
+#pragma unroll
+                for (int q = 0; q < kGroupLookups / kRedChunk; ++q) {
+                    const uint32_t addr = lane_base + lev * kTileN + group * kGroupLookups + q * kRedChunk;
                     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                                 : "=r"(acc[lev - 4][0]), "=r"(acc[lev - 4][1]), "=r"(acc[lev - 4][2]),
-                                   "=r"(acc[lev - 4][3]), "=r"(acc[lev - 4][4]), "=r"(acc[lev - 4][5]),
-                                   "=r"(acc[lev - 4][6]), "=r"(acc[lev - 4][7])
+                                 : "=r"(v[q][0]), "=r"(v[q][1]), "=r"(v[q][2]), "=r"(v[q][3]), "=r"(v[q][4]),
+                                   "=r"(v[q][5]), "=r"(v[q][6]), "=r"(v[q][7])
                                  : "r"(addr));
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
+                const int shift = 39 - 8 * lev;  // 2^(55 - 8 tau), tau = lev + 2
 #pragma unroll
-                for (int j = 0; j < kRedChunk; ++j) {
-                    const float p78 = fmaf(__uint_as_float(acc[2][j]), 0.001953125f, __uint_as_float(acc[1][j]) * 0.5f);
-                    wfix[c0 + j] += static_cast<int64_t>(__float2int_rn(__uint_as_float(acc[0][j]))) * 128 +
-                                    __float2int_rn(p78);
-                }
+                for (int q = 0; q < kGroupLookups / kRedChunk; ++q)
+#pragma unroll
+                    for (int j = 0; j < kRedChunk; ++j)
+                        wfix[q * kRedChunk + j] +=
+                            static_cast<int64_t>(__float2int_rn(__uint_as_float(v[q][j]))) * (int64_t{1} << shift);
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                mbar_arrive(&sh.acc_empty[lev]);  // this level may take the next tile's MMAs
             }
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(&sh.acc_empty);  // accumulators read: the next tile's MMAs may start
 #pragma unroll
             for (int c0 = 0; c0 < kGroupLookups; c0 += kRedChunk) {
                 const int l0 = group * kGroupLookups + c0;
@@ -903,18 +910,14 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         if (lane == 0) {
             const uint32_t idesc = mma_idesc(kRows, kTileN);
             uint32_t a_cnt = 0, b_cnt = 0, tile_cnt = 0;
-            for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile, ++tile_cnt) {
-                if (tile_cnt > 0 && !mbar_wait(&sh.acc_empty, (tile_cnt - 1) & 1)) {
-                    sh.error = 1;
-                    break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                for (int ks = 0; ks < ksteps; ++ks, ++a_cnt, ++b_cnt) {
+            bool ok = true, issued = false;
+            for (uint32_t tile = tile_begin; ok && tile < tile_end && !failed(sh); ++tile, ++tile_cnt) {
+                for (int ks = 0; ok && ks < ksteps; ++ks, ++a_cnt, ++b_cnt) {
                     const int sa = static_cast<int>(a_cnt % kAStages);
                     const int sb = static_cast<int>(b_cnt % kBStages);
                     if (!mbar_wait(&sh.a_full[sa], (a_cnt / kAStages) & 1) ||
                         !mbar_wait(&sh.b_full[sb], (b_cnt / kBStages) & 1)) {
-                        sh.error = 1;
+                        ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -924,24 +927,66 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                     const uint64_t a_desc = smem_desc(smem_addr(sh.a_ring[sa]), 128, 256);
                     const uint64_t b_desc = smem_desc(smem_addr(sh.b_ring[sb]), 128, 256);
                     const uint32_t first = ks > 0 ? 1u : 0u;
+                    // Issue order: the 29 MMAs of a K step interleaved so that two
+                    // MMAs into the same accumulator are at least 3 apart, also
+                    // across consecutive K steps (an MMA waits for the previous
+                    // one into its accumulator). In a tile's first K step the
+                    // accumulators are taken as the epilogue releases them:
+                    // levels 7 and 8 (in the same interleaved order), then 2..6
+                    // one level at a time. Within a level the pairs are always in
+                    // increasing t (t = 8: the eighth digit, last), so each
+                    // accumulator sums its products in the same order.
+                    constexpr int kIssue = 29;
+                    constexpr int8_t kIssueT[kIssue] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 3, 2, 2, 3, 4, 3,
+                                                        1, 5, 4, 3, 4, 3, 6, 2, 5, 7, 5, 4, 6, 8};
+                    constexpr int8_t kIssueTp[kIssue] = {3, 5, 7, 6, 4, 6, 4, 2, 5, 5, 2, 3, 4, 4, 3,
+                                                         1, 3, 3, 2, 2, 1, 2, 1, 2, 1, 1, 1, 1, 1};
+                    auto mma_pair = [&](int t, int tp) {
+                        const int level = t + tp - 2;
+                        mma_f16(tmem + level * kTileN, a_desc + (t - 1) * (kRows * kKStep * 2 / 16),
+                                b_desc + (tp - 1) * (kTileN * kKStep * 2 / 16), idesc, t > 1 ? 1u : first);
+                    };
+                    auto mma_eighth = [&]() {
+                        mma_f16(tmem + (kLevels - 1) * kTileN, a_desc + kSlices * (kRows * kKStep * 2 / 16), b_desc,
+                                idesc, 1u);
+                    };
+                    if (ks == 0 && tile_cnt > 0) {
+                        ok = mbar_wait(&sh.acc_empty[kLevels - 2], (tile_cnt - 1) & 1) &&
+                             mbar_wait(&sh.acc_empty[kLevels - 1], (tile_cnt - 1) & 1);
+                        if (!ok) break;
+                        asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-                    for (int t = 1; t <= kSlices; ++t) {
+                        for (int i = 0; i < kIssue; ++i) {
+                            if (kIssueT[i] == 8) mma_eighth();
+                            else if (kIssueT[i] + kIssueTp[i] - 2 >= kLevels - 2) mma_pair(kIssueT[i], kIssueTp[i]);
+                        }
+                        issued = true;
 #pragma unroll
-                        for (int tp = 1; t + tp <= kLevels + 1; ++tp) {
-                            const int level = t + tp - 2;
-                            mma_f16(tmem + level * kTileN, a_desc + (t - 1) * (kRows * kKStep * 2 / 16),
-                                    b_desc + (tp - 1) * (kTileN * kKStep * 2 / 16), idesc, t > 1 ? 1u : first);
+                        for (int level = 0; level < kLevels - 2 && ok; ++level) {
+                            ok = mbar_wait(&sh.acc_empty[level], (tile_cnt - 1) & 1);
+                            if (!ok) break;
+                            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+                            for (int t = 1; t <= level + 1; ++t) mma_pair(t, level + 2 - t);
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < kIssue; ++i) {
+                            if (kIssueT[i] == 8) mma_eighth();
+                            else mma_pair(kIssueT[i], kIssueTp[i]);
                         }
                     }
-                    mma_f16(tmem + (kLevels - 1) * kTileN, a_desc + kSlices * (kRows * kKStep * 2 / 16), b_desc,
-                            idesc, 1u);
+                    issued = true;
+                    if (!ok) break;
                     mma_commit(&sh.a_empty[sa]);
                     mma_commit(&sh.b_empty[sb]);
                 }
+                if (!ok) break;
                 mma_commit(&sh.acc_full);
             }
+            if (!ok) sh.error = 1;
             // every MMA issued has completed before the columns are freed
-            if (tile_cnt > 0) {
+            if (issued) {
                 mma_commit(&sh.drain);
                 if (!mbar_wait(&sh.drain, 0)) sh.error = 1;
             }
