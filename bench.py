@@ -41,7 +41,7 @@ BATCH = 65536
 SPLIT_SLICE_PAIRS = 29  # tcgen05.mma per K step of the split assembly
 # DRAM bytes (read + write) of one split_assembly launch of the default
 # workload, from one ncu capture (profiles/split_assembly_8x8_d128_n10.md)
-SPLIT_ASSEMBLY_DRAM_BYTES = 12.481185e9 + 0.900138e9
+SPLIT_ASSEMBLY_DRAM_BYTES = 12.500385e9 + 0.901431e9
 ORDER = 10
 L2_FLUSH_BYTES = 512 << 20
 PRESET = "8x8-d128"
