@@ -455,6 +455,73 @@ def run_mcmcmc(args):
     print(json.dumps(out))
 
 
+def run_mixed(args):
+    """--mixed: a batch of uneven orders (a separate line, not the headline):
+    6x6 / U=4 / beta=5 / half lattice / degree 96, 64 chains x 256 proposals
+    = 16,384 configurations per step with orders 1..10 drawn from a truncated
+    geometric distribution (p = 0.3), through the device entry point with the
+    inputs resident; FP64 (bit-identical) and split forms. The FP64 CDet sorts
+    such a batch by order so that the lanes of a warp run equal-length
+    recursions."""
+    import torch
+    from cdet_gb300.integrand import CdetIntegrand
+    from cdet_gb300.params import CdetParams, half_lattice_mask
+    from cdet_gb300.synthetic import truncated_geometric_orders, uniform_configurations
+    from cdet_gb300.tables import build_tables
+    params = CdetParams(n1=6, n2=6, beta="5", mu="0", u="4", alpha_up="0", alpha_down="0",
+                        mask_sites=half_lattice_mask(6, 6), cheb_nu=96, cheb_nv=96)
+    batch, nmax = 64 * 256, 10
+    gpu = CdetIntegrand(params, build_tables(params, device="cuda"))
+    v = torch.from_numpy(uniform_configurations(20261203, batch, nmax)).cuda()
+    o = torch.from_numpy(truncated_geometric_orders(20261204, batch, 0.3, nmax)).cuda()
+    vals = torch.empty(batch, dtype=torch.float64, device="cuda")
+    st = torch.empty(batch, dtype=torch.int32, device="cuda")
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 512 MiB > L2
+    out = {"metric": "configs/s, mixed orders 1..10 (truncated geometric p=0.3)", "unit": "configs/s",
+           "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "config": {"workload": "6x6 Hubbard U=4 beta=5 half lattice, degree 96, 64 chains x 256 proposals "
+                                  "= 16,384 configurations per step, orders 1..10 truncated geometric p=0.3",
+                      "order_histogram": np.bincount(o.cpu().numpy(), minlength=nmax + 1)[1:].tolist(),
+                      "l2": "flushed between steps (512 MiB write)"},
+           "data": "synthetic (seeded uniform vertices, tables from the in-tree precompute)"}
+    values = {}
+    for path in ("fp64", "split"):
+        gpu.set_assembly(path)
+        for _ in range(args.warmup):
+            gpu.integrand_device(v, o, vals, st)
+        torch.cuda.synchronize()
+        total = 0.0
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            gpu.integrand_device(v, o, vals, st)
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        values[path] = vals.cpu().numpy().copy()
+        out[path] = {"value": batch * args.steps / (total / 1e3), "ms_per_step": total / args.steps,
+                     "gpu_launches": gpu.last_launch_count()}
+    out["value"] = out["split"]["value"]
+    # per order: relative error of each configuration, and the normwise error
+    # max |split - fp64| / max |fp64| over the configurations of that order
+    orders = o.cpu().numpy()
+    per_order = {}
+    for n in range(1, nmax + 1):
+        sel = orders == n
+        f, sp = values["fp64"][sel], values["split"][sel]
+        rel = np.abs(sp - f) / np.maximum(np.abs(f), 1e-300)
+        per_order[str(n)] = {"configs": int(sel.sum()), "median_rel": float(np.median(rel)),
+                             "p90_rel": float(np.percentile(rel, 90)),
+                             "normwise": float(np.abs(sp - f).max() / max(np.abs(f).max(), 1e-300)),
+                             "max_abs_fp64": float(np.abs(f).max()),
+                             "max_abs_diff": float(np.abs(sp - f).max())}
+    out["split_vs_fp64_err_by_order"] = per_order
+    out["note"] = ("order 1: twisted - 2 ordinary cancels, so its values are round-off residue of the "
+                   "diagonal terms (compare max_abs_diff with the other orders' magnitudes)")
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -472,11 +539,16 @@ def main():
     ap.add_argument("--mcmcmc", action="store_true",
                     help="time the device MCMCMC chains instead (a separate line, not the headline)")
     ap.add_argument("--chains", type=int, default=128, help="chains for --mcmcmc")
+    ap.add_argument("--mixed", action="store_true",
+                    help="time a batch of mixed orders 1..10 (a separate line, not the headline)")
     ap.add_argument("--mcmcmc-steps", type=int, default=2000, help="timed production steps for --mcmcmc")
     args = ap.parse_args()
     global PRESET, BATCH
     PRESET, BATCH = args.preset, args.batch
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
+    if args.mixed:
+        run_mixed(args)
+        return
     if args.mcmcmc:
         run_mcmcmc(args)
     elif args.impl == "reference":

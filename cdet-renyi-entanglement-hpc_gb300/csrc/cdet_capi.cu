@@ -438,7 +438,8 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         err = cdet::launch_fp64_assembly_only(p, w, stream);
         if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
     }
-    ctx->last_launches = launches;  // kernels of this library (the status reset is a memset)
+    if (!assembly_only && cdet::sorts_orders(p)) launches += 3;  // the order sort of a mixed batch
+    ctx->last_launches = launches;  // kernels of this library (the status and bucket resets are memsets)
     if (events) ctx->pending_launches += launches;
     return CDET_OK;
 }
@@ -528,7 +529,7 @@ int run_fp64_on_scratch(cdet_context* ctx, const double* vertices, const int32_t
     if (err != cudaSuccess) return cuda_fail(err, "cudaMemsetAsync(status)");
     err = launch_fp64_integrand(p, w, ctx->sm_count, stream, nullptr);
     if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
-    ctx->last_launches = 3;
+    ctx->last_launches = 3 + (sorts_orders(p) ? 3 : 0);
     return CDET_OK;
 }
 

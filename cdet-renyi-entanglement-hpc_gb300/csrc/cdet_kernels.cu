@@ -376,7 +376,8 @@ __global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_consta
         const double* su = ws + lay.shifted_up;
         const double* sd = one_spin ? su : ws + lay.shifted_down;
         // a[mask] = up[mask-1] * down[mask-1] (integrand_replica_randomly_sampled.h:254-257)
-        double* a = w.a_int + ((c >> 5) * 2 + set) * static_cast<int64_t>(full) * kWarp + (c & 31);
+        const int64_t slot = p.sorted ? __ldg(w.slot_of + c) : c;  // lane-interleaved position
+        double* a = w.a_int + ((slot >> 5) * 2 + set) * static_cast<int64_t>(full) * kWarp + (slot & 31);
         for (uint32_t m = lane; m < (1u << n); m += kWarp)
             a[static_cast<int64_t>(m) * kWarp] = m == 0 ? 0.0 : dmul(su[m], sd[m]);
         if (fb && lane == 0) atomicOr(p.status + c, kStatusFpmFallback);
@@ -464,16 +465,20 @@ __device__ __forceinline__ double order1_value(const Scalars& s, double su, doub
 
 __global__ void __launch_bounds__(128) cdet_fp64(const __grid_constant__ Problem p,
                                                 const __grid_constant__ Scratch w) {
-    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c >= p.batch) return;
-    const int lane = static_cast<int>(c & 31);
+    // one lane per slot; with p.sorted the slots hold the configurations
+    // in decreasing order, so the lanes of a warp run recursions of (nearly)
+    // equal length
+    const int64_t slot = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (slot >= p.batch) return;
+    const int64_t c = p.sorted ? __ldg(w.config_at + slot) : slot;
+    const int lane = static_cast<int>(slot & 31);
     const int nmax = p.max_order;
     const int64_t full = int64_t{1} << nmax;
     const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
     if (n < 1 || n > nmax) return;
     const Scalars& s = p.s;
     const double threshold = dmul(s.z_eps0, s.z_safety);
-    const int64_t g = c >> 5;
+    const int64_t g = slot >> 5;
     int32_t status = 0;
     const double* diag = w.diag + c * 2 * 2 * nmax;  // [set][spin][i]
 
@@ -809,6 +814,42 @@ cudaError_t launch_fp64_assembly_only(const Problem& p, const Scratch& w, cudaSt
     return cudaGetLastError();
 }
 
+// ------------------------------------------- order-sorted slots ----------
+// A counting sort of a mixed-order batch by decreasing order (invalid orders
+// last): config_at[slot] and slot_of[config]. Slots within one order follow
+// the atomics' arrival, which changes no value: every configuration is
+// computed by the same operations wherever it sits.
+__global__ void order_count(const int32_t* __restrict__ orders, int64_t batch, int max_order, uint32_t* count) {
+    for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < batch;
+         c += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int n = __ldg(orders + c);
+        const int b = (n < 1 || n > max_order) ? max_order + 1 : max_order - n;  // bucket 0: the top order
+        atomicAdd(count + b, 1u);
+    }
+}
+
+__global__ void order_scan(uint32_t* count, int buckets) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t run = 0;
+    for (int b = 0; b < buckets; ++b) {
+        const uint32_t k = count[b];
+        count[b] = run;  // first slot of the bucket, then its next free slot
+        run += k;
+    }
+}
+
+__global__ void order_scatter(const int32_t* __restrict__ orders, int64_t batch, int max_order, uint32_t* next,
+                              int32_t* __restrict__ slot_of, int32_t* __restrict__ config_at) {
+    for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < batch;
+         c += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int n = __ldg(orders + c);
+        const int b = (n < 1 || n > max_order) ? max_order + 1 : max_order - n;
+        const uint32_t slot = atomicAdd(next + b, 1u);
+        slot_of[c] = static_cast<int32_t>(slot);
+        config_at[slot] = static_cast<int32_t>(c);
+    }
+}
+
 size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps) {
     const size_t groups = static_cast<size_t>((batch + 31) / 32);
     const size_t n2 = static_cast<size_t>(max_order) * max_order;
@@ -819,7 +860,8 @@ size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps) {
     total += 2 * groups * 2 * subsets * kWarp;                      // a_int, dp_int
     total += ws_warps * minors_workspace_doubles(max_order);        // minors workspace
     total += ws_warps * kWarp * n2;                                 // LU fallback scratch
-    return total * sizeof(double) + 64 * 6;
+    total += 2 * ((static_cast<size_t>(batch) * 4 + 7) / 8) + 32;   // order-sorted slots, buckets
+    return total * sizeof(double) + 64 * 9;
 }
 
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out) {
@@ -839,11 +881,22 @@ void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Sc
     out->ws_global = take(ws_warps * minors_workspace_doubles(max_order));
     out->lu_scratch = take(ws_warps * kWarp * n2);
     out->ws_warps = ws_warps;
+    out->slot_of = reinterpret_cast<int32_t*>(take((static_cast<size_t>(batch) * 4 + 7) / 8));
+    out->config_at = reinterpret_cast<int32_t*>(take((static_cast<size_t>(batch) * 4 + 7) / 8));
+    out->order_count = reinterpret_cast<uint32_t*>(take(32));
 }
 
-cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_count,
+bool sorts_orders(const Problem& p) {
+    // the lane CDet of a single-order batch (the split path's warp CDet and the
+    // all-subsets forms have no lanes of different orders)
+    return !p.all_subsets && !(p.fused_cdet && p.max_order <= kWarpCdetMaxOrder);
+}
+
+cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_count,
                                   cudaStream_t stream, const KernelEvents* events, bool assembly) {
-    if (p.batch <= 0) return cudaSuccess;
+    if (p_in.batch <= 0) return cudaSuccess;
+    Problem p = p_in;
+    p.sorted = sorts_orders(p) ? 1 : 0;
     auto mark = [&](int k) {
         if (events && events->marks[k]) cudaEventRecord(events->marks[k], stream);
     };
@@ -860,6 +913,19 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& w, int sm_cou
         err = cudaGetLastError();
         if (err != cudaSuccess) return err;
         mark(2);
+    }
+
+    if (p.sorted) {
+        const int buckets = p.max_order + 2;
+        const unsigned grid = static_cast<unsigned>(std::min<int64_t>((p.batch + 255) / 256, 4 * 152));
+        err = cudaMemsetAsync(w.order_count, 0, 32 * sizeof(uint32_t), stream);
+        if (err != cudaSuccess) return err;
+        order_count<<<grid, 256, 0, stream>>>(p.orders, p.batch, p.max_order, w.order_count);
+        order_scan<<<1, 32, 0, stream>>>(w.order_count, buckets);
+        order_scatter<<<grid, 256, 0, stream>>>(p.orders, p.batch, p.max_order, w.order_count, w.slot_of,
+                                                w.config_at);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
     }
 
     // Minors: the per-warp workspace goes to shared memory when at least four

@@ -46,6 +46,9 @@ struct Scratch {
     double* ws_global;  // per-warp minors workspace when it does not fit shared memory
     double* lu_scratch; // per-lane LU fallback scratch, [warps][32][max_order^2]
     size_t ws_warps;    // warps the global workspace holds
+    int32_t* slot_of;   // [batch] order-sorted slot of each configuration (single-order FP64 CDet)
+    int32_t* config_at; // [batch] configuration in each slot
+    uint32_t* order_count;  // [64] counting-sort buckets
 };
 
 // all-subsets CDet work layouts, the values of the C ABI's CDET_FORM_*
@@ -64,6 +67,7 @@ struct Problem {
     int fused_cdet;           // 1: CDet pair updates as FMAs (split assembly); 0: the reference's
                               // separately rounded multiply, subtract and add
     int all_subsets_form;     // kFormAuto / kFormLane / kFormWarp (CDET_FORM_*, cdet_set_all_subsets_form)
+    int sorted;               // set by the launcher: minors and the lane CDet work in order-sorted slots
     DDPair pref_dd[2][kMaxOrder + 1];   // cdet_order_prefactor<DoubleDouble>, [set][order]
     double pref_ld[2][kMaxOrder + 1];   // cdet_order_prefactor<double> (host long double)
     double* values;
@@ -158,5 +162,8 @@ cudaError_t launch_diagonal_order1(const TableDev* const tables[4], int n1, int 
 
 cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& scratch, int sm_count,
                                   cudaStream_t stream, const KernelEvents* events, bool assembly = true);
+// Whether launch_fp64_integrand sorts the batch by order first (three more
+// kernels: the lane CDet of a single-order batch).
+bool sorts_orders(const Problem& p);
 
 }  // namespace cdet
