@@ -4,7 +4,10 @@
 // all-subset integrands through the reference-named free functions, write the
 // values for the Python side to compare with the golden vectors, and check
 // every subset of each all-subset envelope against an independent
-// single-order call within 2e-9 (the audit's tolerance).
+// single-order call within 2e-9 (the audit's tolerance). Then runs the
+// reference's histogram-seeded MCMCMC chains of the set through
+// McmcmcChains, with a checkpoint half-way, and writes their final state and
+// results.
 //
 // usage: adapter_check <dir>  (files written by tests/test_gpu_cpp_adapter.py)
 #include "cdet_gb300.hpp"
@@ -106,7 +109,49 @@ int main(int argc, char** argv) try {
         threw = true;
     }
     if (!threw) throw std::runtime_error("order 0 did not raise");
-    std::printf("PASS adapter_check: %zu single-order, %d subset checks\n", single.size(), checked);
+    // MCMCMC chains through the C++ class: the reference's histogram-seeded
+    // chains of this parameter set (tests/golden/mcmcmc_chains.*), a
+    // checkpoint at half the production steps, then the rest
+    const auto ints = read_all<int32_t>(dir + "/mc_ints.bin");  // omin omax env interval warmup production half bins
+    const auto rate = read_all<double>(dir + "/mc_rate.bin");
+    cdet_mcmcmc_config config{ints[0], ints[1], ints[2], ints[3], rate[0]};
+    const auto seeds = read_all<uint64_t>(dir + "/mc_seeds.bin");
+    cdet_gb300::McmcmcChains chains(gpu, config, seeds, read_all<double>(dir + "/mc_lambdas.bin"));
+    chains.set_histogram(ints[7], read_all<double>(dir + "/mc_tau.bin"), read_all<double>(dir + "/mc_space.bin"),
+                         read_all<double>(dir + "/mc_replica.bin"));
+    cdet_mcmcmc_run_info half{ints[0], ints[4], ints[6]};
+    chains.run_to(half, dir + "/ck_half");
+    cdet_mcmcmc_run_info full{ints[0], ints[4], ints[5]};
+    chains.run_to(full);
+    std::vector<double> verts, lambdas;
+    std::vector<uint64_t> rng;
+    chains.state(verts, lambdas, rng);
+    write_all(dir + "/mc_vertices_out.bin", verts);
+    write_all(dir + "/mc_lambdas_out.bin", lambdas);
+    write_all(dir + "/mc_rng_out.bin", rng);
+    std::vector<uint64_t> counts;
+    std::vector<double> means;
+    const int e1 = config.envelope_order + 1;
+    for (int64_t c = 0; c < chains.chains(); ++c) {
+        const cdet_mcmcmc_chain_result r = chains.result(c);
+        counts.insert(counts.end(), {r.seed, r.warmup_proposed_steps, r.warmup_accepted_steps,
+                                     r.production_proposed_steps, r.production_accepted_steps});
+        counts.insert(counts.end(), r.warmup_chosen_counts, r.warmup_chosen_counts + e1);
+        counts.insert(counts.end(), r.production_chosen_counts, r.production_chosen_counts + e1);
+        for (int o = 0; o < e1; ++o) means.push_back(static_cast<double>(r.order_signal_stats[o].mean));
+    }
+    write_all(dir + "/mc_counts_out.bin", counts);
+    write_all(dir + "/mc_means_out.bin", means);
+    const cdet_gb300::McmcmcSummary sum = chains.summary(config.order_min);
+    std::vector<double> ratios;
+    for (long double r : sum.ratios) ratios.push_back(static_cast<double>(r));
+    write_all(dir + "/mc_ratios_out.bin", ratios);
+    const cdet_mcmcmc_checkpoint ck = cdet_gb300::read_mcmcmc_checkpoint(dir + "/ck_half/chain_000000.chk");
+    if (ck.result.production_proposed_steps != static_cast<uint64_t>(ints[6]))
+        throw std::runtime_error("the half-way checkpoint has the wrong step count");
+
+    std::printf("PASS adapter_check: %zu single-order, %d subset checks, %lld chains\n", single.size(), checked,
+                static_cast<long long>(chains.chains()));
     return 0;
 } catch (const std::exception& error) {
     std::fprintf(stderr, "FAIL adapter_check: %s\n", error.what());
