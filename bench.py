@@ -135,9 +135,9 @@ def time_cpu_integrand(params, tables, vertices, orders, threads):
 
 def run_reference(args):
     """--impl reference: the CPU integrand timed on the host cores."""
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
+    from cdet_gb300 import replicas
+    if replicas.rank_info()[1] != 0:
+        return  # under torchrun, rank 0 alone times the host cores
     import torch
     from cdet_gb300.synthetic import uniform_configurations
     from cdet_gb300.tables import build_tables
@@ -179,12 +179,11 @@ def run_gpu(args):
     import torch
     import torch.distributed as dist
     from cdet_gb300.integrand import CdetIntegrand
-    from cdet_gb300.synthetic import derive_seed, uniform_configurations
+    from cdet_gb300.synthetic import uniform_configurations
     from cdet_gb300.tables import build_tables
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    from cdet_gb300 import replicas
+    world, rank, local_rank = replicas.rank_info()
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local_rank)
@@ -201,8 +200,7 @@ def run_gpu(args):
 
     # K + W distinct batches, resident in HBM before timing; each rank its own seeds
     n_batches = args.steps + args.warmup
-    host_batches = [uniform_configurations(derive_seed(20261203, 100 + rank, s), BATCH, ORDER)
-                    for s in range(n_batches)]
+    host_batches = [uniform_configurations(replicas.batch_seed(rank, s), BATCH, ORDER) for s in range(n_batches)]
     d_vertices = [torch.from_numpy(v).to(dev) for v in host_batches]
     d_orders = torch.full((BATCH,), ORDER, dtype=torch.int32, device=dev)
     d_values = torch.empty(BATCH, dtype=torch.float64, device=dev)
@@ -216,11 +214,7 @@ def run_gpu(args):
         torch.cuda.synchronize(dev)
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.max_over_ranks(x, world, dev)
 
     # the clock sampler starts before the warm-up so that nvidia-smi's start-up
     # is over when the timed regions begin
@@ -278,8 +272,8 @@ def run_gpu(args):
     e2e_match = bool(np.array_equal(pinned_out.numpy().view(np.uint64), values.view(np.uint64)))
 
     total_configs = BATCH * args.steps * world
-    value = total_configs / (elapsed_ms / 1e3)
-    e2e_value = total_configs / e2e_s
+    value = replicas.job_throughput(BATCH, args.steps, world, elapsed_ms / 1e3)
+    e2e_value = replicas.job_throughput(BATCH, args.steps, world, e2e_s)
     hbm_peak, bf16_peak, peak_kind = peaks()
     nu, nv = params.cheb_nu, params.cheb_nv
     lookups = BATCH * 2 * ORDER * ORDER  # table sets x entries (up and down share one table)
