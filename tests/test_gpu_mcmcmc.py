@@ -363,3 +363,44 @@ def test_large_batch_step_path(hist):
         assert np.array_equal(mt64_outputs(rng[c], 8), GOLD[f"{key}.rng"][c]), c
     assert _close(p["signal"].transpose(1, 0, 2)[:8], GOLD[f"{key}.signal"])
     chains.close()
+
+
+def _same_fields(a, b) -> bool:
+    if a.dtype.names is None:
+        return np.array_equal(a, b)
+    return all(_same_fields(a[n], b[n]) for n in a.dtype.names)
+
+
+def test_ring_wraps_and_call_boundaries():
+    """1,100 production steps (the step-output ring holds two halves of 256
+    steps for a small batch): one call and eleven calls of 100 steps record the
+    same steps, end in the same state and results, and choose the oracle
+    chain's masks step for step."""
+    from bindings import Oracle
+    name = "physical_2x2"
+    run = RUNS[name]
+    params, tables, _ = load_case(name)
+    gpu = CdetIntegrand(params, tables)
+    seeds = GOLD[f"{name}.seeds"][:4]
+    steps = 1100
+    outs, states, results = [], [], []
+    for calls in (1, 11):
+        chains = McmcmcChains(gpu, run["order_min"], run["order_max"], run["envelope"], seeds, run["lambdas"],
+                              run["adapt_interval"], run["adapt_rate"])
+        rec = [chains.run(steps // calls, warmup=False, record=True) for _ in range(calls)]
+        outs.append({k: np.concatenate([r[k] for r in rec]) for k in ("chosen", "norms", "signal")})
+        states.append(chains.state())
+        results.append(chains.results())
+        chains.close()
+    for k in ("chosen", "norms", "signal"):
+        assert np.array_equal(outs[0][k].view(np.uint64) if k != "chosen" else outs[0][k],
+                              outs[1][k].view(np.uint64) if k != "chosen" else outs[1][k]), k
+    for a, b in zip(states[0], states[1]):
+        assert np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
+    assert _same_fields(results[0], results[1])  # field by field: struct padding carries no data
+    assert np.all(results[0]["production_proposed_steps"] == steps)
+    orc = Oracle(params.runtime_scalars(), tables)
+    for c, seed in enumerate(seeds):
+        want = orc.mcmcmc_chain(run["order_min"], run["order_max"], run["envelope"], run["lambdas"], 0,
+                                run["adapt_interval"], run["adapt_rate"], steps, int(seed))
+        assert np.array_equal(outs[0]["chosen"][:, c], want["chosen"]), c
