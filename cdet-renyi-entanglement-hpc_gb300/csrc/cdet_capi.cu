@@ -255,9 +255,11 @@ int slice_branch(cdet_context* ctx, const double* coeffs, size_t blocks, SlicedB
 // up/down table, and per record the two branches.
 int build_split_plan(cdet_context* ctx, cdet::SplitPlan* plan) {
     const cdet_runtime_scalars& s = ctx->scalars;
-    if (s.cheb_nu > 128 || s.cheb_nv > 128)
-        return fail(CDET_ERR_INVALID, "split assembly needs CHEB_NU and CHEB_NV <= 128");
+    if (s.cheb_nu > cdet::kSplitMaxDegree || s.cheb_nv > cdet::kSplitMaxDegree)
+        return fail(CDET_ERR_INVALID, "split assembly needs CHEB_NU and CHEB_NV <= 256");
     *plan = cdet::SplitPlan{};
+    cdet::split_geometry(s.cheb_nu, s.cheb_nv, &plan->nrb, &plan->nkc, &plan->ksteps_last);
+    const size_t nsub = static_cast<size_t>(plan->nrb) * plan->nkc;
     const size_t sites2 = static_cast<size_t>(s.n1) * s.n2 * s.n1 * s.n2;
     const int kinds[2][2] = {{CDET_TWISTED_UP, CDET_TWISTED_DOWN}, {CDET_ORDINARY_UP, CDET_ORDINARY_DOWN}};
     uint32_t base = 0;
@@ -280,7 +282,7 @@ int build_split_plan(cdet_context* ctx, cdet::SplitPlan* plan) {
                 plan->slices[seg] = sb->slices;
                 plan->exponents[seg] = sb->exponents;
                 plan->segment_of[set][r][br] = seg;
-                base += static_cast<uint32_t>(blocks);
+                base += static_cast<uint32_t>(blocks * nsub);
                 ++seg;
             }
         }
@@ -288,7 +290,6 @@ int build_split_plan(cdet_context* ctx, cdet::SplitPlan* plan) {
     plan->segments = seg;
     plan->segment_base[seg] = base;
     plan->nblocks = base;
-    plan->ksteps = (s.cheb_nv + 15) / 16;
     return CDET_OK;
 }
 
@@ -303,7 +304,7 @@ int tune_all_subsets_form(cdet_context* ctx, cdet::Problem p, const cdet::Scratc
         cdet::SplitPlan plan;
         rc = build_split_plan(ctx, &plan);
         if (rc != CDET_OK) return rc;
-        const size_t need = cdet::split_scratch_bytes(p.batch, p.max_order, plan.nblocks);
+        const size_t need = cdet::split_scratch_bytes(p.batch, p.max_order, plan);
         if (need > ctx->split_scratch_bytes) {
             cudaDeviceSynchronize();
             if (ctx->split_scratch) cudaFree(ctx->split_scratch);
@@ -407,7 +408,7 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         cdet::SplitPlan plan;
         rc = build_split_plan(ctx, &plan);
         if (rc != CDET_OK) return rc;
-        const size_t need = cdet::split_scratch_bytes(batch, max_order, plan.nblocks);
+        const size_t need = cdet::split_scratch_bytes(batch, max_order, plan);
         if (need > ctx->split_scratch_bytes) {
             cudaDeviceSynchronize();
             if (ctx->split_scratch) cudaFree(ctx->split_scratch);
@@ -424,11 +425,12 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         if (err != cudaSuccess) return cuda_fail(err, "split assembly launch");
         if (events && events->marks[2]) cudaEventRecord(events->marks[2], stream);
         launches = 5 + 2;  // descriptors, scan, scatter, tiles, tensor assembly + minors, CDet
+        if (plan.nrb * plan.nkc > 1) ++launches;  // the sub-block combine
         if (!assembly_only) {
             err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events, false);
             if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
         } else {
-            launches = 5;
+            launches = 5 + (plan.nrb * plan.nkc > 1 ? 1 : 0);
         }
     } else if (!assembly_only) {
         err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events);
@@ -725,8 +727,9 @@ int cdet_set_assembly(cdet_context* ctx, int mode) {
     if (!ctx) return fail(CDET_ERR_INVALID, "null context");
     if (mode != CDET_ASSEMBLY_FP64 && mode != CDET_ASSEMBLY_SPLIT_BF16)
         return fail(CDET_ERR_INVALID, "unknown assembly mode");
-    if (mode == CDET_ASSEMBLY_SPLIT_BF16 && (ctx->scalars.cheb_nu > 128 || ctx->scalars.cheb_nv > 128))
-        return fail(CDET_ERR_INVALID, "split assembly needs CHEB_NU and CHEB_NV <= 128");
+    if (mode == CDET_ASSEMBLY_SPLIT_BF16 &&
+        (ctx->scalars.cheb_nu > cdet::kSplitMaxDegree || ctx->scalars.cheb_nv > cdet::kSplitMaxDegree))
+        return fail(CDET_ERR_INVALID, "split assembly needs CHEB_NU and CHEB_NV <= 256");
     if (ctx->assembly != mode) ++ctx->generation;
     ctx->assembly = mode;
     return CDET_OK;

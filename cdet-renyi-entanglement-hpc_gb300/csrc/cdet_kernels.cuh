@@ -92,14 +92,20 @@ struct SplitPlan {
     int records_per_set[2];         // 1 when up and down share one table, else 2
     int segment_of[2][2][2];        // [set][record][0 upper, 1 lower] -> segment
     int spin_mask[2][2];            // [set][record] -> spins the record writes
-    uint32_t nblocks;
-    int ksteps;                     // ceil(nv / 16)
+    uint32_t nblocks;               // sub-blocks over all segments (the keys of the lookup sort)
+    int nrb, nkc;                   // sub-blocks of a coefficient block: row chunks x column chunks of 128
+    int ksteps_last;                // K steps of the last column chunk (the others have 8)
 };
 
+// Sub-blocks of nu x nv coefficients, K steps of the last column chunk, and
+// the slice bytes of `blocks` blocks (each sub-block 128 rows x its K steps).
+void split_geometry(int nu, int nv, int* nrb, int* nkc, int* ksteps_last);
 size_t split_slices_bytes(int nu, int nv, size_t blocks);
 cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
                                int32_t* exponents, cudaStream_t stream);
-size_t split_scratch_bytes(int64_t batch, int max_order, uint32_t nblocks);
+size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan);
+// Largest CHEB_NU / CHEB_NV the split assembly takes (sub-blocks of 128 x 128).
+constexpr int kSplitMaxDegree = 256;
 cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const SplitPlan& plan, void* scratch,
                                   size_t scratch_bytes, int sm_count, int32_t** error_flag_out,
                                   cudaStream_t stream, const KernelEvents* events);

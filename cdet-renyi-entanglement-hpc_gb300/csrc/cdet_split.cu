@@ -38,6 +38,14 @@
 // three-stage shared-memory ring; the basis slices are generated in shared
 // memory by four producer warps while a single thread issues the MMAs and
 // four epilogue warps drain the previous tile.
+//
+// Degrees above 128 (up to 256) cut each coefficient block into sub-blocks of
+// 128 rows x 128 columns (the last ones shorter: the K steps of a column
+// chunk end at its last column, its rows are zero padded), which keeps every
+// exact level within K <= 128. A lookup becomes one record per sub-block; the
+// producers and the epilogue start the v and u recurrences at the
+// sub-block's first degree, every part is left as an exact 128-bit integer on
+// the block's common scale, and split_combine adds the parts and rounds once.
 #include "cdet_device.cuh"
 #include "cdet_kernels.cuh"
 
@@ -52,9 +60,11 @@ namespace {
 constexpr int kSlices = 7;          // slices of the basis operand
 constexpr int kSlicesA = 8;         // slices of the coefficient operand (the eighth pre-scaled by 2^-8)
 constexpr int kLevels = 7;          // accumulator levels tau = 2..8
+constexpr int kSubK = 128;          // K columns of one sub-block: keeps every exact level below 2^24
 constexpr int kTileN = 64;          // lookups per tile (MMA N)
 constexpr int kRows = 128;          // MMA M (Chebyshev rows a, zero padded)
 constexpr int kKStep = 16;          // MMA K (bf16)
+constexpr int kSubKSteps = kSubK / kKStep;  // K steps of a full column chunk
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
 
 // bytes of one A stage: 8 slices x 128 rows x 16 k x fp16
@@ -243,18 +253,31 @@ __device__ __forceinline__ int core_offset(int row, int k) {
 }
 
 // ---------------------------------------------------------- table slicing --
-// One block of nu x nv FP64 coefficients -> kSlicesA fp16 slices laid out as
-// [kstep][slice][core layout of 128 rows x 16 k], and the block exponent.
+// One sub-block (rows 128 rb.., columns 128 kc..) of a block of nu x nv FP64
+// coefficients -> kSlicesA fp16 slices laid out as [kstep][slice][core layout
+// of 128 rows x 16 k], and (by sub-block 0) the block exponent, taken over the
+// whole block so that all its sub-blocks share one scale. Degrees up to 128
+// make one sub-block per block; up to 256, two per dimension.
 // Within K step ks, position k holds column b = 16 ks + 2k (k < 8) or
 // 16 ks + 2(k - 8) + 1 (k >= 8), the order in which the basis threads produce
 // T_b(v). Slices 1..7 are integers q_t (weight 2^-8t); slice 8 is stored as
 // q_8 * 2^-8 (exact in fp16) so that its one product, with the first basis
 // slice, accumulates at level 8 with the right weight. Eight digits leave a
 // truncation of 2^-65 of the block scale per coefficient.
+__host__ __device__ __forceinline__ int row_ksteps(int nkc, int ksteps_last) {
+    return (nkc - 1) * kSubKSteps + ksteps_last;
+}
+
 __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ coeffs, int nu, int nv,
-                                                    int ksteps, uint16_t* __restrict__ out,
-                                                    int32_t* __restrict__ exponents) {
-    const int64_t block = blockIdx.x;
+                                                    int nrb, int nkc, int ksteps_last,
+                                                    uint16_t* __restrict__ out, int32_t* __restrict__ exponents) {
+    const int nsub = nrb * nkc;
+    const int64_t block = blockIdx.x / nsub;
+    const int sub = static_cast<int>(blockIdx.x - block * nsub);
+    const int rb = sub / nkc, kc = sub - (sub / nkc) * nkc;
+    const int row0 = rb * kRows, col0 = kc * kSubK;
+    const int ksteps = kc == nkc - 1 ? ksteps_last : kSubKSteps;
+    const int rk = row_ksteps(nkc, ksteps_last);
     const double* c = coeffs + block * static_cast<int64_t>(nu) * nv;
     __shared__ double red[256];
     double m = 0.0;
@@ -267,13 +290,14 @@ __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ c
     }
     int e = 0;
     if (red[0] > 0.0) frexp(red[0], &e);  // max < 2^e
-    if (threadIdx.x == 0) exponents[block] = e;
-    uint16_t* dst = out + block * static_cast<int64_t>(ksteps) * kSlicesA * kRows * kKStep;
+    if (threadIdx.x == 0 && sub == 0) exponents[block] = e;
+    uint16_t* dst = out + ((block * nrb + rb) * rk + static_cast<int64_t>(kc) * kSubKSteps) * (kAStageBytes / 2);
     const int total = kRows * ksteps * kKStep;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
         const int a = i / (ksteps * kKStep);
         const int b = i - a * (ksteps * kKStep);
-        double r = (a < nu && b < nv) ? ldexp(c[a * nv + b], -e) : 0.0;  // |r| < 1
+        const int ag = row0 + a, bg = col0 + b;
+        double r = (ag < nu && bg < nv) ? ldexp(c[ag * nv + bg], -e) : 0.0;  // |r| < 1
         const int ks = b / kKStep, bb = b - ks * kKStep;
         const int k = (bb & 1) * 8 + (bb >> 1);
         uint16_t* base = dst + static_cast<int64_t>(ks) * kSlicesA * kRows * kKStep + core_offset(a, k);
@@ -322,9 +346,10 @@ __device__ __forceinline__ double clamp_unit_s(double value) {
 }
 
 // One thread per (configuration, i, j): branch and (u, v) are shared by both
-// table sets; the corner path is evaluated here, every other lookup becomes a
-// record keyed by its coefficient block. Record slots are fixed:
-// ((c * nmax^2 + pair) * 2 + set) * 2 + spin_record.
+// table sets; the corner path is evaluated here, every other lookup becomes
+// one record per sub-block of its coefficient block, keyed by the sub-block.
+// Record slots are fixed: (((c * nmax^2 + pair) * 2 + set) * 2 + spin_record)
+// * nsub + sub.
 __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__ Problem p,
                                                          const __grid_constant__ Scratch w,
                                                          const __grid_constant__ SplitPlan plan,
@@ -336,8 +361,9 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
     const int64_t c = idx / per_c;
     const int pair = static_cast<int>(idx - c * per_c);
     const int i = pair / nmax, j = pair - (pair / nmax) * nmax;
-    const int64_t slot0 = idx * 4;
-    for (int k = 0; k < 4; ++k) rec.key[slot0 + k] = kNoKey;
+    const int nsub = plan.nrb * plan.nkc;
+    const int64_t slot0 = idx * 4 * nsub;
+    for (int k = 0; k < 4 * nsub; ++k) rec.key[slot0 + k] = kNoKey;
     const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
     if (n < 1 || n > nmax) {
         if (pair == 0) atomicOr(p.status + c, kStatusBadInput);
@@ -394,13 +420,16 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
         }
         for (int r = 0; r < plan.records_per_set[set]; ++r) {
             const int seg = plan.segment_of[set][r][upper ? 0 : 1];
-            const uint32_t key = plan.segment_base[seg] + static_cast<uint32_t>(sitepair);
-            const int64_t slot = slot0 + set * 2 + r;
-            rec.key[slot] = key;
-            rec.u[slot] = u;
-            rec.v[slot] = v;
-            rec.info[slot] = pack_info(c, set, plan.spin_mask[set][r], i, j, n);
-            atomicAdd(counts + key, 1u);
+            const uint64_t info = pack_info(c, set, plan.spin_mask[set][r], i, j, n);
+            for (int sub = 0; sub < nsub; ++sub) {
+                const uint32_t key = plan.segment_base[seg] + static_cast<uint32_t>(sitepair * nsub + sub);
+                const int64_t slot = slot0 + (set * 2 + r) * nsub + sub;
+                rec.key[slot] = key;
+                rec.u[slot] = u;
+                rec.v[slot] = v;
+                rec.info[slot] = info;
+                atomicAdd(counts + key, 1u);
+            }
         }
     }
 }
@@ -513,7 +542,8 @@ struct TileMeta {
     uint64_t info[kTileN];
     uint32_t count;
     int32_t exponent;
-    uint32_t pad[2];
+    int32_t sub;
+    uint32_t pad;
 };
 
 struct SplitShared {
@@ -559,13 +589,87 @@ __device__ __forceinline__ bool failed(const SplitShared& sh) {
     return *static_cast<const volatile uint32_t*>(&sh.error) != 0;
 }
 
-__device__ __forceinline__ void tile_source(const SplitPlan& plan, uint32_t block, int ksteps,
-                                            const uint16_t** a_src, int* exponent) {
+// Where the lookups of sort key `key` (one sub-block of one coefficient block)
+// find their coefficient slices, the block exponent, and the sub-block's
+// place: sub = rb * nkc + kc covers rows 128 rb.. and columns 128 kc.. in
+// `ksteps` K steps.
+struct TileSource {
+    const uint16_t* a;
+    int exponent, sub, rb, kc, ksteps;
+};
+template <bool Chunked>
+__device__ __forceinline__ TileSource tile_source(const SplitPlan& plan, uint32_t key) {
     int seg = 0;
-    while (seg + 1 < plan.segments && block >= plan.segment_base[seg + 1]) ++seg;
-    const uint32_t local = block - plan.segment_base[seg];
-    *a_src = plan.slices[seg] + static_cast<int64_t>(local) * ksteps * (kAStageBytes / 2);
-    *exponent = plan.exponents[seg][local];
+    while (seg + 1 < plan.segments && key >= plan.segment_base[seg + 1]) ++seg;
+    const uint32_t local = key - plan.segment_base[seg];
+    if constexpr (!Chunked) {  // one sub-block per block
+        TileSource t;
+        t.sub = t.rb = t.kc = 0;
+        t.ksteps = plan.ksteps_last;
+        t.a = plan.slices[seg] + static_cast<int64_t>(local) * plan.ksteps_last * (kAStageBytes / 2);
+        t.exponent = plan.exponents[seg][local];
+        return t;
+    }
+    const uint32_t nsub = static_cast<uint32_t>(plan.nrb * plan.nkc);
+    const uint32_t block = local / nsub;
+    TileSource t;
+    t.sub = static_cast<int>(local - block * nsub);
+    t.rb = t.sub / plan.nkc;
+    t.kc = t.sub - t.rb * plan.nkc;
+    t.ksteps = t.kc == plan.nkc - 1 ? plan.ksteps_last : kSubKSteps;
+    const int rk = row_ksteps(plan.nkc, plan.ksteps_last);
+    t.a = plan.slices[seg] +
+          ((static_cast<int64_t>(block) * plan.nrb + t.rb) * rk + static_cast<int64_t>(t.kc) * kSubKSteps) *
+              (kAStageBytes / 2);
+    t.exponent = plan.exponents[seg][block];
+    return t;
+}
+
+// Column chunk of sort key `key` and its K steps, without the slice address
+// (constant when the columns make one chunk).
+__device__ __forceinline__ int tile_kc(const SplitPlan& plan, uint32_t key) {
+    if (plan.nkc == 1) return 0;
+    int seg = 0;
+    while (seg + 1 < plan.segments && key >= plan.segment_base[seg + 1]) ++seg;
+    const uint32_t nsub = static_cast<uint32_t>(plan.nrb * plan.nkc);
+    return static_cast<int>(((key - plan.segment_base[seg]) % nsub) % static_cast<uint32_t>(plan.nkc));
+}
+__device__ __forceinline__ int chunk_ksteps(const SplitPlan& plan, int kc) {
+    return kc == plan.nkc - 1 ? plan.ksteps_last : kSubKSteps;
+}
+
+// The Green entries of one lookup's value (both spins of a shared record),
+// with the diagonal shift and the scale, as the FP64 assembly writes them.
+__device__ __forceinline__ void store_green(const Problem& p, const Scratch& w, uint64_t info, double value) {
+    const int nmax = p.max_order;
+    const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
+    const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
+    const int set = static_cast<int>((info >> 32) & 1);
+    const int spins = static_cast<int>((info >> 33) & 3);
+    const int i = static_cast<int>((info >> 35) & 31);
+    const int jj = static_cast<int>((info >> 40) & 31);
+    const int n = static_cast<int>((info >> 45) & 31);
+    const int64_t mslot = (c * 2 + set) * 2;
+    for (int spin = 0; spin < 2; ++spin) {
+        if (!(spins & (1 << spin))) continue;
+        double g = value;
+        if (i == jj) {
+            g = dadd(g, spin == 0 ? p.s.diag_up_shift : p.s.diag_down_shift);
+            w.diag[(mslot + spin) * nmax + i] = g;
+        }
+        w.green[(mslot + spin) * per_c + i * n + jj] = dmul(g, p.s.scale);
+    }
+}
+
+// Record slot of a lookup's sub-block part (the slot its descriptor filled).
+__device__ __forceinline__ int64_t part_slot(uint64_t info, int nmax, int nsub, int sub) {
+    const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
+    const int set = static_cast<int>((info >> 32) & 1);
+    const int spins = static_cast<int>((info >> 33) & 3);
+    const int i = static_cast<int>((info >> 35) & 31);
+    const int jj = static_cast<int>((info >> 40) & 31);
+    const int record = spins == 2 ? 1 : 0;  // the spin-down record of a set with two tables
+    return (((c * nmax + i) * nmax + jj) * 4 + set * 2 + record) * nsub + sub;
 }
 
 // T_parity, T_{parity+2}, T_{parity+4}, ... of x in Q62 fixed point, by the
@@ -610,19 +714,20 @@ struct ChebStride2 {
     }
 };
 
+template <bool Chunked>
 __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __grid_constant__ Problem p,
                                                                       const __grid_constant__ Scratch w,
                                                                       const __grid_constant__ SplitPlan plan,
                                                                       const SplitRecordArrays sorted,
                                                                       const SplitTile* __restrict__ tiles,
                                                                       const uint32_t* __restrict__ totals,
+                                                                      int64_t* __restrict__ parts,
                                                                       int32_t* __restrict__ error_flag) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SplitShared& sh = *reinterpret_cast<SplitShared*>(smem_raw);
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
     const int lane = tid & 31;
-    const int ksteps = plan.ksteps;
     const uint32_t ntiles = totals[1];
     // each CTA takes a contiguous range of the block-sorted tile list, so the
     // later tiles of a coefficient block find its slices in L2
@@ -681,15 +786,21 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 sh.meta[mb].info[l] = live ? sorted.info[tl.start + l] : ~uint64_t{0};
             }
             if (tid == 0) {
-                const uint16_t* a_src;
-                int exponent;
-                tile_source(plan, tl.block, ksteps, &a_src, &exponent);
+                const TileSource src = tile_source<Chunked>(plan, tl.block);
                 sh.meta[mb].count = tl.count;
-                sh.meta[mb].exponent = exponent;
+                sh.meta[mb].exponent = src.exponent;
+                sh.meta[mb].sub = src.sub;
             }
             mbar_arrive(&sh.meta_full[mb]);
+            int ksteps = plan.ksteps_last, b0 = 0;
             ChebStride2 cheb;
             cheb.init(fixed_from_double(v, 62), h);
+            if constexpr (Chunked) {
+                const int kc = tile_kc(plan, tl.block);
+                ksteps = chunk_ksteps(plan, kc);
+                b0 = kc * kSubK;
+                for (int k = 0; k < kc * kSubK / 2; ++k) cheb.next();  // to degree 128 kc + h
+            }
             for (int ks = 0; ks < ksteps; ++ks, ++b_cnt) {
                 const int sb = static_cast<int>(b_cnt % kBStages);
                 if (b_cnt >= kBStages && !mbar_wait(&sh.b_empty[sb], ((b_cnt / kBStages) - 1) & 1)) {
@@ -700,7 +811,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 uint64_t y[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    const int b = ks * kKStep + 2 * j + h;
+                    const int b = b0 + ks * kKStep + 2 * j + h;
                     const int64_t tb = cheb.next();
                     const int64_t x = b < p.s.nv ? (tb + 32) >> 6 : 0;  // Q56
                     y[j] = static_cast<uint64_t>(x) + kDigitBias;
@@ -726,7 +837,6 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         const uint32_t lane_base = tmem + (static_cast<uint32_t>((warp & 3) * 32) << 16);
         const int nu = p.s.nu;
         const int nmax = p.max_order;
-        const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
         int64_t* red = sh.red[group];
         uint32_t tile_cnt = 0;
         for (uint32_t tile = tile_begin; tile < tile_end; ++tile, ++tile_cnt) {
@@ -746,9 +856,14 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 const int l = 16 * (we & 3) + (lane & 15), r = 2 * (we >> 2) + (lane >> 4);
                 ChebStride4 cheb;
                 cheb.init(fixed_from_double(meta.u[l], 62), r);
+                int a0 = 0;  // first row of the sub-block
+                if constexpr (Chunked) {
+                    a0 = (meta.sub / plan.nkc) * kRows;
+                    for (int k = 0; k < a0 / 4; ++k) cheb.next();  // to degree a0 + r
+                }
                 for (int a = r; a < kRows; a += 4) {
                     const int64_t ta = cheb.next();
-                    sh.ubasis[l * kRows + (a ^ (l & 31))] = a < nu ? ta : 0;
+                    sh.ubasis[l * kRows + (a ^ (l & 31))] = a0 + a < nu ? ta : 0;
                 }
             }
             const bool acc_ok = mbar_wait(&sh.acc_full, tile_cnt & 1);
@@ -853,26 +968,19 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 group_sync(group);
             }
             // finalisation: the group's first warp, one lookup per lane, so
-            // that the few FP64 operations are issued once per 32 lookups
+            // that the few FP64 operations are issued once per 32 lookups. A
+            // block of several sub-blocks leaves its exact 128-bit part for
+            // the combine kernel instead.
             const int l = group * kGroupLookups + row;
             if (row < kGroupLookups && static_cast<uint32_t>(l) < count) {
-                const double value = int128_to_double(sh.sums[l][1], static_cast<uint64_t>(sh.sums[l][0]), exponent - 55);
                 const uint64_t info = meta.info[l];
-                const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
-                const int set = static_cast<int>((info >> 32) & 1);
-                const int spins = static_cast<int>((info >> 33) & 3);
-                const int i = static_cast<int>((info >> 35) & 31);
-                const int jj = static_cast<int>((info >> 40) & 31);
-                const int n = static_cast<int>((info >> 45) & 31);
-                const int64_t mslot = (c * 2 + set) * 2;
-                for (int spin = 0; spin < 2; ++spin) {
-                    if (!(spins & (1 << spin))) continue;
-                    double g = value;
-                    if (i == jj) {
-                        g = dadd(g, spin == 0 ? p.s.diag_up_shift : p.s.diag_down_shift);
-                        w.diag[(mslot + spin) * nmax + i] = g;
-                    }
-                    w.green[(mslot + spin) * per_c + i * n + jj] = dmul(g, p.s.scale);
+                if constexpr (!Chunked) {
+                    store_green(p, w, info,
+                                int128_to_double(sh.sums[l][1], static_cast<uint64_t>(sh.sums[l][0]), exponent - 55));
+                } else {
+                    const int64_t slot = part_slot(info, nmax, plan.nrb * plan.nkc, meta.sub);
+                    parts[2 * slot] = sh.sums[l][0];
+                    parts[2 * slot + 1] = sh.sums[l][1];
                 }
             }
             group_sync(group);  // sums are reused by the next tile
@@ -883,18 +991,15 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         if (lane == 0) {
             uint32_t a_cnt = 0;
             for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile) {
-                const SplitTile tl = tiles[tile];
-                const uint16_t* a_src;
-                int exponent;
-                tile_source(plan, tl.block, ksteps, &a_src, &exponent);
-                for (int ks = 0; ks < ksteps; ++ks, ++a_cnt) {
+                const TileSource src = tile_source<Chunked>(plan, tiles[tile].block);
+                for (int ks = 0; ks < src.ksteps; ++ks, ++a_cnt) {
                     const int st = static_cast<int>(a_cnt % kAStages);
                     if (a_cnt >= kAStages && !mbar_wait(&sh.a_empty[st], ((a_cnt / kAStages) - 1) & 1)) {
                         sh.error = 1;
                         break;
                     }
                     mbar_expect_tx(&sh.a_full[st], kAStageBytes);
-                    bulk_copy_g2s(sh.a_ring[st], a_src + static_cast<int64_t>(ks) * (kAStageBytes / 2),
+                    bulk_copy_g2s(sh.a_ring[st], src.a + static_cast<int64_t>(ks) * (kAStageBytes / 2),
                                   kAStageBytes, &sh.a_full[st]);
                 }
             }
@@ -911,7 +1016,14 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
             const uint32_t idesc = mma_idesc(kRows, kTileN);
             uint32_t a_cnt = 0, b_cnt = 0, tile_cnt = 0;
             bool ok = true, issued = false;
+            // with several column chunks the K steps vary by tile: the next
+            // tile's key is loaded while this one's MMAs are issued
+            const bool chunked = Chunked && plan.nkc > 1;
+            uint32_t next_key = chunked && tile_begin < tile_end ? tiles[tile_begin].block : 0;
             for (uint32_t tile = tile_begin; ok && tile < tile_end && !failed(sh); ++tile, ++tile_cnt) {
+                const uint32_t key = next_key;
+                if (chunked && tile + 1 < tile_end) next_key = tiles[tile + 1].block;
+                const int ksteps = chunked ? chunk_ksteps(plan, tile_kc(plan, key)) : plan.ksteps_last;
                 for (int ks = 0; ok && ks < ksteps; ++ks, ++a_cnt, ++b_cnt) {
                     const int sa = static_cast<int>(a_cnt % kAStages);
                     const int sb = static_cast<int>(b_cnt % kBStages);
@@ -1001,28 +1113,70 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
     }
 }
 
+// One thread per (configuration, i, j) of a table with several sub-blocks per
+// coefficient block: each lookup's parts, exact 128-bit integers on the
+// block's common scale, are summed (exactly, so the order does not matter)
+// and rounded once, then stored as the single-sub-block finalisation does.
+__global__ void __launch_bounds__(128) split_combine(const __grid_constant__ Problem p,
+                                                     const __grid_constant__ Scratch w,
+                                                     const __grid_constant__ SplitPlan plan,
+                                                     const SplitRecordArrays rec,
+                                                     const int64_t* __restrict__ parts) {
+    const int64_t per_c = static_cast<int64_t>(p.max_order) * p.max_order;
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= p.batch * per_c) return;
+    const int nsub = plan.nrb * plan.nkc;
+    for (int k = 0; k < 4; ++k) {
+        const int64_t base = (idx * 4 + k) * nsub;
+        const uint32_t key = rec.key[base];
+        if (key == kNoKey) continue;
+        uint64_t lo = 0;
+        int64_t hi = 0;
+        for (int sub = 0; sub < nsub; ++sub) {
+            const uint64_t plo = static_cast<uint64_t>(parts[2 * (base + sub)]);
+            const uint64_t nlo = lo + plo;
+            hi += parts[2 * (base + sub) + 1] + (nlo < lo ? 1 : 0);
+            lo = nlo;
+        }
+        store_green(p, w, rec.info[base], int128_to_double(hi, lo, tile_source<true>(plan, key).exponent - 55));
+    }
+}
+
 }  // namespace
 
+void split_geometry(int nu, int nv, int* nrb, int* nkc, int* ksteps_last) {
+    *nrb = (nu + kRows - 1) / kRows;
+    *nkc = (nv + kSubK - 1) / kSubK;
+    *ksteps_last = (nv - (*nkc - 1) * kSubK + kKStep - 1) / kKStep;
+}
+
 size_t split_slices_bytes(int nu, int nv, size_t blocks) {
-    const int ksteps = (nv + kKStep - 1) / kKStep;
-    return blocks * static_cast<size_t>(ksteps) * kAStageBytes;
+    int nrb, nkc, ksteps_last;
+    split_geometry(nu, nv, &nrb, &nkc, &ksteps_last);
+    return blocks * nrb * static_cast<size_t>(row_ksteps(nkc, ksteps_last)) * kAStageBytes;
 }
 
 cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
                                int32_t* exponents, cudaStream_t stream) {
     if (blocks == 0) return cudaSuccess;
-    const int ksteps = (nv + kKStep - 1) / kKStep;
-    slice_blocks<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(coeffs, nu, nv, ksteps, slices, exponents);
+    int nrb, nkc, ksteps_last;
+    split_geometry(nu, nv, &nrb, &nkc, &ksteps_last);
+    const size_t grid = blocks * nrb * nkc;
+    if (grid > 0x7FFFFFFFu) return cudaErrorInvalidValue;
+    slice_blocks<<<static_cast<unsigned>(grid), 256, 0, stream>>>(coeffs, nu, nv, nrb, nkc, ksteps_last, slices,
+                                                                  exponents);
     return cudaGetLastError();
 }
 
-size_t split_scratch_bytes(int64_t batch, int max_order, uint32_t nblocks) {
-    const size_t nrec = static_cast<size_t>(batch) * max_order * max_order * 4;
+size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan) {
+    const size_t nsub = static_cast<size_t>(plan.nrb) * plan.nkc;
+    const size_t nrec = static_cast<size_t>(batch) * max_order * max_order * 4 * nsub;
     size_t total = 0;
     total += nrec * (4 + 8 + 8 + 8);          // unsorted records
     total += nrec * (8 + 8 + 8);              // sorted records
-    total += static_cast<size_t>(nblocks) * 4 * 4;  // counts, offsets, tile offsets, cursors
-    total += (nrec / kTileN + nblocks + 1) * sizeof(SplitTile);  // tiles
+    total += static_cast<size_t>(plan.nblocks) * 4 * 4;  // counts, offsets, tile offsets, cursors
+    total += (nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile);  // tiles
+    if (nsub > 1) total += nrec * 16;         // 128-bit sub-block parts
     total += 64;                              // totals, error flag
     return total + 16 * 256;
 }
@@ -1031,7 +1185,8 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
                                   size_t scratch_bytes, int sm_count, int32_t** error_flag_out,
                                   cudaStream_t stream, const KernelEvents* events) {
     const int64_t pairs = p.batch * static_cast<int64_t>(p.max_order) * p.max_order;
-    const int64_t nrec = pairs * 4;
+    const int nsub = plan.nrb * plan.nkc;
+    const int64_t nrec = pairs * 4 * nsub;
     char* cursor = static_cast<char*>(scratch);
     auto take = [&](size_t bytes) {
         void* ptr = cursor;
@@ -1047,6 +1202,7 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     uint32_t* tile_offsets = static_cast<uint32_t*>(take(plan.nblocks * 4u));
     uint32_t* cursors = static_cast<uint32_t*>(take(plan.nblocks * 4u));
     SplitTile* tiles = static_cast<SplitTile*>(take((nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile)));
+    int64_t* parts = nsub > 1 ? static_cast<int64_t*>(take(nrec * 16)) : nullptr;
     uint32_t* totals = static_cast<uint32_t*>(take(16));
     int32_t* error_flag = static_cast<int32_t*>(take(16));
     if (static_cast<size_t>(cursor - static_cast<char*>(scratch)) > scratch_bytes) return cudaErrorInvalidValue;
@@ -1068,10 +1224,16 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     if (events && events->marks[1]) cudaEventRecord(events->marks[1], stream);
     const size_t smem = sizeof(SplitShared);
-    err = cudaFuncSetAttribute(split_assembly, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    auto kernel = nsub > 1 ? split_assembly<true> : split_assembly<false>;
+    err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (err != cudaSuccess) return err;
-    split_assembly<<<sm_count, kAssemblyThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, error_flag);
-    return cudaGetLastError();
+    kernel<<<sm_count, kAssemblyThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, parts, error_flag);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if (nsub > 1) {
+        split_combine<<<static_cast<unsigned>((pairs + 127) / 128), 128, 0, stream>>>(p, w, plan, rec, parts);
+        err = cudaGetLastError();
+    }
+    return err;
 }
 
 }  // namespace cdet

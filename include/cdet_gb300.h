@@ -378,7 +378,8 @@ enum cdet_assembly_mode {
      * grouped by coefficient block, each block's Chebyshev contraction as
      * eight-slice bf16 products with exact FP32 accumulation and an integer
      * epilogue (FP64-level accuracy, not bit-identical). Minors and the CDet
-     * recursion stay FP64. Needs CHEB_NU and CHEB_NV <= 128. */
+     * recursion stay FP64. Needs CHEB_NU and CHEB_NV <= 256 (degrees above
+     * 128 run as sub-blocks of at most 128 x 128 coefficients). */
     CDET_ASSEMBLY_SPLIT_BF16 = 1
 };
 

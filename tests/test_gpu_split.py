@@ -119,3 +119,45 @@ def test_split_deterministic_and_full_path():
     a_, b_ = sa[:, singles], fa[:, singles]
     close = np.abs(a_ - b_) / np.maximum(1.0, np.maximum(np.abs(a_), np.abs(b_)))
     assert np.max(close) <= 1e-13
+
+
+@pytest.mark.parametrize("nu,nv", [(160, 160), (192, 192), (256, 256), (136, 200), (200, 100)])
+def test_split_sub_blocks_match_fp64(nu, nv):
+    """Degrees above 128: each coefficient block is assembled as sub-blocks
+    of at most 128 rows x 128 columns whose exact parts are added before one
+    rounding. Non-square degrees cut rows and columns differently. The FP64
+    Clenshaw sum's own round-off grows with the degree, so the bound scales
+    with it."""
+    params = CdetParams(n1=3, n2=3, beta="6", mu="0", u="2",
+                        mask_sites=named_mask("first_column", 3, 3), cheb_nu=nu, cheb_nv=nv)
+    tables = build_tables(params, device="cuda")
+    v = uniform_configurations(900 + nu + nv, 192, 7)
+    orders = np.full(192, 7, dtype=np.int32)
+    orders[::5] = 1
+    gpu, g64, d64, gsp, dsp = _green_both(params, tables, v, orders)
+    tol = GREEN_TOL * max(nu, nv) / 128
+    worst = 0.0
+    for c, n in enumerate(orders):
+        for set_ in range(2):
+            for spin in range(2):
+                a = g64[c, set_, spin, : n * n]
+                b = gsp[c, set_, spin, : n * n]
+                scale = max(np.max(np.abs(a)), 1e-300)
+                worst = max(worst, np.max(np.abs(a - b)) / scale)
+    print(f"degree {nu}x{nv}: max |G_split - G_fp64| / max|G| = {worst:.3e}")
+    assert worst <= tol
+    gpu.set_assembly("split")
+    split_vals, st = gpu.integrand_batch(v, orders)
+    gpu.set_assembly("fp64")
+    ref, st64 = gpu.integrand_batch(v, orders)
+    assert st.max() == 0 and st64.max() == 0
+    close = np.abs(split_vals - ref) / np.maximum(1.0, np.maximum(np.abs(split_vals), np.abs(ref)))
+    assert np.max(close[orders == 1]) <= 1e-13
+
+
+def test_split_refuses_degree_above_256():
+    params = CdetParams(n1=2, n2=2, beta="2", mu="0", u="2",
+                        mask_sites=named_mask("first_column", 2, 2), cheb_nu=264, cheb_nv=32)
+    gpu = CdetIntegrand(params, build_tables(params, device="cuda"))
+    with pytest.raises(Exception, match="<= 256"):
+        gpu.set_assembly("split")
