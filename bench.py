@@ -516,6 +516,146 @@ def run_mixed(args):
     print(json.dumps(out))
 
 
+def run_stress(args):
+    """--stress: the high-order stress case (a separate line, not the
+    headline): 12x12 lattice, t=1, U=6, beta=10, mu=-0.5, subsystem A = the
+    6x12 half lattice, Chebyshev degree 192, 8,192 configurations at order 14
+    per step. Degree 192 runs the split assembly as 2 x 2 sub-blocks of each
+    coefficient block. The tables (98 GB in the reference layout) and their
+    split slices (163 GB) are resident together; the FP64 and split forms
+    are timed on the same batches."""
+    import torch
+    from cdet_gb300.integrand import CdetIntegrand
+    from cdet_gb300.params import CdetParams, half_lattice_mask
+    from cdet_gb300.synthetic import uniform_configurations
+    from cdet_gb300.tables import build_tables
+    params = CdetParams(n1=12, n2=12, beta="10", mu="-0.5", u="6", alpha_up="0", alpha_down="0",
+                        mask_sites=half_lattice_mask(12, 12), cheb_nu=192, cheb_nv=192)
+    batch, order = args.batch if args.batch != 65536 else 8192, 14
+    t0 = time.perf_counter()
+    tables = build_tables(params, device="cuda")
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    torch.cuda.empty_cache()  # the precompute's temporaries; the slices are allocated outside torch
+    gpu = CdetIntegrand(params, tables)
+    gpu.reserve(batch, order)
+    gpu.set_assembly("split")
+    t0 = time.perf_counter()
+    gpu.prepare_split()
+    slice_s = time.perf_counter() - t0
+    free_b, total_b = torch.cuda.mem_get_info()
+    n_batches = args.steps + args.warmup
+    host = [uniform_configurations(20261210 + k, batch, order) for k in range(n_batches)]
+    dv = [torch.from_numpy(x).cuda() for x in host]
+    o = torch.full((batch,), order, dtype=torch.int32, device="cuda")
+    vals = torch.empty(batch, dtype=torch.float64, device="cuda")
+    st = torch.empty(batch, dtype=torch.int32, device="cuda")
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 512 MiB > L2
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(2.0)
+    results = {}
+    for path in ("fp64", "split"):
+        gpu.set_assembly(path)
+        for w in range(args.warmup):
+            flush.fill_(1)
+            gpu.integrand_device(dv[args.steps + w], o, vals, st)
+        torch.cuda.synchronize()
+        gpu.profile(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for k in range(args.steps):
+            flush.fill_(1)
+            gpu.integrand_device(dv[k], o, vals, st)
+        e1.record()
+        torch.cuda.synchronize()
+        stage_ms, launches = gpu.profile_read()
+        gpu.profile(False)
+        results[path] = (e0.elapsed_time(e1), stage_ms, launches, vals.cpu().numpy().copy(), st.cpu().numpy().copy())
+    clock_info = clocks.stop()
+    # end to end (split) through the host-buffer call
+    gpu.set_assembly("split")
+    pv = [torch.from_numpy(x).pin_memory() for x in host[:args.steps]]
+    po = torch.full((batch,), order, dtype=torch.int32).pin_memory()
+    pout = torch.empty(batch, dtype=torch.float64).pin_memory()
+    pst = torch.empty(batch, dtype=torch.int32).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        rc = gpu._lib.cdet_integrand_host(gpu._ctx, pv[k].data_ptr(), po.data_ptr(), batch, order,
+                                          pout.data_ptr(), pst.data_ptr())
+        if rc not in (0, 4):
+            raise RuntimeError("host-buffer evaluation failed: " + gpu._lib.cdet_last_error().decode())
+    e2e_s = time.perf_counter() - t0
+    f_ms, f_stage, f_launch, f_vals, f_st = results["fp64"]
+    s_ms, s_stage, s_launch, s_vals, s_st = results["split"]
+    ok = (f_vals != 0) & (f_st == 0) & (s_st == 0)
+    rel = np.abs(s_vals[ok] - f_vals[ok]) / np.abs(f_vals[ok])
+    # Green matrices of both assemblies on a sample of the last batch
+    sample = dv[args.steps - 1][:1024].contiguous()
+    so = o[:1024].contiguous()
+    gpu.set_assembly("fp64")
+    g64, _, _ = gpu.assemble(sample, so)
+    gpu.set_assembly("split")
+    gsp, _, _ = gpu.assemble(sample, so)
+    torch.cuda.synchronize()
+    gscale = g64.abs().amax(dim=3, keepdim=True).clamp_min(1e-300)
+    green_rel = float(((gsp - g64).abs() / gscale).max().item())
+    _, bf16_peak, peak_kind = peaks()
+    nu, nv = params.cheb_nu, params.cheb_nv
+    lookups = batch * 2 * order * order
+    assembly_ms = s_stage[1] / args.steps
+    achieved = lookups * SPLIT_SLICE_PAIRS * 2.0 * nu * nv / (assembly_ms / 1e3) / 1e12
+
+    def per_step(ms):
+        return {"split_prep": ms[0] / args.steps, "assembly": ms[1] / args.steps,
+                "minors": ms[2] / args.steps, "cdet": ms[3] / args.steps}
+
+    line = {
+        "metric": "configs/s at order 14, 12x12 / degree 192 stress: split assembly vs plain FP64",
+        "value": batch * args.steps / (s_ms / 1e3), "unit": UNIT, "higher_is_better": True, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": s_ms / args.steps,
+        "dtype": "f64 (split fp16-digit tcgen05 assembly, FP64 minors and CDet)",
+        "data": "synthetic (seeded uniform vertices, tables from the in-tree precompute)",
+        "config": {"workload": "12x12 Hubbard t=1 U=6 beta=10 mu=-0.5, 6x12 half-lattice subsystem, "
+                               f"Chebyshev degree 192, order n=14, {batch} configurations per step",
+                   "lattice": "12x12", "U": 6, "beta": 10, "mu": -0.5, "mask": "half lattice x<6",
+                   "cheb_degree": 192, "order": order, "batch": batch,
+                   "l2": "flushed between steps (512 MiB write); tables 98 GB > L2"},
+        "e2e": {"value": batch * args.steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": batch * order * 4 * 8 + batch * 4,
+                "d2h_bytes_per_step": batch * 8 + batch * 4},
+        "gpu_launches": int(s_launch),
+        "stages_ms_per_step": per_step(s_stage),
+        "roofline": {"kernel": "split_assembly<chunked> (tcgen05 fp16 digit slices, 2 x 2 sub-blocks)",
+                     "bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                     "frac": achieved / bf16_peak, "traffic": None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json bf16_tflops)",
+                     "algorithmic": f"lookups x {SPLIT_SLICE_PAIRS} slice pairs x 2 x 192 x 192 "
+                                    "(unpadded; the sub-blocks pad rows 192..255)"},
+        "clocks": clock_info,
+        "fp64_path": {"value": batch * args.steps / (f_ms / 1e3), "unit": UNIT, "ms_per_step": f_ms / args.steps,
+                      "gpu_launches": int(f_launch), "stages_ms_per_step": per_step(f_stage)},
+        "split_over_fp64": f_ms / s_ms,
+        "split_vs_fp64_rel_err_order14": {
+            "configs": int(ok.sum()), "median": float(np.median(rel)), "p90": float(np.percentile(rel, 90)),
+            "max": float(rel.max()),
+            "normwise": float(np.abs(s_vals - f_vals).max() / max(np.abs(f_vals).max(), 1e-300)),
+            "note": "per-configuration relative error; the FP64 integrand's own round-off floor at order 14 "
+                    "(a 1-ulp change of the Green entries moves it by this much)"},
+        "green_split_vs_fp64_max_rel": green_rel,
+        "flagged_configs": {"fp64": int((f_st != 0).sum()), "split": int((s_st != 0).sum())},
+        "setup_s": {"tables": build_s, "slices": slice_s},
+        "device_memory_gb": {"used_after_slicing": (total_b - free_b) / 1e9, "total": total_b / 1e9},
+        "cpu_baseline": None,
+        "cpu_baseline_note": "not timed: the host oracle would need a 98 GB host copy of the tables",
+    }
+    print(json.dumps(line))
+    gpu.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -536,12 +676,17 @@ def main():
     ap.add_argument("--mixed", action="store_true",
                     help="time a batch of mixed orders 1..10 (a separate line, not the headline)")
     ap.add_argument("--mcmcmc-steps", type=int, default=2000, help="timed production steps for --mcmcmc")
+    ap.add_argument("--stress", action="store_true",
+                    help="time the 12x12 / degree-192 / order-14 stress case (a separate line, not the headline)")
     args = ap.parse_args()
     global PRESET, BATCH
     PRESET, BATCH = args.preset, args.batch
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
     if args.mixed:
         run_mixed(args)
+        return
+    if args.stress:
+        run_stress(args)
         return
     if args.mcmcmc:
         run_mcmcmc(args)
