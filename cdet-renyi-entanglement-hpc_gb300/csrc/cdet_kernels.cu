@@ -803,6 +803,178 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
         }
     }
 }
+
+// ------------------------------ 3c. single-top CDet, block per configuration
+// compute_dp_ztransform (integrand_replica_randomly_sampled.h:226-290) for
+// orders 11..14, where a batch holds few configurations and a lane's 2^n-entry
+// recursion would leave the SMs nearly empty: one CTA of 256 threads per
+// configuration, a of the masks without vertex 0 and dp of the masks with it
+// in shared memory (2^(n-1) doubles each; 128 KiB at n = 14), the masks of
+// each popcount level dealt out by colex rank. FP64 form: each mask's
+// submask sum runs on one thread in the reference's descending order with
+// the reference's operations, so the values are cdet_fp64's bit for bit.
+// Fused form (split assembly): the pair updates are FMAs and the round-off
+// filter's magnitudes FP32, as in cdet_split_warp; a level with fewer masks
+// than threads splits each mask's submasks over a group of L lanes (a fixed
+// partition and shuffle order, so the result is deterministic).
+constexpr int kBlockCdetMaxOrder = 14;
+constexpr int kBlockCdetThreads = 256;
+
+// colex unranking with the binomials of n <= 13 in shared memory
+__device__ __forceinline__ uint32_t colex_subset_s(uint32_t r, int m, int n, const uint32_t (*binom)[16]) {
+    uint32_t set = 0;
+    int hi = n - 1;
+    for (int i = m; i >= 1; --i) {
+        int c = hi;
+        while (c >= i && binom[c][i] > r) --c;
+        set |= 1u << c;
+        r -= binom[c][i];
+        hi = c - 1;
+    }
+    return set;
+}
+
+template <bool Fused>
+__global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_constant__ Problem p,
+                                                                const __grid_constant__ Scratch w) {
+    extern __shared__ __align__(16) unsigned char cdet_smem[];
+    __shared__ uint32_t binom[16][16];
+    const int tid = threadIdx.x;
+    const int nmax = p.max_order;
+    const int half = 1 << (nmax - 1);
+    double* a_s = reinterpret_cast<double*>(cdet_smem);  // a of even masks, at mask >> 1
+    double* dp_s = a_s + half;                           // dp of odd masks, at mask >> 1
+    const int64_t slot = blockIdx.x;
+    const int64_t c = p.sorted ? __ldg(w.config_at + slot) : slot;
+    const int64_t g = slot >> 5;
+    const int cl = static_cast<int>(slot & 31);
+    const int n = __ldg(p.orders + c);
+    if (n < 1 || n > nmax) return;  // the whole block
+    if (tid < 16 * 16) {
+        const int nn = tid >> 4, kk = tid & 15;
+        binom[nn][kk] = (nn <= 24 && kk <= nn) ? kBinomial.c[nn][kk] : 0u;
+    }
+    const Scalars& s = p.s;
+    const double threshold = dmul(s.z_eps0, s.z_safety);
+    const bool filter = threshold > 0.0;
+    const float thresholdf = static_cast<float>(threshold);
+    const int64_t full = int64_t{1} << nmax;
+    const double* diag = w.diag + c * 2 * 2 * nmax;
+    int32_t status = 0;
+    DD value[2] = {DD{0.0, 0.0}, DD{0.0, 0.0}};
+    for (int set = 0; set < 2; ++set) {
+        const int r = set == 0 ? 2 : 1;
+        if (n == 1) {
+            value[set] = DD{order1_value(s, diag[(set * 2) * nmax], diag[(set * 2 + 1) * nmax], r), 0.0};
+            continue;
+        }
+        const double* ag = w.a_int + (g * 2 + set) * full * kWarp + cl;
+        const int count = 1 << n;
+        int e = 0;
+        if constexpr (Fused) {
+            const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(ag[1 * kWarp]));
+            const int field = static_cast<int>((bits >> 52) & 0x7FF);
+            if (field != 0 && field != 0x7FF) e = field - 1023;
+            e = e > 60 ? 60 : (e < -60 ? -60 : e);  // |e| * n stays within 1000
+        }
+        for (int m2 = tid; m2 < count / 2; m2 += kBlockCdetThreads) a_s[m2] = ag[static_cast<int64_t>(2 * m2) * kWarp];
+        if (tid == 0) dp_s[0] = ag[1 * kWarp];
+        __syncthreads();
+        const int nbits = n - 1;
+        for (int k = 2; k <= n; ++k) {
+            const int kk = k - 1;            // rest = mask >> 1 has kk of nbits bits
+            const int masks = static_cast<int>(binom[nbits][kk]);
+            const int subs = 1 << kk;        // submasks of rest, rest itself included
+            const int field_bias = 127 - 2046 - e * k;
+            for (int base = 0; base < masks;) {
+                const int remaining = masks - base;
+                int L = 1, take = kBlockCdetThreads;
+                if (Fused && remaining < kBlockCdetThreads) {
+                    while (L * 2 * remaining <= kBlockCdetThreads && L * 2 <= subs && L < kWarp) L *= 2;
+                    take = remaining;
+                    if (4 * L * remaining < 3 * kBlockCdetThreads && L * 2 <= subs && L < kWarp) {
+                        L *= 2;  // < 75% of the threads busy
+                        take = kBlockCdetThreads / L;
+                    }
+                }
+                const int q = __ffs(L) - 1;
+                const int idx = base + (tid >> q);
+                const bool active = (tid >> q) < take && idx < masks;
+                if constexpr (!Fused) {
+                    if (active) {
+                        const uint32_t rest = colex_subset_s(static_cast<uint32_t>(idx), kk, nbits, binom);
+                        const uint32_t mask = (rest << 1) | 1u;
+                        double acc = ag[static_cast<int64_t>(mask) * kWarp];
+                        double rhs = fabs(acc);
+                        for (uint32_t sl = (rest - 1u) & rest;; sl = (sl - 1u) & rest) {
+                            const uint32_t sub = (sl << 1) | 1u;
+                            pair_update<false>(dp_s[sub >> 1], a_s[(mask ^ sub) >> 1], acc, rhs);
+                            if (sl == 0) break;
+                        }
+                        if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
+                        dp_s[mask >> 1] = acc;
+                    }
+                } else {
+                    const int j = tid & (L - 1);
+                    double part = 0.0;
+                    float rpart = 0.0f;
+                    uint32_t mask = 0;
+                    if (active) {
+                        const uint32_t rest = colex_subset_s(static_cast<uint32_t>(idx), kk, nbits, binom);
+                        mask = (rest << 1) | 1u;
+                        // the top q bits of rest are fixed by the lane's index in its group
+                        uint32_t top = 0, low = rest;
+                        for (int t = 0; t < q; ++t) {
+                            const uint32_t hb = 1u << (31 - __clz(low));
+                            top |= hb;
+                            low ^= hb;
+                        }
+                        uint32_t fixed = 0, tb = top;
+                        for (int t = 0; t < q; ++t) {
+                            const uint32_t lb = tb & (~tb + 1u);
+                            if ((j >> t) & 1) fixed |= lb;
+                            tb ^= lb;
+                        }
+                        for (uint32_t sl = low;; sl = (sl - 1u) & low) {
+                            const uint32_t sm = fixed | sl;
+                            if (sm != rest) {
+                                const uint32_t sub = (sm << 1) | 1u;
+                                const double x = dp_s[sub >> 1], y = a_s[(mask ^ sub) >> 1];
+                                part = __fma_rn(x, y, part);
+                                rpart += product_magnitude(x, y, field_bias);
+                            }
+                            if (sl == 0) break;
+                        }
+                    }
+                    for (int off = 1; off < L; off <<= 1) {
+                        part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));
+                        rpart += __shfl_xor_sync(0xffffffffu, rpart, off);
+                    }
+                    if (active && j == 0) {
+                        const double am = ag[static_cast<int64_t>(mask) * kWarp];
+                        double acc = dsub(am, part);
+                        const float rhs = scaled_magnitude(am, -e * k) + rpart;
+                        if (filter && scaled_magnitude(acc, -e * k) < thresholdf * rhs) acc = 0.0;
+                        dp_s[mask >> 1] = acc;
+                    }
+                }
+                base += take;
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            const DDPair pf = p.pref_dd[set][n];
+            value[set] = dd_mul(DD{pf.hi, pf.lo}, DD{dp_s[(count - 1) >> 1], 0.0});
+            if (!dd_finite(value[set])) status |= kStatusNonFinite;
+        }
+        __syncthreads();  // the next set reuses the arrays
+    }
+    if (tid == 0) {
+        const DD result = dd_sub(value[0], dd_mul(DD{2.0, 0.0}, value[1]));
+        p.values[c] = dadd(result.hi, result.lo);
+        if (status) atomicOr(p.status + c, status);
+    }
+}
 }  // namespace
 
 size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).total; }
@@ -985,6 +1157,20 @@ cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_
             if (err != cudaSuccess) return err;
             cdet_all_warp<false><<<static_cast<unsigned>((p.batch + warps - 1) / warps), warps * kWarp, csmem,
                                    stream>>>(p, w);
+        }
+    } else if (!p.all_subsets && p.max_order > kWarpCdetMaxOrder && p.max_order <= kBlockCdetMaxOrder) {
+        // orders 11..14: one block per configuration (slots in decreasing order)
+        const size_t csmem = sizeof(double) * (size_t{1} << p.max_order);
+        if (p.fused_cdet) {
+            err = cudaFuncSetAttribute(cdet_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(csmem));
+            if (err != cudaSuccess) return err;
+            cdet_block<true><<<static_cast<unsigned>(p.batch), kBlockCdetThreads, csmem, stream>>>(p, w);
+        } else {
+            err = cudaFuncSetAttribute(cdet_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(csmem));
+            if (err != cudaSuccess) return err;
+            cdet_block<false><<<static_cast<unsigned>(p.batch), kBlockCdetThreads, csmem, stream>>>(p, w);
         }
     } else {
         cdet_fp64<<<static_cast<unsigned>((p.batch + threads - 1) / threads), threads, 0, stream>>>(p, w);

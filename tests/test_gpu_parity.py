@@ -125,13 +125,22 @@ def test_oracle_mixed_orders_and_high_orders():
     got, st = gpu.integrand_batch(v, orders)
     want, wst = orc.integrand_batch(v, orders, threads=THREADS)
     assert np.array_equal(st, wst) and bits_equal(got, want)
-    # high orders: 12 and 14
-    for n, count in ((12, 64), (14, 16)):
+    # high orders 11..14 (one block per configuration): fixed orders, and a
+    # batch of orders 1..13 whose slots are sorted by order
+    for n, count in ((11, 64), (12, 64), (13, 32), (14, 16)):
         v = uniform_configurations(100 + n, count, n)
         orders = np.full(count, n, dtype=np.int32)
         got, st = gpu.integrand_batch(v, orders)
         want, wst = orc.integrand_batch(v, orders, threads=THREADS)
         assert np.array_equal(st, wst) and bits_equal(got, want), n
+    v = uniform_configurations(113, 96, 13)
+    orders = np.random.default_rng(114).integers(1, 14, size=96).astype(np.int32)
+    orders[5] = 0  # flagged, its value unspecified
+    got, st = gpu.integrand_batch(v, orders)
+    want, wst = orc.integrand_batch(v, orders, threads=THREADS)
+    ok = orders > 0
+    assert np.array_equal(st, wst) and st[5] & L.CONFIG_BAD_INPUT
+    assert bits_equal(got[ok], want[ok])
     # all-subsets at envelope 9
     v = uniform_configurations(13, 64, 9)
     got, _ = gpu.all_subsets_batch(v)
