@@ -674,6 +674,59 @@ __device__ __forceinline__ float product_magnitude(double x, double y, int field
     return mx * my * __int_as_float(field << 23);
 }
 
+// The fused pair updates of one lane: over the submasks sm = fixed | sl of
+// rest (sl a subset of low, sm != rest), part += dp[sm] a[rest ^ sm] as FMAs
+// and rpart += their scaled magnitudes, with dp and a indexed by mask >> 1.
+// The three lowest bits of low are enumerated inside an unrolled block of
+// eight terms (independent loads and magnitudes, two alternating FMA chains)
+// and the other bits by the outer loop, in a fixed order, so the result is
+// deterministic. The excluded submask sm = rest (its dp is this level's, not
+// yet written) contributes exact zeros.
+__device__ __forceinline__ void fused_submask_sum(const double* dp_s, const double* a_s, uint32_t rest,
+                                                  uint32_t fixed, uint32_t low, int field_bias, double& part,
+                                                  float& rpart) {
+    if (__popc(low) < 3) {
+        for (uint32_t sl = low;; sl = (sl - 1u) & low) {
+            const uint32_t sm = fixed | sl;
+            if (sm != rest) {
+                const double x = dp_s[sm], y = a_s[rest ^ sm];
+                part = __fma_rn(x, y, part);
+                rpart += product_magnitude(x, y, field_bias);
+            }
+            if (sl == 0) break;
+        }
+        return;
+    }
+    const uint32_t b0 = low & (~low + 1u);
+    const uint32_t r1 = low ^ b0;
+    const uint32_t b1 = r1 & (~r1 + 1u);
+    const uint32_t r2 = r1 ^ b1;
+    const uint32_t b2 = r2 & (~r2 + 1u);
+    const uint32_t hi = r2 ^ b2;
+    double p0 = 0.0, p1 = 0.0;
+    float m0 = 0.0f, m1 = 0.0f;
+    for (uint32_t h = hi;; h = (h - 1u) & hi) {
+        const uint32_t base = fixed | h;
+#pragma unroll
+        for (int j = 7; j >= 0; --j) {
+            const uint32_t sm = base | ((j & 4) ? b2 : 0u) | ((j & 2) ? b1 : 0u) | ((j & 1) ? b0 : 0u);
+            const bool skip = sm == rest;
+            const double x = skip ? 0.0 : dp_s[sm];
+            const double y = skip ? 0.0 : a_s[rest ^ sm];
+            if (j & 1) {
+                p1 = __fma_rn(x, y, p1);
+                m1 += product_magnitude(x, y, field_bias);
+            } else {
+                p0 = __fma_rn(x, y, p0);
+                m0 += product_magnitude(x, y, field_bias);
+            }
+        }
+        if (h == 0) break;
+    }
+    part = dadd(part, dadd(p1, p0));
+    rpart += m1 + m0;
+}
+
 // |v| * 2^k as a float, clamped to the finite range (|k| <= 1000).
 __device__ __forceinline__ float scaled_magnitude(double v, int k) {
     const double p2 = __longlong_as_double(static_cast<long long>(1023 + k) << 52);
@@ -764,17 +817,7 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
                             if ((j >> t) & 1) fixed |= lb;
                             tb ^= lb;
                         }
-                        for (uint32_t sl = low;; sl = (sl - 1u) & low) {
-                            const uint32_t sm = fixed | sl;
-                            if (sm != rest) {
-                                const uint32_t sub = (sm << 1) | 1u;
-                                const uint32_t other = mask ^ sub;
-                                const double x = dp_s[sub >> 1], y = a_s[other >> 1];
-                                part = __fma_rn(x, y, part);
-                                rpart += product_magnitude(x, y, field_bias);
-                            }
-                            if (sl == 0) break;
-                        }
+                        fused_submask_sum(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
                     }
                     for (int off = 1; off < L; off <<= 1) {
                         part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));
@@ -935,16 +978,7 @@ __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_con
                             if ((j >> t) & 1) fixed |= lb;
                             tb ^= lb;
                         }
-                        for (uint32_t sl = low;; sl = (sl - 1u) & low) {
-                            const uint32_t sm = fixed | sl;
-                            if (sm != rest) {
-                                const uint32_t sub = (sm << 1) | 1u;
-                                const double x = dp_s[sub >> 1], y = a_s[(mask ^ sub) >> 1];
-                                part = __fma_rn(x, y, part);
-                                rpart += product_magnitude(x, y, field_bias);
-                            }
-                            if (sl == 0) break;
-                        }
+                        fused_submask_sum(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
                     }
                     for (int off = 1; off < L; off <<= 1) {
                         part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));
