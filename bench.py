@@ -523,15 +523,19 @@ def run_stress(args):
     per step. Degree 192 runs the split assembly as 2 x 2 sub-blocks of each
     coefficient block. The tables (98 GB in the reference layout) and their
     split slices (163 GB) are resident together; the FP64 and split forms
-    are timed on the same batches."""
+    are timed on the same batches. With --stress-small the same kernels run
+    on a 3x3 lattice (2,048 configurations) whose tables suit profiler
+    captures; that is not a bench line."""
     import torch
     from cdet_gb300.integrand import CdetIntegrand
     from cdet_gb300.params import CdetParams, half_lattice_mask
     from cdet_gb300.synthetic import uniform_configurations
     from cdet_gb300.tables import build_tables
-    params = CdetParams(n1=12, n2=12, beta="10", mu="-0.5", u="6", alpha_up="0", alpha_down="0",
-                        mask_sites=half_lattice_mask(12, 12), cheb_nu=192, cheb_nv=192)
-    batch, order = args.batch if args.batch != 65536 else 8192, 14
+    side = 3 if args.stress_small else 12
+    params = CdetParams(n1=side, n2=side, beta="10", mu="-0.5", u="6", alpha_up="0", alpha_down="0",
+                        mask_sites=half_lattice_mask(side, side), cheb_nu=192, cheb_nv=192)
+    default_batch = 2048 if args.stress_small else 8192
+    batch, order = args.batch if args.batch != 65536 else default_batch, 14
     t0 = time.perf_counter()
     tables = build_tables(params, device="cuda")
     torch.cuda.synchronize()
@@ -619,11 +623,11 @@ def run_stress(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": s_ms / args.steps,
         "dtype": "f64 (split fp16-digit tcgen05 assembly, FP64 minors and CDet)",
         "data": "synthetic (seeded uniform vertices, tables from the in-tree precompute)",
-        "config": {"workload": "12x12 Hubbard t=1 U=6 beta=10 mu=-0.5, 6x12 half-lattice subsystem, "
+        "config": {"workload": f"{side}x{side} Hubbard t=1 U=6 beta=10 mu=-0.5, half-lattice subsystem, "
                                f"Chebyshev degree 192, order n=14, {batch} configurations per step",
-                   "lattice": "12x12", "U": 6, "beta": 10, "mu": -0.5, "mask": "half lattice x<6",
+                   "lattice": f"{side}x{side}", "U": 6, "beta": 10, "mu": -0.5, "mask": "half lattice x<6",
                    "cheb_degree": 192, "order": order, "batch": batch,
-                   "l2": "flushed between steps (512 MiB write); tables 98 GB > L2"},
+                   "l2": "flushed between steps (512 MiB write)"},
         "e2e": {"value": batch * args.steps / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": batch * order * 4 * 8 + batch * 4,
                 "d2h_bytes_per_step": batch * 8 + batch * 4},
@@ -650,7 +654,7 @@ def run_stress(args):
         "setup_s": {"tables": build_s, "slices": slice_s},
         "device_memory_gb": {"used_after_slicing": (total_b - free_b) / 1e9, "total": total_b / 1e9},
         "cpu_baseline": None,
-        "cpu_baseline_note": "not timed: the host oracle would need a 98 GB host copy of the tables",
+        "cpu_baseline_note": "not timed: the host oracle would need a host copy of the tables (98 GB at 12x12)",
     }
     print(json.dumps(line))
     gpu.close()
@@ -678,6 +682,8 @@ def main():
     ap.add_argument("--mcmcmc-steps", type=int, default=2000, help="timed production steps for --mcmcmc")
     ap.add_argument("--stress", action="store_true",
                     help="time the 12x12 / degree-192 / order-14 stress case (a separate line, not the headline)")
+    ap.add_argument("--stress-small", action="store_true",
+                    help="with --stress: a 3x3 lattice and 2,048 configurations, for profiler captures")
     args = ap.parse_args()
     global PRESET, BATCH
     PRESET, BATCH = args.preset, args.batch
