@@ -17,6 +17,7 @@ a device synchronize and the maximum over ranks is reported.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import subprocess
@@ -131,6 +132,15 @@ def time_cpu_integrand(params, tables, vertices, orders, threads):
     t0 = time.perf_counter()
     values, _ = orc.integrand_batch(vertices, orders, threads=threads)
     return time.perf_counter() - t0, values
+
+
+def long_double_truth(params, tables, vertices, orders, threads):
+    """The oracle's long double evaluation of the same integrand (the checker
+    of the precision statement, not a measured path)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from bindings import Oracle
+    values, status = Oracle(params.runtime_scalars(), tables).integrand_ld_batch(vertices, orders, threads=threads)
+    return np.where(status == 0, values, np.nan)
 
 
 def run_reference(args):
@@ -372,6 +382,35 @@ def run_gpu(args):
             "bit_identical_to_gpu_fp64_path": bool(np.array_equal(cpu_values.view(np.uint64),
                                                                   gpu_first.view(np.uint64))),
         }
+        if head == "split":
+            # the checker's long double truth on a sample of the same batch:
+            # relative errors of the split and FP64 forms against it
+            n_truth = min(128, sample)
+            t0 = time.perf_counter()
+            truth = long_double_truth(params, host, v[:n_truth], np.full(n_truth, ORDER, np.int32), threads)
+            truth_s = time.perf_counter() - t0
+            den = np.maximum(np.abs(truth), 1e-300)
+
+            def errors(ctx):
+                out = {}
+                for path in ("split", "fp64"):
+                    ctx.set_assembly(path)
+                    ctx.integrand_device(d_vertices[0], d_orders, d_values, d_status, stream)
+                    torch.cuda.synchronize(dev)
+                    e = np.abs(d_values.cpu().numpy()[:n_truth] - truth) / den
+                    out[path] = {"median": float(np.median(e)), "p90": float(np.percentile(e, 90))}
+                return out
+
+            # the same forms with the z-transform round-off filter off
+            # (ZTRANSFORM_SAFETY_FACTOR = 0), on the same device tables
+            unfiltered = CdetIntegrand(dataclasses.replace(params, z_safety="0"), tables, device=local_rank)
+            line["precision_vs_long_double_truth"] = {
+                "configs": n_truth, "order": ORDER,
+                "filter_on": errors(integrand), "filter_off": errors(unfiltered),
+                "truth": f"oracle long double integrand without the round-off filter ({threads} threads, "
+                         f"{truth_s:.1f} s), pinned to the reference's VECTOR_REAL=long_double / "
+                         "INTEGRAND_REAL=double_double mode"}
+            unfiltered.close()
     if rank == 0:
         print(json.dumps(line))
     integrand.close()

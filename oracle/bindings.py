@@ -83,6 +83,8 @@ class Oracle:
                                                C.c_int, _DP, _IP, C.c_int]
         lib.oracle_all_subsets_batch.argtypes = [C.c_void_p, C.c_void_p, _DP, C.c_int,
                                                  C.c_int64, _DP, _IP, C.c_int]
+        lib.oracle_integrand_ld_batch.argtypes = [C.c_void_p, C.c_void_p, _DP, _IP, C.c_int64,
+                                                  C.c_int, _DP, _IP, C.c_int]
         lib.oracle_mat2pm.argtypes = [_DP, C.c_int, C.c_double, C.c_double, _DP]
         lib.oracle_minors_by_lu.argtypes = [_DP, C.c_int, _DP]
         lib.oracle_ztransform.argtypes = [_DP, _DP, C.c_int, C.c_double, C.c_double]
@@ -135,6 +137,21 @@ class Oracle:
         rc = self.lib.oracle_integrand_batch(C.byref(self.scalars), C.byref(self.tables),
                                              _ptr(v), o.ctypes.data_as(_IP), batch, max_order,
                                              _ptr(out), st.ctypes.data_as(_IP), threads)
+        if rc != 0:
+            raise RuntimeError("oracle thread start failed")
+        return out, st
+
+    def integrand_ld_batch(self, vertices: np.ndarray, orders: np.ndarray, threads: int = 1):
+        """The long double truth of each configuration's integrand (rounded
+        to double), for error measurements; see oracle_integrand_ld."""
+        v = np.ascontiguousarray(vertices, dtype=np.float64)
+        o = np.ascontiguousarray(orders, dtype=np.int32)
+        batch, max_order = v.shape[0], v.shape[1]
+        out = np.zeros(batch)
+        st = np.zeros(batch, dtype=np.int32)
+        rc = self.lib.oracle_integrand_ld_batch(C.byref(self.scalars), C.byref(self.tables),
+                                                _ptr(v), o.ctypes.data_as(_IP), batch, max_order,
+                                                _ptr(out), st.ctypes.data_as(_IP), threads)
         if rc != 0:
             raise RuntimeError("oracle thread start failed")
         return out, st
@@ -289,6 +306,7 @@ class Reference:
         lib.ref_corner_count.restype = C.c_size_t
         lib.ref_get_table.argtypes = [C.c_int, _DP, _DP, _DP, _DP]
         lib.ref_set_table.argtypes = [C.c_int, _DP, _DP, _DP, _DP]
+        lib.ref_set_table_long_double.argtypes = [C.c_int, _DP, _DP, _DP, _DP]
         lib.ref_eval_integrand.argtypes = [_DP, C.c_int, _DP]
         lib.ref_eval_integrand_batch.argtypes = [_DP, C.POINTER(C.c_int), C.c_int, C.c_int, _DP,
                                                  C.c_int]
@@ -335,6 +353,10 @@ class Reference:
     def build_tables(self, threads: int = 4):
         self._check(self.lib.ref_build_tables(threads))
 
+    def set_precision(self, vector_real: str, integrand_real: str) -> None:
+        """VECTOR_REAL / INTEGRAND_REAL of later evaluations (precision_config.h:15-26)."""
+        self._check(self.lib.ref_set_precision(vector_real.encode(), integrand_real.encode()))
+
     def get_tables(self) -> Dict[str, Dict[str, np.ndarray]]:
         nc, nk = self.lib.ref_coeff_count(), self.lib.ref_corner_count()
         out = {}
@@ -347,12 +369,14 @@ class Reference:
             out[kind] = t
         return out
 
-    def set_tables(self, tables: Dict[str, Dict]):
+    def set_tables(self, tables: Dict[str, Dict], long_double: bool = False):
+        """Resident tables (double; or widened to long double for
+        VECTOR_REAL=long_double)."""
+        setter = self.lib.ref_set_table_long_double if long_double else self.lib.ref_set_table
         for i, kind in enumerate(KINDS):
             t = _as_numpy_table(tables[kind])
-            self._check(self.lib.ref_set_table(i, _ptr(t["upper"]), _ptr(t["lower"]),
-                                               _ptr(t["upper_corners"]),
-                                               _ptr(t["lower_corners"])))
+            self._check(setter(i, _ptr(t["upper"]), _ptr(t["lower"]), _ptr(t["upper_corners"]),
+                               _ptr(t["lower_corners"])))
 
     def integrand(self, vertices) -> float:
         v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 4)

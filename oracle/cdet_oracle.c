@@ -640,6 +640,177 @@ int oracle_all_subsets(const oracle_scalars* s, const oracle_tables* t, const do
     return status;
 }
 
+/* ------------------------------------------------- long double truth --- */
+/* A higher-precision evaluation of the same integrand for error studies, the
+ * role the reference gives its INTEGRAND_REAL=double_double /
+ * VECTOR_REAL=long_double mode (precision_config.h:15-26): the same decoded
+ * vertices and the same double (u, v) as the FP64 form, then the Chebyshev
+ * sums, the diagonal shifts and the scale, every principal minor (a
+ * partial-pivot LU of each principal submatrix), the anchored connected
+ * recursion without the round-off filter and the prefactor, all in long
+ * double (64-bit significand on x86-64, 113-bit on AArch64). It follows no
+ * reference operation order and is compared with nothing bit for bit: it is
+ * the value the FP64 and split forms approximate. */
+static long double clenshaw_ld(const double* c, int degree, long double x) {
+    if (degree < 0) return 0.0L;
+    if (degree == 0) return (long double)c[0];
+    const long double two_x = 2.0L * x;
+    long double b1 = 0.0L, b2 = 0.0L;
+    for (int k = degree; k >= 1; --k) {
+        const long double bk = (long double)c[k] + two_x * b1 - b2;
+        b2 = b1;
+        b1 = bk;
+    }
+    return (long double)c[0] + b1 * x - b2;
+}
+
+static long double chebyshev_2d_ld(const double* block, double u, double v, int nu, int nv) {
+    long double rows[512];
+    for (int a = 0; a < nu; ++a) rows[a] = clenshaw_ld(block + (size_t)a * (size_t)nv, nv - 1, (long double)v);
+    /* the outer sum over rows, on long double row values */
+    if (nu == 1) return rows[0];
+    const long double x = (long double)u, two_x = 2.0L * x;
+    long double b1 = 0.0L, b2 = 0.0L;
+    for (int k = nu - 1; k >= 1; --k) {
+        const long double bk = rows[k] + two_x * b1 - b2;
+        b2 = b1;
+        b1 = bk;
+    }
+    return rows[0] + b1 * x - b2;
+}
+
+static long double minor_lu_ld(const long double* a, int n, uint64_t mask) {
+    int idx[ORACLE_MAX_ORDER];
+    long double m[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER];
+    int k = 0;
+    for (int i = 0; i < n; ++i)
+        if (mask & ((uint64_t)1 << i)) idx[k++] = i;
+    for (int r = 0; r < k; ++r)
+        for (int c = 0; c < k; ++c) m[r * k + c] = a[idx[r] * n + idx[c]];
+    long double det = 1.0L;
+    for (int col = 0; col < k; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < k; ++r)
+            if (fabsl(m[r * k + col]) > fabsl(m[piv * k + col])) piv = r;
+        if (m[piv * k + col] == 0.0L) return 0.0L;
+        if (piv != col) {
+            for (int c = col; c < k; ++c) {
+                const long double t = m[col * k + c];
+                m[col * k + c] = m[piv * k + c];
+                m[piv * k + c] = t;
+            }
+            det = -det;
+        }
+        const long double p = m[col * k + col];
+        det *= p;
+        for (int r = col + 1; r < k; ++r) {
+            const long double f = m[r * k + col] / p;
+            for (int c = col + 1; c < k; ++c) m[r * k + c] -= f * m[col * k + c];
+        }
+    }
+    return det;
+}
+
+static int integrand_one_set_ld(const oracle_scalars* s, const oracle_table* tu, const oracle_table* td,
+                                const double* args, int order, int replica_count, long double* value) {
+    vertex vx[ORACLE_MAX_ORDER];
+    long double mu[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER], md[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER];
+    if (decode_vertices(s, args, order, replica_count, vx)) return ORACLE_BAD_INPUT;
+    for (int idx = 0; idx < order * order; ++idx) {
+        const int i = idx / order;
+        const int j = idx - i * order;
+        const int upper = (i != j) && (vx[i].tau_unit > vx[j].tau_unit);
+        int corner;
+        uint64_t index;
+        double u, v;
+        oracle_lookup_descriptor(vx[i].replica, vx[j].replica, vx[i].tau, vx[j].tau, vx[i].x, vx[i].y,
+                                 vx[j].x, vx[j].y, s->beta, s->branch_eps, s->cheb_nu, s->cheb_nv, s->n1,
+                                 s->n2, upper, &corner, &index, &u, &v);
+        long double up, down;
+        if (corner) {
+            up = (long double)(upper ? tu->upper_corners[index] : tu->lower_corners[index]);
+            down = (long double)(upper ? td->upper_corners[index] : td->lower_corners[index]);
+        } else {
+            up = chebyshev_2d_ld((upper ? tu->upper_coeffs : tu->lower_coeffs) + index, u, v, s->cheb_nu,
+                                 s->cheb_nv);
+            down = chebyshev_2d_ld((upper ? td->upper_coeffs : td->lower_coeffs) + index, u, v, s->cheb_nu,
+                                   s->cheb_nv);
+        }
+        if (i == j) {
+            up += (long double)s->diag_up_shift;
+            down += (long double)s->diag_down_shift;
+        }
+        mu[idx] = up * (long double)s->scale;
+        md[idx] = down * (long double)s->scale;
+    }
+    const uint64_t count = (uint64_t)1 << order;
+    long double* a = (long double*)malloc(count * sizeof(long double));
+    long double* dp = (long double*)malloc(count * sizeof(long double));
+    if (!a || !dp) {
+        free(a);
+        free(dp);
+        return ORACLE_BAD_INPUT;
+    }
+    a[0] = 0.0L;
+    for (uint64_t m = 1; m < count; ++m) a[m] = minor_lu_ld(mu, order, m) * minor_lu_ld(md, order, m);
+    dp[1] = a[1];
+    for (int bits = 2; bits <= order; ++bits) {
+        for (uint64_t mask = 1; mask < count; mask += 2) {
+            if (popcount64(mask) != bits) continue;
+            long double acc = a[mask];
+            for (uint64_t sub = (mask - 1) & mask; sub; sub = (sub - 1) & mask)
+                if (sub & 1u) acc -= dp[sub] * a[mask ^ sub];
+            dp[mask] = acc;
+        }
+    }
+    long double pref = 1.0L;
+    for (int i = 0; i < order; ++i) pref *= -(long double)replica_count;
+    long double den = (long double)s->n1 * (long double)s->n2;
+    for (int i = 2; i <= order; ++i) den *= (long double)i;
+    *value = pref / den * dp[count - 1];
+    free(a);
+    free(dp);
+    return 0;
+}
+
+int oracle_integrand_ld(const oracle_scalars* s, const oracle_tables* t, const double* args, int order,
+                        double* value) {
+    *value = 0.0;
+    if (order <= 0 || order > ORACLE_MAX_ORDER) return ORACLE_BAD_INPUT;
+    long double v[2];
+    const oracle_table* tabs[2][2] = {{&t->twisted_up, &t->twisted_down}, {&t->ordinary_up, &t->ordinary_down}};
+    for (int set = 0; set < 2; ++set) {
+        const int r = set == 0 ? 2 : 1;
+        if (order == 1) {
+            vertex vx[1];
+            if (decode_vertices(s, args, 1, r, vx)) return ORACLE_BAD_INPUT;
+            int corner;
+            uint64_t index;
+            double u, w;
+            oracle_lookup_descriptor(vx[0].replica, vx[0].replica, vx[0].tau, vx[0].tau, vx[0].x, vx[0].y,
+                                     vx[0].x, vx[0].y, s->beta, s->branch_eps, s->cheb_nu, s->cheb_nv, s->n1,
+                                     s->n2, 0, &corner, &index, &u, &w);
+            long double up, down;
+            if (corner) {
+                up = (long double)tabs[set][0]->lower_corners[index];
+                down = (long double)tabs[set][1]->lower_corners[index];
+            } else {
+                up = chebyshev_2d_ld(tabs[set][0]->lower_coeffs + index, u, w, s->cheb_nu, s->cheb_nv);
+                down = chebyshev_2d_ld(tabs[set][1]->lower_coeffs + index, u, w, s->cheb_nu, s->cheb_nv);
+            }
+            const long double su = up + (long double)s->diag_up_shift;
+            const long double sd = down + (long double)s->diag_down_shift;
+            const long double counter = (long double)s->diag_up_shift * (long double)s->diag_down_shift;
+            v[set] = -(long double)r * (long double)s->u * (long double)s->beta * (su * sd - counter);
+        } else {
+            const int st = integrand_one_set_ld(s, tabs[set][0], tabs[set][1], args, order, r, &v[set]);
+            if (st) return st;
+        }
+    }
+    *value = (double)(v[0] - 2.0L * v[1]);
+    return isfinite(*value) ? 0 : ORACLE_NONFINITE;
+}
+
 /* ---------------------------------------------------------- thread batch --- */
 
 typedef struct batch_job {
@@ -648,7 +819,7 @@ typedef struct batch_job {
     const double* vertices;
     const int32_t* orders;
     int max_order;
-    int all_subsets;
+    int all_subsets;  /* 1: all-subset values; 2: the long double truth */
     int64_t begin, end;
     double* values;
     int32_t* status;
@@ -659,9 +830,11 @@ static void* batch_worker(void* arg) {
     for (int64_t c = job->begin; c < job->end; ++c) {
         const double* v = job->vertices + (size_t)c * (size_t)job->max_order * 4u;
         int st;
-        if (job->all_subsets) {
+        if (job->all_subsets == 1) {
             st = oracle_all_subsets(job->s, job->t, v, job->max_order,
                                     job->values + (size_t)c * ((size_t)1 << job->max_order));
+        } else if (job->all_subsets == 2) {
+            st = oracle_integrand_ld(job->s, job->t, v, job->orders[c], job->values + c);
         } else {
             st = oracle_integrand(job->s, job->t, v, job->orders[c], job->values + c);
         }
@@ -699,6 +872,13 @@ int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
                              const double* unit_vertices, int envelope_order, int64_t batch,
                              double* values, int32_t* status, int threads) {
     batch_job proto = {s, t, unit_vertices, NULL, envelope_order, 1, 0, 0, values, status};
+    return run_batch(proto, batch, threads);
+}
+
+int oracle_integrand_ld_batch(const oracle_scalars* s, const oracle_tables* t, const double* unit_vertices,
+                              const int32_t* orders, int64_t batch, int max_order, double* values,
+                              int32_t* status, int threads) {
+    batch_job proto = {s, t, unit_vertices, orders, max_order, 2, 0, 0, values, status};
     return run_batch(proto, batch, threads);
 }
 

@@ -100,6 +100,17 @@ int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
                              const double* unit_vertices, int envelope_order, int64_t batch,
                              double* values, int32_t* status, int threads);
 
+/* Long double evaluation of the same integrand (the same decoded vertices
+ * and double (u, v); Chebyshev sums, minors by LU, the connected recursion
+ * without the round-off filter and the prefactor in long double): a truth
+ * for measuring the FP64 and split forms' errors, compared bit for bit with
+ * nothing. Same batch layout as oracle_integrand_batch. */
+int oracle_integrand_ld(const oracle_scalars* s, const oracle_tables* t,
+                        const double* unit_vertices, int order, double* value);
+int oracle_integrand_ld_batch(const oracle_scalars* s, const oracle_tables* t,
+                              const double* unit_vertices, const int32_t* orders, int64_t batch,
+                              int max_order, double* values, int32_t* status, int threads);
+
 /* Deterministic order-1 diagonal observable (diagonal_green_observable.h:237-327):
  * out[0] = twisted - 2 * ordinary (the normalised first-order coefficient of
  * ln Z_2[A]), out[1] = the twisted (two-replica) part, out[2] = the ordinary

@@ -186,6 +186,22 @@ int ref_set_table(int kind, const double* upper, const double* lower, const doub
     });
 }
 
+// The same table widened to long double (exactly), for the reference's
+// VECTOR_REAL=long_double mode, which requires resident tables of that type.
+int ref_set_table_long_double(int kind, const double* upper, const double* lower,
+                              const double* upper_corners, const double* lower_corners) {
+    return guarded([&] {
+        GreenFunctionTableLongDouble table;
+        const std::size_t coeffs = ref_coeff_count();
+        const std::size_t corners = ref_corner_count();
+        table.upper_coeffs.assign(upper, upper + coeffs);
+        table.lower_coeffs.assign(lower, lower + coeffs);
+        table.upper_corners.assign(upper_corners, upper_corners + corners);
+        table.lower_corners.assign(lower_corners, lower_corners + corners);
+        table_slot(kind) = std::move(table);
+    });
+}
+
 int ref_eval_integrand(const double* unit_vertices, int order, double* out) {
     return guarded([&] {
         *out = evaluate_cdet_density_integrand_double(unpack_vertices(unit_vertices, order));

@@ -25,6 +25,7 @@ from cdet_gb300.integrand import CdetIntegrand  # noqa: E402
 from cdet_gb300.params import CdetParams, named_mask  # noqa: E402
 from cdet_gb300.synthetic import uniform_configurations  # noqa: E402
 from cdet_gb300.tables import build_tables  # noqa: E402
+from bindings import Oracle  # noqa: E402
 from helpers import bits_equal, load_case  # noqa: E402
 
 GREEN_TOL = 2e-15
@@ -185,3 +186,42 @@ def test_split_high_order_block_cdet():
         rel = np.abs(a - ref) / np.maximum(np.abs(ref), 1e-300)
         print(f"order {n}: split vs FP64 median rel {np.median(rel):.3e}, max {rel.max():.3e}")
         assert np.median(rel) <= 1e-6, n
+
+
+def _errors_against_truth(params, tables, v, orders, threads=16):
+    """Per-configuration relative errors of the split and FP64 forms against
+    the oracle's long double truth."""
+    gpu = CdetIntegrand(params, tables)
+    fp64, st64 = gpu.integrand_batch(v, orders)
+    gpu.set_assembly("split")
+    split, st = gpu.integrand_batch(v, orders)
+    host = {k: {kk: (vv.cpu().numpy() if hasattr(vv, "cpu") else vv) for kk, vv in t.items()}
+            for k, t in tables.items()}
+    truth, tst = Oracle(params.runtime_scalars(), host).integrand_ld_batch(v, orders, threads=threads)
+    assert st.max() == 0 and st64.max() == 0 and tst.max() == 0
+    den = np.maximum(np.abs(truth), 1e-300)
+    return np.abs(split - truth) / den, np.abs(fp64 - truth) / den
+
+
+def test_split_error_against_long_double_truth():
+    """Against the long double truth (pinned to the reference's own
+    high-precision mode) the split form is as accurate as the FP64 form,
+    order by order: the split Green matrices are closer to the exact series
+    than the FP64 Clenshaw sums, and the minors and CDet are FP64 in both."""
+    params, tables, data = load_case("column_3x3")
+    v, orders = data["single.vertices"], data["single.orders"]
+    e_split, e_fp64 = _errors_against_truth(params, tables, v, orders)
+    for n in range(1, 9):
+        sel = orders == n
+        ms, mf = np.median(e_split[sel]), np.median(e_fp64[sel])
+        print(f"column 3x3 order {n}: median rel error vs truth split {ms:.2e} fp64 {mf:.2e}")
+        assert ms <= 3.0 * mf + 1e-15, n
+    params = CdetParams(n1=4, n2=4, beta="6", mu="0", u="2",
+                        mask_sites=named_mask("origin_square", 4, 4, 1), cheb_nu=64, cheb_nv=64)
+    tables = build_tables(params, device="cuda")
+    v = uniform_configurations(4242, 256, 8)
+    orders = np.full(256, 8, dtype=np.int32)
+    e_split, e_fp64 = _errors_against_truth(params, tables, v, orders)
+    print(f"4x4 degree 64 order 8: median rel error vs truth split {np.median(e_split):.2e} "
+          f"fp64 {np.median(e_fp64):.2e}")
+    assert np.median(e_split) <= 3.0 * np.median(e_fp64) + 1e-15

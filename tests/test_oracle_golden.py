@@ -7,6 +7,7 @@ The known-answer checks of the reference audit (tests/test_fpm_cdet.cpp) are
 repeated on the oracle with the audit's own tolerances.
 """
 import dataclasses
+import os
 from fractions import Fraction
 import itertools
 
@@ -156,3 +157,27 @@ def test_prefactors(order, sites, r):
     assert abs(Fraction(hi) + Fraction(lo) - exact) <= abs(exact) * Fraction(1, 2 ** 100)
     if order >= 2:
         assert abs(Fraction(ld) - exact) <= abs(exact) * Fraction(1, 2 ** 52)
+
+
+def test_long_double_truth_against_reference_high_precision():
+    """The oracle's long double integrand (the truth the FP64 and split forms
+    are measured against) agrees with the reference's own high-precision mode
+    (VECTOR_REAL=long_double, INTEGRAND_REAL=double_double; golden values of
+    precision_3x3.npz) about a hundred times more closely than the FP64
+    integrand does, order by order. The residual is the reference forming
+    (u, v) from double-double vertices, which the truth takes in double as
+    both GPU forms do."""
+    params, tables, _ = load_case("column_3x3")
+    d = np.load(os.path.join(GOLDEN, "precision_3x3.npz"))
+    orc = Oracle(params.runtime_scalars(), tables)
+    truth, st = orc.integrand_ld_batch(d["vertices"], d["orders"], threads=4)
+    fp64, _ = orc.integrand_batch(d["vertices"], d["orders"], threads=4)
+    assert st.max() == 0
+    assert bits_equal(fp64, d["values_double"])
+    high, orders = d["values_high"], d["orders"]
+    den = np.maximum(np.abs(high), 1e-300)
+    for n in range(1, 9):
+        sel = orders == n
+        truth_err = np.median(np.abs(truth - high)[sel] / den[sel])
+        fp64_err = np.median(np.abs(fp64 - high)[sel] / den[sel])
+        assert truth_err <= max(1e-15, 0.01 * fp64_err), (n, truth_err, fp64_err)
