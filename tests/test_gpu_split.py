@@ -154,6 +154,18 @@ def test_split_sub_blocks_match_fp64(nu, nv):
     assert st.max() == 0 and st64.max() == 0
     close = np.abs(split_vals - ref) / np.maximum(1.0, np.maximum(np.abs(split_vals), np.abs(ref)))
     assert np.max(close[orders == 1]) <= 1e-13
+    if (nu, nv) == (192, 192):
+        # the all-subsets (MCMCMC envelope) path through the sub-blocks: the
+        # singletons are order-1 values, functions of the diagonal only
+        env = uniform_configurations(77 + nu, 32, 6)
+        gpu.set_assembly("split")
+        sa, sst = gpu.all_subsets_batch(env)
+        gpu.set_assembly("fp64")
+        fa, fst = gpu.all_subsets_batch(env)
+        assert sst.max() == 0 and fst.max() == 0
+        singles = [1 << i for i in range(6)]
+        a_, b_ = sa[:, singles], fa[:, singles]
+        assert np.max(np.abs(a_ - b_) / np.maximum(1.0, np.maximum(np.abs(a_), np.abs(b_)))) <= 1e-13
 
 
 def test_split_refuses_degree_above_256():
