@@ -160,7 +160,14 @@ int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
     if (ctx->scratch && batch <= ctx->scratch_batch && max_order <= ctx->scratch_order) return CDET_OK;
     const int64_t new_batch = batch > ctx->scratch_batch ? batch : ctx->scratch_batch;
     const int new_order = max_order > ctx->scratch_order ? max_order : ctx->scratch_order;
-    const size_t ws_warps = static_cast<size_t>(ctx->sm_count) * 8;
+    // minors warps with a global workspace (orders whose workspace does not
+    // fit shared memory): up to 32 per SM, as many as 4 GiB of workspace holds
+    const size_t per_warp = (cdet::minors_workspace_doubles(new_order) +
+                             static_cast<size_t>(32) * new_order * new_order) * sizeof(double);
+    size_t ws_warps = static_cast<size_t>(ctx->sm_count) * 32;
+    const size_t ws_cap = (size_t{4} << 30) / per_warp;
+    if (ws_warps > ws_cap) ws_warps = ws_cap;
+    if (ws_warps < static_cast<size_t>(ctx->sm_count) * 8) ws_warps = static_cast<size_t>(ctx->sm_count) * 8;
     const size_t bytes = cdet::scratch_bytes(new_batch, new_order, ws_warps);
     if (ctx->scratch) {
         cudaDeviceSynchronize();
