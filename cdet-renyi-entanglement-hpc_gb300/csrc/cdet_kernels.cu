@@ -228,6 +228,65 @@ __device__ double minor_by_lu(const double* a, int n, uint32_t mask, double* m) 
     return sign < 0 ? -det : det;
 }
 
+// The shift removal of mat2pm (fast_principle_minors.h:230-243) for
+// 2^11..2^14 minors, blocked so that each value is read and written twice
+// instead of once per bit: first the bits above 9, a column of 2^(n-10)
+// values per lane in registers, then bits 9..0 on chunks of 1,024 values (32
+// per lane; bits 5..9 between a lane's registers, bits 0..4 across lanes by
+// shuffles). Every value takes the same fma(-p, partner, value) updates in
+// the same (descending-bit) order as the unblocked loop, so the minors are
+// bit for bit the same.
+template <int HighBits>
+__device__ __forceinline__ void remove_shift_high(double* shifted, double p, int lane) {
+    constexpr int kCount = 1 << HighBits;
+    for (uint32_t c = lane; c < 1024u; c += kWarp) {
+        double r[kCount];
+#pragma unroll
+        for (int k = 0; k < kCount; ++k) r[k] = shifted[c + 1024u * k];
+#pragma unroll
+        for (int b = HighBits - 1; b >= 0; --b)
+#pragma unroll
+            for (int k = 0; k < kCount; ++k)
+                if (k & (1 << b)) r[k] = dfma(-p, r[k ^ (1 << b)], r[k]);
+#pragma unroll
+        for (int k = 0; k < kCount; ++k) shifted[c + 1024u * k] = r[k];
+    }
+}
+
+__device__ __forceinline__ void remove_shift_blocked(double* shifted, int n, double p, int lane) {
+    switch (n) {  // n = 11..14
+        case 11: remove_shift_high<1>(shifted, p, lane); break;
+        case 12: remove_shift_high<2>(shifted, p, lane); break;
+        case 13: remove_shift_high<3>(shifted, p, lane); break;
+        case 14: remove_shift_high<4>(shifted, p, lane); break;
+        default: break;
+    }
+    __syncwarp();
+    const uint32_t subsets = 1u << n;
+    for (uint32_t h = 0; h < subsets; h += 1024u) {
+        double r[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) r[j] = shifted[h + lane + kWarp * j];
+#pragma unroll
+        for (int b = 4; b >= 0; --b)  // bits 9..5: between registers
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (j & (1 << b)) r[j] = dfma(-p, r[j ^ (1 << b)], r[j]);
+#pragma unroll
+        for (int b = 4; b >= 0; --b) {  // bits 4..0: across lanes
+            const int m = 1 << b;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const double v = __shfl_xor_sync(0xffffffffu, r[j], m);
+                if (lane & m) r[j] = dfma(-p, v, r[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) shifted[h + lane + kWarp * j] = r[j];
+    }
+    __syncwarp();
+}
+
 // mat2pm_from_buffer (fast_principle_minors.h:120-246) for one matrix, by a
 // whole warp. On return shifted[mask] (mask >= 1) holds the principal minor
 // of the rows/columns in mask. Returns true when a pivot sent the matrix to
@@ -326,6 +385,10 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
         __syncwarp();
     }
     // remove the uniform shift by multilinearity
+    if (n >= 11 && n <= 14) {  // (at order 10 the unblocked loop on shared memory is faster)
+        remove_shift_blocked(shifted, n, p, lane);
+        return false;
+    }
     for (uint32_t step = subsets; step > 1; step >>= 1) {
         const uint32_t half = step >> 1;
         for (uint32_t q = lane; q < subsets / 2; q += kWarp) {
