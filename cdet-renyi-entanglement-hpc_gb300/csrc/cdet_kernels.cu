@@ -913,8 +913,9 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
 // ------------------------------ 3c. single-top CDet, block per configuration
 // compute_dp_ztransform (integrand_replica_randomly_sampled.h:226-290) for
 // orders 11..14, where a batch holds few configurations and a lane's 2^n-entry
-// recursion would leave the SMs nearly empty: one CTA of 256 threads per
-// configuration, a of the masks without vertex 0 and dp of the masks with it
+// recursion would leave the SMs nearly empty: one CTA per configuration (256
+// threads; 512 at n = 14, where the shared memory leaves one CTA per SM),
+// a of the masks without vertex 0 and dp of the masks with it
 // in shared memory (2^(n-1) doubles each; 128 KiB at n = 14), the masks of
 // each popcount level dealt out by colex rank. FP64 form: each mask's
 // submask sum runs on one thread in the reference's descending order with
@@ -924,7 +925,6 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
 // than threads splits each mask's submasks over a group of L lanes (a fixed
 // partition and shuffle order, so the result is deterministic).
 constexpr int kBlockCdetMaxOrder = 14;
-constexpr int kBlockCdetThreads = 256;
 
 // colex unranking with the binomials of n <= 13 in shared memory
 __device__ __forceinline__ uint32_t colex_subset_s(uint32_t r, int m, int n, const uint32_t (*binom)[16]) {
@@ -940,7 +940,7 @@ __device__ __forceinline__ uint32_t colex_subset_s(uint32_t r, int m, int n, con
     return set;
 }
 
-template <bool Fused>
+template <bool Fused, int kBlockCdetThreads>
 __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_constant__ Problem p,
                                                                 const __grid_constant__ Scratch w) {
     extern __shared__ __align__(16) unsigned char cdet_smem[];
@@ -1258,17 +1258,12 @@ cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_
     } else if (!p.all_subsets && p.max_order > kWarpCdetMaxOrder && p.max_order <= kBlockCdetMaxOrder) {
         // orders 11..14: one block per configuration (slots in decreasing order)
         const size_t csmem = sizeof(double) * (size_t{1} << p.max_order);
-        if (p.fused_cdet) {
-            err = cudaFuncSetAttribute(cdet_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(csmem));
-            if (err != cudaSuccess) return err;
-            cdet_block<true><<<static_cast<unsigned>(p.batch), kBlockCdetThreads, csmem, stream>>>(p, w);
-        } else {
-            err = cudaFuncSetAttribute(cdet_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(csmem));
-            if (err != cudaSuccess) return err;
-            cdet_block<false><<<static_cast<unsigned>(p.batch), kBlockCdetThreads, csmem, stream>>>(p, w);
-        }
+        const bool wide = p.max_order == kBlockCdetMaxOrder;
+        auto kernel = p.fused_cdet ? (wide ? cdet_block<true, 512> : cdet_block<true, 256>)
+                                   : (wide ? cdet_block<false, 512> : cdet_block<false, 256>);
+        err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csmem));
+        if (err != cudaSuccess) return err;
+        kernel<<<static_cast<unsigned>(p.batch), wide ? 512 : 256, csmem, stream>>>(p, w);
     } else {
         cdet_fp64<<<static_cast<unsigned>((p.batch + threads - 1) / threads), threads, 0, stream>>>(p, w);
     }
