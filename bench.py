@@ -134,6 +134,17 @@ def time_cpu_integrand(params, tables, vertices, orders, threads):
     return time.perf_counter() - t0, values
 
 
+def derived_rates(configs_per_s: float, order: int) -> dict:
+    """The integrand rate in the counting conventions of the workload
+    description: principal-minor subsets (2^n per matrix, 4 matrices per
+    configuration: 2 table sets x up/down, counted even where up and down
+    share one table) and subset pairs (3^n per recursion, 2 recursions per
+    configuration)."""
+    return {"principal_minor_subsets_per_s": configs_per_s * 4 * 2 ** order,
+            "subset_pairs_per_s": configs_per_s * 2 * 3 ** order,
+            "conventions": "4 x 2^n principal-minor subsets and 2 x 3^n subset pairs per configuration"}
+
+
 def long_double_truth(params, tables, vertices, orders, threads):
     """The oracle's long double evaluation of the same integrand (the checker
     of the precision statement, not a measured path)."""
@@ -332,6 +343,7 @@ def run_gpu(args):
         "stages_ms_per_step": per_step(stage_ms),
         "roofline": roofline,
         "clocks": clock_info,
+        "derived": derived_rates(value, ORDER),
         "flagged_configs": int((status & 5).astype(bool).sum()),
         "fpm_fallbacks": int((status & 2).astype(bool).sum()),
         "e2e_bit_identical": e2e_match,
@@ -689,6 +701,7 @@ def run_stress(args):
             "note": "per-configuration relative error; the FP64 integrand's own round-off floor at order 14 "
                     "(a 1-ulp change of the Green entries moves it by this much)"},
         "green_split_vs_fp64_max_rel": green_rel,
+        "derived": derived_rates(batch * args.steps / (s_ms / 1e3), order),
         "flagged_configs": {"fp64": int((f_st != 0).sum()), "split": int((s_st != 0).sum())},
         "setup_s": {"tables": build_s, "slices": slice_s},
         "device_memory_gb": {"used_after_slicing": (total_b - free_b) / 1e9, "total": total_b / 1e9},
