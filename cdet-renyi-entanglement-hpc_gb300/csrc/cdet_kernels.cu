@@ -940,16 +940,78 @@ __device__ __forceinline__ uint32_t colex_subset_s(uint32_t r, int m, int n, con
     return set;
 }
 
+// The top levels of the FP64 recursion at order 14 (at most 32 masks of
+// 2^12..2^13 terms each): the pair-update products are formed by all threads
+// into shared memory, chunk by chunk, and the two serial sums of each mask --
+// acc = acc - term and rhs = rhs + |term|, in the reference's submask order --
+// run on lane i of two different warps (so on two SM sub-partitions) instead
+// of one thread doing product, difference and sum in turn. The same
+// operations on the same operands in the same order: bit-identical.
+template <int kThreads>
+__device__ __forceinline__ void fp64_top_level(const double* ag, const double* a_s, double* dp_s, double* terms,
+                                               int terms_capacity, int masks, int kk, int nbits,
+                                               const uint32_t (*binom)[16], double threshold, bool filter,
+                                               double* chain_rhs) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int total = (1 << kk) - 1;                         // submasks of rest other than rest
+    const int chunk = terms_capacity / masks;                // terms per mask per chunk
+    const bool chain = warp < 2 && lane < masks;
+    uint32_t rest = 0;
+    double acc = 0.0, rhs = 0.0;
+    if (chain) {
+        rest = colex_subset_s(static_cast<uint32_t>(lane), kk, nbits, binom);
+        acc = ag[static_cast<int64_t>((rest << 1) | 1u) * kWarp];
+        rhs = fabs(acc);
+    }
+    for (int s0 = 0; s0 < total; s0 += chunk) {
+        const int len = min(chunk, total - s0);
+        // the products of this chunk: term j of mask i at terms[j * masks + i]
+        for (int e = tid; e < len * masks; e += kThreads) {
+            const int j = e / masks, i = e - j * masks;
+            const uint32_t r = colex_subset_s(static_cast<uint32_t>(i), kk, nbits, binom);
+            // the (s0 + j)-th submask in descending order: deposit the bits
+            // of 2^kk - 2 - (s0 + j) into the set bits of r
+            uint32_t x = static_cast<uint32_t>((1 << kk) - 2 - (s0 + j)), bits = r, sl = 0;
+            while (bits) {
+                const uint32_t lb = bits & (~bits + 1u);
+                if (x & 1u) sl |= lb;
+                x >>= 1;
+                bits ^= lb;
+            }
+            terms[j * masks + i] = dmul(dp_s[sl], a_s[r ^ sl]);
+        }
+        __syncthreads();
+        if (chain) {
+            if (warp == 0) {
+                for (int j = 0; j < len; ++j) acc = dsub(acc, terms[j * masks + lane]);
+            } else {
+                for (int j = 0; j < len; ++j) rhs = dadd(rhs, fabs(terms[j * masks + lane]));
+            }
+        }
+        __syncthreads();
+    }
+    if (chain && warp == 1) chain_rhs[lane] = rhs;
+    __syncthreads();
+    if (chain && warp == 0) {
+        if (filter && fabs(acc) < dmul(threshold, chain_rhs[lane])) acc = 0.0;
+        dp_s[rest] = acc;  // dp of mask (rest << 1) | 1, at mask >> 1
+    }
+}
+
 template <bool Fused, int kBlockCdetThreads>
 __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_constant__ Problem p,
                                                                 const __grid_constant__ Scratch w) {
     extern __shared__ __align__(16) unsigned char cdet_smem[];
     __shared__ uint32_t binom[16][16];
+    __shared__ double chain_rhs[kWarp];
     const int tid = threadIdx.x;
     const int nmax = p.max_order;
     const int half = 1 << (nmax - 1);
     double* a_s = reinterpret_cast<double*>(cdet_smem);  // a of even masks, at mask >> 1
     double* dp_s = a_s + half;                           // dp of odd masks, at mask >> 1
+    // FP64 form at order 14: the top levels' products (see fp64_top_level)
+    constexpr bool kChains = !Fused && kBlockCdetThreads == 512;
+    double* terms = dp_s + half;
     const int64_t slot = blockIdx.x;
     const int64_t c = p.sorted ? __ldg(w.config_at + slot) : slot;
     const int64_t g = slot >> 5;
@@ -991,6 +1053,14 @@ __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_con
             const int kk = k - 1;            // rest = mask >> 1 has kk of nbits bits
             const int masks = static_cast<int>(binom[nbits][kk]);
             const int subs = 1 << kk;        // submasks of rest, rest itself included
+            if constexpr (kChains) {
+                if (masks <= kWarp && subs >= 1024) {
+                    fp64_top_level<kBlockCdetThreads>(ag, a_s, dp_s, terms, half, masks, kk, nbits, binom,
+                                                      threshold, filter, chain_rhs);
+                    __syncthreads();
+                    continue;
+                }
+            }
             const int field_bias = 127 - 2046 - e * k;
             for (int base = 0; base < masks;) {
                 const int remaining = masks - base;
@@ -1257,8 +1327,9 @@ cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_
         }
     } else if (!p.all_subsets && p.max_order > kWarpCdetMaxOrder && p.max_order <= kBlockCdetMaxOrder) {
         // orders 11..14: one block per configuration (slots in decreasing order)
-        const size_t csmem = sizeof(double) * (size_t{1} << p.max_order);
         const bool wide = p.max_order == kBlockCdetMaxOrder;
+        // a and dp, plus (FP64 form at order 14) as much again / 2 for the top levels' products
+        const size_t csmem = sizeof(double) * (size_t{1} << p.max_order) * (wide && !p.fused_cdet ? 3 : 2) / 2;
         auto kernel = p.fused_cdet ? (wide ? cdet_block<true, 512> : cdet_block<true, 256>)
                                    : (wide ? cdet_block<false, 512> : cdet_block<false, 256>);
         err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csmem));
