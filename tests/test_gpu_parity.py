@@ -141,6 +141,14 @@ def test_oracle_mixed_orders_and_high_orders():
     ok = orders > 0
     assert np.array_equal(st, wst) and st[5] & L.CONFIG_BAD_INPUT
     assert bits_equal(got[ok], want[ok])
+    # orders 1..14 in one batch: the order-14 kernel (512 threads, the top
+    # levels' serial sums on separate warps) also runs the lower orders
+    v = uniform_configurations(115, 32, 14)
+    orders = np.random.default_rng(116).integers(1, 15, size=32).astype(np.int32)
+    orders[:4] = (14, 13, 12, 11)
+    got, st = gpu.integrand_batch(v, orders)
+    want, wst = orc.integrand_batch(v, orders, threads=THREADS)
+    assert np.array_equal(st, wst) and bits_equal(got, want)
     # all-subsets at envelope 9
     v = uniform_configurations(13, 64, 9)
     got, _ = gpu.all_subsets_batch(v)
