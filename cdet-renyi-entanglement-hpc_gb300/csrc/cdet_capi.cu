@@ -162,12 +162,14 @@ int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
     const int new_order = max_order > ctx->scratch_order ? max_order : ctx->scratch_order;
     // minors warps with a global workspace (orders whose workspace does not
     // fit shared memory): up to 32 per SM, as many as 4 GiB of workspace holds
+    // (at least eight, the largest block of the minors kernel, which runs
+    // no more warps than the workspace has)
     const size_t per_warp = (cdet::minors_workspace_doubles(new_order) +
                              static_cast<size_t>(32) * new_order * new_order) * sizeof(double);
     size_t ws_warps = static_cast<size_t>(ctx->sm_count) * 32;
     const size_t ws_cap = (size_t{4} << 30) / per_warp;
     if (ws_warps > ws_cap) ws_warps = ws_cap;
-    if (ws_warps < static_cast<size_t>(ctx->sm_count) * 8) ws_warps = static_cast<size_t>(ctx->sm_count) * 8;
+    if (ws_warps < 8) ws_warps = 8;
     const size_t bytes = cdet::scratch_bytes(new_batch, new_order, ws_warps);
     if (ctx->scratch) {
         cudaDeviceSynchronize();
