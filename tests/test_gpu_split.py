@@ -122,7 +122,8 @@ def test_split_deterministic_and_full_path():
     assert np.max(close) <= 1e-13
 
 
-@pytest.mark.parametrize("nu,nv", [(160, 160), (192, 192), (256, 256), (136, 200), (200, 100)])
+@pytest.mark.parametrize("nu,nv", [(160, 160), (192, 192), (256, 256), (136, 200), (200, 100), (96, 160),
+                                   (129, 129)])
 def test_split_sub_blocks_match_fp64(nu, nv):
     """Degrees above 128: each coefficient block is assembled as sub-blocks
     of at most 128 rows x 128 columns whose exact parts are added before one
