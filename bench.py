@@ -360,7 +360,7 @@ def run_gpu(args):
             line["split_vs_fp64_rel_err_order10"] = {
                 "median": float(np.median(rel)), "p90": float(np.percentile(rel, 90)),
                 "note": "FP64 round-off floor at order 10 (any 1-ulp change of the Green entries "
-                        "moves the FP64 integrand by this much); see DESIGN.md"}
+                        "moves the FP64 integrand by this much); see precision_vs_long_double_truth"}
     if rank == 0 and head == "split":
         # Green-matrix agreement of the two assemblies on a 2048-configuration sample
         sample = d_vertices[0][:2048].contiguous()
