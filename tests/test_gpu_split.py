@@ -134,6 +134,7 @@ def test_split_sub_blocks_match_fp64(nu, nv):
                         mask_sites=named_mask("first_column", 3, 3), cheb_nu=nu, cheb_nv=nv)
     tables = build_tables(params, device="cuda")
     v = uniform_configurations(900 + nu + nv, 192, 7)
+    v[::11, 0, 0] = 0.0  # vertex 0 at tau = 0: its pairs take the corner path
     orders = np.full(192, 7, dtype=np.int32)
     orders[::5] = 1
     gpu, g64, d64, gsp, dsp = _green_both(params, tables, v, orders)
