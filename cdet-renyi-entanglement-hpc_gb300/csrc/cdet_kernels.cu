@@ -745,6 +745,12 @@ __device__ __forceinline__ float product_magnitude(double x, double y, int field
 // and the other bits by the outer loop, in a fixed order, so the result is
 // deterministic. The excluded submask sm = rest (its dp is this level's, not
 // yet written) contributes exact zeros.
+// Shared-memory slot of entry x of a warp's a or dp array in cdet_split_warp:
+// bits 4..7 folded into the bank bits 0..3, which spreads the lanes' entries
+// (masks of one level) over more banks.
+__device__ __forceinline__ uint32_t swz(uint32_t x) { return x ^ ((x >> 4) & 15u); }
+
+template <bool Swz>
 __device__ __forceinline__ void fused_submask_sum(const double* dp_s, const double* a_s, uint32_t rest,
                                                   uint32_t fixed, uint32_t low, int field_bias, double& part,
                                                   float& rpart) {
@@ -752,7 +758,7 @@ __device__ __forceinline__ void fused_submask_sum(const double* dp_s, const doub
         for (uint32_t sl = low;; sl = (sl - 1u) & low) {
             const uint32_t sm = fixed | sl;
             if (sm != rest) {
-                const double x = dp_s[sm], y = a_s[rest ^ sm];
+                const double x = dp_s[Swz ? swz(sm) : sm], y = a_s[Swz ? swz(rest ^ sm) : (rest ^ sm)];
                 part = __fma_rn(x, y, part);
                 rpart += product_magnitude(x, y, field_bias);
             }
@@ -774,8 +780,8 @@ __device__ __forceinline__ void fused_submask_sum(const double* dp_s, const doub
         for (int j = 7; j >= 0; --j) {
             const uint32_t sm = base | ((j & 4) ? b2 : 0u) | ((j & 2) ? b1 : 0u) | ((j & 1) ? b0 : 0u);
             const bool skip = sm == rest;
-            const double x = skip ? 0.0 : dp_s[sm];
-            const double y = skip ? 0.0 : a_s[rest ^ sm];
+            const double x = skip ? 0.0 : dp_s[Swz ? swz(sm) : sm];
+            const double y = skip ? 0.0 : a_s[Swz ? swz(rest ^ sm) : (rest ^ sm)];
             if (j & 1) {
                 p1 = __fma_rn(x, y, p1);
                 m1 += product_magnitude(x, y, field_bias);
@@ -837,9 +843,9 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
                 if (field != 0 && field != 0x7FF) e = field - 1023;
                 e = e > 90 ? 90 : (e < -90 ? -90 : e);  // |e| * nmax stays within 1000
             }
-            for (int m2 = lane; m2 < count / 2; m2 += kWarp) a_s[m2] = ag[static_cast<int64_t>(2 * m2) * kWarp];
+            for (int m2 = lane; m2 < count / 2; m2 += kWarp) a_s[swz(m2)] = ag[static_cast<int64_t>(2 * m2) * kWarp];
             __syncwarp();
-            if (lane == 0) dp_s[0] = ag[1 * kWarp];
+            if (lane == 0) dp_s[swz(0)] = ag[1 * kWarp];
             __syncwarp();
             const int nbits = n - 1;
             for (int k = 2; k <= n; ++k) {
@@ -880,7 +886,7 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
                             if ((j >> t) & 1) fixed |= lb;
                             tb ^= lb;
                         }
-                        fused_submask_sum(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
+                        fused_submask_sum<true>(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
                     }
                     for (int off = 1; off < L; off <<= 1) {
                         part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));
@@ -891,14 +897,14 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
                         double acc = dsub(am, part);
                         const float rhs = scaled_magnitude(am, -e * k) + rpart;
                         if (filter && scaled_magnitude(acc, -e * k) < thresholdf * rhs) acc = 0.0;
-                        dp_s[mask >> 1] = acc;
+                        dp_s[swz(mask >> 1)] = acc;
                     }
                     base += take;
                 }
                 __syncwarp();
             }
             const DDPair pf = p.pref_dd[set][n];
-            value = dd_mul(DD{pf.hi, pf.lo}, DD{dp_s[(count - 1) >> 1], 0.0});
+            value = dd_mul(DD{pf.hi, pf.lo}, DD{dp_s[swz((count - 1) >> 1)], 0.0});
             if (!dd_finite(value)) status |= kStatusNonFinite;
             __syncwarp();  // the next set reuses the arrays
         }
@@ -1111,7 +1117,7 @@ __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_con
                             if ((j >> t) & 1) fixed |= lb;
                             tb ^= lb;
                         }
-                        fused_submask_sum(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
+                        fused_submask_sum<false>(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
                     }
                     for (int off = 1; off < L; off <<= 1) {
                         part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));

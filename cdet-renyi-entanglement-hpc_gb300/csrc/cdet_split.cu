@@ -346,11 +346,16 @@ __device__ __forceinline__ double clamp_unit_s(double value) {
     return value;
 }
 
+// Records per vertex pair: one per distinct up/down table of each set.
+__host__ __device__ __forceinline__ int records_per_pair(const SplitPlan& plan) {
+    return plan.records_per_set[0] + plan.records_per_set[1];
+}
+
 // One thread per (configuration, i, j): branch and (u, v) are shared by both
 // table sets; the corner path is evaluated here, every other lookup becomes
 // one record per sub-block of its coefficient block, keyed by the sub-block.
-// Record slots are fixed: (((c * nmax^2 + pair) * 2 + set) * 2 + spin_record)
-// * nsub + sub.
+// Record slots are fixed: ((c * nmax^2 + pair) * records_per_pair + record)
+// * nsub + sub, the set's records after those of the sets before it.
 __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__ Problem p,
                                                          const __grid_constant__ Scratch w,
                                                          const __grid_constant__ SplitPlan plan,
@@ -363,8 +368,9 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
     const int pair = static_cast<int>(idx - c * per_c);
     const int i = pair / nmax, j = pair - (pair / nmax) * nmax;
     const int nsub = plan.nrb * plan.nkc;
-    const int64_t slot0 = idx * 4 * nsub;
-    for (int k = 0; k < 4 * nsub; ++k) rec.key[slot0 + k] = kNoKey;
+    const int rpp = records_per_pair(plan);
+    const int64_t slot0 = idx * rpp * nsub;
+    for (int k = 0; k < rpp * nsub; ++k) rec.key[slot0 + k] = kNoKey;
     const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
     if (n < 1 || n > nmax) {
         if (pair == 0) atomicOr(p.status + c, kStatusBadInput);
@@ -424,7 +430,7 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
             const uint64_t info = pack_info(c, set, plan.spin_mask[set][r], i, j, n);
             for (int sub = 0; sub < nsub; ++sub) {
                 const uint32_t key = plan.segment_base[seg] + static_cast<uint32_t>(sitepair * nsub + sub);
-                const int64_t slot = slot0 + (set * 2 + r) * nsub + sub;
+                const int64_t slot = slot0 + ((set ? plan.records_per_set[0] : 0) + r) * nsub + sub;
                 rec.key[slot] = key;
                 rec.u[slot] = u;
                 rec.v[slot] = v;
@@ -663,14 +669,16 @@ __device__ __forceinline__ void store_green(const Problem& p, const Scratch& w, 
 }
 
 // Record slot of a lookup's sub-block part (the slot its descriptor filled).
-__device__ __forceinline__ int64_t part_slot(uint64_t info, int nmax, int nsub, int sub) {
+__device__ __forceinline__ int64_t part_slot(uint64_t info, const SplitPlan& plan, int nmax, int sub) {
     const int64_t c = static_cast<int64_t>(info & 0xFFFFFFFFu);
     const int set = static_cast<int>((info >> 32) & 1);
     const int spins = static_cast<int>((info >> 33) & 3);
     const int i = static_cast<int>((info >> 35) & 31);
     const int jj = static_cast<int>((info >> 40) & 31);
     const int record = spins == 2 ? 1 : 0;  // the spin-down record of a set with two tables
-    return (((c * nmax + i) * nmax + jj) * 4 + set * 2 + record) * nsub + sub;
+    const int64_t nsub = plan.nrb * plan.nkc;
+    return (((c * nmax + i) * nmax + jj) * records_per_pair(plan) + (set ? plan.records_per_set[0] : 0) + record) *
+               nsub + sub;
 }
 
 // T_parity, T_{parity+2}, T_{parity+4}, ... of x in Q62 fixed point, by the
@@ -979,7 +987,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                     store_green(p, w, info,
                                 int128_to_double(sh.sums[l][1], static_cast<uint64_t>(sh.sums[l][0]), exponent - 55));
                 } else {
-                    const int64_t slot = part_slot(info, nmax, plan.nrb * plan.nkc, meta.sub);
+                    const int64_t slot = part_slot(info, plan, nmax, meta.sub);
                     parts[2 * slot] = sh.sums[l][0];
                     parts[2 * slot + 1] = sh.sums[l][1];
                 }
@@ -1127,8 +1135,9 @@ __global__ void __launch_bounds__(128) split_combine(const __grid_constant__ Pro
     const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= p.batch * per_c) return;
     const int nsub = plan.nrb * plan.nkc;
-    for (int k = 0; k < 4; ++k) {
-        const int64_t base = (idx * 4 + k) * nsub;
+    const int rpp = records_per_pair(plan);
+    for (int k = 0; k < rpp; ++k) {
+        const int64_t base = (idx * rpp + k) * nsub;
         const uint32_t key = rec.key[base];
         if (key == kNoKey) continue;
         uint64_t lo = 0;
@@ -1171,7 +1180,7 @@ cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t bloc
 
 size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan) {
     const size_t nsub = static_cast<size_t>(plan.nrb) * plan.nkc;
-    const size_t nrec = static_cast<size_t>(batch) * max_order * max_order * 4 * nsub;
+    const size_t nrec = static_cast<size_t>(batch) * max_order * max_order * records_per_pair(plan) * nsub;
     size_t total = 0;
     total += nrec * (4 + 8 + 8 + 8);          // unsorted records
     total += nrec * (8 + 8 + 8);              // sorted records
@@ -1187,7 +1196,7 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
                                   cudaStream_t stream, const KernelEvents* events) {
     const int64_t pairs = p.batch * static_cast<int64_t>(p.max_order) * p.max_order;
     const int nsub = plan.nrb * plan.nkc;
-    const int64_t nrec = pairs * 4 * nsub;
+    const int64_t nrec = pairs * records_per_pair(plan) * nsub;
     char* cursor = static_cast<char*>(scratch);
     auto take = [&](size_t bytes) {
         void* ptr = cursor;

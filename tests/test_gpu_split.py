@@ -240,3 +240,18 @@ def test_split_error_against_long_double_truth():
     print(f"4x4 degree 64 order 8: median rel error vs truth split {np.median(e_split):.2e} "
           f"fp64 {np.median(e_fp64):.2e}")
     assert np.median(e_split) <= 3.0 * np.median(e_fp64) + 1e-15
+
+
+def test_split_sub_blocks_unaliased():
+    """Degree above 128 with four distinct tables (alpha_up != alpha_down:
+    two records per set, each cut into sub-blocks)."""
+    params = CdetParams(n1=2, n2=2, beta="2.5", mu="0.3", u="1.7", alpha_up="0.55", alpha_down="0.4",
+                        mask_sites=named_mask("first_row", 2, 2), cheb_nu=144, cheb_nv=144)
+    tables = build_tables(params, device="cuda")
+    v = uniform_configurations(1444, 128, 6)
+    v[::9, 0, 0] = 0.0
+    orders = np.full(128, 6, dtype=np.int32)
+    orders[::4] = 1
+    _, g64, d64, gsp, dsp = _green_both(params, tables, v, orders)
+    _check_green(g64, gsp, orders, 6)
+    assert np.max(np.abs(d64 - dsp)) <= GREEN_TOL * np.max(np.abs(d64))
