@@ -59,6 +59,13 @@ def workload_params():
                       mask_sites=named_mask("origin_square", 8, 8, 2), cheb_nu=128, cheb_nv=128)
 
 
+def line_config(head: str, world: int) -> dict:
+    """The `config` of the bench line, shared by both arms so that the
+    reference arm's line names the same workload."""
+    return dict(WORKLOAD, path=head, parallelism=f"replicas x{world}",
+                l2="flushed between steps (512 MiB write); tables 8.6 GB > L2")
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -186,9 +193,11 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform vertices)",
-        "config": dict(WORKLOAD, batch_per_step=sample),
+        "config": line_config("split", args.gpus),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{sample} configurations per step of the workload, "
+                         "batch_per_step": sample,
+                         "sample": f"{sample} configurations per step of the workload's 65,536 "
+                                   f"(same lattice, tables, order and vertex distribution), "
                                    f"{threads} threads (C restatement of the reference integrand, "
                                    "bit-identical to it on the golden vectors)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

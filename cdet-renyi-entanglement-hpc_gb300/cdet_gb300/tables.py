@@ -105,6 +105,27 @@ def branch_node_times(tables: NodeTables, beta: float, upper: bool):
     return tau, tau_p
 
 
+_LINALG_PRELOADED = False
+
+
+def _preload_cuda_linalg() -> None:
+    """Loads torch's CUDA linear-algebra library by its full path before the
+    first batched solve on the GPU. torch opens it lazily by bare file name,
+    which resolves through its own library's search path; a process whose
+    dlopen calls are interposed (a profiler's launch capture) resolves the
+    bare name without that path and fails. A library already loaded by its
+    soname satisfies the later bare-name open."""
+    global _LINALG_PRELOADED
+    if _LINALG_PRELOADED:
+        return
+    _LINALG_PRELOADED = True
+    import ctypes
+    import os
+    path = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
+    if os.path.exists(path):
+        ctypes.CDLL(path, mode=ctypes.RTLD_GLOBAL)
+
+
 class ReplicaGreenCalculator:
     """The free two-replica Green function of one spin species, in batches of
     imaginary-time nodes (ReplicaGreenCalculator, replica_free_greens.h:171-701)."""
@@ -115,6 +136,8 @@ class ReplicaGreenCalculator:
         self.n1, self.n2, self.beta = n1, n2, float(beta)
         self.sites = n1 * n2
         self.device = torch.device(device)
+        if self.device.type == "cuda":
+            _preload_cuda_linalg()
         h = square_lattice_hamiltonian(n1, n2, float(mu), float(hopping_t), pbc)
         evals, evecs = np.linalg.eigh(h)
         self.eigenvalues = evals

@@ -525,22 +525,33 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
 namespace cdet {
 
 // Runs the FP64 form on scratch memory the caller provides (at least
-// scratch_bytes(batch, max_order, ws_warps) bytes), allocating nothing and
-// recording no profiling events. Used by the no-allocation entry point.
+// scratch_bytes(batch, max_order, ws_warps, regions) bytes), allocating
+// nothing and recording no profiling events. Used by the no-allocation entry
+// point.
 int run_fp64_on_scratch(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
                         int max_order, double* values, int32_t* status, void* scratch, size_t ws_warps,
-                        cudaStream_t stream) {
+                        ScratchRegions regions, cudaStream_t stream) {
     Problem p;
     int rc = build_problem(ctx, vertices, orders, batch, max_order, 0, values, status, &p);
     if (rc != CDET_OK) return rc;
     p.fused_cdet = 0;  // the FP64 form throughout, whatever assembly the context selects
     Scratch w;
-    carve_scratch(scratch, batch, max_order, ws_warps, &w);
+    carve_scratch(scratch, batch, max_order, ws_warps, &w, regions);
     cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);
     if (err != cudaSuccess) return cuda_fail(err, "cudaMemsetAsync(status)");
     err = launch_fp64_integrand(p, w, ctx->sm_count, stream, nullptr);
     if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
     ctx->last_launches = 3 + (sorts_orders(p) ? 3 : 0);
+    return CDET_OK;
+}
+
+// Whether some table set evaluates two spins (distinct up and down tables or
+// diagonal shifts); the minors then keep the spin-down minors too.
+int context_two_spins(cdet_context* ctx, bool* two_spins) {
+    Problem p;
+    const int rc = build_problem(ctx, nullptr, nullptr, 0, 1, 0, nullptr, nullptr, &p);
+    if (rc != CDET_OK) return rc;
+    *two_spins = !(p.same_spin[0] && p.same_spin[1]);
     return CDET_OK;
 }
 

@@ -1152,6 +1152,23 @@ __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_con
 
 size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).total; }
 
+// Warps of the minors kernel whose workspaces fit one block's shared memory
+// (at most 8); the kernel uses shared memory when this is at least 4.
+static int minors_warps_in_shared_memory(int max_order, bool two_spins) {
+    const size_t ws_bytes = ws_layout(max_order, two_spins).total * sizeof(double);
+    const size_t smem_budget = 227 * 1024;
+    return static_cast<int>(std::min<size_t>(8, smem_budget / ws_bytes));
+}
+
+bool minors_use_global_workspace(int max_order, bool two_spins) {
+    return minors_warps_in_shared_memory(max_order, two_spins) < 4;
+}
+
+bool fp64_single_order_uses_dp_lanes(int max_order) {
+    // orders 11..14 run the block CDet (a and dp in shared memory)
+    return !(max_order > kWarpCdetMaxOrder && max_order <= kBlockCdetMaxOrder);
+}
+
 cudaError_t launch_fp64_assembly_only(const Problem& p, const Scratch& w, cudaStream_t stream) {
     if (p.batch <= 0) return cudaSuccess;
     const int64_t entries = p.batch * 2 * static_cast<int64_t>(p.max_order) * p.max_order;
@@ -1195,21 +1212,22 @@ __global__ void order_scatter(const int32_t* __restrict__ orders, int64_t batch,
     }
 }
 
-size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps) {
+size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps, ScratchRegions regions) {
     const size_t groups = static_cast<size_t>((batch + 31) / 32);
     const size_t n2 = static_cast<size_t>(max_order) * max_order;
     const size_t subsets = static_cast<size_t>(1) << max_order;
     size_t total = 0;
     total += static_cast<size_t>(batch) * 4 * n2;                   // green
     total += static_cast<size_t>(batch) * 4 * max_order;            // diag
-    total += 2 * groups * 2 * subsets * kWarp;                      // a_int, dp_int
-    total += ws_warps * minors_workspace_doubles(max_order);        // minors workspace
+    total += (regions.dp_lanes ? 2 : 1) * groups * 2 * subsets * kWarp;  // a_int, dp_int
+    if (regions.minors_workspace) total += ws_warps * minors_workspace_doubles(max_order);  // minors workspace
     total += ws_warps * kWarp * n2;                                 // LU fallback scratch
     total += 2 * ((static_cast<size_t>(batch) * 4 + 7) / 8) + 32;   // order-sorted slots, buckets
     return total * sizeof(double) + 64 * 9;
 }
 
-void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out) {
+void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out,
+                   ScratchRegions regions) {
     const size_t groups = static_cast<size_t>((batch + 31) / 32);
     const size_t n2 = static_cast<size_t>(max_order) * max_order;
     const size_t subsets = static_cast<size_t>(1) << max_order;
@@ -1222,8 +1240,8 @@ void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Sc
     out->green = take(static_cast<size_t>(batch) * 4 * n2);
     out->diag = take(static_cast<size_t>(batch) * 4 * max_order);
     out->a_int = take(groups * 2 * subsets * kWarp);
-    out->dp_int = take(groups * 2 * subsets * kWarp);
-    out->ws_global = take(ws_warps * minors_workspace_doubles(max_order));
+    out->dp_int = regions.dp_lanes ? take(groups * 2 * subsets * kWarp) : nullptr;
+    out->ws_global = regions.minors_workspace ? take(ws_warps * minors_workspace_doubles(max_order)) : nullptr;
     out->lu_scratch = take(ws_warps * kWarp * n2);
     out->ws_warps = ws_warps;
     out->slot_of = reinterpret_cast<int32_t*>(take((static_cast<size_t>(batch) * 4 + 7) / 8));
@@ -1279,8 +1297,7 @@ cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_
     // otherwise to the global workspace (4 warps per block).
     const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
     const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(double);
-    const size_t smem_budget = 227 * 1024;
-    const int fit = static_cast<int>(std::min<size_t>(8, smem_budget / ws_bytes));
+    const int fit = minors_warps_in_shared_memory(p.max_order, two_spins);
     const bool use_smem = fit >= 4;
     const int warps_per_block = use_smem ? fit : 4;
     const int64_t items = p.batch * 2;

@@ -112,8 +112,23 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
 
 cudaError_t launch_fp64_assembly_only(const Problem& p, const Scratch& scratch, cudaStream_t stream);
 size_t minors_workspace_doubles(int max_order);
-size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps);
-void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out);
+// Whether the minors kernel keeps its per-warp workspace in global memory
+// (orders whose workspace does not fit four warps' worth of shared memory).
+bool minors_use_global_workspace(int max_order, bool two_spins);
+// Whether the FP64 form's CDet of a single-order batch (not all-subsets)
+// keeps dp in the lane-interleaved global array.
+bool fp64_single_order_uses_dp_lanes(int max_order);
+// Which optional regions a scratch carve holds: the global minors workspace
+// and the lane-interleaved dp array of the lane-per-configuration CDet. Both
+// default to present; a caller with a fixed budget leaves out what its
+// launches do not touch.
+struct ScratchRegions {
+    bool minors_workspace = true;
+    bool dp_lanes = true;
+};
+size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps, ScratchRegions regions = {});
+void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out,
+                   ScratchRegions regions = {});
 // assembly = true launches the FP64 Green-matrix assembly first; false
 // expects the Green matrices already in scratch (split-precision assembly).
 // One MCMCMC step for a batch of chains (uniform or histogram seed kernel),

@@ -129,18 +129,28 @@ int cdet_all_subsets_device(cdet_context* ctx, const double* vertices, int envel
                             int64_t batch, double* values, int32_t* status, void* stream);
 
 /* No counterpart in the reference. The single-order FP64 integrand of
- * cdet_integrand_device, for callers that cannot let the library allocate
- * device memory: a driver that captures its step into a CUDA graph (no
- * allocation is allowed during stream capture), or a process that has given
- * HBM to its tables or to its own pool. Its scratch is a fixed 64 MiB array
- * of device memory held by every GPU that loads the library; batches that
- * need more (about 1,200 configurations of order 10, or more at lower order)
- * are rejected with CDET_ERR_INVALID and a message. Tables must already be
+ * cdet_integrand_device (same values bit for bit), for callers that cannot
+ * let the library allocate device memory: a process that has given HBM to
+ * its tables or to a pool allocator of its own, where a library's
+ * cudaMalloc would take memory the owner has not accounted for. Its scratch
+ * is a fixed 64 MiB array of device memory held by every GPU that loads the
+ * library. A batch whose regions leave room for fewer than eight warps of
+ * minors workspace is rejected with CDET_ERR_INVALID and a message; the
+ * largest batches accepted, by maximum order:
+ *
+ *   order      1..4         5      6      7      8      9     10
+ *   batch   >= 57,823  33,662 19,712 11,360  6,368  3,456  1,824
+ *   order     11     12     13     14     15    >= 16
+ *   batch  1,774    928    448    224     32   refused
+ *
+ * (near these limits the minors run on few warps). Tables must already be
  * on the device (cdet_bind_device_table allocates nothing). The first call
  * on a device looks up the array's device address, so it should come before
- * any stream capture. All calls share the array: calls that overlap on the
- * GPU race, so keep them on one stream or order them. Always the FP64
- * assembly (the split assembly needs allocations). */
+ * any stream capture; the address is cached for the life of the process
+ * (the device's primary context must not be reset in between). All calls
+ * share the array: calls that overlap on the GPU race, so keep them on one
+ * stream or order them. Always the FP64 assembly, whatever the context's
+ * assembly setting (the split assembly needs allocations). */
 int cdet_integrand_device_noalloc(cdet_context* ctx, const double* vertices, const int32_t* orders,
                                   int64_t batch, int max_order, double* values, int32_t* status,
                                   void* stream);

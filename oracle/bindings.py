@@ -85,6 +85,8 @@ class Oracle:
                                                  C.c_int64, _DP, _IP, C.c_int]
         lib.oracle_integrand_ld_batch.argtypes = [C.c_void_p, C.c_void_p, _DP, _IP, C.c_int64,
                                                   C.c_int, _DP, _IP, C.c_int]
+        lib.oracle_integrand_ld_parts_batch.argtypes = [C.c_void_p, C.c_void_p, _DP, _IP, C.c_int64,
+                                                        C.c_int, _DP, _DP, _IP, C.c_int]
         lib.oracle_mat2pm.argtypes = [_DP, C.c_int, C.c_double, C.c_double, _DP]
         lib.oracle_minors_by_lu.argtypes = [_DP, C.c_int, _DP]
         lib.oracle_ztransform.argtypes = [_DP, _DP, C.c_int, C.c_double, C.c_double]
@@ -155,6 +157,22 @@ class Oracle:
         if rc != 0:
             raise RuntimeError("oracle thread start failed")
         return out, st
+
+    def integrand_ld_parts_batch(self, vertices: np.ndarray, orders: np.ndarray, threads: int = 1):
+        """The long double truth with its twisted and ordinary parts:
+        returns (values [batch], parts [batch][2], status [batch])."""
+        v = np.ascontiguousarray(vertices, dtype=np.float64)
+        o = np.ascontiguousarray(orders, dtype=np.int32)
+        batch, max_order = v.shape[0], v.shape[1]
+        out = np.zeros(batch)
+        parts = np.zeros((batch, 2))
+        st = np.zeros(batch, dtype=np.int32)
+        rc = self.lib.oracle_integrand_ld_parts_batch(C.byref(self.scalars), C.byref(self.tables),
+                                                      _ptr(v), o.ctypes.data_as(_IP), batch, max_order,
+                                                      _ptr(out), _ptr(parts), st.ctypes.data_as(_IP), threads)
+        if rc != 0:
+            raise RuntimeError("oracle thread start failed")
+        return out, parts, st
 
     def all_subsets_batch(self, vertices: np.ndarray, threads: int = 1):
         v = np.ascontiguousarray(vertices, dtype=np.float64)

@@ -775,7 +775,13 @@ static int integrand_one_set_ld(const oracle_scalars* s, const oracle_table* tu,
 
 int oracle_integrand_ld(const oracle_scalars* s, const oracle_tables* t, const double* args, int order,
                         double* value) {
+    return oracle_integrand_ld_parts(s, t, args, order, value, NULL);
+}
+
+int oracle_integrand_ld_parts(const oracle_scalars* s, const oracle_tables* t, const double* args, int order,
+                              double* value, double* parts) {
     *value = 0.0;
+    if (parts) parts[0] = parts[1] = 0.0;
     if (order <= 0 || order > ORACLE_MAX_ORDER) return ORACLE_BAD_INPUT;
     long double v[2];
     const oracle_table* tabs[2][2] = {{&t->twisted_up, &t->twisted_down}, {&t->ordinary_up, &t->ordinary_down}};
@@ -808,6 +814,10 @@ int oracle_integrand_ld(const oracle_scalars* s, const oracle_tables* t, const d
         }
     }
     *value = (double)(v[0] - 2.0L * v[1]);
+    if (parts) {
+        parts[0] = (double)v[0];
+        parts[1] = (double)v[1];
+    }
     return isfinite(*value) ? 0 : ORACLE_NONFINITE;
 }
 
@@ -823,6 +833,7 @@ typedef struct batch_job {
     int64_t begin, end;
     double* values;
     int32_t* status;
+    double* parts;    /* mode 2: the truth's twisted and ordinary parts, [batch][2], or NULL */
 } batch_job;
 
 static void* batch_worker(void* arg) {
@@ -834,7 +845,8 @@ static void* batch_worker(void* arg) {
             st = oracle_all_subsets(job->s, job->t, v, job->max_order,
                                     job->values + (size_t)c * ((size_t)1 << job->max_order));
         } else if (job->all_subsets == 2) {
-            st = oracle_integrand_ld(job->s, job->t, v, job->orders[c], job->values + c);
+            st = oracle_integrand_ld_parts(job->s, job->t, v, job->orders[c], job->values + c,
+                                           job->parts ? job->parts + 2 * c : NULL);
         } else {
             st = oracle_integrand(job->s, job->t, v, job->orders[c], job->values + c);
         }
@@ -864,21 +876,28 @@ static int run_batch(batch_job proto, int64_t batch, int threads) {
 int oracle_integrand_batch(const oracle_scalars* s, const oracle_tables* t,
                            const double* unit_vertices, const int32_t* orders, int64_t batch,
                            int max_order, double* values, int32_t* status, int threads) {
-    batch_job proto = {s, t, unit_vertices, orders, max_order, 0, 0, 0, values, status};
+    batch_job proto = {s, t, unit_vertices, orders, max_order, 0, 0, 0, values, status, NULL};
     return run_batch(proto, batch, threads);
 }
 
 int oracle_all_subsets_batch(const oracle_scalars* s, const oracle_tables* t,
                              const double* unit_vertices, int envelope_order, int64_t batch,
                              double* values, int32_t* status, int threads) {
-    batch_job proto = {s, t, unit_vertices, NULL, envelope_order, 1, 0, 0, values, status};
+    batch_job proto = {s, t, unit_vertices, NULL, envelope_order, 1, 0, 0, values, status, NULL};
     return run_batch(proto, batch, threads);
 }
 
 int oracle_integrand_ld_batch(const oracle_scalars* s, const oracle_tables* t, const double* unit_vertices,
                               const int32_t* orders, int64_t batch, int max_order, double* values,
                               int32_t* status, int threads) {
-    batch_job proto = {s, t, unit_vertices, orders, max_order, 2, 0, 0, values, status};
+    batch_job proto = {s, t, unit_vertices, orders, max_order, 2, 0, 0, values, status, NULL};
+    return run_batch(proto, batch, threads);
+}
+
+int oracle_integrand_ld_parts_batch(const oracle_scalars* s, const oracle_tables* t, const double* unit_vertices,
+                                    const int32_t* orders, int64_t batch, int max_order, double* values,
+                                    double* parts, int32_t* status, int threads) {
+    batch_job proto = {s, t, unit_vertices, orders, max_order, 2, 0, 0, values, status, parts};
     return run_batch(proto, batch, threads);
 }
 

@@ -110,6 +110,17 @@ int oracle_integrand_ld(const oracle_scalars* s, const oracle_tables* t,
 int oracle_integrand_ld_batch(const oracle_scalars* s, const oracle_tables* t,
                               const double* unit_vertices, const int32_t* orders, int64_t batch,
                               int max_order, double* values, int32_t* status, int threads);
+/* The same truth with its two parts: parts[0] = the twisted (r = 2) set's
+ * value, parts[1] = the ordinary (r = 1) set's, value = parts[0] - 2 parts[1]
+ * (each rounded to double from long double); parts may be NULL. The batch
+ * form writes parts[c][2]. |twisted| + 2 |ordinary| is the magnitude against
+ * which the combine's cancellation-free error is measured. */
+int oracle_integrand_ld_parts(const oracle_scalars* s, const oracle_tables* t,
+                              const double* unit_vertices, int order, double* value, double* parts);
+int oracle_integrand_ld_parts_batch(const oracle_scalars* s, const oracle_tables* t,
+                                    const double* unit_vertices, const int32_t* orders, int64_t batch,
+                                    int max_order, double* values, double* parts, int32_t* status,
+                                    int threads);
 
 /* Deterministic order-1 diagonal observable (diagonal_green_observable.h:237-327):
  * out[0] = twisted - 2 * ordinary (the normalised first-order coefficient of

@@ -1,10 +1,10 @@
 """A chunked load-data directory written by the reference's own workflow, for
 the chunk loader (cdet_load_chunks).
 
-Run from the repository root in a checkout that has the reference at
-REFERENCE (default /root/reference):
+Run from the repository root with the environment variable REFERENCE set
+to the reference checkout:
 
-    python tests/golden/make_chunk_golden.py
+    REFERENCE=<reference checkout> python tests/golden/make_chunk_golden.py
 
 Runs every stage of the reference's chunked load-data workflow (plan, node
 samples, corners, sitepair transforms, diagonal reduce, validate;

@@ -1,9 +1,9 @@
 """Golden values of the order-1 diagonal observable, from the reference itself.
 
-Run from the repository root in a checkout that has the reference at
-REFERENCE (default /root/reference), after make_golden.py:
+Run from the repository root with the environment variable REFERENCE set
+to the reference checkout, after make_golden.py:
 
-    python tests/golden/make_diagonal_golden.py
+    REFERENCE=<reference checkout> python tests/golden/make_diagonal_golden.py
 
 For each golden parameter set it loads the reference-built tables stored in
 <name>.npz into the reference build (oracle/_ref/libcdet_ref.so), evaluates

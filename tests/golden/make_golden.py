@@ -1,9 +1,9 @@
 """Generates the golden vectors in this directory from the reference itself.
 
-Run from the repository root in a checkout that has the reference at
-REFERENCE (default /root/reference):
+Run from the repository root with the environment variable REFERENCE set
+to the reference checkout:
 
-    python tests/golden/make_golden.py
+    REFERENCE=<reference checkout> python tests/golden/make_golden.py
 
 It builds oracle/_ref/libcdet_ref.so (the reference's own headers compiled
 with the quad-precision Boost stand-in) and records, for a few small
@@ -27,7 +27,9 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import bindings  # noqa: E402
 
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("REFERENCE", "")
+if not REFERENCE:
+    raise SystemExit("set REFERENCE to the reference checkout (the generator compiles its headers)")
 
 # Parameter sets: name -> reference configure() arguments.
 CASES = {

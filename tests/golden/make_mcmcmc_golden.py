@@ -1,10 +1,10 @@
 """Reference MCMCMC chain trajectories (uniform seed kernel) for the device
 chain step, from the reference itself.
 
-Run from the repository root in a checkout that has the reference at
-REFERENCE (default /root/reference), after make_golden.py:
+Run from the repository root with the environment variable REFERENCE set
+to the reference checkout, after make_golden.py:
 
-    python tests/golden/make_mcmcmc_golden.py
+    REFERENCE=<reference checkout> python tests/golden/make_mcmcmc_golden.py
 
 For each golden parameter set it loads the reference-built tables stored in
 <name>.npz into the reference build and runs, per chain, the step loop of

@@ -1,9 +1,9 @@
 """Golden values of the reference's high-precision integrand mode.
 
-Run from the repository root in a checkout that has the reference at
-REFERENCE (default /root/reference), after make_golden.py:
+Run from the repository root with the environment variable REFERENCE set
+to the reference checkout, after make_golden.py:
 
-    python tests/golden/make_precision_golden.py
+    REFERENCE=<reference checkout> python tests/golden/make_precision_golden.py
 
 It loads the 3x3 one-column tables of column_3x3.npz into the reference's
 own integrand (oracle/_ref/libcdet_ref.so), selects VECTOR_REAL=long_double
@@ -27,7 +27,9 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import bindings  # noqa: E402
 from make_golden import CASES  # noqa: E402
 
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("REFERENCE", "")
+if not REFERENCE:
+    raise SystemExit("set REFERENCE to the reference checkout (the generator compiles its headers)")
 
 
 def main() -> None:
