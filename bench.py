@@ -343,8 +343,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f64 (split fp16-digit tcgen05 assembly, FP64 minors and CDet)" if head == "split" else "f64",
         "data": "synthetic (seeded uniform vertices, tables from the in-tree precompute)",
-        "config": dict(WORKLOAD, path=head, parallelism=f"replicas x{world}",
-                       l2="flushed between steps (512 MiB write); tables 8.6 GB > L2"),
+        "config": line_config(head, world),
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": BATCH * ORDER * 4 * 8 + BATCH * 4,
                 "d2h_bytes_per_step": BATCH * 8 + BATCH * 4},

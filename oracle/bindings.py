@@ -159,13 +159,14 @@ class Oracle:
         return out, st
 
     def integrand_ld_parts_batch(self, vertices: np.ndarray, orders: np.ndarray, threads: int = 1):
-        """The long double truth with its twisted and ordinary parts:
-        returns (values [batch], parts [batch][2], status [batch])."""
+        """The long double truth with its parts: returns (values [batch],
+        parts [batch][4] = twisted, ordinary, twisted magnitude, ordinary
+        magnitude (see oracle_integrand_ld_parts), status [batch])."""
         v = np.ascontiguousarray(vertices, dtype=np.float64)
         o = np.ascontiguousarray(orders, dtype=np.int32)
         batch, max_order = v.shape[0], v.shape[1]
         out = np.zeros(batch)
-        parts = np.zeros((batch, 2))
+        parts = np.zeros((batch, 4))
         st = np.zeros(batch, dtype=np.int32)
         rc = self.lib.oracle_integrand_ld_parts_batch(C.byref(self.scalars), C.byref(self.tables),
                                                       _ptr(v), o.ctypes.data_as(_IP), batch, max_order,

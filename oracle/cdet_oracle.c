@@ -711,8 +711,13 @@ static long double minor_lu_ld(const long double* a, int n, uint64_t mask) {
     return det;
 }
 
+/* magnitude (may be NULL): the same prefactor times the connected recursion
+ * run on absolute values, |dp|[m] = |a[m]| + sum |dp|[s] |a[m \ s]| (the
+ * recursion's condition scale: the sum of the magnitudes of every term that
+ * enters the top mask's value, through every level). */
 static int integrand_one_set_ld(const oracle_scalars* s, const oracle_table* tu, const oracle_table* td,
-                                const double* args, int order, int replica_count, long double* value) {
+                                const double* args, int order, int replica_count, long double* value,
+                                long double* magnitude) {
     vertex vx[ORACLE_MAX_ORDER];
     long double mu[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER], md[ORACLE_MAX_ORDER * ORACLE_MAX_ORDER];
     if (decode_vertices(s, args, order, replica_count, vx)) return ORACLE_BAD_INPUT;
@@ -743,24 +748,33 @@ static int integrand_one_set_ld(const oracle_scalars* s, const oracle_table* tu,
         mu[idx] = up * (long double)s->scale;
         md[idx] = down * (long double)s->scale;
     }
+    if (order < 2) return ORACLE_BAD_INPUT;  /* order 1 is the singleton form */
     const uint64_t count = (uint64_t)1 << order;
     long double* a = (long double*)malloc(count * sizeof(long double));
     long double* dp = (long double*)malloc(count * sizeof(long double));
-    if (!a || !dp) {
+    long double* adp = magnitude ? (long double*)malloc(count * sizeof(long double)) : NULL;
+    if (!a || !dp || (magnitude && !adp)) {
         free(a);
         free(dp);
+        free(adp);
         return ORACLE_BAD_INPUT;
     }
     a[0] = 0.0L;
     for (uint64_t m = 1; m < count; ++m) a[m] = minor_lu_ld(mu, order, m) * minor_lu_ld(md, order, m);
     dp[1] = a[1];
+    if (adp) adp[1] = fabsl(a[1]);
     for (int bits = 2; bits <= order; ++bits) {
         for (uint64_t mask = 1; mask < count; mask += 2) {
             if (popcount64(mask) != bits) continue;
             long double acc = a[mask];
-            for (uint64_t sub = (mask - 1) & mask; sub; sub = (sub - 1) & mask)
-                if (sub & 1u) acc -= dp[sub] * a[mask ^ sub];
+            long double mag = fabsl(a[mask]);
+            for (uint64_t sub = (mask - 1) & mask; sub; sub = (sub - 1) & mask) {
+                if (!(sub & 1u)) continue;
+                acc -= dp[sub] * a[mask ^ sub];
+                if (adp) mag += adp[sub] * fabsl(a[mask ^ sub]);
+            }
             dp[mask] = acc;
+            if (adp) adp[mask] = mag;
         }
     }
     long double pref = 1.0L;
@@ -768,8 +782,10 @@ static int integrand_one_set_ld(const oracle_scalars* s, const oracle_table* tu,
     long double den = (long double)s->n1 * (long double)s->n2;
     for (int i = 2; i <= order; ++i) den *= (long double)i;
     *value = pref / den * dp[count - 1];
+    if (magnitude) *magnitude = fabsl(pref / den) * adp[count - 1];
     free(a);
     free(dp);
+    free(adp);
     return 0;
 }
 
@@ -781,9 +797,9 @@ int oracle_integrand_ld(const oracle_scalars* s, const oracle_tables* t, const d
 int oracle_integrand_ld_parts(const oracle_scalars* s, const oracle_tables* t, const double* args, int order,
                               double* value, double* parts) {
     *value = 0.0;
-    if (parts) parts[0] = parts[1] = 0.0;
+    if (parts) parts[0] = parts[1] = parts[2] = parts[3] = 0.0;
     if (order <= 0 || order > ORACLE_MAX_ORDER) return ORACLE_BAD_INPUT;
-    long double v[2];
+    long double v[2], mag[2];
     const oracle_table* tabs[2][2] = {{&t->twisted_up, &t->twisted_down}, {&t->ordinary_up, &t->ordinary_down}};
     for (int set = 0; set < 2; ++set) {
         const int r = set == 0 ? 2 : 1;
@@ -808,8 +824,11 @@ int oracle_integrand_ld_parts(const oracle_scalars* s, const oracle_tables* t, c
             const long double sd = down + (long double)s->diag_down_shift;
             const long double counter = (long double)s->diag_up_shift * (long double)s->diag_down_shift;
             v[set] = -(long double)r * (long double)s->u * (long double)s->beta * (su * sd - counter);
+            mag[set] = (long double)r * fabsl((long double)s->u * (long double)s->beta) *
+                       (fabsl(su * sd) + fabsl(counter));
         } else {
-            const int st = integrand_one_set_ld(s, tabs[set][0], tabs[set][1], args, order, r, &v[set]);
+            const int st = integrand_one_set_ld(s, tabs[set][0], tabs[set][1], args, order, r, &v[set],
+                                                parts ? &mag[set] : NULL);
             if (st) return st;
         }
     }
@@ -817,6 +836,8 @@ int oracle_integrand_ld_parts(const oracle_scalars* s, const oracle_tables* t, c
     if (parts) {
         parts[0] = (double)v[0];
         parts[1] = (double)v[1];
+        parts[2] = (double)mag[0];
+        parts[3] = (double)mag[1];
     }
     return isfinite(*value) ? 0 : ORACLE_NONFINITE;
 }
@@ -833,7 +854,7 @@ typedef struct batch_job {
     int64_t begin, end;
     double* values;
     int32_t* status;
-    double* parts;    /* mode 2: the truth's twisted and ordinary parts, [batch][2], or NULL */
+    double* parts;    /* mode 2: the truth's twisted and ordinary parts, [batch][4] (parts and magnitudes), or NULL */
 } batch_job;
 
 static void* batch_worker(void* arg) {
@@ -846,7 +867,7 @@ static void* batch_worker(void* arg) {
                                     job->values + (size_t)c * ((size_t)1 << job->max_order));
         } else if (job->all_subsets == 2) {
             st = oracle_integrand_ld_parts(job->s, job->t, v, job->orders[c], job->values + c,
-                                           job->parts ? job->parts + 2 * c : NULL);
+                                           job->parts ? job->parts + 4 * c : NULL);
         } else {
             st = oracle_integrand(job->s, job->t, v, job->orders[c], job->values + c);
         }

@@ -110,11 +110,15 @@ int oracle_integrand_ld(const oracle_scalars* s, const oracle_tables* t,
 int oracle_integrand_ld_batch(const oracle_scalars* s, const oracle_tables* t,
                               const double* unit_vertices, const int32_t* orders, int64_t batch,
                               int max_order, double* values, int32_t* status, int threads);
-/* The same truth with its two parts: parts[0] = the twisted (r = 2) set's
+/* The same truth with its parts: parts[0] = the twisted (r = 2) set's
  * value, parts[1] = the ordinary (r = 1) set's, value = parts[0] - 2 parts[1]
- * (each rounded to double from long double); parts may be NULL. The batch
- * form writes parts[c][2]. |twisted| + 2 |ordinary| is the magnitude against
- * which the combine's cancellation-free error is measured. */
+ * (each rounded to double from long double); parts[2], parts[3] = each
+ * set's magnitude: its prefactor's absolute value times the connected
+ * recursion run on absolute values (|dp|[m] = |a[m]| + sum |dp|[s]
+ * |a[m \ s]|), the scale of every term that enters the set's value (order
+ * 1: the two terms of the singleton). parts may be NULL; the batch form
+ * writes parts[c][4]. |twisted| + 2 |ordinary| measures the combine's
+ * cancellation, parts[2] + 2 parts[3] the whole recursion's. */
 int oracle_integrand_ld_parts(const oracle_scalars* s, const oracle_tables* t,
                               const double* unit_vertices, int order, double* value, double* parts);
 int oracle_integrand_ld_parts_batch(const oracle_scalars* s, const oracle_tables* t,
