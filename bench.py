@@ -39,10 +39,17 @@ WORKLOAD = {
     "cheb_degree": 128, "order": 10, "batch_per_gpu": 65536,
 }
 BATCH = 65536
-SPLIT_SLICE_PAIRS = 29  # tcgen05.mma per K step of the split assembly
-# DRAM bytes (read + write) of one split_assembly launch of the default
-# workload, from one ncu capture (profiles/split_assembly_8x8_d128_n10.md)
-SPLIT_ASSEMBLY_DRAM_BYTES = 12.500385e9 + 0.901431e9
+# DRAM traffic of one split_assembly launch, modelled as every coefficient
+# block's slices once (a block's tiles run back to back on one SM, so its
+# later tiles read them from L2) plus, per lookup, its record (u, v and
+# packed slot: 24 B read) and its Green entry and diagonal writes (16 B).
+# SPLIT_TRAFFIC_RATIO is measured / model from one ncu capture of the small
+# 6x6 / degree-96 case (dram__bytes_read.sum + dram__bytes_write.sum,
+# profiles/split_assembly_traffic_6x6_d96_n10.md); the bench's traffic is
+# that ratio times the model of its own workload.
+SPLIT_TRAFFIC_RATIO = None
+SPLIT_TRAFFIC_RULE = ("model (distinct coefficient blocks x slice bytes + 40 B per lookup) x measured/model ratio "
+                      "of the 6x6-d96 ncu capture")
 ORDER = 10
 L2_FLUSH_BYTES = 512 << 20
 PRESET = "8x8-d128"
@@ -57,6 +64,22 @@ def workload_params():
                           mask_sites=half_lattice_mask(6, 6), cheb_nu=96, cheb_nv=96)
     return CdetParams(n1=8, n2=8, beta="8", mu="0", u="4", alpha_up="0", alpha_down="0",
                       mask_sites=named_mask("origin_square", 8, 8, 2), cheb_nu=128, cheb_nv=128)
+
+
+def split_model_bytes(params, lookups: int) -> float:
+    """The traffic model of one split assembly launch (see SPLIT_TRAFFIC_RATIO):
+    the slices of every coefficient block the lookups reach (twisted: 4 S^2
+    site pairs, ordinary: its replica-(0,0) S^2, two branches each; all of
+    them at the benchmark batch) plus 40 B per lookup."""
+    s2 = params.sites ** 2
+    ksteps = (params.cheb_nv + 15) // 16
+    row_chunks = (params.cheb_nu + 127) // 128
+    blocks = (4 * s2 + s2) * 2
+    return blocks * row_chunks * ksteps * 32768.0 + 40.0 * lookups
+
+
+def split_dram_bytes(params, lookups: int):
+    return None if SPLIT_TRAFFIC_RATIO is None else SPLIT_TRAFFIC_RATIO * split_model_bytes(params, lookups)
 
 
 def line_config(head: str, world: int) -> dict:
@@ -330,6 +353,8 @@ def run_gpu(args):
 
     results = {path: timed(path) for path in paths}
     clock_info = clocks.stop()
+    # tcgen05.mma instructions and slice bytes of the last split assembly (one launch)
+    split_counters = integrand.split_counters() if "split" in paths else (0, 0)
     head = "split" if "split" in paths else "fp64"
     elapsed_ms, stage_ms, launches, values, status = results[head]
 
@@ -366,20 +391,30 @@ def run_gpu(args):
                 "minors": ms[2] / args.steps, "cdet": ms[3] / args.steps}
 
     if head == "split":
-        # tcgen05 kernel: 29 fp16 slice-pair products of nu x nv per lookup
-        # (28 digit pairs of levels 2..8 and the pre-scaled eighth coefficient
-        # digit); fp16 and bf16 share the dense tensor rate
+        # algorithmic work of the assembly (2 nu nv flops per lookup: the
+        # bilinear Chebyshev sum; 2 sets x n^2 lookups per configuration, one
+        # table per set since up and down share it) against the dense tensor
+        # peak; the emulation's own tensor work (the MMAs the kernel issued,
+        # counted on the device) is reported beside it
         per_launch_ms = stage_ms[1] / args.steps
-        flops = lookups * SPLIT_SLICE_PAIRS * 2.0 * nu * nv
+        flops = lookups * 2.0 * nu * nv
         achieved = flops / (per_launch_ms / 1e3) / 1e12
+        mmas, streamed = split_counters
+        issued_tflops = mmas * 2.0 * 128 * 64 * 16 / (per_launch_ms / 1e3) / 1e12
         roofline = {"kernel": "split_assembly (tcgen05 fp16 digit slices)", "bound": "tensor",
                     "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                     "frac": achieved / bf16_peak,
                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json bf16_tflops, burst; fp16 dense rate is the same)",
-                    "traffic": SPLIT_ASSEMBLY_DRAM_BYTES if PRESET == "8x8-d128" and BATCH == 65536 else None,
-                    "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                    "profiles/split_assembly_8x8_d128_n10.md)",
-                    "algorithmic": f"lookups x {SPLIT_SLICE_PAIRS} slice pairs x 2 x nu x nv"}
+                    "algorithmic": "lookups x 2 x nu x nv (2 sets x n^2 lookups per configuration)",
+                    "traffic": split_dram_bytes(params, lookups),
+                    "traffic_model_bytes": split_model_bytes(params, lookups),
+                    "traffic_rule": SPLIT_TRAFFIC_RULE,
+                    "tcgen05_mma_per_launch": mmas,
+                    "tensor_issue_tflops": issued_tflops,
+                    "tensor_issue_frac": issued_tflops / bf16_peak,
+                    "tensor_issue_note": "M=128 N=64 K=16 fp16 MMAs the kernel issued (counted on the device), "
+                                         "2*128*64*16 flops each: the emulation's tensor work, not the algorithm's",
+                    "slice_bytes_streamed_per_launch": streamed}
     else:
         per_launch_ms = stage_ms[1] / args.steps
         alg_bytes = lookups * 8 * nu * nv
@@ -667,6 +702,8 @@ def run_stress(args):
         stage_ms, launches = gpu.profile_read()
         gpu.profile(False)
         results[path] = (e0.elapsed_time(e1), stage_ms, launches, vals.cpu().numpy().copy(), st.cpu().numpy().copy())
+        if path == "split":
+            split_counters = gpu.split_counters()
     clock_info = clocks.stop()
     # end to end (split) through the host-buffer call
     gpu.set_assembly("split")
@@ -702,7 +739,8 @@ def run_stress(args):
     nu, nv = params.cheb_nu, params.cheb_nv
     lookups = batch * 2 * order * order
     assembly_ms = s_stage[1] / args.steps
-    achieved = lookups * SPLIT_SLICE_PAIRS * 2.0 * nu * nv / (assembly_ms / 1e3) / 1e12
+    achieved = lookups * 2.0 * nu * nv / (assembly_ms / 1e3) / 1e12
+    issued_tflops = split_counters[0] * 2.0 * 128 * 64 * 16 / (assembly_ms / 1e3) / 1e12
 
     def per_step(ms):
         return {"split_prep": ms[0] / args.steps, "assembly": ms[1] / args.steps,
@@ -728,8 +766,10 @@ def run_stress(args):
                      "bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": achieved / bf16_peak, "traffic": None,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json bf16_tflops)",
-                     "algorithmic": f"lookups x {SPLIT_SLICE_PAIRS} slice pairs x 2 x 192 x 192 "
-                                    "(unpadded; the sub-blocks pad rows 192..255)"},
+                     "algorithmic": "lookups x 2 x 192 x 192 (2 sets x n^2 lookups per configuration)",
+                     "tcgen05_mma_per_launch": split_counters[0],
+                     "tensor_issue_tflops": issued_tflops, "tensor_issue_frac": issued_tflops / bf16_peak,
+                     "slice_bytes_streamed_per_launch": split_counters[1]},
         "clocks": clock_info,
         "fp64_path": {"value": batch * args.steps / (f_ms / 1e3), "unit": UNIT, "ms_per_step": f_ms / args.steps,
                       "gpu_launches": int(f_launch), "stages_ms_per_step": per_step(f_stage)},

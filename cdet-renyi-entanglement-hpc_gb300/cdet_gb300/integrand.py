@@ -242,6 +242,13 @@ class CdetIntegrand:
         L.check(self._lib.cdet_profile_read(self._ctx, ms, C.byref(launches)))
         return list(ms), launches.value
 
+    def split_counters(self):
+        """(tcgen05.mma instructions issued, coefficient-slice bytes streamed)
+        by the last split-assembly evaluation; waits for it."""
+        out = (C.c_uint64 * 2)(0, 0)
+        L.check(self._lib.cdet_split_counters(self._ctx, out))
+        return int(out[0]), int(out[1])
+
     # --------------------------------------------- reference entry points ---
     def evaluate_cdet_density_integrand_double(self, vertices) -> float:
         v = _as_vertex_array(vertices)

@@ -35,6 +35,7 @@ EXPORTED = (
     "cdet_mcmcmc_destroy", "cdet_mcmcmc_set_histogram", "cdet_mcmcmc_learn_histogram", "cdet_mcmcmc_result",
     "cdet_mcmcmc_summary", "cdet_mcmcmc_estimates", "cdet_write_mcmcmc_checkpoint", "cdet_read_mcmcmc_checkpoint",
     "cdet_mcmcmc_save_checkpoints", "cdet_mcmcmc_load_checkpoints", "cdet_mcmcmc_launch_count", "cdet_set_all_subsets_form", "cdet_all_subsets_form_tuned", "cdet_load_chunks",
+    "cdet_split_counters",
 )
 
 ASSEMBLY_FP64 = 0
@@ -163,6 +164,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_assemble_device.argtypes = [vp, vp, vp, i64, i32, vp, vp, vp, vp]
     lib.cdet_profile_enable.argtypes = [vp, i32]
     lib.cdet_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.cdet_split_counters.argtypes = [vp, C.POINTER(C.c_uint64)]
     _LIB = lib
     return lib
 

@@ -238,6 +238,34 @@ def learn_histogram(integrand: CdetIntegrand, order_min: int, order_max: int, en
     return tau, space, rep, total.value
 
 
+def jackknife_ratios(results: np.ndarray, order_min: int, order_max: int, normalization_order: int) -> dict:
+    """Chain-level jackknife of the per-order ratios the reference reports
+    (run_mcmcmc_chains_parallel, mcmcmc_sampler.h:1118-1146): each chain's
+    production mean of the order signal is one sample, the ratio of order n
+    is mean over chains at n / mean over chains at the normalisation order.
+    Leaving out one chain at a time gives the jackknife estimates R_(c);
+    the error is sqrt((C - 1)/C sum_c (R_(c) - mean R_(.))^2). Returns
+    {"ratio": [envelope + 1], "error": [envelope + 1]} (NaN outside the
+    sampled orders), from `results` = McmcmcChains.results()."""
+    means = np.asarray(results["order_signal_stats"]["mean"], dtype=np.float64)  # [chains][max envelope + 1]
+    counts = np.asarray(results["order_signal_stats"]["count"])
+    chains = means.shape[0]
+    e1 = means.shape[1]
+    ratio = np.full(e1, np.nan)
+    error = np.full(e1, np.nan)
+    ref = normalization_order
+    for n in range(order_min, order_max + 1):
+        use = (counts[:, n] > 0) & (counts[:, ref] > 0)
+        m, r = means[use, n], means[use, ref]
+        k = m.size
+        if k < 2 or r.sum() == 0.0:
+            continue
+        ratio[n] = m.sum() / r.sum()
+        loo = (m.sum() - m) / (r.sum() - r)
+        error[n] = float(np.sqrt((k - 1) / k * np.sum((loo - loo.mean()) ** 2)))
+    return {"ratio": ratio, "error": error, "chains": chains}
+
+
 def mt64_outputs(state: np.ndarray, count: int) -> np.ndarray:
     """The next `count` outputs of an mt19937_64 from its [313] state (312
     words and position), without changing it."""

@@ -832,6 +832,17 @@ int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches) {
     return CDET_OK;
 }
 
+int cdet_split_counters(cdet_context* ctx, uint64_t* out) {
+    if (!ctx || !out) return fail(CDET_ERR_INVALID, "bad argument");
+    out[0] = out[1] = 0;
+    if (!ctx->split_error) return CDET_OK;
+    DeviceGuard guard(ctx->device);
+    const cudaError_t err = cudaMemcpy(out, reinterpret_cast<const char*>(ctx->split_error) + 8, 2 * sizeof(uint64_t),
+                                       cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMemcpy(split counters)");
+    return CDET_OK;
+}
+
 }  // extern "C"
 
 // ------------------------------------------------ chunked table directory --

@@ -104,6 +104,10 @@ size_t split_slices_bytes(int nu, int nv, size_t blocks);
 cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
                                int32_t* exponents, cudaStream_t stream);
 size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan);
+// Bytes of the split assembly's status region: its error flag (int32 at
+// byte 0) and counters (uint64 at byte 8: tcgen05.mma instructions issued;
+// at byte 16: coefficient-slice bytes streamed from global memory).
+constexpr size_t kSplitStatusBytes = 32;
 // Largest CHEB_NU / CHEB_NV the split assembly takes (sub-blocks of 128 x 128).
 constexpr int kSplitMaxDegree = 256;
 cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const SplitPlan& plan, void* scratch,

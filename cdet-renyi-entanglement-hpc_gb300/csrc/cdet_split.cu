@@ -731,7 +731,8 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                                                                       const SplitTile* __restrict__ tiles,
                                                                       const uint32_t* __restrict__ totals,
                                                                       int64_t* __restrict__ parts,
-                                                                      int32_t* __restrict__ error_flag) {
+                                                                      int32_t* __restrict__ error_flag,
+                                                                      unsigned long long* __restrict__ counters) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SplitShared& sh = *reinterpret_cast<SplitShared*>(smem_raw);
     const int tid = threadIdx.x;
@@ -999,6 +1000,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         // ----------------------------------------- coefficient streaming --
         if (lane == 0) {
             uint32_t a_cnt = 0;
+            unsigned long long streamed = 0;
             for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile) {
                 const TileSource src = tile_source<Chunked>(plan, tiles[tile].block);
                 for (int ks = 0; ks < src.ksteps; ++ks, ++a_cnt) {
@@ -1010,8 +1012,10 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                     mbar_expect_tx(&sh.a_full[st], kAStageBytes);
                     bulk_copy_g2s(sh.a_ring[st], src.a + static_cast<int64_t>(ks) * (kAStageBytes / 2),
                                   kAStageBytes, &sh.a_full[st]);
+                    streamed += kAStageBytes;
                 }
             }
+            if (counters) atomicAdd(counters + 1, streamed);
             // copies still in flight (only after an error) land before the CTA exits
             for (uint32_t st = 0; st < static_cast<uint32_t>(kAStages); ++st) {
                 if (a_cnt <= st) continue;
@@ -1024,6 +1028,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         if (lane == 0) {
             const uint32_t idesc = mma_idesc(kRows, kTileN);
             uint32_t a_cnt = 0, b_cnt = 0, tile_cnt = 0;
+            unsigned long long mmas = 0;
             bool ok = true, issued = false;
             // with several column chunks the K steps vary by tile: the next
             // tile's key is loaded while this one's MMAs are issued
@@ -1099,6 +1104,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                     }
                     issued = true;
                     if (!ok) break;
+                    mmas += kIssue;
                     mma_commit(&sh.a_empty[sa]);
                     mma_commit(&sh.b_empty[sb]);
                 }
@@ -1106,6 +1112,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 mma_commit(&sh.acc_full);
             }
             if (!ok) sh.error = 1;
+            if (counters) atomicAdd(counters, mmas);
             // every MMA issued has completed before the columns are freed
             if (issued) {
                 mma_commit(&sh.drain);
@@ -1187,7 +1194,7 @@ size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan) 
     total += static_cast<size_t>(plan.nblocks) * 4 * 4;  // counts, offsets, tile offsets, cursors
     total += (nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile);  // tiles
     if (nsub > 1) total += nrec * 16;         // 128-bit sub-block parts
-    total += 64;                              // totals, error flag
+    total += 16 + kSplitStatusBytes;          // totals, error flag and counters
     return total + 16 * 256;
 }
 
@@ -1214,13 +1221,16 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     SplitTile* tiles = static_cast<SplitTile*>(take((nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile)));
     int64_t* parts = nsub > 1 ? static_cast<int64_t*>(take(nrec * 16)) : nullptr;
     uint32_t* totals = static_cast<uint32_t*>(take(16));
-    int32_t* error_flag = static_cast<int32_t*>(take(16));
+    // the error flag (int32 at byte 0) and the assembly's counters (uint64 at
+    // bytes 8 and 16: MMAs issued, coefficient-slice bytes streamed)
+    int32_t* error_flag = static_cast<int32_t*>(take(kSplitStatusBytes));
+    unsigned long long* counters = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(error_flag) + 8);
     if (static_cast<size_t>(cursor - static_cast<char*>(scratch)) > scratch_bytes) return cudaErrorInvalidValue;
     if (error_flag_out) *error_flag_out = error_flag;
 
     cudaError_t err = cudaMemsetAsync(counts, 0, plan.nblocks * 4u, stream);
     if (err != cudaSuccess) return err;
-    err = cudaMemsetAsync(error_flag, 0, 4, stream);
+    err = cudaMemsetAsync(error_flag, 0, kSplitStatusBytes, stream);
     if (err != cudaSuccess) return err;
     split_descriptors<<<static_cast<unsigned>((pairs + 127) / 128), 128, 0, stream>>>(p, w, plan, rec, counts);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
@@ -1237,7 +1247,8 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     auto kernel = nsub > 1 ? split_assembly<true> : split_assembly<false>;
     err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (err != cudaSuccess) return err;
-    kernel<<<sm_count, kAssemblyThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, parts, error_flag);
+    kernel<<<sm_count, kAssemblyThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, parts, error_flag,
+                                                         counters);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     if (nsub > 1) {
         split_combine<<<static_cast<unsigned>((pairs + 127) / 128), 128, 0, stream>>>(p, w, plan, rec, parts);

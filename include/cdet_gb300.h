@@ -440,6 +440,13 @@ int cdet_assemble_device(cdet_context* ctx, const double* vertices, const int32_
 int cdet_profile_enable(cdet_context* ctx, int enable);
 int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches);
 
+/* Measurement hook; no counterpart in the reference. Counters of the last
+ * split-assembly evaluation on this context (waits for it): out[0] = the
+ * tcgen05.mma instructions its assembly kernel issued, out[1] = the
+ * coefficient-slice bytes it streamed from global memory. Both are zero
+ * before the first split evaluation. */
+int cdet_split_counters(cdet_context* ctx, uint64_t* out);
+
 #ifdef __cplusplus
 }
 #endif
