@@ -42,14 +42,15 @@ BATCH = 65536
 # DRAM traffic of one split_assembly launch, modelled as every coefficient
 # block's slices once (a block's tiles run back to back on one SM, so its
 # later tiles read them from L2) plus, per lookup, its record (u, v and
-# packed slot: 24 B read) and its Green entry and diagonal writes (16 B).
-# SPLIT_TRAFFIC_RATIO is measured / model from one ncu capture of the small
-# 6x6 / degree-96 case (dram__bytes_read.sum + dram__bytes_write.sum,
+# packed slot: 24 B read) and its two Green-entry writes (8 B each, a 32-byte
+# DRAM sector each: 64 B). SPLIT_TRAFFIC_RATIO is measured / model from one
+# ncu capture of the small 6x6 / degree-96 case (dram__bytes_read.sum +
+# dram__bytes_write.sum = 4.658 GB against a model of 3.701 GB,
 # profiles/split_assembly_traffic_6x6_d96_n10.md); the bench's traffic is
 # that ratio times the model of its own workload.
-SPLIT_TRAFFIC_RATIO = None
-SPLIT_TRAFFIC_RULE = ("model (distinct coefficient blocks x slice bytes + 40 B per lookup) x measured/model ratio "
-                      "of the 6x6-d96 ncu capture")
+SPLIT_TRAFFIC_RATIO = 4.658041856e9 / 3.70147328e9
+SPLIT_TRAFFIC_RULE = ("model (distinct coefficient blocks x slice bytes + 88 B per lookup) x the measured/model "
+                      "ratio 1.258 of the 6x6-d96 ncu capture")
 ORDER = 10
 L2_FLUSH_BYTES = 512 << 20
 PRESET = "8x8-d128"
@@ -70,12 +71,12 @@ def split_model_bytes(params, lookups: int) -> float:
     """The traffic model of one split assembly launch (see SPLIT_TRAFFIC_RATIO):
     the slices of every coefficient block the lookups reach (twisted: 4 S^2
     site pairs, ordinary: its replica-(0,0) S^2, two branches each; all of
-    them at the benchmark batch) plus 40 B per lookup."""
+    them at the benchmark batch) plus 88 B per lookup."""
     s2 = params.sites ** 2
     ksteps = (params.cheb_nv + 15) // 16
     row_chunks = (params.cheb_nu + 127) // 128
     blocks = (4 * s2 + s2) * 2
-    return blocks * row_chunks * ksteps * 32768.0 + 40.0 * lookups
+    return blocks * row_chunks * ksteps * 32768.0 + 88.0 * lookups
 
 
 def split_dram_bytes(params, lookups: int):
