@@ -515,7 +515,7 @@ def run_mcmcmc(args):
     both assemblies; the oracle's single-threaded histogram chain beside it."""
     import torch
     from cdet_gb300.integrand import CdetIntegrand
-    from cdet_gb300.mcmcmc import STREAM_TAG, McmcmcChains, learn_histogram
+    from cdet_gb300.mcmcmc import STREAM_TAG, McmcmcChains, jackknife_ratios, learn_histogram
     from cdet_gb300.params import CdetParams, half_lattice_mask
     from cdet_gb300.synthetic import derive_seed
     from cdet_gb300.tables import build_tables
@@ -552,12 +552,23 @@ def run_mcmcmc(args):
         chains.run(steps, warmup=False)
         dt = time.perf_counter() - t0
         l1, g1 = chains.launch_count()
-        out[path] = {"value": chains_n * steps / dt, "ms_per_step": 1e3 * dt / steps,
+        jack = jackknife_ratios(chains.results(), omin, omax, 1)
+        out[path] = {"ratios_to_order1": [float(x) for x in jack["ratio"][omin:omax + 1]],
+                     "jackknife_errors": [float(x) for x in jack["error"][omin:omax + 1]],"value": chains_n * steps / dt, "ms_per_step": 1e3 * dt / steps,
                      "hours_for_1e5_steps": dt / steps * 1e5 / 3600, "histogram_learning_s": learn_s,
                      "gpu_launches": l1 - l0, "graph_steps": g1 - g0}
         chains.close()
     out["value"] = out["split"]["value"]
     out["gpu_launches"] = out["split"]["gpu_launches"]
+    # split-assembly chains against FP64-assembly chains (the reference's
+    # chains): per order, the difference of the ratios to order 1 in units
+    # of the combined chain-level jackknife error
+    dz = []
+    for k in range(omax - omin + 1):
+        a, b = out["split"], out["fp64"]
+        sigma = float(np.hypot(a["jackknife_errors"][k], b["jackknife_errors"][k]))
+        dz.append((a["ratios_to_order1"][k] - b["ratios_to_order1"][k]) / sigma if sigma > 0 else None)
+    out["split_vs_fp64_ratio_delta_over_sigma"] = dz
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         from bindings import Oracle
