@@ -400,8 +400,8 @@ def run_gpu(args):
         per_launch_ms = stage_ms[1] / args.steps
         flops = lookups * 2.0 * nu * nv
         achieved = flops / (per_launch_ms / 1e3) / 1e12
-        mmas, streamed = split_counters
-        issued_tflops = mmas * 2.0 * 128 * 64 * 16 / (per_launch_ms / 1e3) / 1e12
+        mma_columns, streamed = split_counters
+        issued_tflops = mma_columns * 2.0 * 128 * 16 / (per_launch_ms / 1e3) / 1e12
         roofline = {"kernel": "split_assembly (tcgen05 fp16 digit slices)", "bound": "tensor",
                     "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                     "frac": achieved / bf16_peak,
@@ -410,11 +410,12 @@ def run_gpu(args):
                     "traffic": split_dram_bytes(params, lookups),
                     "traffic_model_bytes": split_model_bytes(params, lookups),
                     "traffic_rule": SPLIT_TRAFFIC_RULE,
-                    "tcgen05_mma_per_launch": mmas,
+                    "tcgen05_mma_columns_per_launch": mma_columns,
                     "tensor_issue_tflops": issued_tflops,
                     "tensor_issue_frac": issued_tflops / bf16_peak,
-                    "tensor_issue_note": "M=128 N=64 K=16 fp16 MMAs the kernel issued (counted on the device), "
-                                         "2*128*64*16 flops each: the emulation's tensor work, not the algorithm's",
+                    "tensor_issue_note": "accumulator columns written by the M=128 K=16 fp16 MMAs the kernel "
+                                         "issued (counted on the device), 2*128*16 flops each: the emulation's "
+                                         "tensor work, not the algorithm's",
                     "slice_bytes_streamed_per_launch": streamed}
     else:
         per_launch_ms = stage_ms[1] / args.steps
@@ -752,7 +753,7 @@ def run_stress(args):
     lookups = batch * 2 * order * order
     assembly_ms = s_stage[1] / args.steps
     achieved = lookups * 2.0 * nu * nv / (assembly_ms / 1e3) / 1e12
-    issued_tflops = split_counters[0] * 2.0 * 128 * 64 * 16 / (assembly_ms / 1e3) / 1e12
+    issued_tflops = split_counters[0] * 2.0 * 128 * 16 / (assembly_ms / 1e3) / 1e12
 
     def per_step(ms):
         return {"split_prep": ms[0] / args.steps, "assembly": ms[1] / args.steps,
@@ -779,7 +780,7 @@ def run_stress(args):
                      "frac": achieved / bf16_peak, "traffic": None,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json bf16_tflops)",
                      "algorithmic": "lookups x 2 x 192 x 192 (2 sets x n^2 lookups per configuration)",
-                     "tcgen05_mma_per_launch": split_counters[0],
+                     "tcgen05_mma_columns_per_launch": split_counters[0],
                      "tensor_issue_tflops": issued_tflops, "tensor_issue_frac": issued_tflops / bf16_peak,
                      "slice_bytes_streamed_per_launch": split_counters[1]},
         "clocks": clock_info,

@@ -243,8 +243,9 @@ class CdetIntegrand:
         return list(ms), launches.value
 
     def split_counters(self):
-        """(tcgen05.mma instructions issued, coefficient-slice bytes streamed)
-        by the last split-assembly evaluation; waits for it."""
+        """(accumulator columns written by the issued tcgen05.mma, each
+        2 x 128 x 16 flops; coefficient-slice bytes streamed) of the last
+        split-assembly evaluation; waits for it."""
         out = (C.c_uint64 * 2)(0, 0)
         L.check(self._lib.cdet_split_counters(self._ctx, out))
         return int(out[0]), int(out[1])

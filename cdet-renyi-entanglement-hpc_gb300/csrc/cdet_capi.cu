@@ -240,15 +240,22 @@ int slice_branch(cdet_context* ctx, const double* coeffs, size_t blocks, SlicedB
         return CDET_OK;
     }
     const cdet_runtime_scalars& s = ctx->scalars;
+    // slices, then the level rows (8-byte aligned), the exponents and the K-step leads
     const size_t sbytes = cdet::split_slices_bytes(s.cheb_nu, s.cheb_nv, blocks);
+    const size_t rbytes = cdet::split_level_rows_bytes(s.cheb_nu, s.cheb_nv, blocks);
+    const size_t lbytes = cdet::split_leads_bytes(s.cheb_nu, s.cheb_nv, blocks);
     SlicedBranch b;
-    cudaError_t err = cudaMalloc(&b.mem, sbytes + blocks * sizeof(int32_t) + 256);
+    cudaError_t err = cudaMalloc(&b.mem, sbytes + rbytes + blocks * sizeof(int32_t) + lbytes + 256);
     if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(split slices)");
-    b.slices = static_cast<const uint16_t*>(b.mem);
-    b.exponents = reinterpret_cast<const int32_t*>(static_cast<char*>(b.mem) + sbytes);
+    char* base = static_cast<char*>(b.mem);
+    b.slices = reinterpret_cast<const uint16_t*>(base);
+    b.level_rows = reinterpret_cast<const uint64_t*>(base + sbytes);
+    b.exponents = reinterpret_cast<const int32_t*>(base + sbytes + rbytes);
+    b.leads = reinterpret_cast<const uint8_t*>(base + sbytes + rbytes + blocks * sizeof(int32_t));
     b.blocks = blocks;
     err = cdet::launch_slice_table(coeffs, s.cheb_nu, s.cheb_nv, blocks, const_cast<uint16_t*>(b.slices),
-                                   const_cast<int32_t*>(b.exponents), nullptr);
+                                   const_cast<int32_t*>(b.exponents), const_cast<uint8_t*>(b.leads),
+                                   const_cast<uint64_t*>(b.level_rows), nullptr);
     if (err == cudaSuccess) err = cudaDeviceSynchronize();
     if (err != cudaSuccess) {
         cudaFree(b.mem);
@@ -290,6 +297,8 @@ int build_split_plan(cdet_context* ctx, cdet::SplitPlan* plan) {
                 plan->segment_base[seg] = base;
                 plan->slices[seg] = sb->slices;
                 plan->exponents[seg] = sb->exponents;
+                plan->leads[seg] = sb->leads;
+                plan->level_rows[seg] = sb->level_rows;
                 plan->segment_of[set][r][br] = seg;
                 base += static_cast<uint32_t>(blocks * nsub);
                 ++seg;

@@ -29,6 +29,8 @@ struct SlicedBranch {
     void* mem = nullptr;  // slices followed by exponents
     const uint16_t* slices = nullptr;
     const int32_t* exponents = nullptr;
+    const uint64_t* level_rows = nullptr;  // rows reaching each accumulator level, per sub-block
+    const uint8_t* leads = nullptr;        // first nonzero slice per K step
     size_t blocks = 0;
 };
 

@@ -89,6 +89,8 @@ struct SplitPlan {
     uint32_t segment_base[9];       // ascending; [segments] = total blocks
     const uint16_t* slices[8];      // bf16 slices of the segment's blocks
     const int32_t* exponents[8];    // binary exponent of each block
+    const uint8_t* leads[8];        // first nonzero slice of each K step of each sub-block row
+    const uint64_t* level_rows[8];  // per sub-block: rows reaching each accumulator level (a byte per level)
     int records_per_set[2];         // 1 when up and down share one table, else 2
     int segment_of[2][2][2];        // [set][record][0 upper, 1 lower] -> segment
     int spin_mask[2][2];            // [set][record] -> spins the record writes
@@ -101,12 +103,17 @@ struct SplitPlan {
 // the slice bytes of `blocks` blocks (each sub-block 128 rows x its K steps).
 void split_geometry(int nu, int nv, int* nrb, int* nkc, int* ksteps_last);
 size_t split_slices_bytes(int nu, int nv, size_t blocks);
+// bytes of the per-K-step leads of `blocks` blocks (one byte per K step of each row chunk)
+size_t split_leads_bytes(int nu, int nv, size_t blocks);
+// bytes of the per-sub-block level rows of `blocks` blocks (8 per sub-block)
+size_t split_level_rows_bytes(int nu, int nv, size_t blocks);
 cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
-                               int32_t* exponents, cudaStream_t stream);
+                               int32_t* exponents, uint8_t* leads, uint64_t* level_rows, cudaStream_t stream);
 size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan);
 // Bytes of the split assembly's status region: its error flag (int32 at
-// byte 0) and counters (uint64 at byte 8: tcgen05.mma instructions issued;
-// at byte 16: coefficient-slice bytes streamed from global memory).
+// byte 0) and counters (uint64 at byte 8: the accumulator columns its
+// tcgen05.mma instructions wrote, each 2 x 128 x 16 flops of issued tensor
+// work; at byte 16: coefficient-slice bytes streamed from global memory).
 constexpr size_t kSplitStatusBytes = 32;
 // Largest CHEB_NU / CHEB_NV the split assembly takes (sub-blocks of 128 x 128).
 constexpr int kSplitMaxDegree = 256;

@@ -62,16 +62,18 @@ constexpr int kSlices = 7;          // slices of the basis operand
 constexpr int kSlicesA = 8;         // slices of the coefficient operand (the eighth pre-scaled by 2^-8)
 constexpr int kLevels = 7;          // accumulator levels tau = 2..8
 constexpr int kSubK = 128;          // K columns of one sub-block: keeps every exact level below 2^24
-constexpr int kTileN = 64;          // lookups per tile (MMA N)
-constexpr int kRows = 128;          // MMA M (Chebyshev rows a, zero padded)
+constexpr int kTileN = 128;         // lookups per tile (MMA M: TMEM lanes)
+constexpr int kRows = 128;          // coefficient rows a of a sub-block (MMA N at most, zero padded)
 constexpr int kKStep = 16;          // MMA K (bf16)
 constexpr int kSubKSteps = kSubK / kKStep;  // K steps of a full column chunk
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
 
-// bytes of one A stage: 8 slices x 128 rows x 16 k x fp16
-constexpr uint32_t kAStageBytes = kSlicesA * kRows * kKStep * 2;      // 32 KiB
-// bytes of the B operand of one K step: 7 slices x 64 lookups x 16 k x fp16
-constexpr uint32_t kBStepBytes = kSlices * kTileN * kKStep * 2;       // 14 KiB
+// bytes of one slice of either operand: 128 rows x 16 k x fp16
+constexpr uint32_t kSliceBytes = kRows * kKStep * 2;                  // 4 KiB
+// bytes of the coefficient operand of one K step: 8 slices x 128 rows x 16 k x fp16
+constexpr uint32_t kAStageBytes = kSlicesA * kSliceBytes;             // 32 KiB
+// bytes of the basis operand of one K step: 7 slices x 128 lookups x 16 k x fp16
+constexpr uint32_t kBStepBytes = kSlices * kTileN * kKStep * 2;       // 28 KiB
 // Q56 basis value -> byte digits: +128 on each of the six low bytes makes
 // every byte a balanced digit plus 128; +256 at bit 56 makes the top field
 // (bits 48 and up) the leading digit plus 256, in [0, 512].
@@ -269,9 +271,21 @@ __host__ __device__ __forceinline__ int row_ksteps(int nkc, int ksteps_last) {
     return (nkc - 1) * kSubKSteps + ksteps_last;
 }
 
+// Each K step also records its lead: the first slice t (1..8) holding a
+// nonzero digit in any of its 128 rows x 16 columns, 9 when all are zero.
+// Chebyshev coefficients decay with the degree, so the high K steps of a
+// block hold only low-weight digits: a product with a slice before the lead
+// is exactly zero and the assembly neither streams nor multiplies it.
+// leads[(block * nrb + rb) * row_ksteps + ks], one byte per K step.
+// Each sub-block also records its level rows: for each accumulator level
+// tau = 2..8, the number of leading rows that have a digit able to reach it
+// (rows with a nonzero digit t <= tau - 1; for tau = 8 also the eighth
+// digit), byte tau - 2 of level_rows[block * nrb * nkc + sub]. Rows below
+// that count contribute exactly zero to the level.
 __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ coeffs, int nu, int nv,
                                                     int nrb, int nkc, int ksteps_last,
-                                                    uint16_t* __restrict__ out, int32_t* __restrict__ exponents) {
+                                                    uint16_t* __restrict__ out, int32_t* __restrict__ exponents,
+                                                    uint8_t* __restrict__ leads, uint64_t* __restrict__ level_rows) {
     const int nsub = nrb * nkc;
     const int64_t block = blockIdx.x / nsub;
     const int sub = static_cast<int>(blockIdx.x - block * nsub);
@@ -281,6 +295,12 @@ __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ c
     const int rk = row_ksteps(nkc, ksteps_last);
     const double* c = coeffs + block * static_cast<int64_t>(nu) * nv;
     __shared__ double red[256];
+    __shared__ int s_lead[kSubKSteps];
+    __shared__ int s_row_lead[kRows];
+    __shared__ int s_level_rows[kLevels];
+    if (threadIdx.x < kSubKSteps) s_lead[threadIdx.x] = kSlicesA + 1;
+    if (threadIdx.x < kRows) s_row_lead[threadIdx.x] = kSlicesA + 1;
+    if (threadIdx.x < kLevels) s_level_rows[threadIdx.x] = 0;
     double m = 0.0;
     for (int i = threadIdx.x; i < nu * nv; i += blockDim.x) m = fmax(m, fabs(c[i]));
     red[threadIdx.x] = m;
@@ -294,6 +314,9 @@ __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ c
     if (threadIdx.x == 0 && sub == 0) exponents[block] = e;
     uint16_t* dst = out + ((block * nrb + rb) * rk + static_cast<int64_t>(kc) * kSubKSteps) * (kAStageBytes / 2);
     const int total = kRows * ksteps * kKStep;
+    int lead[kSubKSteps];  // this thread's first nonzero slice per K step
+#pragma unroll
+    for (int ks = 0; ks < kSubKSteps; ++ks) lead[ks] = kSlicesA + 1;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
         const int a = i / (ksteps * kKStep);
         const int b = i - a * (ksteps * kKStep);
@@ -302,15 +325,47 @@ __global__ void __launch_bounds__(256) slice_blocks(const double* __restrict__ c
         const int ks = b / kKStep, bb = b - ks * kKStep;
         const int k = (bb & 1) * 8 + (bb >> 1);
         uint16_t* base = dst + static_cast<int64_t>(ks) * kSlicesA * kRows * kKStep + core_offset(a, k);
+        int first = kSlicesA + 1;
         for (int t = 0; t < kSlicesA; ++t) {
             // exact: r * 256 has the same significand, and subtracting the
             // nearest integer leaves the (representable) remainder
             const double scaled = r * 256.0;
             const double q = rint(scaled);
             r = scaled - q;
+            if (q != 0.0 && first > kSlicesA) first = t + 1;
             const float stored = t < kSlicesA - 1 ? static_cast<float>(q) : static_cast<float>(q) * 0.00390625f;
             base[t * kRows * kKStep] = __half_as_ushort(__float2half_rn(stored));
         }
+#pragma unroll
+        for (int q = 0; q < kSubKSteps; ++q)
+            if (q == ks) lead[q] = min(lead[q], first);
+        if (first <= kSlicesA) atomicMin(&s_row_lead[a], first);
+    }
+#pragma unroll
+    for (int q = 0; q < kSubKSteps; ++q) {
+        int v = lead[q];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, off));
+        if ((threadIdx.x & 31) == 0 && v <= kSlicesA) atomicMin(&s_lead[q], v);
+    }
+    __syncthreads();
+    if (threadIdx.x < static_cast<unsigned>(ksteps))
+        leads[(block * nrb + rb) * rk + static_cast<int64_t>(kc) * kSubKSteps + threadIdx.x] =
+            static_cast<uint8_t>(s_lead[threadIdx.x]);
+    if (threadIdx.x < kRows) {
+        const int rl = s_row_lead[threadIdx.x];
+#pragma unroll
+        for (int lv = 0; lv < kLevels; ++lv) {
+            // level tau = lv + 2 takes digits t <= tau - 1 (and, at tau = 8, the eighth)
+            const int reach = lv == kLevels - 1 ? kSlicesA : lv + 1;
+            if (rl <= reach) atomicMax(&s_level_rows[lv], static_cast<int>(threadIdx.x) + 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t packed = 0;
+        for (int lv = 0; lv < kLevels; ++lv) packed |= static_cast<uint64_t>(s_level_rows[lv]) << (8 * lv);
+        level_rows[block * nsub + sub] = packed;
     }
 }
 
@@ -441,7 +496,7 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
     }
 }
 
-// Exclusive scan of block counts (offsets) and of their 64-lookup tile counts
+// Exclusive scan of block counts (offsets) and of their 128-lookup tile counts
 // (tile offsets); one CTA of 1024 threads. totals[0] = lookups, totals[1] = tiles.
 __global__ void __launch_bounds__(1024) split_scan(const uint32_t* __restrict__ counts, uint32_t nblocks,
                                                    uint32_t* __restrict__ offsets,
@@ -516,37 +571,64 @@ __global__ void __launch_bounds__(256) split_tiles(const uint32_t* __restrict__ 
 }
 
 // ------------------------------------------------------------- assembly --
-// Warp-specialised persistent kernel, one CTA of 10 warps per SM:
-//   warps 0-3  basis producers: the eight bf16 slices of T_b(v) for each
-//              K step of a tile, into a two-stage ring (16-byte stores of
-//              whole core-matrix rows, conflict-free);
-//   warps 4-7  epilogue: the Q62 u-basis of the tile (while the MMAs run),
-//              then the TMEM levels row by row (warp w reads lanes
-//              32(w-4)..), combined in fixed point and summed over rows
-//              through a shared-memory stage, and the Green entries written;
-//   warp 8     one thread streams the coefficient slices of every K step
-//              into a three-stage ring with cp.async.bulk;
-//   warp 9     one thread issues the 37 tcgen05.mma of each K step and
-//              owns the 512 TMEM columns (eight levels x 64 lookups).
-// The accumulators are single-buffered: the MMAs of a tile start when the
-// epilogue has released the previous tile's TMEM.
-constexpr int kAStages = 3;
-constexpr int kBStages = 3;
-constexpr int kMetaBufs = 3;
+// Warp-specialised persistent kernel, one CTA of 14 warps per SM. A tile is
+// up to 128 lookups of one sort key (one sub-block of one coefficient
+// block). For every lookup l (a TMEM lane) and coefficient row a (a TMEM
+// column) the MMAs accumulate, level by level, W[l][a] = sum_b T_b(v_l) C[a][b]:
+//   warps 0-3   basis producers: thread l generates T_b(v_l) for the 16 b of
+//               each K step (eight chains of stride 8) and writes the digit
+//               slices the step's MMAs read into a three-stage ring (the
+//               MMA's A operand: 128 lookups x 16 k per slice, whole 16-byte
+//               core-matrix rows);
+//   warps 4-11  epilogue, two groups of four warps: thread (group g, lane l)
+//               owns lookup l and, of every 16 coefficient rows, the rows
+//               4g..4g+3 and 8+4g..8+4g+3. It reads its rows' levels from
+//               tensor memory, combines them in fixed point, multiplies by
+//               T_a(u_l) from its own recurrences and sums over a in
+//               registers; the two groups' sums are added at the tile's end;
+//   warp 12     one thread streams the coefficient slices of every K step
+//               (the MMA's B operand: the sub-block's rows x 16 k per slice)
+//               into a three-stage ring with cp.async.bulk;
+//   warp 13     one thread issues the MMAs (kind::f16, M = 128, K = 16) and
+//               owns the 512 TMEM columns.
+// Each level's accumulator spans only the rows whose coefficients have a
+// digit that can reach that level (the sub-block's level rows, recorded at
+// slicing): the high rows of a decaying Chebyshev block hold only
+// low-weight digits, so the leading levels are narrow (MMA N = their rows).
+// When the levels' columns exceed the 496 below the sink the tile runs as
+// two passes, over rows 0..63 and 64..127. The accumulators are
+// single-buffered: a pass's MMAs start when the epilogue has drained the
+// previous pass.
+//
+// Where only the low-weight levels reach, 32-bit arithmetic suffices and the
+// kernel uses it: a K step whose lead is 6 or more multiplies only basis
+// digits 1 and 2, so from the first K step after which every lead is at
+// least 6 the producers run their chains in Q30 (error ~2^-26 against the
+// 2^-16 resolution those digits need); rows that no level below 7 reaches
+// (|W| < 2^24 units of 2^-55) take their T_a(u) from Q30 chains, a 32 x 32
+// product and a 64-bit sum.
+constexpr int kCStages = 3;   // coefficient ring
+constexpr int kBStages = 3;   // basis ring
+constexpr int kMetaBufs = 2;
 constexpr int kProducerWarps = 4;
-constexpr int kEpilogueGroups = 2;                    // each reads all 128 TMEM lanes for half the lookups
+constexpr int kEpilogueGroups = 2;
 constexpr int kEpilogueWarps = 4 * kEpilogueGroups;
-constexpr int kGroupLookups = kTileN / kEpilogueGroups;
 constexpr int kWarpCopy = kProducerWarps + kEpilogueWarps;
 constexpr int kWarpMma = kWarpCopy + 1;
+// 14 warps: each SM sub-partition (16K registers) holds four of them, which
+// caps the kernel at 128 registers per thread
 constexpr int kAssemblyThreads = (kWarpMma + 1) * 32;
-constexpr int kRedChunk = 8;  // lookups per epilogue reduction chunk
-constexpr uint32_t kEpiBarrier = 1;       // named barrier of all epilogue warps (votes)
-constexpr uint32_t kGroupBarrier0 = 2;    // named barriers of the epilogue groups: 2, 3
+constexpr int kTmemColumns = 512;
+constexpr int kTmemSink = kTmemColumns - 16;  // 16 columns no level uses (the writes of empty levels)
+constexpr uint32_t kEpiBarrier = 1;           // named barrier of all epilogue warps (votes)
+constexpr int kTailLead = 6;                  // K steps from this lead on read basis digits 1 and 2 only
+static_assert(kProducerWarps * 32 == kTileN, "one basis producer thread per lookup");
+
 
 struct TileMeta {
     double u[kTileN];
     uint64_t info[kTileN];
+    uint64_t rows;  // level rows of the tile's sub-block
     uint32_t count;
     int32_t exponent;
     int32_t sub;
@@ -554,17 +636,15 @@ struct TileMeta {
 };
 
 struct SplitShared {
-    alignas(1024) uint16_t a_ring[kAStages][kAStageBytes / 2];  // 3 x 32 KiB
-    alignas(1024) uint16_t b_ring[kBStages][kBStepBytes / 2];   // 3 x 14 KiB
-    alignas(16) int64_t ubasis[kTileN * kRows];                 // 64 KiB, [l][a ^ (l & 31)]
-    alignas(16) int64_t red[kEpilogueGroups][kRedChunk * kRows];  // 2 x 8 KiB, [j][row]
-    alignas(16) int64_t sums[kTileN][2];                        // 1 KiB, (lo, hi) per lookup
+    alignas(1024) uint16_t coeff_ring[kCStages][kAStageBytes / 2];  // 3 x 32 KiB
+    alignas(1024) uint16_t basis_ring[kBStages][kBStepBytes / 2];   // 3 x 28 KiB
+    alignas(16) int64_t sums[kTileN][2];                             // second group's (lo, hi) per lookup
     TileMeta meta[kMetaBufs];
-    uint64_t a_full[kAStages], a_empty[kAStages];
+    uint32_t c_lead[kCStages];  // first coefficient slice streamed into each stage (written before its copy)
+    uint64_t c_full[kCStages], c_empty[kCStages];
     uint64_t b_full[kBStages], b_empty[kBStages];
     uint64_t meta_full[kMetaBufs], meta_empty[kMetaBufs];
-    uint64_t acc_full;
-    uint64_t acc_empty[kLevels];  // per accumulator level: drained, the next tile may write it
+    uint64_t acc_full, acc_empty;
     uint64_t drain;  // last commit of the MMA thread, waited on before dealloc
     uint32_t tmem_base;
     uint32_t error;
@@ -572,11 +652,6 @@ struct SplitShared {
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-// barrier of one epilogue group (128 threads)
-__device__ __forceinline__ void group_sync(int group) {
-    asm volatile("bar.sync %0, %1;" ::"r"(kGroupBarrier0 + group), "n"(128) : "memory");
 }
 
 // Barrier of all epilogue warps that also ORs a predicate over them: every
@@ -597,52 +672,91 @@ __device__ __forceinline__ bool failed(const SplitShared& sh) {
 }
 
 // Where the lookups of sort key `key` (one sub-block of one coefficient block)
-// find their coefficient slices, the block exponent, and the sub-block's
-// place: sub = rb * nkc + kc covers rows 128 rb.. and columns 128 kc.. in
-// `ksteps` K steps.
+// find their coefficient slices, K-step leads, level rows and block exponent,
+// and the sub-block's place: sub = rb * nkc + kc covers rows 128 rb.. and
+// columns 128 kc.. in `ksteps` K steps.
 struct TileSource {
     const uint16_t* a;
-    int exponent, sub, rb, kc, ksteps;
+    const uint8_t* leads;  // lead of each of the sub-block's K steps
+    const uint64_t* rows;  // the sub-block's level rows
+    const int32_t* exponent;
+    int sub, rb, kc, ksteps;
 };
 template <bool Chunked>
 __device__ __forceinline__ TileSource tile_source(const SplitPlan& plan, uint32_t key) {
     int seg = 0;
     while (seg + 1 < plan.segments && key >= plan.segment_base[seg + 1]) ++seg;
     const uint32_t local = key - plan.segment_base[seg];
+    TileSource t;
+    t.rows = plan.level_rows[seg] + local;
     if constexpr (!Chunked) {  // one sub-block per block
-        TileSource t;
         t.sub = t.rb = t.kc = 0;
         t.ksteps = plan.ksteps_last;
         t.a = plan.slices[seg] + static_cast<int64_t>(local) * plan.ksteps_last * (kAStageBytes / 2);
-        t.exponent = plan.exponents[seg][local];
+        t.leads = plan.leads[seg] + static_cast<int64_t>(local) * plan.ksteps_last;
+        t.exponent = plan.exponents[seg] + local;
         return t;
     }
     const uint32_t nsub = static_cast<uint32_t>(plan.nrb * plan.nkc);
     const uint32_t block = local / nsub;
-    TileSource t;
     t.sub = static_cast<int>(local - block * nsub);
     t.rb = t.sub / plan.nkc;
     t.kc = t.sub - t.rb * plan.nkc;
     t.ksteps = t.kc == plan.nkc - 1 ? plan.ksteps_last : kSubKSteps;
     const int rk = row_ksteps(plan.nkc, plan.ksteps_last);
-    t.a = plan.slices[seg] +
-          ((static_cast<int64_t>(block) * plan.nrb + t.rb) * rk + static_cast<int64_t>(t.kc) * kSubKSteps) *
-              (kAStageBytes / 2);
-    t.exponent = plan.exponents[seg][block];
+    const int64_t step0 = (static_cast<int64_t>(block) * plan.nrb + t.rb) * rk + static_cast<int64_t>(t.kc) * kSubKSteps;
+    t.a = plan.slices[seg] + step0 * (kAStageBytes / 2);
+    t.leads = plan.leads[seg] + step0;
+    t.exponent = plan.exponents[seg] + block;
     return t;
 }
 
-// Column chunk of sort key `key` and its K steps, without the slice address
-// (constant when the columns make one chunk).
-__device__ __forceinline__ int tile_kc(const SplitPlan& plan, uint32_t key) {
-    if (plan.nkc == 1) return 0;
-    int seg = 0;
-    while (seg + 1 < plan.segments && key >= plan.segment_base[seg + 1]) ++seg;
-    const uint32_t nsub = static_cast<uint32_t>(plan.nrb * plan.nkc);
-    return static_cast<int>(((key - plan.segment_base[seg]) % nsub) % static_cast<uint32_t>(plan.nkc));
+// Lead of K step ks as the assembly uses it: a tile's first K step is always
+// complete (its MMAs initialise every accumulator level), a K step with no
+// nonzero digit still streams and multiplies the eighth slice.
+__device__ __forceinline__ int step_lead(const uint8_t* leads, int ks) {
+    return ks == 0 ? 1 : min(static_cast<int>(__ldg(leads + ks)), kSlicesA);
 }
-__device__ __forceinline__ int chunk_ksteps(const SplitPlan& plan, int kc) {
-    return kc == plan.nkc - 1 ? plan.ksteps_last : kSubKSteps;
+
+// The first K step from which every lead is kTailLead or more (ksteps when
+// none): from there the basis digits 1 and 2 are all the MMAs read.
+__device__ __forceinline__ int tail_kstep(const uint8_t* leads, int ksteps) {
+    int first = ksteps;
+    for (int ks = ksteps - 1; ks >= 1 && step_lead(leads, ks) >= kTailLead; --ks) first = ks;
+    return first;
+}
+
+// Tensor-memory layout of one pass of a tile: level lv (tau = lv + 2) takes
+// n[lv] columns (its rows from row0, rounded up to 16; 0 when no digit of
+// the sub-block reaches it) from column col[lv]. A tile whose levels fit in
+// the 496 columns below the sink is one pass over all rows; otherwise two
+// passes over rows 0..63 and 64..127 (at most 7 x 64 = 448 columns each).
+struct PassGeom {
+    int npass, row0, cols;  // cols: the widest level's columns
+    int n[kLevels], col[kLevels];
+};
+__device__ __forceinline__ PassGeom pass_geom(uint64_t packed, int pass) {
+    PassGeom g;
+    int rows[kLevels], total = 0;
+#pragma unroll
+    for (int lv = 0; lv < kLevels; ++lv) {
+        rows[lv] = static_cast<int>((packed >> (8 * lv)) & 0xFFu);
+        total += (rows[lv] + 15) & ~15;
+    }
+    g.npass = total <= kTmemSink ? 1 : 2;
+    g.row0 = g.npass == 1 ? 0 : 64 * pass;
+    const int span = g.npass == 1 ? kRows : 64;
+    int c = 0;
+    g.cols = 0;
+#pragma unroll
+    for (int lv = 0; lv < kLevels; ++lv) {
+        const int r = min(max(rows[lv] - g.row0, 0), span);
+        g.n[lv] = (r + 15) & ~15;
+        g.col[lv] = c;
+        c += g.n[lv];
+        g.cols = max(g.cols, g.n[lv]);
+    }
+    return g;
 }
 
 // The Green entries of one lookup's value (both spins of a shared record),
@@ -681,47 +795,82 @@ __device__ __forceinline__ int64_t part_slot(uint64_t info, const SplitPlan& pla
                nsub + sub;
 }
 
-// T_parity, T_{parity+2}, T_{parity+4}, ... of x in Q62 fixed point, by the
-// stride-2 recurrence T_{n+2} = 2 T_2(x) T_n - T_{n-2}, started from
-// (T_{-2}, T_0) = (T_2, 1) or (T_{-1}, T_1) = (x, x). The recurrence in
-// w = T_2(x) has half the steps of the stride-1 one and its rounding error
-// grows like the square of the step count.
-struct ChebStride2;
-// T_r, T_{r+4}, T_{r+8}, ... (r = 0..3) of x in Q62 fixed point, by
-// T_{n+4} = 2 T_4(x) T_n - T_{n-4}, started from (T_{r-4}, T_r) = (T_{4-r}, T_r).
-struct ChebStride4 {
-    int64_t w, prev, cur;
-    __device__ __forceinline__ void init(int64_t xfix, int r) {
-        const int64_t one = int64_t{1} << 62;
-        const int64_t t2 = cheb_step_q62(xfix, xfix, one);
-        const int64_t t3 = cheb_step_q62(xfix, t2, xfix);
-        const int64_t t4 = cheb_step_q62(xfix, t3, t2);
-        w = t4;
-        cur = r == 0 ? one : r == 1 ? xfix : r == 2 ? t2 : t3;
-        prev = r == 0 ? t4 : r == 1 ? t3 : r == 2 ? t2 : xfix;
-    }
-    __device__ __forceinline__ int64_t next() {
+// T_0 .. T_8 of x in Q62 fixed point by the stride-1 recurrence
+// T_{k+1} = 2 x T_k - T_{k-1} (the start values of the chains below).
+__device__ __forceinline__ void cheb_table8(int64_t xfix, int64_t (&t)[9]) {
+    t[0] = int64_t{1} << 62;
+    t[1] = xfix;
+#pragma unroll
+    for (int k = 1; k < 8; ++k) t[k + 1] = cheb_step_q62(xfix, t[k], t[k - 1]);
+}
+
+// Chains of stride 8: T_{m+8} = 2 T_8(x) T_m - T_{m-8}. A thread runs
+// several 8-apart chains side by side, so their steps are independent
+// instructions rather than one long dependent recurrence; each chain's
+// rounding error grows like the square of its own step count. The Q62 form
+// feeds the digits and the rows that need all 55 bits; the Q30 form (int32,
+// 1 = 2^30) the ones that need about 25.
+struct ChebChain {
+    int64_t prev, cur;  // T_{m-8}, T_m in Q62
+    __device__ __forceinline__ int64_t next(int64_t t8) {
         const int64_t t = cur;
-        cur = cheb_step_q62(w, cur, prev);
+        cur = cheb_step_q62(t8, cur, prev);
+        prev = t;
+        return t;
+    }
+};
+__device__ __forceinline__ int32_t q62_to_q30(int64_t x) {
+    return static_cast<int32_t>((x + (int64_t{1} << 31)) >> 32);
+}
+struct ChebChain30 {
+    int32_t prev, cur;  // T_{m-8}, T_m in Q30
+    __device__ __forceinline__ int32_t next(int32_t t8) {
+        const int32_t t = cur;
+        // round(2 T_8 T_m / 2^30) - T_{m-8}
+        cur = static_cast<int32_t>((static_cast<int64_t>(t8) * cur + (int64_t{1} << 28)) >> 29) - prev;
         prev = t;
         return t;
     }
 };
 
-struct ChebStride2 {
-    int64_t w, prev, cur;
-    __device__ __forceinline__ void init(int64_t xfix, int parity) {
-        w = cheb_step_q62(xfix, xfix, int64_t{1} << 62);  // 2 x^2 - 1
-        prev = parity ? xfix : w;
-        cur = parity ? xfix : (int64_t{1} << 62);
+// Columns addr..addr + 3 and addr + 8..addr + 11 of this warp's 32 lanes
+// from tensor memory (an epilogue thread's 8 columns of a 16-column chunk).
+__device__ __forceinline__ void tmem_load_4x2(uint32_t addr, uint32_t (&v)[8]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%8];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4,%5,%6,%7}, [%9];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+        : "r"(addr), "r"(addr + 8));
+}
+
+// The 29 digit-pair MMAs of a K step: coefficient slice t (8: the pre-scaled
+// eighth digit) against basis slice t', interleaved so that two MMAs into
+// the same accumulator are at least 3 apart; within a level the pairs are in
+// increasing t (the eighth digit last), so each accumulator sums its
+// products in the same order and its first MMA (t = 1, in a tile's first K
+// step, which is always complete) initialises it.
+constexpr int kIssue = 29;
+__device__ constexpr int8_t kIssueT[kIssue] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 3, 2, 2, 3, 4, 3,
+                                               1, 5, 4, 3, 4, 3, 6, 2, 5, 7, 5, 4, 6, 8};
+__device__ constexpr int8_t kIssueTp[kIssue] = {3, 5, 7, 6, 4, 6, 4, 2, 5, 5, 2, 3, 4, 4, 3,
+                                                1, 3, 3, 2, 2, 1, 2, 1, 2, 1, 1, 1, 1, 1};
+
+// One K step's MMAs with coefficient slices from Lead on, as straight-line
+// code: every operand is in a register before the first MMA, so the single
+// issuing thread puts them into the tensor pipe back to back (computing an
+// operand or branching between two MMAs costs the thread tens of clocks of
+// latency, which the tensor pipe would spend idle).
+template <int Lead, bool First>
+__device__ __forceinline__ void issue_kstep(const uint32_t (&d)[kLevels], const uint32_t (&idesc)[kLevels],
+                                            const uint64_t (&ad)[kSlices], const uint64_t (&bd)[kSlicesA]) {
+#pragma unroll
+    for (int i = 0; i < kIssue; ++i) {
+        const int t = kIssueT[i], tp = kIssueTp[i];
+        if (t < Lead) continue;
+        const int lv = t == 8 ? kLevels - 1 : t + tp - 2;
+        mma_f16(d[lv], ad[tp - 1], bd[t - 1], idesc[lv], (First && t == 1) ? 0u : 1u);
     }
-    __device__ __forceinline__ int64_t next() {
-        const int64_t t = cur;
-        cur = cheb_step_q62(w, cur, prev);
-        prev = t;
-        return t;
-    }
-};
+}
 
 template <bool Chunked>
 __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __grid_constant__ Problem p,
@@ -747,9 +896,9 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
         static_cast<uint32_t>((static_cast<uint64_t>(ntiles) * (blockIdx.x + 1)) / gridDim.x);
 
     if (tid == 0) {
-        for (int i = 0; i < kAStages; ++i) {
-            mbar_init(&sh.a_full[i], 1);
-            mbar_init(&sh.a_empty[i], 1);
+        for (int i = 0; i < kCStages; ++i) {
+            mbar_init(&sh.c_full[i], 1);
+            mbar_init(&sh.c_empty[i], 1);
         }
         for (int i = 0; i < kBStages; ++i) {
             mbar_init(&sh.b_full[i], kProducerWarps * 32);
@@ -760,14 +909,15 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
             mbar_init(&sh.meta_empty[i], kEpilogueWarps * 32);
         }
         mbar_init(&sh.acc_full, 1);
-        for (int i = 0; i < kLevels; ++i) mbar_init(&sh.acc_empty[i], kEpilogueWarps * 32);
+        mbar_init(&sh.acc_empty, kEpilogueWarps * 32);
         mbar_init(&sh.drain, 1);
         sh.error = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     if (warp == kWarpMma) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
-            smem_addr(&sh.tmem_base)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_addr(&sh.tmem_base)),
+                     "n"(kTmemColumns));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -777,10 +927,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
 
     if (warp < kProducerWarps) {
         // ---------------------------------------------- basis producers --
-        // lanes 0-15 of a warp: lookups 16w..16w+15, even degrees; lanes
-        // 16-31: the same lookups, odd degrees
-        const int l = warp * 16 + (lane & 15);  // lookup of this thread
-        const int h = lane >> 4;                // parity of its degrees = which 8 of the 16 k
+        const int l = tid;  // the lookup of this thread
         uint32_t b_cnt = 0, tile_cnt = 0;
         for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile, ++tile_cnt) {
             const SplitTile tl = tiles[tile];
@@ -789,327 +936,419 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                 sh.error = 1;
                 break;
             }
+            const TileSource src = tile_source<Chunked>(plan, tl.block);
+            const uint64_t rows = __ldg(reinterpret_cast<const unsigned long long*>(src.rows));
             const bool live = static_cast<uint32_t>(l) < tl.count;
             const double v = live ? sorted.v[tl.start + l] : 0.0;
-            if (h == 0) {
-                sh.meta[mb].u[l] = live ? sorted.u[tl.start + l] : 0.0;
-                sh.meta[mb].info[l] = live ? sorted.info[tl.start + l] : ~uint64_t{0};
-            }
-            if (tid == 0) {
-                const TileSource src = tile_source<Chunked>(plan, tl.block);
+            sh.meta[mb].u[l] = live ? sorted.u[tl.start + l] : 0.0;
+            sh.meta[mb].info[l] = live ? sorted.info[tl.start + l] : ~uint64_t{0};
+            if (l == 0) {
                 sh.meta[mb].count = tl.count;
-                sh.meta[mb].exponent = src.exponent;
+                sh.meta[mb].exponent = __ldg(src.exponent);
                 sh.meta[mb].sub = src.sub;
+                sh.meta[mb].rows = rows;
             }
             mbar_arrive(&sh.meta_full[mb]);
-            int ksteps = plan.ksteps_last, b0 = 0;
-            ChebStride2 cheb;
-            cheb.init(fixed_from_double(v, 62), h);
-            if constexpr (Chunked) {
-                const int kc = tile_kc(plan, tl.block);
-                ksteps = chunk_ksteps(plan, kc);
-                b0 = kc * kSubK;
-                for (int k = 0; k < kc * kSubK / 2; ++k) cheb.next();  // to degree 128 kc + h
-            }
-            for (int ks = 0; ks < ksteps; ++ks, ++b_cnt) {
-                const int sb = static_cast<int>(b_cnt % kBStages);
-                if (b_cnt >= kBStages && !mbar_wait(&sh.b_empty[sb], ((b_cnt / kBStages) - 1) & 1)) {
-                    sh.error = 1;
-                    break;
-                }
-                // k = 8h + j holds b = 16 ks + 2j + h
-                uint64_t y[8];
+            const int npass = pass_geom(rows, 0).npass;
+            const int ks_tail = tail_kstep(src.leads, src.ksteps);
+            const int64_t vfix = fixed_from_double(v, 62);
+            const int b0 = src.kc * kSubK;
+            bool ok = true;
+            for (int pass = 0; pass < npass && ok; ++pass) {
+                // T_b(v) by eight chains of stride 8 (chain j: b = j, j + 8,
+                // ...), from T_0..T_8 by the stride-1 recurrence; Q30 from
+                // the tail K step on
+                ChebChain ch[8];
+                int64_t w8;
+                {
+                    int64_t t8[9];
+                    cheb_table8(vfix, t8);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int b = b0 + ks * kKStep + 2 * j + h;
-                    const int64_t tb = cheb.next();
-                    const int64_t x = b < p.s.nv ? (tb + 32) >> 6 : 0;  // Q56
-                    y[j] = static_cast<uint64_t>(x) + kDigitBias;
+                    for (int j = 0; j < 8; ++j) ch[j] = ChebChain{t8[8 - j], t8[j]};
+                    w8 = t8[8];
                 }
-                uint16_t* base = sh.b_ring[sb] + core_offset(l, 8 * h);
+                for (int k = 0; k < b0 / 8; ++k)  // to degrees b0 + j
 #pragma unroll
-                for (int t = 1; t <= kSlices; ++t) {
-                    const uint32_t addr = smem_addr(base + (t - 1) * kTileN * kKStep);
-                    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(digit_pair(y[0], y[1], t)),
-                                 "r"(digit_pair(y[2], y[3], t)), "r"(digit_pair(y[4], y[5], t)),
-                                 "r"(digit_pair(y[6], y[7], t))
-                                 : "memory");
+                    for (int j = 0; j < 8; ++j) ch[j].next(w8);
+                // one K step's digits (biased Q56 values of b = b0 + 16 ks + m:
+                // k = 0..7 hold the even m, k = 8..15 the odd m) into a stage
+                auto emit = [&](int ks, const uint64_t (&ye)[8], const uint64_t (&yo)[8]) -> bool {
+                    const int sb = static_cast<int>(b_cnt % kBStages);
+                    if (b_cnt >= kBStages && !mbar_wait(&sh.b_empty[sb], ((b_cnt / kBStages) - 1) & 1)) {
+                        sh.error = 1;
+                        return false;
+                    }
+                    // only the basis slices the K step's MMAs read: t' <= 8 - lead
+                    const int tmax = max(1, kSlicesA - step_lead(src.leads, ks));
+                    uint16_t* base = sh.basis_ring[sb] + core_offset(l, 0);
+#pragma unroll
+                    for (int t = 1; t <= kSlices; ++t) {
+                        if (t > tmax) break;
+                        const uint32_t addr = smem_addr(base + (t - 1) * kTileN * kKStep);
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr),
+                                     "r"(digit_pair(ye[0], ye[1], t)), "r"(digit_pair(ye[2], ye[3], t)),
+                                     "r"(digit_pair(ye[4], ye[5], t)), "r"(digit_pair(ye[6], ye[7], t))
+                                     : "memory");
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr + 128),
+                                     "r"(digit_pair(yo[0], yo[1], t)), "r"(digit_pair(yo[2], yo[3], t)),
+                                     "r"(digit_pair(yo[4], yo[5], t)), "r"(digit_pair(yo[6], yo[7], t))
+                                     : "memory");
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_arrive(&sh.b_full[sb]);
+                    ++b_cnt;
+                    return true;
+                };
+                int ks = 0;
+                for (; ks < ks_tail && ok; ++ks) {  // Q62: all seven digits
+                    uint64_t ye[8], yo[8];
+                    const int bs = b0 + ks * kKStep;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int64_t first = ch[j].next(w8), second = ch[j].next(w8);
+                        const uint64_t y1 = static_cast<uint64_t>(bs + j < p.s.nv ? (first + 32) >> 6 : 0) + kDigitBias;
+                        const uint64_t y2 =
+                            static_cast<uint64_t>(bs + 8 + j < p.s.nv ? (second + 32) >> 6 : 0) + kDigitBias;
+                        if (j & 1) {
+                            yo[j >> 1] = y1;
+                            yo[(j >> 1) + 4] = y2;
+                        } else {
+                            ye[j >> 1] = y1;
+                            ye[(j >> 1) + 4] = y2;
+                        }
+                    }
+                    ok = emit(ks, ye, yo);
                 }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(&sh.b_full[sb]);
+                if (ks < src.ksteps && ok) {  // Q30 from the tail K step on: digits 1 and 2
+                    ChebChain30 c30[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) c30[j] = ChebChain30{q62_to_q30(ch[j].prev), q62_to_q30(ch[j].cur)};
+                    const int32_t w30 = q62_to_q30(w8);
+                    for (; ks < src.ksteps && ok; ++ks) {
+                        uint64_t ye[8], yo[8];
+                        const int bs = b0 + ks * kKStep;
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int32_t first = c30[j].next(w30), second = c30[j].next(w30);
+                            const uint64_t y1 =
+                                (bs + j < p.s.nv ? static_cast<uint64_t>(static_cast<int64_t>(first) << 26) : 0) +
+                                kDigitBias;
+                            const uint64_t y2 =
+                                (bs + 8 + j < p.s.nv ? static_cast<uint64_t>(static_cast<int64_t>(second) << 26) : 0) +
+                                kDigitBias;
+                            if (j & 1) {
+                                yo[j >> 1] = y1;
+                                yo[(j >> 1) + 4] = y2;
+                            } else {
+                                ye[j >> 1] = y1;
+                                ye[(j >> 1) + 4] = y2;
+                            }
+                        }
+                        ok = emit(ks, ye, yo);
+                    }
+                }
             }
+            if (!ok) break;
         }
     } else if (warp < kProducerWarps + kEpilogueWarps) {
         // ------------------------------------------------------ epilogue --
-        const int e = tid - kProducerWarps * 32;       // 0..255
-        const int group = e >> 7;                      // lookups [32 group, 32 group + 32)
-        const int row = e & (kRows - 1);               // TMEM lane = Chebyshev row a
+        const int e = tid - kProducerWarps * 32;  // 0..255
+        const int group = e >> 7;                 // columns 4 group + (0..3, 8..11) of every 16
+        const int l = e & (kTileN - 1);           // TMEM lane = lookup (warp w reads lanes 32 (w & 3)..)
         const uint32_t lane_base = tmem + (static_cast<uint32_t>((warp & 3) * 32) << 16);
-        const int nu = p.s.nu;
         const int nmax = p.max_order;
-        int64_t* red = sh.red[group];
-        uint32_t tile_cnt = 0;
+        uint32_t tile_cnt = 0, pass_cnt = 0;
         for (uint32_t tile = tile_begin; tile < tile_end; ++tile, ++tile_cnt) {
             const int mb = static_cast<int>(tile_cnt % kMetaBufs);
             const bool meta_ok = mbar_wait(&sh.meta_full[mb], (tile_cnt / kMetaBufs) & 1);
-            // (also: every epilogue thread is done with the previous tile's u basis)
+            // (also: the previous tile's second-group sums have been read)
             if (epilogue_any(!meta_ok || failed(sh))) {
                 sh.error = 1;
                 break;
             }
             const TileMeta& meta = sh.meta[mb];
-            // u basis of the tile, four threads per lookup (degrees r mod 4);
-            // each half-warp holds 16 lookups of one residue, so its stores
-            // hit 16 distinct bank pairs
-            {
-                const int we = e >> 5;
-                const int l = 16 * (we & 3) + (lane & 15), r = 2 * (we >> 2) + (lane >> 4);
-                ChebStride4 cheb;
-                cheb.init(fixed_from_double(meta.u[l], 62), r);
-                int a0 = 0;  // first row of the sub-block
-                if constexpr (Chunked) {
-                    a0 = (meta.sub / plan.nkc) * kRows;
-                    for (int k = 0; k < a0 / 4; ++k) cheb.next();  // to degree a0 + r
+            const uint64_t rows = meta.rows;
+            const int a_sub = Chunked ? (meta.sub / plan.nkc) * kRows : 0;  // first row of the sub-block
+            const int64_t ufix = fixed_from_double(meta.u[l], 62);
+            uint64_t slo = 0;  // 128-bit sum over the rows some level below 7 reaches
+            int64_t shi = 0;
+            int64_t tail = 0;  // 64-bit sum over the rows only levels 7 and 8 reach
+            const int npass = pass_geom(rows, 0).npass;
+            bool ok = true;
+            for (int pass = 0; pass < npass; ++pass, ++pass_cnt) {
+                const PassGeom g = pass_geom(rows, pass);
+                // T_a(u) by four chains of stride 8 (chain q: a = 4 group + q,
+                // + 8, ...), from T_0..T_8 by the stride-1 recurrence
+                ChebChain ch[4];
+                int64_t w8;
+                {
+                    int64_t t8[9];
+                    cheb_table8(ufix, t8);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        ch[q] = group ? ChebChain{t8[4 - q], t8[4 + q]} : ChebChain{t8[8 - q], t8[q]};
+                    w8 = t8[8];
                 }
-                for (int a = r; a < kRows; a += 4) {
-                    const int64_t ta = cheb.next();
-                    sh.ubasis[l * kRows + (a ^ (l & 31))] = a0 + a < nu ? ta : 0;
+                for (int k = 0; k < (a_sub + g.row0) / 8; ++k)  // to the pass's first row
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) ch[q].next(w8);
+                // the chunks from c_tail on hold only levels 7 and 8
+                const int c_tail = g.n[kLevels - 3];
+                const bool acc_ok = mbar_wait(&sh.acc_full, pass_cnt & 1);
+                if (epilogue_any(!acc_ok)) {
+                    ok = false;
+                    break;
                 }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const int c_head = min(c_tail, g.cols);
+                for (int c0 = 0; c0 < c_head; c0 += 16) {
+                    // this thread's 8 columns c0 + 4 group + (0..3, 8..11):
+                    // value q is row a = c0 + 4 group + (q & 3) + 8 (q >> 2).
+                    // W * 2^55 = sum_tau L_tau 2^(55 - 8 tau): levels 7 and 8
+                    // folded in FP32, levels 2..6 exact integers
+                    const uint32_t col = lane_base + c0 + 4 * group;
+                    int64_t wfix[8];
+                    {  // levels 8, 7 and 6
+                        uint32_t v8[8], v7[8], v6[8];
+                        tmem_load_4x2(col + g.col[kLevels - 1], v8);
+                        const bool has7 = g.n[kLevels - 2] > c0;
+                        if (has7) tmem_load_4x2(col + g.col[kLevels - 2], v7);
+                        tmem_load_4x2(col + g.col[kLevels - 3], v6);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const float f7 = has7 ? __uint_as_float(v7[q]) * 0.5f : 0.0f;
+                            wfix[q] = __float2int_rn(fmaf(__uint_as_float(v8[q]), 0.001953125f, f7));
+                            wfix[q] += static_cast<int64_t>(__float2int_rn(__uint_as_float(v6[q]))) << 7;
+                        }
+                    }
+                    if (g.n[kLevels - 4] > c0) {  // levels 2..5
+                        uint32_t v[kLevels - 3][8];
+#pragma unroll
+                        for (int lv = 0; lv < kLevels - 3; ++lv)
+                            if (g.n[lv] > c0) tmem_load_4x2(col + g.col[lv], v[lv]);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                        for (int lv = 0; lv < kLevels - 3; ++lv) {
+                            if (g.n[lv] <= c0) continue;
+                            const int shift = 39 - 8 * lv;  // 2^(55 - 8 tau), tau = lv + 2
+#pragma unroll
+                            for (int q = 0; q < 8; ++q)
+                                wfix[q] += static_cast<int64_t>(__float2int_rn(__uint_as_float(v[lv][q]))) << shift;
+                        }
+                    }
+                    // sum_a T_a(u) W_a: products rounded to 2^-55, summed exactly
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int64_t tf = ch[q & 3].next(w8);
+                        const uint64_t plo = static_cast<uint64_t>(wfix[q]) * static_cast<uint64_t>(tf);
+                        int64_t phi = __mul64hi(wfix[q], tf);
+                        const uint64_t plo2 = plo + (uint64_t{1} << 61);
+                        phi += plo2 < plo ? 1 : 0;
+                        const int64_t prod = static_cast<int64_t>((static_cast<uint64_t>(phi) << 2) | (plo2 >> 62));
+                        const uint64_t nlo = slo + static_cast<uint64_t>(prod);
+                        shi += (prod < 0 ? -1 : 0) + (nlo < slo ? 1 : 0);
+                        slo = nlo;
+                    }
+                }
+                if (c_head < g.cols) {
+                    // the rows only levels 7 and 8 reach: the levels folded in
+                    // FP32 (|W| < 2^24 units of 2^-55), T_a(u) in Q30, 32 x 32
+                    // products, a 64-bit sum
+                    ChebChain30 c30[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c30[q] = ChebChain30{q62_to_q30(ch[q].prev), q62_to_q30(ch[q].cur)};
+                    const int32_t w30 = q62_to_q30(w8);
+                    for (int c0 = c_head; c0 < g.cols; c0 += 16) {
+                        const uint32_t col = lane_base + c0 + 4 * group;
+                        uint32_t v8[8], v7[8];
+                        tmem_load_4x2(col + g.col[kLevels - 1], v8);
+                        const bool has7 = g.n[kLevels - 2] > c0;
+                        if (has7) tmem_load_4x2(col + g.col[kLevels - 2], v7);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const float f7 = has7 ? __uint_as_float(v7[q]) * 0.5f : 0.0f;
+                            const int32_t wf = __float2int_rn(fmaf(__uint_as_float(v8[q]), 0.001953125f, f7));
+                            const int32_t t30 = c30[q & 3].next(w30);
+                            tail += (static_cast<int64_t>(wf) * t30 + (int64_t{1} << 29)) >> 30;
+                        }
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                mbar_arrive(&sh.acc_empty);  // the next pass's MMAs may write the columns
             }
-            const bool acc_ok = mbar_wait(&sh.acc_full, tile_cnt & 1);
-            if (epilogue_any(!acc_ok)) {  // also orders the u-basis stores before their reads
+            if (!ok) {
                 sh.error = 1;
                 break;
             }
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t count = meta.count;
-            const int exponent = meta.exponent;
-            // Drain: every accumulator of this thread's row and the group's 32
-            // lookups into 64-bit fixed point, W * 2^55 = sum_tau P_tau
-            // 2^(55 - 8 tau), tau = 2..8 (levels 2..6 exact integers, 7 and 8
-            // folded in FP32), in registers. Each level is released as soon as
-            // it is read, so the next tile's MMAs into it (issued level by
-            // level in the same order) start while the rest drains: levels 7
-            // and 8 first (folded together), then 2..6. The products and row
-            // sums below then run alongside the next tile's MMAs.
-            int64_t wfix[kGroupLookups];
-#pragma unroll
-            for (int c0 = 0; c0 < kGroupLookups; c0 += kRedChunk) {
-                const int l0 = group * kGroupLookups + c0;
-                uint32_t p7[8], p8[8];
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                             : "=r"(p7[0]), "=r"(p7[1]), "=r"(p7[2]), "=r"(p7[3]), "=r"(p7[4]), "=r"(p7[5]),
-                               "=r"(p7[6]), "=r"(p7[7])
-                             : "r"(lane_base + 5 * kTileN + l0));
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                             : "=r"(p8[0]), "=r"(p8[1]), "=r"(p8[2]), "=r"(p8[3]), "=r"(p8[4]), "=r"(p8[5]),
-                               "=r"(p8[6]), "=r"(p8[7])
-                             : "r"(lane_base + 6 * kTileN + l0));
-                asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-                for (int j = 0; j < kRedChunk; ++j)
-                    wfix[c0 + j] = __float2int_rn(
-                        fmaf(__uint_as_float(p8[j]), 0.001953125f, __uint_as_float(p7[j]) * 0.5f));
+            {  // the 64-bit tail sum into the 128-bit sum
+                const uint64_t nlo = slo + static_cast<uint64_t>(tail);
+                shi += (tail < 0 ? -1 : 0) + (nlo < slo ? 1 : 0);
+                slo = nlo;
             }
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(&sh.acc_empty[5]);
-            mbar_arrive(&sh.acc_empty[6]);
-#pragma unroll
-            for (int lev = 0; lev < 5; ++lev) {
-                uint32_t v[kGroupLookups / kRedChunk][8];
-#pragma unroll
-                for (int q = 0; q < kGroupLookups / kRedChunk; ++q) {
-                    const uint32_t addr = lane_base + lev * kTileN + group * kGroupLookups + q * kRedChunk;
-                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                                 : "=r"(v[q][0]), "=r"(v[q][1]), "=r"(v[q][2]), "=r"(v[q][3]), "=r"(v[q][4]),
-                                   "=r"(v[q][5]), "=r"(v[q][6]), "=r"(v[q][7])
-                                 : "r"(addr));
-                }
-                asm volatile("tcgen05.wait::ld.sync.aligned;");
-                const int shift = 39 - 8 * lev;  // 2^(55 - 8 tau), tau = lev + 2
-#pragma unroll
-                for (int q = 0; q < kGroupLookups / kRedChunk; ++q)
-#pragma unroll
-                    for (int j = 0; j < kRedChunk; ++j)
-                        wfix[q * kRedChunk + j] +=
-                            static_cast<int64_t>(__float2int_rn(__uint_as_float(v[q][j]))) * (int64_t{1} << shift);
-                asm volatile("tcgen05.fence::before_thread_sync;");
-                mbar_arrive(&sh.acc_empty[lev]);  // this level may take the next tile's MMAs
+            // the second group's sums to the first group's threads, which
+            // finish: one thread per lookup, so that the few FP64 operations
+            // are issued once per lookup. A block of several sub-blocks
+            // leaves its exact 128-bit part for the combine kernel instead.
+            if (group == 1) {
+                sh.sums[l][0] = static_cast<int64_t>(slo);
+                sh.sums[l][1] = shi;
             }
-#pragma unroll
-            for (int c0 = 0; c0 < kGroupLookups; c0 += kRedChunk) {
-                const int l0 = group * kGroupLookups + c0;
-#pragma unroll
-                for (int j = 0; j < kRedChunk; ++j) {
-                    const int l = l0 + j;
-                    const int64_t tf = sh.ubasis[l * kRows + (row ^ (l & 31))];
-                    const uint64_t lo = static_cast<uint64_t>(wfix[c0 + j]) * static_cast<uint64_t>(tf);
-                    int64_t hi = __mul64hi(wfix[c0 + j], tf);
-                    const uint64_t lo2 = lo + (uint64_t{1} << 61);
-                    hi += lo2 < lo ? 1 : 0;
-                    red[j * kRows + row] = static_cast<int64_t>((static_cast<uint64_t>(hi) << 2) | (lo2 >> 62));
-                }
-                group_sync(group);
-                // 16 threads per lookup sum 8 rows each (rows part + 16 i), then 4 shuffle levels
-                {
-                    const int j = row >> 4, part = row & 15;
-                    uint64_t slo = 0;
-                    int64_t shi = 0;
-#pragma unroll
-                    for (int i = 0; i < kRows / 16; ++i) {
-                        const int64_t t = red[j * kRows + part + 16 * i];
-                        const uint64_t nlo = slo + static_cast<uint64_t>(t);
-                        shi += (t < 0 ? -1 : 0) + (nlo < slo ? 1 : 0);
-                        slo = nlo;
-                    }
-#pragma unroll
-                    for (int off = 8; off > 0; off >>= 1) {
-                        const uint64_t olo = __shfl_xor_sync(0xffffffffu, slo, off);
-                        const int64_t ohi = __shfl_xor_sync(0xffffffffu, shi, off);
-                        const uint64_t nlo = slo + olo;
-                        shi += ohi + (nlo < slo ? 1 : 0);
-                        slo = nlo;
-                    }
-                    if (part == 0) {
-                        sh.sums[l0 + j][0] = static_cast<int64_t>(slo);
-                        sh.sums[l0 + j][1] = shi;
-                    }
-                }
-                group_sync(group);
-            }
-            // finalisation: the group's first warp, one lookup per lane, so
-            // that the few FP64 operations are issued once per 32 lookups. A
-            // block of several sub-blocks leaves its exact 128-bit part for
-            // the combine kernel instead.
-            const int l = group * kGroupLookups + row;
-            if (row < kGroupLookups && static_cast<uint32_t>(l) < count) {
+            epilogue_any(false);
+            if (group == 0 && static_cast<uint32_t>(l) < meta.count) {
+                const uint64_t olo = static_cast<uint64_t>(sh.sums[l][0]);
+                const uint64_t nlo = slo + olo;
+                shi += sh.sums[l][1] + (nlo < slo ? 1 : 0);
+                slo = nlo;
                 const uint64_t info = meta.info[l];
                 if constexpr (!Chunked) {
-                    store_green(p, w, info,
-                                int128_to_double(sh.sums[l][1], static_cast<uint64_t>(sh.sums[l][0]), exponent - 55));
+                    store_green(p, w, info, int128_to_double(shi, slo, meta.exponent - 55));
                 } else {
                     const int64_t slot = part_slot(info, plan, nmax, meta.sub);
-                    parts[2 * slot] = sh.sums[l][0];
-                    parts[2 * slot + 1] = sh.sums[l][1];
+                    parts[2 * slot] = static_cast<int64_t>(slo);
+                    parts[2 * slot + 1] = shi;
                 }
             }
-            group_sync(group);  // sums are reused by the next tile
             mbar_arrive(&sh.meta_empty[mb]);
         }
     } else if (warp == kWarpCopy) {
         // ----------------------------------------- coefficient streaming --
         if (lane == 0) {
-            uint32_t a_cnt = 0;
+            uint32_t c_cnt = 0;
             unsigned long long streamed = 0;
-            for (uint32_t tile = tile_begin; tile < tile_end && !failed(sh); ++tile) {
+            bool ok = true;
+            for (uint32_t tile = tile_begin; ok && tile < tile_end && !failed(sh); ++tile) {
                 const TileSource src = tile_source<Chunked>(plan, tiles[tile].block);
-                for (int ks = 0; ks < src.ksteps; ++ks, ++a_cnt) {
-                    const int st = static_cast<int>(a_cnt % kAStages);
-                    if (a_cnt >= kAStages && !mbar_wait(&sh.a_empty[st], ((a_cnt / kAStages) - 1) & 1)) {
-                        sh.error = 1;
-                        break;
+                const uint64_t rows = __ldg(reinterpret_cast<const unsigned long long*>(src.rows));
+                const int npass = pass_geom(rows, 0).npass;
+                for (int pass = 0; ok && pass < npass; ++pass) {
+                    const PassGeom g = pass_geom(rows, pass);
+                    for (int ks = 0; ks < src.ksteps; ++ks, ++c_cnt) {
+                        const int st = static_cast<int>(c_cnt % kCStages);
+                        if (c_cnt >= kCStages && !mbar_wait(&sh.c_empty[st], ((c_cnt / kCStages) - 1) & 1)) {
+                            sh.error = 1;
+                            ok = false;
+                            break;
+                        }
+                        // slices lead..8 (the ones before the lead are zero), the
+                        // pass's rows (at least one 16-row group, so that every
+                        // stage completes by a copy)
+                        const int lead = step_lead(src.leads, ks);
+                        const uint16_t* from = src.a + static_cast<int64_t>(ks) * (kAStageBytes / 2);
+                        sh.c_lead[st] = static_cast<uint32_t>(lead);
+                        const int cols = max(g.cols, 16);
+                        if (g.row0 == 0 && cols == kRows) {  // whole slices: one copy
+                            const uint32_t offset = static_cast<uint32_t>(lead - 1) * (kRows * kKStep);
+                            const uint32_t bytes = kAStageBytes - offset * 2;
+                            mbar_expect_tx(&sh.c_full[st], bytes);
+                            bulk_copy_g2s(sh.coeff_ring[st] + offset, from + offset, bytes, &sh.c_full[st]);
+                            streamed += bytes;
+                        } else {  // each slice's rows row0 .. row0 + cols
+                            const uint32_t bytes = static_cast<uint32_t>(cols) * kKStep * 2;
+                            mbar_expect_tx(&sh.c_full[st], bytes * static_cast<uint32_t>(kSlicesA + 1 - lead));
+                            for (int t = lead; t <= kSlicesA; ++t) {
+                                const uint32_t offset = static_cast<uint32_t>(t - 1) * (kRows * kKStep) +
+                                                        static_cast<uint32_t>(g.row0) * kKStep;
+                                bulk_copy_g2s(sh.coeff_ring[st] + offset, from + offset, bytes, &sh.c_full[st]);
+                                streamed += bytes;
+                            }
+                        }
                     }
-                    mbar_expect_tx(&sh.a_full[st], kAStageBytes);
-                    bulk_copy_g2s(sh.a_ring[st], src.a + static_cast<int64_t>(ks) * (kAStageBytes / 2),
-                                  kAStageBytes, &sh.a_full[st]);
-                    streamed += kAStageBytes;
                 }
             }
             if (counters) atomicAdd(counters + 1, streamed);
             // copies still in flight (only after an error) land before the CTA exits
-            for (uint32_t st = 0; st < static_cast<uint32_t>(kAStages); ++st) {
-                if (a_cnt <= st) continue;
-                const uint32_t last = a_cnt - 1 - (a_cnt - 1 - st) % kAStages;
-                if (!mbar_wait(&sh.a_full[st], (last / kAStages) & 1)) sh.error = 1;
+            for (uint32_t st = 0; st < static_cast<uint32_t>(kCStages); ++st) {
+                if (c_cnt <= st) continue;
+                const uint32_t last = c_cnt - 1 - (c_cnt - 1 - st) % kCStages;
+                if (!mbar_wait(&sh.c_full[st], (last / kCStages) & 1)) sh.error = 1;
             }
         }
     } else if (warp == kWarpMma) {
         // ---------------------------------------------------- MMA issue --
         if (lane == 0) {
-            const uint32_t idesc = mma_idesc(kRows, kTileN);
-            uint32_t a_cnt = 0, b_cnt = 0, tile_cnt = 0;
+            uint32_t c_cnt = 0, b_cnt = 0, pass_cnt = 0;
             unsigned long long mmas = 0;
             bool ok = true, issued = false;
-            // with several column chunks the K steps vary by tile: the next
-            // tile's key is loaded while this one's MMAs are issued
-            const bool chunked = Chunked && plan.nkc > 1;
-            uint32_t next_key = chunked && tile_begin < tile_end ? tiles[tile_begin].block : 0;
-            for (uint32_t tile = tile_begin; ok && tile < tile_end && !failed(sh); ++tile, ++tile_cnt) {
-                const uint32_t key = next_key;
-                if (chunked && tile + 1 < tile_end) next_key = tiles[tile + 1].block;
-                const int ksteps = chunked ? chunk_ksteps(plan, tile_kc(plan, key)) : plan.ksteps_last;
-                for (int ks = 0; ok && ks < ksteps; ++ks, ++a_cnt, ++b_cnt) {
-                    const int sa = static_cast<int>(a_cnt % kAStages);
-                    const int sb = static_cast<int>(b_cnt % kBStages);
-                    if (!mbar_wait(&sh.a_full[sa], (a_cnt / kAStages) & 1) ||
-                        !mbar_wait(&sh.b_full[sb], (b_cnt / kBStages) & 1)) {
+            for (uint32_t tile = tile_begin; ok && tile < tile_end && !failed(sh); ++tile) {
+                const TileSource src = tile_source<Chunked>(plan, tiles[tile].block);
+                const uint64_t rows = __ldg(reinterpret_cast<const unsigned long long*>(src.rows));
+                const int npass = pass_geom(rows, 0).npass;
+                for (int pass = 0; ok && pass < npass; ++pass, ++pass_cnt) {
+                    const PassGeom g = pass_geom(rows, pass);
+                    // the previous pass's accumulators have been drained
+                    if (pass_cnt > 0 && !mbar_wait(&sh.acc_empty, (pass_cnt - 1) & 1)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    // descriptors of the stage's first slices; a slice further
-                    // on is the same descriptor plus its byte offset / 16 (the
-                    // 14-bit address field cannot carry: shared memory < 256 KiB)
-                    const uint64_t a_desc = smem_desc(smem_addr(sh.a_ring[sa]), 128, 256);
-                    const uint64_t b_desc = smem_desc(smem_addr(sh.b_ring[sb]), 128, 256);
-                    const uint32_t first = ks > 0 ? 1u : 0u;
-                    // Issue order: the 29 MMAs of a K step interleaved so that two
-                    // MMAs into the same accumulator are at least 3 apart, also
-                    // across consecutive K steps (an MMA waits for the previous
-                    // one into its accumulator). In a tile's first K step the
-                    // accumulators are taken as the epilogue releases them:
-                    // levels 7 and 8 (in the same interleaved order), then 2..6
-                    // one level at a time. Within a level the pairs are always in
-                    // increasing t (t = 8: the eighth digit, last), so each
-                    // accumulator sums its products in the same order.
-                    constexpr int kIssue = 29;
-                    constexpr int8_t kIssueT[kIssue] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 3, 2, 2, 3, 4, 3,
-                                                        1, 5, 4, 3, 4, 3, 6, 2, 5, 7, 5, 4, 6, 8};
-                    constexpr int8_t kIssueTp[kIssue] = {3, 5, 7, 6, 4, 6, 4, 2, 5, 5, 2, 3, 4, 4, 3,
-                                                         1, 3, 3, 2, 2, 1, 2, 1, 2, 1, 1, 1, 1, 1};
-                    auto mma_pair = [&](int t, int tp) {
-                        const int level = t + tp - 2;
-                        mma_f16(tmem + level * kTileN, a_desc + (t - 1) * (kRows * kKStep * 2 / 16),
-                                b_desc + (tp - 1) * (kTileN * kKStep * 2 / 16), idesc, t > 1 ? 1u : first);
-                    };
-                    auto mma_eighth = [&]() {
-                        mma_f16(tmem + (kLevels - 1) * kTileN, a_desc + kSlices * (kRows * kKStep * 2 / 16), b_desc,
-                                idesc, 1u);
-                    };
-                    if (ks == 0 && tile_cnt > 0) {
-                        ok = mbar_wait(&sh.acc_empty[kLevels - 2], (tile_cnt - 1) & 1) &&
-                             mbar_wait(&sh.acc_empty[kLevels - 1], (tile_cnt - 1) & 1);
-                        if (!ok) break;
-                        asm volatile("tcgen05.fence::after_thread_sync;");
+                    // per-level accumulator addresses and instruction descriptors
+                    // of the pass; a level without columns writes 16 columns of
+                    // the sink at the top of tensor memory, which nothing reads
+                    uint32_t dcol[kLevels], idesc[kLevels];
 #pragma unroll
-                        for (int i = 0; i < kIssue; ++i) {
-                            if (kIssueT[i] == 8) mma_eighth();
-                            else if (kIssueT[i] + kIssueTp[i] - 2 >= kLevels - 2) mma_pair(kIssueT[i], kIssueTp[i]);
-                        }
-                        issued = true;
-#pragma unroll
-                        for (int level = 0; level < kLevels - 2 && ok; ++level) {
-                            ok = mbar_wait(&sh.acc_empty[level], (tile_cnt - 1) & 1);
-                            if (!ok) break;
-                            asm volatile("tcgen05.fence::after_thread_sync;");
-#pragma unroll
-                            for (int t = 1; t <= level + 1; ++t) mma_pair(t, level + 2 - t);
-                        }
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < kIssue; ++i) {
-                            if (kIssueT[i] == 8) mma_eighth();
-                            else mma_pair(kIssueT[i], kIssueTp[i]);
-                        }
+                    for (int lv = 0; lv < kLevels; ++lv) {
+                        dcol[lv] = tmem + static_cast<uint32_t>(g.n[lv] > 0 ? g.col[lv] : kTmemSink);
+                        idesc[lv] = mma_idesc(kTileN, g.n[lv] > 0 ? g.n[lv] : 16);
                     }
-                    issued = true;
+                    // accumulator columns a K step's MMAs write, by its lead (the
+                    // counter of issued tensor work: 2 x 128 x 16 flops per column)
+                    uint32_t cols_at_lead[kSlicesA + 1] = {};
+#pragma unroll
+                    for (int i = 0; i < kIssue; ++i) {
+                        const int t = kIssueT[i], tp = kIssueTp[i];
+                        const int lv = t == 8 ? kLevels - 1 : t + tp - 2;
+#pragma unroll
+                        for (int lead = 1; lead <= kSlicesA; ++lead)
+                            if (t >= lead) cols_at_lead[lead] += g.n[lv] > 0 ? g.n[lv] : 16;
+                    }
+                    for (int ks = 0; ks < src.ksteps; ++ks, ++c_cnt, ++b_cnt) {
+                        const int sc = static_cast<int>(c_cnt % kCStages);
+                        const int sb = static_cast<int>(b_cnt % kBStages);
+                        if (!mbar_wait(&sh.c_full[sc], (c_cnt / kCStages) & 1) ||
+                            !mbar_wait(&sh.b_full[sb], (b_cnt / kBStages) & 1)) {
+                            ok = false;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        // the stage's lead (1 in a tile's first K step): pairs
+                        // with a coefficient slice before it are zero, not issued
+                        const int lead = static_cast<int>(*static_cast<volatile uint32_t*>(&sh.c_lead[sc]));
+                        // descriptors of every slice of the two stages (rows row0..
+                        // of the coefficients), all in registers before the MMAs;
+                        // a slice further on is the same descriptor plus its byte
+                        // offset / 16 (the 14-bit address field cannot carry:
+                        // shared memory < 256 KiB)
+                        uint64_t ad[kSlices], bd[kSlicesA];
+                        const uint64_t a0 = smem_desc(smem_addr(sh.basis_ring[sb]), 128, 256);
+                        const uint64_t b0 = smem_desc(smem_addr(sh.coeff_ring[sc] + g.row0 * kKStep), 128, 256);
+#pragma unroll
+                        for (int k = 0; k < kSlices; ++k) ad[k] = a0 + k * (kSliceBytes / 16);
+#pragma unroll
+                        for (int k = 0; k < kSlicesA; ++k) bd[k] = b0 + k * (kSliceBytes / 16);
+                        if (ks == 0) {
+                            issue_kstep<1, true>(dcol, idesc, ad, bd);
+                        } else {
+                            switch (lead) {
+                                case 1: issue_kstep<1, false>(dcol, idesc, ad, bd); break;
+                                case 2: issue_kstep<2, false>(dcol, idesc, ad, bd); break;
+                                case 3: issue_kstep<3, false>(dcol, idesc, ad, bd); break;
+                                case 4: issue_kstep<4, false>(dcol, idesc, ad, bd); break;
+                                case 5: issue_kstep<5, false>(dcol, idesc, ad, bd); break;
+                                case 6: issue_kstep<6, false>(dcol, idesc, ad, bd); break;
+                                case 7: issue_kstep<7, false>(dcol, idesc, ad, bd); break;
+                                default: issue_kstep<8, false>(dcol, idesc, ad, bd); break;
+                            }
+                        }
+                        mmas += cols_at_lead[ks == 0 ? 1 : lead];
+                        issued = true;
+                        mma_commit(&sh.c_empty[sc]);
+                        mma_commit(&sh.b_empty[sb]);
+                    }
                     if (!ok) break;
-                    mmas += kIssue;
-                    mma_commit(&sh.a_empty[sa]);
-                    mma_commit(&sh.b_empty[sb]);
+                    mma_commit(&sh.acc_full);
                 }
-                if (!ok) break;
-                mma_commit(&sh.acc_full);
             }
             if (!ok) sh.error = 1;
             if (counters) atomicAdd(counters, mmas);
@@ -1125,7 +1364,7 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
     if (tid == 0 && sh.error) atomicExch(error_flag, 1);
     if (warp == kWarpMma) {
         asm volatile("tcgen05.fence::after_thread_sync;");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemColumns));
     }
 }
 
@@ -1155,7 +1394,7 @@ __global__ void __launch_bounds__(128) split_combine(const __grid_constant__ Pro
             hi += parts[2 * (base + sub) + 1] + (nlo < lo ? 1 : 0);
             lo = nlo;
         }
-        store_green(p, w, rec.info[base], int128_to_double(hi, lo, tile_source<true>(plan, key).exponent - 55));
+        store_green(p, w, rec.info[base], int128_to_double(hi, lo, *tile_source<true>(plan, key).exponent - 55));
     }
 }
 
@@ -1173,15 +1412,27 @@ size_t split_slices_bytes(int nu, int nv, size_t blocks) {
     return blocks * nrb * static_cast<size_t>(row_ksteps(nkc, ksteps_last)) * kAStageBytes;
 }
 
+size_t split_leads_bytes(int nu, int nv, size_t blocks) {
+    int nrb, nkc, ksteps_last;
+    split_geometry(nu, nv, &nrb, &nkc, &ksteps_last);
+    return blocks * nrb * static_cast<size_t>(row_ksteps(nkc, ksteps_last));
+}
+
+size_t split_level_rows_bytes(int nu, int nv, size_t blocks) {
+    int nrb, nkc, ksteps_last;
+    split_geometry(nu, nv, &nrb, &nkc, &ksteps_last);
+    return blocks * nrb * nkc * sizeof(uint64_t);
+}
+
 cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
-                               int32_t* exponents, cudaStream_t stream) {
+                               int32_t* exponents, uint8_t* leads, uint64_t* level_rows, cudaStream_t stream) {
     if (blocks == 0) return cudaSuccess;
     int nrb, nkc, ksteps_last;
     split_geometry(nu, nv, &nrb, &nkc, &ksteps_last);
     const size_t grid = blocks * nrb * nkc;
     if (grid > 0x7FFFFFFFu) return cudaErrorInvalidValue;
     slice_blocks<<<static_cast<unsigned>(grid), 256, 0, stream>>>(coeffs, nu, nv, nrb, nkc, ksteps_last, slices,
-                                                                  exponents);
+                                                                  exponents, leads, level_rows);
     return cudaGetLastError();
 }
 

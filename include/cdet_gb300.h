@@ -442,7 +442,8 @@ int cdet_profile_read(cdet_context* ctx, double* kernel_ms, int64_t* launches);
 
 /* Measurement hook; no counterpart in the reference. Counters of the last
  * split-assembly evaluation on this context (waits for it): out[0] = the
- * tcgen05.mma instructions its assembly kernel issued, out[1] = the
+ * accumulator columns its tcgen05.mma instructions wrote (M = 128, K = 16:
+ * 2 x 128 x 16 flops of issued tensor work each), out[1] = the
  * coefficient-slice bytes it streamed from global memory. Both are zero
  * before the first split evaluation. */
 int cdet_split_counters(cdet_context* ctx, uint64_t* out);
