@@ -350,8 +350,10 @@ def run_gpu(args):
         elapsed = max_over_ranks(start.elapsed_time(stop))
         stage_ms, launches = integrand.profile_read()
         integrand.profile(False)
+        tuned_forms[path] = integrand.integrand_form_tuned(ORDER, BATCH)
         return elapsed, stage_ms, launches, d_values.cpu().numpy(), d_status.cpu().numpy()
 
+    tuned_forms = {}
     results = {path: timed(path) for path in paths}
     clock_info = clocks.stop()
     # tcgen05.mma instructions and slice bytes of the last split assembly (one launch)
@@ -387,9 +389,14 @@ def run_gpu(args):
     nu, nv = params.cheb_nu, params.cheb_nv
     lookups = BATCH * 2 * ORDER * ORDER  # table sets x entries (up and down share one table)
 
-    def per_step(ms):
-        return {"split_prep": ms[0] / args.steps, "assembly": ms[1] / args.steps,
-                "minors": ms[2] / args.steps, "cdet": ms[3] / args.steps}
+    def per_step(ms, path):
+        # the queue form runs minors and CDet in one kernel: one stage
+        stages = {"split_prep": ms[0] / args.steps, "assembly": ms[1] / args.steps}
+        if tuned_forms.get(path, {}).get("form") == "queue":
+            stages["minors_and_cdet"] = (ms[2] + ms[3]) / args.steps
+        else:
+            stages.update({"minors": ms[2] / args.steps, "cdet": ms[3] / args.steps})
+        return stages
 
     if head == "split":
         # algorithmic work of the assembly (2 nu nv flops per lookup: the
@@ -438,7 +445,8 @@ def run_gpu(args):
                 "h2d_bytes_per_step": BATCH * ORDER * 4 * 8 + BATCH * 4,
                 "d2h_bytes_per_step": BATCH * 8 + BATCH * 4},
         "gpu_launches": int(launches),
-        "stages_ms_per_step": per_step(stage_ms),
+        "stages_ms_per_step": per_step(stage_ms, head),
+        "integrand_form": tuned_forms.get(head),
         "roofline": roofline,
         "clocks": clock_info,
         "derived": derived_rates(value, ORDER),
@@ -449,7 +457,8 @@ def run_gpu(args):
     if "fp64" in results:
         f_ms, f_stage, _, f_values, _ = results["fp64"]
         line["fp64_path"] = {"value": total_configs / (f_ms / 1e3), "unit": UNIT,
-                             "ms_per_step": f_ms / args.steps, "stages_ms_per_step": per_step(f_stage),
+                             "ms_per_step": f_ms / args.steps, "stages_ms_per_step": per_step(f_stage, "fp64"),
+                             "integrand_form": tuned_forms.get("fp64"),
                              "bit_identical_to_reference": None}
         if head == "split":
             line["split_over_fp64"] = value / line["fp64_path"]["value"]
@@ -593,9 +602,11 @@ def run_mixed(args):
     6x6 / U=4 / beta=5 / half lattice / degree 96, 64 chains x 256 proposals
     = 16,384 configurations per step with orders 1..10 drawn from a truncated
     geometric distribution (p = 0.3), through the device entry point with the
-    inputs resident; FP64 (bit-identical) and split forms. The FP64 CDet sorts
-    such a batch by order so that the lanes of a warp run equal-length
-    recursions."""
+    inputs resident; FP64 (bit-identical) and split forms. Each form is timed
+    staged (minors kernel, a[] in HBM, CDet kernel), as the persistent queue
+    kernel (one and two warps per configuration) and under the autotuner,
+    whose kept choice gives the line's value; all forms' values are checked
+    bit for bit against the staged form's."""
     import torch
     from cdet_gb300.integrand import CdetIntegrand
     from cdet_gb300.params import CdetParams, half_lattice_mask
@@ -618,23 +629,38 @@ def run_mixed(args):
                       "l2": "flushed between steps (512 MiB write)"},
            "data": "synthetic (seeded uniform vertices, tables from the in-tree precompute)"}
     values = {}
+    forms = (("staged", {}), ("queue", {}), ("queue", {"pair": True}), ("auto", {}))
     for path in ("fp64", "split"):
         gpu.set_assembly(path)
-        for _ in range(args.warmup):
-            gpu.integrand_device(v, o, vals, st)
-        torch.cuda.synchronize()
-        total = 0.0
-        for _ in range(args.steps):
-            flush.fill_(1)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            gpu.integrand_device(v, o, vals, st)
-            e1.record()
+        per_form = []
+        for form, shape in forms:
+            gpu.set_integrand_form(form, **shape)
+            for _ in range(args.warmup):  # under "auto" the first call measures the candidates
+                gpu.integrand_device(v, o, vals, st)
             torch.cuda.synchronize()
-            total += e0.elapsed_time(e1)
-        values[path] = vals.cpu().numpy().copy()
-        out[path] = {"value": batch * args.steps / (total / 1e3), "ms_per_step": total / args.steps,
-                     "gpu_launches": gpu.last_launch_count()}
+            total = 0.0
+            for _ in range(args.steps):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                gpu.integrand_device(v, o, vals, st)
+                e1.record()
+                torch.cuda.synchronize()
+                total += e0.elapsed_time(e1)
+            got = vals.cpu().numpy().copy()
+            if path not in values:
+                values[path] = got
+            entry = {"form": form, **shape, "ms_per_step": total / args.steps,
+                     "configs_per_s": batch * args.steps / (total / 1e3),
+                     "gpu_launches": gpu.last_launch_count(),
+                     "bit_identical_to_staged": bool(np.array_equal(got.view(np.uint64),
+                                                                    values[path].view(np.uint64)))}
+            if form == "auto":
+                entry["tuned"] = gpu.integrand_form_tuned(nmax, batch)
+            per_form.append(entry)
+        auto = per_form[-1]
+        out[path] = {"value": auto["configs_per_s"], "ms_per_step": auto["ms_per_step"],
+                     "gpu_launches": auto["gpu_launches"], "tuned": auto["tuned"], "forms": per_form}
     out["value"] = out["split"]["value"]
     # per order: relative error of each configuration, and the normwise error
     # max |split - fp64| / max |fp64| over the configurations of that order

@@ -205,6 +205,26 @@ class CdetIntegrand:
                                                       int(batch), C.byref(form)))
         return {0: "auto", 1: "lane", 2: "warp"}[form.value]
 
+    def set_integrand_form(self, form: str, warps_per_sm: int = 0, pair: bool = False, grab: int = 1) -> None:
+        """'auto', 'staged' or 'queue': how a single-top batch of order <= 10
+        runs after its Green matrices (same values bit for bit, different
+        speed). For 'queue' also the launch shape: resident warps per SM (0:
+        as many as shared memory holds), two warps per configuration (pair)
+        and the slots a warp takes per queue pop (grab)."""
+        code = {"auto": 0, "staged": 1, "queue": 2}[form]
+        L.check(self._lib.cdet_set_integrand_form(self._ctx, code, int(warps_per_sm), int(bool(pair)), int(grab)))
+
+    def integrand_form_tuned(self, max_order: int, batch: int) -> dict:
+        """The form the autotuner kept for this order and batch size class
+        under the current assembly ({'form': 'auto'} before a measurement)."""
+        out = [C.c_int() for _ in range(4)]
+        L.check(self._lib.cdet_integrand_form_tuned(self._ctx, int(max_order), int(self._assembly == "split"),
+                                                    int(batch), *[C.byref(x) for x in out]))
+        form = {0: "auto", 1: "staged", 2: "queue"}[out[0].value]
+        if form != "queue":
+            return {"form": form}
+        return {"form": form, "warps_per_sm": out[1].value, "pair": bool(out[2].value), "grab": out[3].value}
+
     def set_assembly(self, mode: str) -> None:
         """"fp64": the reference's Clenshaw in FP64, bit-identical (default);
         "split": batched split-bf16 tcgen05 assembly, FP64-level accuracy."""

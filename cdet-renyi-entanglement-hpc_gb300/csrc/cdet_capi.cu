@@ -219,6 +219,9 @@ int build_problem(cdet_context* ctx, const double* vertices, const int32_t* orde
     p->all_subsets = all_subsets;
     p->fused_cdet = ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16 ? 1 : 0;
     p->all_subsets_form = ctx->all_subsets_form;
+    p->sorted = 0;
+    p->integrand_form = cdet::kIntegrandStaged;
+    p->queue = cdet::QueueShape{};
     for (int set = 0; set < 2; ++set) {
         const int r = set == 0 ? 2 : 1;
         for (int n = 0; n <= cdet::kMaxOrder; ++n) {
@@ -369,6 +372,50 @@ int tune_all_subsets_form(cdet_context* ctx, cdet::Problem p, const cdet::Scratc
     return CDET_OK;
 }
 
+// Times the post-assembly stages of a single-top batch in every candidate
+// form on the Green matrices already in scratch (each candidate twice, the
+// second round timed, so none pays first-launch costs alone) and returns the
+// fastest. Every form writes the same values and status bits, so the
+// evaluation's outputs stand whichever ran last.
+int tune_integrand_form(cdet_context* ctx, cdet::Problem p, const cdet::Scratch& w, cudaStream_t stream,
+                        std::pair<int, cdet::QueueShape>* best) {
+    std::vector<std::pair<int, cdet::QueueShape>> cand;
+    cand.push_back({cdet::kIntegrandStaged, cdet::QueueShape{}});
+    cdet::QueueShape q;
+    q.warps_per_sm = 0, q.pair = 0, q.grab = 1;
+    cand.push_back({cdet::kIntegrandQueue, q});  // one warp per configuration, as many as fit
+    q.pair = 1;
+    cand.push_back({cdet::kIntegrandQueue, q});  // two warps per configuration
+    q.pair = 0, q.grab = 4;
+    cand.push_back({cdet::kIntegrandQueue, q});  // four slots per pop
+    q.grab = 1, q.warps_per_sm = 4;
+    cand.push_back({cdet::kIntegrandQueue, q});  // four warps per SM (more L1 per warp)
+    std::vector<cudaEvent_t> ev(cand.size() + 1);
+    for (cudaEvent_t& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+    std::vector<float> ms(cand.size(), 0.0f);
+    cudaError_t err = cudaSuccess;
+    for (int round = 0; round < 2 && err == cudaSuccess; ++round) {
+        err = cudaEventRecord(ev[0], stream);
+        for (size_t i = 0; i < cand.size() && err == cudaSuccess; ++i) {
+            p.integrand_form = cand[i].first;
+            p.queue = cand[i].second;
+            err = cdet::launch_post_assembly(p, w, ctx->sm_count, stream);
+            if (err == cudaSuccess) err = cudaEventRecord(ev[i + 1], stream);
+        }
+        if (err == cudaSuccess) err = cudaEventSynchronize(ev[cand.size()]);
+        for (size_t i = 0; round == 1 && i < cand.size() && err == cudaSuccess; ++i)
+            err = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+    }
+    for (cudaEvent_t& e : ev) cudaEventDestroy(e);
+    if (err != cudaSuccess) return cuda_fail(err, "timing the integrand forms");
+    size_t k = 0;
+    for (size_t i = 1; i < cand.size(); ++i)
+        if (ms[i] < ms[k]) k = i;
+    *best = cand[k];
+    return CDET_OK;
+}
+
 int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
         int max_order, int all_subsets, double* values, int32_t* status, cudaStream_t stream,
         bool assembly_only = false) {
@@ -422,6 +469,40 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         }
         if (it != ctx->form_tuned.end()) p.all_subsets_form = it->second;
     }
+    // Single-top batches: the post-assembly form, fixed by
+    // cdet_set_integrand_form or, under CDET_INTEGRAND_AUTO, measured once per
+    // (order, fused, batch size class) outside a capture (staged until then).
+    bool tune_post = false;
+    std::tuple<int, int, int> post_key;
+    if (!p.all_subsets && !assembly_only && max_order <= cdet::kQueueMaxOrder) {
+        if (ctx->integrand_form != CDET_INTEGRAND_AUTO) {
+            p.integrand_form = ctx->integrand_form;
+            p.queue = ctx->queue_shape;
+        } else {
+            int log2b = 0;
+            while ((int64_t{2} << log2b) <= batch) ++log2b;
+            post_key = std::make_tuple(max_order, p.fused_cdet, log2b);
+            auto it = ctx->integrand_tuned.find(post_key);
+            if (it != ctx->integrand_tuned.end()) {
+                p.integrand_form = it->second.first;
+                p.queue = it->second.second;
+            } else if (!ctx->profiling) {
+                cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+                tune_post = cudaStreamIsCapturing(stream, &capture) == cudaSuccess &&
+                            capture == cudaStreamCaptureStatusNone;
+            }
+        }
+    }
+    auto settle_post_form = [&]() -> int {
+        if (!tune_post) return CDET_OK;
+        std::pair<int, cdet::QueueShape> best;
+        const int trc = tune_integrand_form(ctx, p, w, stream, &best);
+        if (trc != CDET_OK) return trc;
+        ctx->integrand_tuned.emplace(post_key, best);
+        p.integrand_form = best.first;
+        p.queue = best.second;
+        return CDET_OK;
+    };
     if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16) {
         cdet::SplitPlan plan;
         rc = build_split_plan(ctx, &plan);
@@ -442,17 +523,29 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
                                           ctx->sm_count, &ctx->split_error, stream, events);
         if (err != cudaSuccess) return cuda_fail(err, "split assembly launch");
         if (events && events->marks[2]) cudaEventRecord(events->marks[2], stream);
-        launches = 5 + 2;  // descriptors, scan, scatter, tiles, tensor assembly + minors, CDet
-        if (plan.nrb * plan.nkc > 1) ++launches;  // the sub-block combine
         if (!assembly_only) {
+            rc = settle_post_form();
+            if (rc != CDET_OK) return rc;
             err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events, false);
             if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+            // descriptors, scan, scatter, tiles, tensor assembly + minors, CDet (or the queue kernel)
+            launches = 5 + (cdet::uses_queue_form(p) ? 1 : 2);
         } else {
-            launches = 5 + (plan.nrb * plan.nkc > 1 ? 1 : 0);
+            launches = 5;
         }
+        if (plan.nrb * plan.nkc > 1) ++launches;  // the sub-block combine
     } else if (!assembly_only) {
-        err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events);
+        if (tune_post) {
+            err = cdet::launch_fp64_assembly_only(p, w, stream);
+            if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+            rc = settle_post_form();
+            if (rc != CDET_OK) return rc;
+            err = cdet::launch_post_assembly(p, w, ctx->sm_count, stream);
+        } else {
+            err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events);
+        }
         if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
+        launches = cdet::uses_queue_form(p) ? 2 : 3;  // assembly + minors, CDet (or the queue kernel)
     } else {
         launches = 1;
         err = cdet::launch_fp64_assembly_only(p, w, stream);
@@ -749,6 +842,36 @@ int cdet_set_all_subsets_form(cdet_context* ctx, int form) {
                       CDET_FORM_WARP == cdet::kFormWarp,
                   "form codes");
     ctx->all_subsets_form = form;
+    return CDET_OK;
+}
+
+int cdet_set_integrand_form(cdet_context* ctx, int form, int warps_per_sm, int pair, int grab) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    static_assert(CDET_INTEGRAND_AUTO == cdet::kIntegrandAuto && CDET_INTEGRAND_STAGED == cdet::kIntegrandStaged &&
+                      CDET_INTEGRAND_QUEUE == cdet::kIntegrandQueue,
+                  "integrand form codes");
+    if (form != CDET_INTEGRAND_AUTO && form != CDET_INTEGRAND_STAGED && form != CDET_INTEGRAND_QUEUE)
+        return fail(CDET_ERR_INVALID, "unknown integrand form");
+    if (warps_per_sm < 0 || warps_per_sm > 32 || (pair != 0 && pair != 1) || grab < 1 || grab > 64)
+        return fail(CDET_ERR_INVALID, "queue shape: warps_per_sm in 0..32, pair 0 or 1, grab in 1..64");
+    ctx->integrand_form = form;
+    ctx->queue_shape.warps_per_sm = warps_per_sm;
+    ctx->queue_shape.pair = pair;
+    ctx->queue_shape.grab = grab;
+    return CDET_OK;
+}
+
+int cdet_integrand_form_tuned(const cdet_context* ctx, int max_order, int fused, int64_t batch, int* form,
+                              int* warps_per_sm, int* pair, int* grab) {
+    if (!ctx || !form || !warps_per_sm || !pair || !grab) return fail(CDET_ERR_INVALID, "null argument");
+    int log2b = 0;
+    while ((int64_t{2} << log2b) <= batch) ++log2b;
+    const auto it = ctx->integrand_tuned.find(std::make_tuple(max_order, fused ? 1 : 0, log2b));
+    const cdet::QueueShape q = it == ctx->integrand_tuned.end() ? cdet::QueueShape{} : it->second.second;
+    *form = it == ctx->integrand_tuned.end() ? CDET_INTEGRAND_AUTO : it->second.first;
+    *warps_per_sm = q.warps_per_sm;
+    *pair = q.pair;
+    *grab = q.grab;
     return CDET_OK;
 }
 

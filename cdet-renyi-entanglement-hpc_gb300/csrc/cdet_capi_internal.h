@@ -58,6 +58,11 @@ struct cdet_context {
     int all_subsets_form = CDET_FORM_AUTO;
     // all-subsets CDet form measured fastest, per (order, fused, floor(log2 batch))
     std::map<std::tuple<int, int, int>, int> form_tuned;
+    // single-top post-assembly form: fixed (cdet_set_integrand_form) or measured
+    // per (order, fused, floor(log2 batch)) under CDET_INTEGRAND_AUTO
+    int integrand_form = CDET_INTEGRAND_AUTO;
+    cdet::QueueShape queue_shape{};
+    std::map<std::tuple<int, int, int>, std::pair<int, cdet::QueueShape>> integrand_tuned;
     std::map<std::pair<const double*, size_t>, capi::SlicedBranch> sliced;  // (coeffs, blocks) -> slices
     void* split_scratch = nullptr;
     size_t split_scratch_bytes = 0;

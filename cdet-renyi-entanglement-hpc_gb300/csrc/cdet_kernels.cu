@@ -802,6 +802,84 @@ __device__ __forceinline__ float scaled_magnitude(double v, int k) {
     return fminf(static_cast<float>(fabs(dmul(v, p2))), 3.0e38f);
 }
 
+// The fused single-top recursion of one set of one configuration on one warp
+// (order n >= 2): a_s[swz(m >> 1)] holds a of the even masks, a_odd[mask *
+// stride] a of the odd ones, and dp of the odd masks goes to dp_s[swz(mask >>
+// 1)]. Returns dp of the full mask (every lane). cdet_split_warp and the
+// queue form both call it, so their values are the same bit for bit.
+__device__ __forceinline__ double split_cdet_recursion(const double* a_s, double* dp_s, const double* a_odd,
+                                                       int64_t stride, int n, double threshold, int lane) {
+    const bool filter = threshold > 0.0;
+    const float thresholdf = static_cast<float>(threshold);
+    const int count = 1 << n;
+    int e = 0;
+    {
+        const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(a_odd[1 * stride]));
+        const int field = static_cast<int>((bits >> 52) & 0x7FF);
+        if (field != 0 && field != 0x7FF) e = field - 1023;
+        e = e > 90 ? 90 : (e < -90 ? -90 : e);  // |e| * nmax stays within 1000
+    }
+    if (lane == 0) dp_s[swz(0)] = a_odd[1 * stride];
+    __syncwarp();
+    const int nbits = n - 1;
+    for (int k = 2; k <= n; ++k) {
+        const int kk = k - 1;                 // rest = mask >> 1 has kk of nbits bits
+        const int masks = kBinom[nbits][kk];
+        const int subs = 1 << kk;             // submasks of rest, rest itself included
+        for (int base = 0; base < masks;) {
+            const int remaining = masks - base;
+            int L = 1, take = kWarp;
+            if (remaining < kWarp) {
+                while (L * 2 * remaining <= kWarp && L * 2 <= subs) L *= 2;
+                take = remaining;
+                if (4 * L * remaining < 3 * kWarp && L * 2 <= subs) {  // < 75% of lanes busy
+                    L *= 2;
+                    take = kWarp / L;
+                }
+            }
+            const int q = __ffs(L) - 1;
+            const int idx = base + (lane >> q);
+            const int j = lane & (L - 1);
+            const bool active = (lane >> q) < take && idx < masks;
+            double part = 0.0;
+            float rpart = 0.0f;
+            uint32_t mask = 0;
+            const int field_bias = 127 - 2046 - e * k;
+            if (active) {
+                const uint32_t rest = colex_unrank(static_cast<uint32_t>(idx), kk, nbits);
+                mask = (rest << 1) | 1u;
+                uint32_t top = 0, low = rest;
+                for (int t = 0; t < q; ++t) {
+                    const uint32_t hb = 1u << (31 - __clz(low));
+                    top |= hb;
+                    low ^= hb;
+                }
+                uint32_t fixed = 0, tb = top;
+                for (int t = 0; t < q; ++t) {
+                    const uint32_t lb = tb & (~tb + 1u);
+                    if ((j >> t) & 1) fixed |= lb;
+                    tb ^= lb;
+                }
+                fused_submask_sum<true>(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
+            }
+            for (int off = 1; off < L; off <<= 1) {
+                part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));
+                rpart += __shfl_xor_sync(0xffffffffu, rpart, off);
+            }
+            if (active && j == 0) {
+                const double am = a_odd[static_cast<int64_t>(mask) * stride];
+                double acc = dsub(am, part);
+                const float rhs = scaled_magnitude(am, -e * k) + rpart;
+                if (filter && scaled_magnitude(acc, -e * k) < thresholdf * rhs) acc = 0.0;
+                dp_s[swz(mask >> 1)] = acc;
+            }
+            base += take;
+        }
+        __syncwarp();
+    }
+    return dp_s[swz((count - 1) >> 1)];
+}
+
 __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const __grid_constant__ Problem p,
                                                                        const __grid_constant__ Scratch w) {
     extern __shared__ __align__(16) unsigned char cdet_smem[];
@@ -815,8 +893,6 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
     double* dp_s = a_s + full_n / 2;
     const Scalars& s = p.s;
     const double threshold = dmul(s.z_eps0, s.z_safety);
-    const bool filter = threshold > 0.0;
-    const float thresholdf = static_cast<float>(threshold);
     const int64_t g = blockIdx.x;
     for (int cl = warp; cl < kWarp; cl += kWarpCdetWarps) {
         const int64_t c = g * kWarp + cl;
@@ -836,75 +912,11 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
             }
             const double* ag = w.a_int + (g * 2 + set) * static_cast<int64_t>(full_n) * kWarp + cl;
             const int count = 1 << n;
-            int e = 0;
-            {
-                const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(ag[1 * kWarp]));
-                const int field = static_cast<int>((bits >> 52) & 0x7FF);
-                if (field != 0 && field != 0x7FF) e = field - 1023;
-                e = e > 90 ? 90 : (e < -90 ? -90 : e);  // |e| * nmax stays within 1000
-            }
             for (int m2 = lane; m2 < count / 2; m2 += kWarp) a_s[swz(m2)] = ag[static_cast<int64_t>(2 * m2) * kWarp];
             __syncwarp();
-            if (lane == 0) dp_s[swz(0)] = ag[1 * kWarp];
-            __syncwarp();
-            const int nbits = n - 1;
-            for (int k = 2; k <= n; ++k) {
-                const int kk = k - 1;                 // rest = mask >> 1 has kk of nbits bits
-                const int masks = kBinom[nbits][kk];
-                const int subs = 1 << kk;             // submasks of rest, rest itself included
-                for (int base = 0; base < masks;) {
-                    const int remaining = masks - base;
-                    int L = 1, take = kWarp;
-                    if (remaining < kWarp) {
-                        while (L * 2 * remaining <= kWarp && L * 2 <= subs) L *= 2;
-                        take = remaining;
-                        if (4 * L * remaining < 3 * kWarp && L * 2 <= subs) {  // < 75% of lanes busy
-                            L *= 2;
-                            take = kWarp / L;
-                        }
-                    }
-                    const int q = __ffs(L) - 1;
-                    const int idx = base + (lane >> q);
-                    const int j = lane & (L - 1);
-                    const bool active = (lane >> q) < take && idx < masks;
-                    double part = 0.0;
-                    float rpart = 0.0f;
-                    uint32_t mask = 0;
-                    const int field_bias = 127 - 2046 - e * k;
-                    if (active) {
-                        const uint32_t rest = colex_unrank(static_cast<uint32_t>(idx), kk, nbits);
-                        mask = (rest << 1) | 1u;
-                        uint32_t top = 0, low = rest;
-                        for (int t = 0; t < q; ++t) {
-                            const uint32_t hb = 1u << (31 - __clz(low));
-                            top |= hb;
-                            low ^= hb;
-                        }
-                        uint32_t fixed = 0, tb = top;
-                        for (int t = 0; t < q; ++t) {
-                            const uint32_t lb = tb & (~tb + 1u);
-                            if ((j >> t) & 1) fixed |= lb;
-                            tb ^= lb;
-                        }
-                        fused_submask_sum<true>(dp_s, a_s, rest, fixed, low, field_bias, part, rpart);
-                    }
-                    for (int off = 1; off < L; off <<= 1) {
-                        part = dadd(part, __shfl_xor_sync(0xffffffffu, part, off));
-                        rpart += __shfl_xor_sync(0xffffffffu, rpart, off);
-                    }
-                    if (active && j == 0) {
-                        const double am = ag[static_cast<int64_t>(mask) * kWarp];
-                        double acc = dsub(am, part);
-                        const float rhs = scaled_magnitude(am, -e * k) + rpart;
-                        if (filter && scaled_magnitude(acc, -e * k) < thresholdf * rhs) acc = 0.0;
-                        dp_s[swz(mask >> 1)] = acc;
-                    }
-                    base += take;
-                }
-                __syncwarp();
-            }
+            const double top = split_cdet_recursion(a_s, dp_s, ag, kWarp, n, threshold, lane);
             const DDPair pf = p.pref_dd[set][n];
-            value = dd_mul(DD{pf.hi, pf.lo}, DD{dp_s[swz((count - 1) >> 1)], 0.0});
+            value = dd_mul(DD{pf.hi, pf.lo}, DD{top, 0.0});
             if (!dd_finite(value)) status |= kStatusNonFinite;
             __syncwarp();  // the next set reuses the arrays
         }
@@ -1148,6 +1160,175 @@ __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_con
         if (status) atomicOr(p.status + c, status);
     }
 }
+
+// ------------------------------------------ 4. persistent queue form -------
+// Minors, CDet and combine of each configuration in one persistent kernel,
+// with no global a array between them. The warps take configurations from
+// the order-sorted slots (decreasing order: the longest recursions start
+// first, the short ones fill the tail) through an atomic queue head, `grab`
+// slots at a time. One warp per configuration (both sets in turn) or a pair
+// of warps (one set each, meeting at a named barrier). A warp's shared-memory
+// region is the minors workspace; after a set's Schur recursion its lists are
+// free and hold the CDet arrays: a of the odd masks replaces the shifted
+// minors in place, a of the even masks and dp of the odd ones take the two
+// list regions (each holds at least 2^(n-1) doubles: the last Schur level has
+// 2^(n-1) lists of one entry). Every set goes through the staged form's
+// operations (mat2pm_warp, a = up * down, split_cdet_recursion or the
+// reference's descending submask sums), so the values are the staged form's
+// bit for bit.
+
+constexpr uint32_t kQueueHeadIndex = 48;  // the queue head's uint32 slot in Scratch::order_count
+
+// compute_dp_ztransform (integrand_replica_randomly_sampled.h:226-290) on one
+// warp, for order n >= 2: a[mask] for every mask, dp of the odd masks into
+// dp_s[mask >> 1]. The masks of a popcount level are dealt to the lanes by
+// colex rank; each mask's submask sum runs on one lane in the reference's
+// descending order with the reference's operations, so the result is
+// cdet_single's bit for bit.
+__device__ double fp64_single_warp(const double* a, double* dp_s, int n, double threshold, int lane) {
+    const bool filter = threshold > 0.0;
+    if (lane == 0) dp_s[0] = a[1];
+    __syncwarp();
+    const int nbits = n - 1;
+    for (int k = 2; k <= n; ++k) {
+        const int kk = k - 1;
+        const int masks = kBinom[nbits][kk];
+        for (int idx = lane; idx < masks; idx += kWarp) {
+            const uint32_t rest = colex_unrank(static_cast<uint32_t>(idx), kk, nbits);
+            double acc = a[(rest << 1) | 1u];
+            double rhs = fabs(acc);
+            for (uint32_t sm = (rest - 1u) & rest;; sm = (sm - 1u) & rest) {
+                pair_update<false>(dp_s[sm], a[(rest ^ sm) << 1], acc, rhs);
+                if (sm == 0) break;
+            }
+            if (filter && fabs(acc) < dmul(threshold, rhs)) acc = 0.0;
+            dp_s[rest] = acc;
+        }
+        __syncwarp();  // the next level reads this one
+    }
+    return dp_s[(1u << nbits) - 1u];
+}
+
+// One set of configuration c (order n) on one warp: the prefactored value of
+// that set; status collects the FPM-fallback and non-finite bits.
+template <bool Fused>
+__device__ __forceinline__ DD queue_set_value(const Problem& p, const Scratch& w, int64_t c, int set, int n,
+                                              const WsLayout& lay, double* ws, double* lu_lane, int lane,
+                                              int32_t& status) {
+    const Scalars& s = p.s;
+    const int nmax = p.max_order;
+    if (n == 1) {  // the order-1 branch: no minors, no finiteness check
+        const double* diag = w.diag + c * 2 * 2 * nmax;
+        return DD{order1_value(s, diag[(set * 2) * nmax], diag[(set * 2 + 1) * nmax], set == 0 ? 2 : 1), 0.0};
+    }
+    const double* green = w.green + (c * 2 + set) * 2 * static_cast<int64_t>(nmax) * nmax;
+    double* A = ws + lay.a;
+    bool fb = false;
+    for (int k = lane; k < n * n; k += kWarp) A[k] = green[k];
+    __syncwarp();
+    double* su = ws + lay.shifted_up;
+    fb |= mat2pm_warp(A, n, s.tol_fpm, s.fpm_shift, lay, ws, su, lu_lane, lane);
+    const bool one_spin = p.same_spin[set] != 0;
+    if (!one_spin) {
+        for (int k = lane; k < n * n; k += kWarp) A[k] = green[static_cast<int64_t>(nmax) * nmax + k];
+        __syncwarp();
+        fb |= mat2pm_warp(A, n, s.tol_fpm, s.fpm_shift, lay, ws, ws + lay.shifted_down, lu_lane, lane);
+    }
+    const double* sd = one_spin ? su : ws + lay.shifted_down;
+    const uint32_t count = 1u << n;
+    const double threshold = dmul(s.z_eps0, s.z_safety);
+    double top;
+    if constexpr (Fused) {
+        // a = up * down (integrand_replica_randomly_sampled.h:254-257): the
+        // even masks to the first list region (swizzled like cdet_split_warp's),
+        // the odd ones in place
+        double* a_even = ws + lay.new_list;
+        for (uint32_t m = lane; m < count; m += kWarp) {
+            const double am = m == 0 ? 0.0 : dmul(su[m], sd[m]);
+            if (m & 1u) su[m] = am;
+            else a_even[swz(m >> 1)] = am;
+        }
+        __syncwarp();
+        top = split_cdet_recursion(a_even, ws + lay.old_list, su, 1, n, threshold, lane);
+    } else {
+        for (uint32_t m = lane; m < count; m += kWarp) su[m] = m == 0 ? 0.0 : dmul(su[m], sd[m]);
+        __syncwarp();
+        top = fp64_single_warp(su, ws + lay.old_list, n, threshold, lane);
+    }
+    const DDPair pf = p.pref_dd[set][n];
+    const DD value = dd_mul(DD{pf.hi, pf.lo}, DD{top, 0.0});
+    if (!dd_finite(value)) status |= kStatusNonFinite;
+    if (fb) status |= kStatusFpmFallback;
+    __syncwarp();  // the next set reuses the workspace
+    return value;
+}
+
+__device__ __forceinline__ void pair_barrier(int pair) {
+    asm volatile("bar.sync %0, 64;" ::"r"(pair + 1) : "memory");
+}
+
+template <bool Fused, bool Pair>
+__global__ void __launch_bounds__(256) integrand_queue(const __grid_constant__ Problem p,
+                                                      const __grid_constant__ Scratch w, int grab) {
+    extern __shared__ double queue_smem[];
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int warp_in_block = threadIdx.x / kWarp;
+    const int warps_per_block = blockDim.x / kWarp;
+    const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
+    const int nmax = p.max_order;
+    const WsLayout lay = ws_layout(nmax, !(p.same_spin[0] && p.same_spin[1]));
+    double* ws = queue_smem + static_cast<size_t>(warp_in_block) * lay.total;
+    double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
+    uint32_t* head = w.order_count + kQueueHeadIndex;
+    const uint32_t batch = static_cast<uint32_t>(p.batch);
+    // pair exchange (after the workspaces): [pair] {first slot, status, value hi, value lo}
+    const int pair = warp_in_block >> 1, set_of_warp = warp_in_block & 1;
+    double* exchange = queue_smem + static_cast<size_t>(warps_per_block) * lay.total + pair * 4;
+    for (;;) {
+        uint32_t first = 0;
+        if constexpr (Pair) {
+            if (set_of_warp == 0 && lane == 0)
+                reinterpret_cast<uint32_t*>(exchange)[0] = atomicAdd(head, static_cast<uint32_t>(grab));
+            pair_barrier(pair);
+            first = reinterpret_cast<const volatile uint32_t*>(exchange)[0];
+            pair_barrier(pair);  // both warps hold the slot before the next pop
+        } else {
+            if (lane == 0) first = atomicAdd(head, static_cast<uint32_t>(grab));
+            first = __shfl_sync(0xffffffffu, first, 0);
+        }
+        if (first >= batch) break;
+        const uint32_t last = min(first + static_cast<uint32_t>(grab), batch);
+        for (uint32_t slot = first; slot < last; ++slot) {
+            const int64_t c = __ldg(w.config_at + slot);
+            const int n = __ldg(p.orders + c);
+            if (n < 1 || n > nmax) continue;  // flagged by the assembly
+            int32_t status = 0;
+            if constexpr (Pair) {
+                const DD v = queue_set_value<Fused>(p, w, c, set_of_warp, n, lay, ws, lu_lane, lane, status);
+                if (lane == 0 && set_of_warp == 1) {
+                    exchange[2] = v.hi;
+                    exchange[3] = v.lo;
+                }
+                if (lane == 0 && status) atomicOr(p.status + c, status);
+                pair_barrier(pair);
+                if (lane == 0 && set_of_warp == 0) {
+                    const DD ordinary{exchange[2], exchange[3]};
+                    const DD result = dd_sub(v, dd_mul(DD{2.0, 0.0}, ordinary));
+                    p.values[c] = dadd(result.hi, result.lo);
+                }
+                pair_barrier(pair);  // the exchange is read before the next write
+            } else {
+                const DD twisted = queue_set_value<Fused>(p, w, c, 0, n, lay, ws, lu_lane, lane, status);
+                const DD ordinary = queue_set_value<Fused>(p, w, c, 1, n, lay, ws, lu_lane, lane, status);
+                if (lane == 0) {
+                    const DD result = dd_sub(twisted, dd_mul(DD{2.0, 0.0}, ordinary));
+                    p.values[c] = dadd(result.hi, result.lo);
+                    if (status) atomicOr(p.status + c, status);
+                }
+            }
+        }
+    }
+}
 }  // namespace
 
 size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).total; }
@@ -1249,39 +1430,20 @@ void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Sc
     out->order_count = reinterpret_cast<uint32_t*>(take(32));
 }
 
-bool sorts_orders(const Problem& p) {
-    // the lane CDet of a single-order batch (the split path's warp CDet and the
-    // all-subsets forms have no lanes of different orders)
-    return !p.all_subsets && !(p.fused_cdet && p.max_order <= kWarpCdetMaxOrder);
-}
-
-cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_count,
-                                  cudaStream_t stream, const KernelEvents* events, bool assembly) {
-    if (p_in.batch <= 0) return cudaSuccess;
+// Sort, minors and CDet (or the queue kernel) on the Green matrices in scratch.
+static cudaError_t post_assembly(const Problem& p_in, const Scratch& w, int sm_count, cudaStream_t stream,
+                                 const KernelEvents* events) {
     Problem p = p_in;
     p.sorted = sorts_orders(p) ? 1 : 0;
     auto mark = [&](int k) {
         if (events && events->marks[k]) cudaEventRecord(events->marks[k], stream);
     };
-    if (assembly) {
-        mark(0);
-        mark(1);
-    }
-    const int64_t entries = p.batch * 2 * static_cast<int64_t>(p.max_order) * p.max_order;
     const int threads = 128;
     cudaError_t err = cudaSuccess;
-    if (assembly) {
-        green_assembly_fp64<<<static_cast<unsigned>((entries + threads - 1) / threads), threads, 0,
-                              stream>>>(p, w);
-        err = cudaGetLastError();
-        if (err != cudaSuccess) return err;
-        mark(2);
-    }
-
     if (p.sorted) {
         const int buckets = p.max_order + 2;
         const unsigned grid = static_cast<unsigned>(std::min<int64_t>((p.batch + 255) / 256, 4 * 152));
-        err = cudaMemsetAsync(w.order_count, 0, 32 * sizeof(uint32_t), stream);
+        err = cudaMemsetAsync(w.order_count, 0, 64 * sizeof(uint32_t), stream);  // buckets, queue head
         if (err != cudaSuccess) return err;
         order_count<<<grid, 256, 0, stream>>>(p.orders, p.batch, p.max_order, w.order_count);
         order_scan<<<1, 32, 0, stream>>>(w.order_count, buckets);
@@ -1289,6 +1451,22 @@ cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_
                                                 w.config_at);
         err = cudaGetLastError();
         if (err != cudaSuccess) return err;
+    }
+
+    if (uses_queue_form(p)) {
+        int wpb = 0, blocks = 0;
+        size_t smem = 0;
+        queue_launch_shape(p, w, sm_count, &wpb, &blocks, &smem);
+        auto kernel = p.fused_cdet ? (p.queue.pair ? integrand_queue<true, true> : integrand_queue<true, false>)
+                                   : (p.queue.pair ? integrand_queue<false, true> : integrand_queue<false, false>);
+        err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (err != cudaSuccess) return err;
+        kernel<<<static_cast<unsigned>(blocks), wpb * kWarp, smem, stream>>>(p, w, std::max(1, p.queue.grab));
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        mark(3);
+        mark(4);
+        return cudaSuccess;
     }
 
     // Minors: the per-warp workspace goes to shared memory when at least four
@@ -1365,6 +1543,66 @@ cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_
     if (err != cudaSuccess) return err;
     mark(4);
     return cudaSuccess;
+}
+
+
+bool uses_queue_form(const Problem& p) {
+    return p.integrand_form == kIntegrandQueue && !p.all_subsets && p.max_order >= 1 &&
+           p.max_order <= kQueueMaxOrder;
+}
+
+bool sorts_orders(const Problem& p) {
+    // the lane CDet of a single-order batch (the split path's warp CDet and the
+    // all-subsets forms have no lanes of different orders), and the queue form
+    return !p.all_subsets && (uses_queue_form(p) || !(p.fused_cdet && p.max_order <= kWarpCdetMaxOrder));
+}
+
+void queue_launch_shape(const Problem& p, const Scratch& w, int sm_count, int* warps_per_block, int* blocks,
+                        size_t* smem) {
+    const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
+    const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(double);
+    const size_t sm_bytes = 227 * 1024;  // shared memory of one SM this kernel can use (a block's limit too)
+    const int sms = sm_count > 0 ? sm_count : 152;
+    int per_sm = static_cast<int>(std::min<size_t>(32, sm_bytes / (ws_bytes + 16)));
+    if (p.queue.warps_per_sm > 0) per_sm = std::min(per_sm, p.queue.warps_per_sm);
+    if (p.queue.pair) per_sm &= ~1;
+    per_sm = std::max(per_sm, p.queue.pair ? 2 : 1);
+    int wpb = std::min(8, per_sm);
+    if (p.queue.pair) wpb &= ~1;
+    size_t bytes = ws_bytes * wpb + (p.queue.pair ? 16 * sizeof(double) : 0);
+    int per_sm_blocks = std::max(1, per_sm / wpb);
+    while (per_sm_blocks > 1 && per_sm_blocks * (bytes + 1024) > sm_bytes + 1024) --per_sm_blocks;
+    int64_t grid = static_cast<int64_t>(sms) * per_sm_blocks;
+    // the LU-fallback scratch holds ws_warps warps; no more warps than configurations need
+    grid = std::min<int64_t>(grid, std::max<int64_t>(1, static_cast<int64_t>(w.ws_warps) / wpb));
+    const int64_t warps_needed = p.batch * (p.queue.pair ? 2 : 1);
+    grid = std::min<int64_t>(grid, std::max<int64_t>(1, (warps_needed + wpb - 1) / wpb));
+    *warps_per_block = wpb;
+    *blocks = static_cast<int>(grid);
+    *smem = bytes;
+}
+
+cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_count,
+                                  cudaStream_t stream, const KernelEvents* events, bool assembly) {
+    if (p_in.batch <= 0) return cudaSuccess;
+    auto mark = [&](int k) {
+        if (events && events->marks[k]) cudaEventRecord(events->marks[k], stream);
+    };
+    if (assembly) {
+        mark(0);
+        mark(1);
+        const int64_t entries = p_in.batch * 2 * static_cast<int64_t>(p_in.max_order) * p_in.max_order;
+        green_assembly_fp64<<<static_cast<unsigned>((entries + 127) / 128), 128, 0, stream>>>(p_in, w);
+        const cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        mark(2);
+    }
+    return post_assembly(p_in, w, sm_count, stream, events);
+}
+
+cudaError_t launch_post_assembly(const Problem& p, const Scratch& w, int sm_count, cudaStream_t stream) {
+    if (p.batch <= 0) return cudaSuccess;
+    return post_assembly(p, w, sm_count, stream, nullptr);
 }
 
 int all_subsets_lane_form_min_batch(int sm_count) {

@@ -55,6 +55,19 @@ struct Scratch {
 constexpr int kFormAuto = 0, kFormLane = 1, kFormWarp = 2;
 constexpr int kAllWarpMaxOrder = 11;  // the warp form holds a and dp of one set in shared memory
 
+// How a single-top batch runs after its Green matrices (the values of the C
+// ABI's CDET_INTEGRAND_*): staged (minors kernel, global a array, CDet
+// kernel) or the persistent queue kernel (minors and CDet of a configuration
+// on one warp or a pair of warps, configurations taken from order-sorted
+// slots). Both give the same values bit for bit.
+constexpr int kIntegrandAuto = 0, kIntegrandStaged = 1, kIntegrandQueue = 2;
+constexpr int kQueueMaxOrder = 10;  // the queue form keeps a configuration's workspace in shared memory
+struct QueueShape {
+    int warps_per_sm = 0;  // resident warps per SM (0: as many as the shared memory holds)
+    int pair = 0;          // 1: two warps per configuration (one per set)
+    int grab = 1;          // slots a warp (pair) takes per queue pop
+};
+
 struct Problem {
     Scalars s;
     TableDev up[2], down[2];  // set 0 = twisted (r=2), set 1 = ordinary (r=1)
@@ -68,6 +81,8 @@ struct Problem {
                               // separately rounded multiply, subtract and add
     int all_subsets_form;     // kFormAuto / kFormLane / kFormWarp (CDET_FORM_*, cdet_set_all_subsets_form)
     int sorted;               // set by the launcher: minors and the lane CDet work in order-sorted slots
+    int integrand_form;       // kIntegrandStaged or kIntegrandQueue (single-top batches of order <= 10)
+    QueueShape queue;         // launch shape of the queue form
     DDPair pref_dd[2][kMaxOrder + 1];   // cdet_order_prefactor<DoubleDouble>, [set][order]
     double pref_ld[2][kMaxOrder + 1];   // cdet_order_prefactor<double> (host long double)
     double* values;
@@ -195,7 +210,15 @@ cudaError_t launch_diagonal_order1(const TableDev* const tables[4], int n1, int 
 cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& scratch, int sm_count,
                                   cudaStream_t stream, const KernelEvents* events, bool assembly = true);
 // Whether launch_fp64_integrand sorts the batch by order first (three more
-// kernels: the lane CDet of a single-order batch).
+// kernels: the lane CDet of a single-order batch, and the queue form).
 bool sorts_orders(const Problem& p);
+// Whether the batch runs the queue form (p.integrand_form and the orders it supports).
+bool uses_queue_form(const Problem& p);
+// The post-assembly stages alone (sort, minors, CDet, or the queue kernel),
+// on Green matrices already in scratch: what the autotuner times.
+cudaError_t launch_post_assembly(const Problem& p, const Scratch& scratch, int sm_count, cudaStream_t stream);
+// Grid of the queue form for this problem: warps per block, blocks, shared bytes per block.
+void queue_launch_shape(const Problem& p, const Scratch& scratch, int sm_count, int* warps_per_block, int* blocks,
+                        size_t* smem);
 
 }  // namespace cdet

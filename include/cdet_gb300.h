@@ -416,6 +416,34 @@ int cdet_set_all_subsets_form(cdet_context* ctx, int form);
  * for the split assembly. */
 int cdet_all_subsets_form_tuned(const cdet_context* ctx, int max_order, int fused, int64_t batch, int* form);
 
+/* How a single-top batch (cdet_integrand_device / _host) of max_order <= 10
+ * runs after its Green matrices are assembled. Every form performs the same
+ * operations per configuration, so all give the same values bit for bit.
+ * Replaces nothing in the reference: its integrand evaluates one
+ * configuration per call (integrand_replica_randomly_sampled.h:498-560);
+ * these are the batched layouts of that call. */
+enum cdet_integrand_form {
+    CDET_INTEGRAND_AUTO = 0,   /* measured per (order, assembly, batch size class); see below */
+    CDET_INTEGRAND_STAGED = 1, /* minors kernel (a warp per configuration and set), a[] in HBM, CDet kernel */
+    CDET_INTEGRAND_QUEUE = 2   /* one persistent kernel: minors and CDet of a configuration in shared
+                                  memory, configurations taken from order-sorted slots (decreasing
+                                  order) through an atomic queue head */
+};
+
+/* Selects the form; for CDET_INTEGRAND_QUEUE also its launch shape:
+ * warps_per_sm = resident warps per SM (0: as many as shared memory holds),
+ * pair = 1 for two warps per configuration (one per table set), grab = slots
+ * a warp takes per queue pop (>= 1). CDET_INTEGRAND_AUTO (the default) makes
+ * the first evaluation of each (max_order, assembly, floor(log2 batch))
+ * outside a CUDA-graph capture time the staged form and four queue shapes on
+ * its own Green matrices and keep the fastest. */
+int cdet_set_integrand_form(cdet_context* ctx, int form, int warps_per_sm, int pair, int grab);
+
+/* The form the tuner kept for (max_order, fused = 1 for the split assembly,
+ * batch): *form is CDET_INTEGRAND_AUTO before any measurement of that key. */
+int cdet_integrand_form_tuned(const cdet_context* ctx, int max_order, int fused, int64_t batch, int* form,
+                              int* warps_per_sm, int* pair, int* grab);
+
 /* Builds the bf16 slices of every uploaded table for the split assembly
  * (otherwise done by the first split evaluation). Allocates about twice the
  * FP64 table size of device memory. */
