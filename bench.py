@@ -563,10 +563,27 @@ def run_mcmcmc(args):
         dt = time.perf_counter() - t0
         l1, g1 = chains.launch_count()
         jack = jackknife_ratios(chains.results(), omin, omax, 1)
+        # the same chains continued with every Green pair evaluated each step
+        # (the values do not change), then the fraction of pairs reused
+        chains.set_green_reuse(False)
+        n_off = max(20, steps // 4)
+        chains.run(5, warmup=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        chains.run(n_off, warmup=False)
+        dt_off = time.perf_counter() - t0
+        chains.set_green_reuse(True)
+        rec = chains.run(50, warmup=False, record=True)
+        kept = np.vectorize(lambda m: bin(int(m)).count("1"))(rec["chosen"]).astype(np.float64)
         out[path] = {"ratios_to_order1": [float(x) for x in jack["ratio"][omin:omax + 1]],
-                     "jackknife_errors": [float(x) for x in jack["error"][omin:omax + 1]],"value": chains_n * steps / dt, "ms_per_step": 1e3 * dt / steps,
+                     "jackknife_errors": [float(x) for x in jack["error"][omin:omax + 1]],
+                     "value": chains_n * steps / dt, "ms_per_step": 1e3 * dt / steps,
                      "hours_for_1e5_steps": dt / steps * 1e5 / 3600, "histogram_learning_s": learn_s,
-                     "gpu_launches": l1 - l0, "graph_steps": g1 - g0}
+                     "gpu_launches": l1 - l0, "graph_steps": g1 - g0,
+                     "green_reuse": {"ms_per_step_without": 1e3 * dt_off / n_off,
+                                     "pairs_reused_fraction": float((kept ** 2).mean() / env ** 2),
+                                     "note": "production steps copy the Green entries of pairs of retained "
+                                             "vertices from the previous step; without: every pair evaluated"}}
         chains.close()
     out["value"] = out["split"]["value"]
     out["gpu_launches"] = out["split"]["gpu_launches"]

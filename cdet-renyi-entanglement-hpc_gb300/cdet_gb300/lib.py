@@ -36,6 +36,7 @@ EXPORTED = (
     "cdet_mcmcmc_summary", "cdet_mcmcmc_estimates", "cdet_write_mcmcmc_checkpoint", "cdet_read_mcmcmc_checkpoint",
     "cdet_mcmcmc_save_checkpoints", "cdet_mcmcmc_load_checkpoints", "cdet_mcmcmc_launch_count", "cdet_set_all_subsets_form", "cdet_all_subsets_form_tuned", "cdet_load_chunks",
     "cdet_split_counters", "cdet_set_integrand_form", "cdet_integrand_form_tuned",
+    "cdet_mcmcmc_set_green_reuse",
 )
 
 ASSEMBLY_FP64 = 0
@@ -153,6 +154,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_set_all_subsets_form.argtypes = [vp, i32]
     lib.cdet_all_subsets_form_tuned.argtypes = [vp, i32, i32, i64, C.POINTER(C.c_int)]
     lib.cdet_set_integrand_form.argtypes = [vp, i32, i32, i32, i32]
+    lib.cdet_mcmcmc_set_green_reuse.argtypes = [vp, i32]
     lib.cdet_integrand_form_tuned.argtypes = [vp, i32, i32, i64] + [C.POINTER(C.c_int)] * 4
     lib.cdet_mcmcmc_launch_count.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.cdet_mcmcmc_learn_histogram.argtypes = [vp, C.POINTER(McmcmcConfig), C.POINTER(HistogramConfig), C.c_uint64,

@@ -119,6 +119,12 @@ class McmcmcChains:
                                                        int(require), C.byref(restored)))
         return restored.value
 
+    def set_green_reuse(self, enable: bool) -> None:
+        """Green-pair reuse across steps (default on): pairs of retained
+        vertices are copied from the previous step's Green matrices; the
+        chains are the same bit for bit either way."""
+        L.check(self._lib.cdet_mcmcmc_set_green_reuse(self._h, int(bool(enable))))
+
     def launch_count(self) -> tuple:
         """(kernels launched by the runs so far, steps replayed from a CUDA graph)."""
         n, g = C.c_int64(), C.c_int64()

@@ -222,6 +222,9 @@ int build_problem(cdet_context* ctx, const double* vertices, const int32_t* orde
     p->sorted = 0;
     p->integrand_form = cdet::kIntegrandStaged;
     p->queue = cdet::QueueShape{};
+    p->reuse_green = nullptr;
+    p->reuse_diag = nullptr;
+    p->reuse_mask = nullptr;
     for (int set = 0; set < 2; ++set) {
         const int r = set == 0 ? 2 : 1;
         for (int n = 0; n <= cdet::kMaxOrder; ++n) {
@@ -418,7 +421,7 @@ int tune_integrand_form(cdet_context* ctx, cdet::Problem p, const cdet::Scratch&
 
 int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch,
         int max_order, int all_subsets, double* values, int32_t* status, cudaStream_t stream,
-        bool assembly_only = false) {
+        bool assembly_only = false, const cdet::GreenReuse* reuse = nullptr) {
     if (batch < 0) return fail(CDET_ERR_INVALID, "batch must be non-negative");
     if (batch == 0) return CDET_OK;
     if (!vertices || !values || !status || (!all_subsets && !orders))
@@ -432,6 +435,13 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
     cdet::carve_scratch(ctx->scratch, ctx->scratch_batch, ctx->scratch_order, ctx->ws_warps, &w);
     // The carve above is for the reserved (batch, order); the kernels index
     // with the call's max_order, which only needs less.
+    if (reuse) {
+        w.green = reuse->green;
+        w.diag = reuse->diag;
+        p.reuse_green = reuse->prev_green;
+        p.reuse_diag = reuse->prev_diag;
+        p.reuse_mask = reuse->mask;
+    }
     cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);
     if (err != cudaSuccess) return cuda_fail(err, "cudaMemsetAsync(status)");
     cdet::KernelEvents* events = nullptr;
@@ -546,6 +556,7 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         }
         if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
         launches = cdet::uses_queue_form(p) ? 2 : 3;  // assembly + minors, CDet (or the queue kernel)
+        if (p.reuse_mask && p.all_subsets) launches += 2;  // the reuse scan and the copies
     } else {
         launches = 1;
         err = cdet::launch_fp64_assembly_only(p, w, stream);
@@ -618,8 +629,10 @@ namespace capi {
 const cdet::TableDev* resolve(const cdet_context* ctx, int kind) { return ::resolve(ctx, kind); }
 
 int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch, int max_order,
-        int all_subsets, double* values, int32_t* status, cudaStream_t stream, bool assembly_only) {
-    return ::run(ctx, vertices, orders, batch, max_order, all_subsets, values, status, stream, assembly_only);
+        int all_subsets, double* values, int32_t* status, cudaStream_t stream, bool assembly_only,
+        const cdet::GreenReuse* reuse) {
+    return ::run(ctx, vertices, orders, batch, max_order, all_subsets, values, status, stream, assembly_only,
+                 reuse);
 }
 
 }  // namespace capi

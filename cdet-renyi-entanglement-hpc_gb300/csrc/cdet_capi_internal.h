@@ -103,8 +103,11 @@ const cdet::TableDev* resolve(const cdet_context* ctx, int kind);
 
 // Launches one evaluation of the context's assembly on `stream` (device
 // buffers; all_subsets = 1: the 2^max_order subset values of each envelope).
-// Asynchronous once the context's scratch holds the batch.
+// Asynchronous once the context's scratch holds the batch. With `reuse` the
+// Green matrices go to the caller's buffers and pairs of retained vertices are
+// copied from the previous evaluation's (the MCMCMC step).
 int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_t batch, int max_order,
-        int all_subsets, double* values, int32_t* status, cudaStream_t stream, bool assembly_only = false);
+        int all_subsets, double* values, int32_t* status, cudaStream_t stream, bool assembly_only = false,
+        const cdet::GreenReuse* reuse = nullptr);
 
 }  // namespace capi

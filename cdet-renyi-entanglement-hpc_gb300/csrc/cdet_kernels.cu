@@ -72,25 +72,13 @@ __device__ __forceinline__ double clamp_unit(double value) {
 }
 
 // ------------------------------------------------------ 1. assembly -------
-__global__ void __launch_bounds__(128) green_assembly_fp64(const __grid_constant__ Problem p,
-                                                          const __grid_constant__ Scratch w) {
+// Entry (i, j) of table set `set` of configuration c (order n): decode,
+// descriptor, Clenshaw sums, shifts and scale. With copy_retained, a pair of
+// vertices retained from the previous evaluation is copied instead.
+__device__ __forceinline__ void assemble_entry(const Problem& p, const Scratch& w, int64_t c, int set, int i, int j,
+                                               int n, bool copy_retained) {
     const int nmax = p.max_order;
     const int64_t per_set = static_cast<int64_t>(nmax) * nmax;
-    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= p.batch * 2 * per_set) return;
-    const int64_t c = idx / (2 * per_set);
-    const int64_t rem = idx - c * 2 * per_set;
-    const int set = static_cast<int>(rem / per_set);
-    const int pair = static_cast<int>(rem - set * per_set);
-    const int i = pair / nmax;
-    const int j = pair - i * nmax;
-    const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
-    if (n < 1 || n > nmax) {
-        if (rem == 0) atomicOr(p.status + c, kStatusBadInput);
-        return;
-    }
-    if (i >= n || j >= n) return;
-
     const Scalars& s = p.s;
     const int replica_count = set == 0 ? 2 : 1;
     bool bad = false;
@@ -101,6 +89,7 @@ __global__ void __launch_bounds__(128) green_assembly_fp64(const __grid_constant
         atomicOr(p.status + c, kStatusBadInput);
         return;
     }
+    if (copy_retained && copy_reused_pair(p, w.green, w.diag, c, set, i, j, n)) return;
 
     // prepare_green_lookup_descriptor (g_funcs.h:609-653).
     const bool upper = (i != j) && (vi.tau_unit > vj.tau_unit);
@@ -152,6 +141,123 @@ __global__ void __launch_bounds__(128) green_assembly_fp64(const __grid_constant
     }
     w.green[mslot * per_set + i * n + j] = dmul(up, s.scale);
     w.green[(mslot + 1) * per_set + i * n + j] = dmul(down, s.scale);
+}
+
+// One thread per (configuration, set, i, j) entry.
+__global__ void __launch_bounds__(128) green_assembly_fp64(const __grid_constant__ Problem p,
+                                                          const __grid_constant__ Scratch w) {
+    const int nmax = p.max_order;
+    const int64_t per_set = static_cast<int64_t>(nmax) * nmax;
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= p.batch * 2 * per_set) return;
+    const int64_t c = idx / (2 * per_set);
+    const int64_t rem = idx - c * 2 * per_set;
+    const int set = static_cast<int>(rem / per_set);
+    const int pair = static_cast<int>(rem - set * per_set);
+    const int i = pair / nmax;
+    const int j = pair - i * nmax;
+    const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
+    if (n < 1 || n > nmax) {
+        if (rem == 0) atomicOr(p.status + c, kStatusBadInput);
+        return;
+    }
+    if (i >= n || j >= n) return;
+    assemble_entry(p, w, c, set, i, j, n, p.reuse_mask != nullptr);
+}
+
+// Green-pair reuse in the FP64 assembly (all-subsets batches): the copies and
+// the evaluations go to separate launches, so no warp waits on another lane's
+// Clenshaw sums while its own lanes only copy. reuse_offsets: per
+// configuration the first of its fresh entries, 2 (n^2 - k^2) of them with k
+// retained vertices, exclusive over configurations, and the total.
+constexpr uint32_t kReuseTotalIndex = 56;  // the total's uint32 slot in Scratch::order_count
+
+__global__ void __launch_bounds__(1024) reuse_scan(const __grid_constant__ Problem p, int32_t* offsets,
+                                                   uint32_t* total) {
+    __shared__ uint32_t part[1024];
+    const int n = p.max_order;
+    const int64_t per = (p.batch + 1023) / 1024;
+    const int64_t begin = threadIdx.x * per, end = min(p.batch, begin + per);
+    uint32_t sum = 0;
+    for (int64_t c = begin; c < end; ++c) {
+        const int k = __popcll(__ldg(p.reuse_mask + c));
+        sum += 2u * static_cast<uint32_t>(n * n - k * k);
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // inclusive scan of the thread sums
+        const uint32_t add = threadIdx.x >= static_cast<unsigned>(off) ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += add;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+    for (int64_t c = begin; c < end; ++c) {
+        offsets[c] = static_cast<int32_t>(run);
+        const int k = __popcll(__ldg(p.reuse_mask + c));
+        run += 2u * static_cast<uint32_t>(n * n - k * k);
+    }
+    if (threadIdx.x == 1023) *total = part[1023];
+}
+
+// The copies: one thread per entry of the retained block (i, j < k).
+__global__ void __launch_bounds__(128) green_copy_retained(const __grid_constant__ Problem p,
+                                                          const __grid_constant__ Scratch w) {
+    const int n = p.max_order;
+    const int64_t per_set = static_cast<int64_t>(n) * n;
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= p.batch * 2 * per_set) return;
+    const int64_t c = idx / (2 * per_set);
+    const int64_t rem = idx - c * 2 * per_set;
+    const int set = static_cast<int>(rem / per_set);
+    const int pair = static_cast<int>(rem - set * per_set);
+    const int i = pair / n, j = pair - (pair / n) * n;
+    const int k = __popcll(__ldg(p.reuse_mask + c));
+    if (i >= k || j >= k) return;
+    bool bad = false;  // the decode's checks, so the status bits are a fresh evaluation's
+    const double* vbase = p.vertices + c * n * 4;
+    decode_vertex(vbase + 4 * i, p.s, set == 0 ? 2 : 1, bad);
+    decode_vertex(vbase + 4 * j, p.s, set == 0 ? 2 : 1, bad);
+    if (bad) {
+        atomicOr(p.status + c, kStatusBadInput);
+        return;
+    }
+    copy_reused_pair(p, w.green, w.diag, c, set, i, j, n);
+}
+
+// The evaluations: one thread per fresh entry, compacted over the batch.
+// Fresh entries of a set, in order: rows i < k at columns k..n-1, then rows
+// i >= k at every column.
+__global__ void __launch_bounds__(128) green_assembly_fp64_fresh(const __grid_constant__ Problem p,
+                                                                const __grid_constant__ Scratch w,
+                                                                const int32_t* __restrict__ offsets,
+                                                                const uint32_t* __restrict__ total) {
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= static_cast<int64_t>(__ldg(total))) return;
+    // the configuration: the last offset <= idx
+    int64_t lo = 0, hi = p.batch - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (static_cast<int64_t>(__ldg(offsets + mid)) <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t c = lo;
+    const int n = p.max_order;
+    const int k = __popcll(__ldg(p.reuse_mask + c));
+    const int per = n * n - k * k;  // fresh entries per set (> 0 here: this configuration owns idx)
+    const int r = static_cast<int>(idx - __ldg(offsets + c));
+    const int set = r >= per ? 1 : 0;
+    const int rr = r - set * per;
+    int i, j;
+    if (rr < k * (n - k)) {
+        i = rr / (n - k);
+        j = k + (rr - i * (n - k));
+    } else {
+        const int q = rr - k * (n - k);
+        i = k + q / n;
+        j = q - (q / n) * n;
+    }
+    assemble_entry(p, w, c, set, i, j, n, false);
 }
 
 // ------------------------------------------------- 2. principal minors ----
@@ -1592,7 +1698,16 @@ cudaError_t launch_fp64_integrand(const Problem& p_in, const Scratch& w, int sm_
         mark(0);
         mark(1);
         const int64_t entries = p_in.batch * 2 * static_cast<int64_t>(p_in.max_order) * p_in.max_order;
-        green_assembly_fp64<<<static_cast<unsigned>((entries + 127) / 128), 128, 0, stream>>>(p_in, w);
+        const unsigned grid = static_cast<unsigned>((entries + 127) / 128);
+        if (p_in.reuse_mask && p_in.all_subsets) {
+            // Green-pair reuse: scan of the fresh entries, copies, compacted evaluations
+            // (the configurations' slot array is free in an all-subsets evaluation)
+            reuse_scan<<<1, 1024, 0, stream>>>(p_in, w.slot_of, w.order_count + kReuseTotalIndex);
+            green_copy_retained<<<grid, 128, 0, stream>>>(p_in, w);
+            green_assembly_fp64_fresh<<<grid, 128, 0, stream>>>(p_in, w, w.slot_of, w.order_count + kReuseTotalIndex);
+        } else {
+            green_assembly_fp64<<<grid, 128, 0, stream>>>(p_in, w);
+        }
         const cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return err;
         mark(2);

@@ -83,11 +83,65 @@ struct Problem {
     int sorted;               // set by the launcher: minors and the lane CDet work in order-sorted slots
     int integrand_form;       // kIntegrandStaged or kIntegrandQueue (single-top batches of order <= 10)
     QueueShape queue;         // launch shape of the queue form
+    // Green-pair reuse (all-subsets batches of MCMCMC chains): when reuse_mask
+    // is set, configuration c's first popcount(reuse_mask[c]) vertices are the
+    // vertices of the previous evaluation selected by that mask, in increasing
+    // order, and the Green entries (and shifted diagonals) of pairs of them are
+    // copied from reuse_green / reuse_diag (the previous evaluation's layout)
+    // instead of evaluated: the same values, since an entry depends only on its
+    // two vertices (integrand_replica_randomly_sampled.h:57-86, 664-696)
+    const double* reuse_green;
+    const double* reuse_diag;
+    const uint64_t* reuse_mask;
     DDPair pref_dd[2][kMaxOrder + 1];   // cdet_order_prefactor<DoubleDouble>, [set][order]
     double pref_ld[2][kMaxOrder + 1];   // cdet_order_prefactor<double> (host long double)
     double* values;
     int32_t* status;
 };
+
+// This evaluation's Green matrices and diagonals in caller-owned buffers
+// (replacing the scratch's), and the previous evaluation's with the masks of
+// retained vertices: Green-pair reuse of the MCMCMC step (Problem::reuse_*).
+struct GreenReuse {
+    double* green;              // [batch][2][2][max_order^2]
+    double* diag;               // [batch][2][2][max_order]
+    const double* prev_green;   // the previous evaluation's, same layout
+    const double* prev_diag;
+    const uint64_t* mask;       // [batch] or null (no reuse this evaluation)
+};
+
+#ifdef __CUDACC__
+// Index of the i-th lowest set bit of m (i < popcount(m)).
+__device__ __forceinline__ int nth_set_bit(uint64_t m, int i) {
+    for (int t = 0; t < i; ++t) m &= m - 1;
+    return __ffsll(static_cast<long long>(m)) - 1;
+}
+
+// Green-pair reuse of entry (i, j) of one table set of configuration c (order
+// n): when both vertices were retained from the previous evaluation, copies
+// both spins' entries (and the shifted diagonals when i == j) from it and
+// returns true. A copy equals a fresh evaluation bit for bit: the same two
+// vertices, the same operations.
+__device__ __forceinline__ bool copy_reused_pair(const Problem& p, double* green, double* diag, int64_t c, int set,
+                                                 int i, int j, int n) {
+    if (!p.reuse_mask) return false;
+    const uint64_t kept = __ldg(p.reuse_mask + c);
+    const int k = __popcll(kept);
+    if (i >= k || j >= k) return false;
+    const int oi = nth_set_bit(kept, i);
+    const int oj = i == j ? oi : nth_set_bit(kept, j);
+    const int nmax = p.max_order;
+    const int64_t per_set = static_cast<int64_t>(nmax) * nmax;
+    const int64_t mslot = (c * 2 + set) * 2;
+    green[mslot * per_set + i * n + j] = __ldg(p.reuse_green + mslot * per_set + oi * n + oj);
+    green[(mslot + 1) * per_set + i * n + j] = __ldg(p.reuse_green + (mslot + 1) * per_set + oi * n + oj);
+    if (i == j) {
+        diag[mslot * nmax + i] = __ldg(p.reuse_diag + mslot * nmax + oi);
+        diag[(mslot + 1) * nmax + i] = __ldg(p.reuse_diag + (mslot + 1) * nmax + oi);
+    }
+    return true;
+}
+#endif
 
 // Optional events bracketing the stages of one evaluation: [0] start,
 // [1] assembly prep done (descriptors and sort of the split form; equal to
@@ -178,6 +232,9 @@ struct McmcmcStepArgs {
     // chosen_out[r][chains], norm_out[r][chains], signal_out[r][chains][envelope + 1]
     const int64_t* ring_row;
     uint64_t* chosen_out;           // or null
+    uint64_t* retained_out;         // or null: [chains] the chosen mask whose vertices lead next_vertices
+                                    // (0 when the chain made no step), read by the next evaluation's
+                                    // Green-pair reuse
     double* norm_out;               // or null
     double* signal_out;             // or null
     // histogram seed kernel when tau_bins > 0: row probabilities and their

@@ -284,6 +284,7 @@ __device__ void finish_step(const McmcmcStepArgs& a, int64_t c, int64_t row, con
     }
     const int order = __popcll(chosen);
     if (a.chosen_out) a.chosen_out[row * a.chains + c] = chosen;
+    if (a.retained_out) a.retained_out[c] = chosen;
     if (a.norm_out) a.norm_out[row * a.chains + c] = norm;
     if (a.warmup) ++a.counts[c * (env + 1) + order];
 }
@@ -296,6 +297,7 @@ __global__ void __launch_bounds__(128) mcmcmc_step(const __grid_constant__ Mcmcm
     if (c >= a.chains) return;
     const int64_t row = a.ring_row ? *a.ring_row : 0;
     if (a.chosen_out) a.chosen_out[row * a.chains + c] = 0;  // 0: no step (a failed chain)
+    if (a.retained_out) a.retained_out[c] = 0;
     if (a.error[c]) return;  // a chain that failed stays where it stopped
     if (a.integrand_status[c] & kStatusNonFinite) {
         a.error[c] = 1;  // "Error (all-subset integrand): Value is not finite"
@@ -383,6 +385,7 @@ __device__ void finish_step_warp(const McmcmcStepArgs& a, int64_t c, int64_t row
         ++size;
     }
     if (a.chosen_out) a.chosen_out[row * a.chains + c] = chosen;
+    if (a.retained_out) a.retained_out[c] = chosen;
     if (a.norm_out) a.norm_out[row * a.chains + c] = norm;
     if (a.warmup) ++a.counts[c * (env + 1) + __popcll(chosen)];
 }
@@ -405,6 +408,7 @@ __global__ void __launch_bounds__(32) mcmcmc_step_warp(const __grid_constant__ M
     double* cd0 = sd + env * env;
     const int64_t row = a.ring_row ? *a.ring_row : 0;
     if (lane == 0 && a.chosen_out) a.chosen_out[row * a.chains + c] = 0;  // 0: no step (a failed chain)
+    if (lane == 0 && a.retained_out) a.retained_out[c] = 0;
     if (a.error[c]) return;  // the same value on every lane
     if (a.integrand_status[c] & kStatusNonFinite) {
         if (lane == 0) a.error[c] = 1;  // "Error (all-subset integrand): Value is not finite"

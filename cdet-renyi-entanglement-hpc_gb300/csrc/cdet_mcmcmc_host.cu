@@ -82,6 +82,17 @@ struct cdet_mcmcmc {
     int launches_per_step = 0;
     int64_t kernel_launches = 0;
     int64_t graph_steps = 0;
+    // Green-pair reuse: the Green matrices and diagonals of the evaluation of
+    // vert[b] in green2[b] / diag2[b], and per chain the chosen mask whose
+    // vertices lead the next vertex buffer (written by the step kernel);
+    // zeroed whenever the previous matrices cannot be reused (first step,
+    // restored vertices, new tables or buffers, another assembly)
+    void* reuse_block = nullptr;
+    double* green2[2] = {nullptr, nullptr};
+    double* diag2[2] = {nullptr, nullptr};
+    uint64_t* retained = nullptr;
+    bool green_reuse = true;
+    uint64_t reuse_generation = ~uint64_t{0};
 };
 
 namespace {
@@ -161,6 +172,7 @@ cdet::McmcmcStepArgs step_args(const cdet_mcmcmc* m, int warmup) {
     a.error = m->error;
     a.ring_row = m->d_row;
     a.chosen_out = m->d_chosen;
+    a.retained_out = m->retained;
     a.norm_out = m->d_norm;
     a.signal_out = m->d_signal;
     if (m->tau_bins > 0) {
@@ -181,8 +193,12 @@ cdet::McmcmcStepArgs step_args(const cdet_mcmcmc* m, int warmup) {
 // Enqueues one step (integrand, step kernel, ring row advance) on the
 // chains' stream; *launches = the kernels it launches.
 int enqueue_step(cdet_mcmcmc* m, int warmup, int* launches) {
+    // the Green matrices of this step's vertices go to green2[cur]; pairs of
+    // retained vertices are copied from green2[cur ^ 1], the previous step's
+    const cdet::GreenReuse reuse{m->green2[m->cur], m->diag2[m->cur], m->green2[m->cur ^ 1], m->diag2[m->cur ^ 1],
+                                 m->green_reuse ? m->retained : nullptr};
     int rc = run(m->ctx, m->vert[m->cur], nullptr, m->chains, m->cfg.envelope_order, 1, m->values, m->istatus,
-                 m->stream);
+                 m->stream, false, &reuse);
     if (rc != CDET_OK) return rc;
     int step_kernels = 0;
     cudaError_t err = cdet::launch_mcmcmc_step(step_args(m, warmup), m->stream, &step_kernels);
@@ -206,6 +222,13 @@ void drop_graphs(cdet_mcmcmc* m) {
 // context's current generation).
 int launch_step(cdet_mcmcmc* m, int warmup) {
     cdet_context* ctx = m->ctx;
+    // the previous step's Green matrices came from other tables, buffers or
+    // another assembly (each bumps the context's generation): none is reused
+    if (m->reuse_generation != ctx->generation) {
+        const cudaError_t err = cudaMemsetAsync(m->retained, 0, static_cast<size_t>(m->chains) * 8, m->stream);
+        if (err != cudaSuccess) return cuda_fail(err, "MCMCMC Green-pair reuse reset");
+        m->reuse_generation = ctx->generation;
+    }
     const bool graphs = m->use_graphs && !ctx->profiling;
     if (graphs && m->graph_generation != ctx->generation) {
         drop_graphs(m);
@@ -341,6 +364,7 @@ void free_chains(cdet_mcmcmc* m) {
     if (m->ring) cudaFree(m->ring);
     if (m->block) cudaFree(m->block);
     if (m->hist_block) cudaFree(m->hist_block);
+    if (m->reuse_block) cudaFree(m->reuse_block);
     delete m;
 }
 
@@ -398,7 +422,10 @@ int cdet_mcmcmc_create(cdet_context* ctx, const cdet_mcmcmc_config* config, int6
     const size_t per_step = static_cast<size_t>(chains) * (2 + e1) * 8;
     m->ring_steps = std::max<int64_t>(1, std::min<int64_t>(256, static_cast<int64_t>((size_t{16} << 20) / per_step)));
     const size_t ring_bytes = up(8) + 2 * static_cast<size_t>(m->ring_steps) * per_step;
+    const size_t ng = static_cast<size_t>(chains) * 4 * env * env, nd = static_cast<size_t>(chains) * 4 * env;
+    const size_t reuse_bytes = 2 * up(ng * 8) + 2 * up(nd * 8) + up(chains * 8);
     cudaError_t err = cudaMalloc(&m->block, bytes);
+    if (err == cudaSuccess) err = cudaMalloc(&m->reuse_block, reuse_bytes);
     if (err == cudaSuccess) err = cudaMalloc(&m->ring, ring_bytes);
     if (err == cudaSuccess) err = cudaMallocHost(&m->pinned, ring_bytes);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
@@ -424,6 +451,10 @@ int cdet_mcmcmc_create(cdet_context* ctx, const cdet_mcmcmc_config* config, int6
     m->counts = static_cast<uint64_t*>(take(nl * 8));
     m->error = static_cast<int32_t*>(take(chains * 4));
     uint64_t* dseeds = static_cast<uint64_t*>(take(chains * 8));
+    p = static_cast<char*>(m->reuse_block);
+    for (int b = 0; b < 2; ++b) m->green2[b] = static_cast<double*>(take(ng * 8));
+    for (int b = 0; b < 2; ++b) m->diag2[b] = static_cast<double*>(take(nd * 8));
+    m->retained = static_cast<uint64_t*>(take(chains * 8));
     const size_t rows = 2 * static_cast<size_t>(m->ring_steps);
     m->d_row = static_cast<int64_t*>(m->ring);
     m->d_chosen = reinterpret_cast<uint64_t*>(static_cast<char*>(m->ring) + up(8));
@@ -437,6 +468,7 @@ int cdet_mcmcmc_create(cdet_context* ctx, const cdet_mcmcmc_config* config, int6
     if (err == cudaSuccess) err = cudaMemset(m->counts, 0, nl * 8);
     if (err == cudaSuccess) err = cudaMemset(m->error, 0, chains * 4);
     if (err == cudaSuccess) err = cudaMemset(m->d_row, 0, 8);
+    if (err == cudaSuccess) err = cudaMemset(m->retained, 0, chains * 8);  // the first step reuses nothing
     if (err == cudaSuccess) err = cdet::launch_mcmcmc_init(chains, env, dseeds, m->mt, m->mt_index, m->vert[0], nullptr);
     if (err == cudaSuccess) err = cudaDeviceSynchronize();
     if (err != cudaSuccess) {
@@ -547,6 +579,17 @@ int cdet_mcmcmc_destroy(cdet_mcmcmc* m) {
     DeviceGuard guard(m->ctx->device);
     cudaDeviceSynchronize();
     free_chains(m);
+    return CDET_OK;
+}
+
+int cdet_mcmcmc_set_green_reuse(cdet_mcmcmc* m, int enable) {
+    if (!m) return fail(CDET_ERR_INVALID, "null chains");
+    DeviceGuard guard(m->ctx->device);
+    cudaError_t err = cudaStreamSynchronize(m->stream);
+    if (err == cudaSuccess) err = cudaMemset(m->retained, 0, static_cast<size_t>(m->chains) * 8);
+    if (err != cudaSuccess) return cuda_fail(err, "MCMCMC Green-pair reuse switch");
+    m->green_reuse = enable != 0;
+    drop_graphs(m);  // their evaluations were captured with the other setting
     return CDET_OK;
 }
 
@@ -1181,6 +1224,7 @@ int cdet_mcmcmc_load_checkpoints(cdet_mcmcmc* m, const char* dir, const cdet_mcm
     if (err == cudaSuccess) err = cudaMemcpy(m->mt, words.data(), words.size() * 8, cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaMemcpy(m->mt_index, index.data(), index.size() * 4, cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaMemset(m->error, 0, chains * 4);
+    if (err == cudaSuccess) err = cudaMemset(m->retained, 0, chains * 8);  // restored vertices: no reuse
     if (err != cudaSuccess) return cuda_fail(err, "MCMCMC checkpoint restore");
     m->warmup_done = static_cast<int64_t>(wp);
     return CDET_OK;

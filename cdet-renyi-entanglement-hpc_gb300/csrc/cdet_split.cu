@@ -448,6 +448,10 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
         atomicOr(p.status + c, kStatusBadInput);
         return;
     }
+    if (copy_reused_pair(p, w.green, w.diag, c, 0, i, j, n)) {  // both vertices retained: no records
+        copy_reused_pair(p, w.green, w.diag, c, 1, i, j, n);
+        return;
+    }
     const bool upper = (i != j) && (tui > tuj);
     const double t_outer = upper ? taui : tauj;
     const double t_inner = upper ? tauj : taui;

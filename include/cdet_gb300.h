@@ -340,6 +340,15 @@ int cdet_mcmcmc_destroy(cdet_mcmcmc* m);
  * (either may be null). */
 int cdet_mcmcmc_launch_count(const cdet_mcmcmc* m, int64_t* launches, int64_t* graph_steps);
 
+/* Green-pair reuse across steps (on by default): a step's envelope keeps the
+ * chosen subset's vertices first, and the Green entries of pairs of them are
+ * copied from the previous step's matrices instead of evaluated again, as the
+ * reference's integrand reuses the entries of retained vertices from its
+ * previous call (integrand_replica_randomly_sampled.h:57-86, 664-696,
+ * 778-791). An entry depends only on its two vertices, so the chains are the
+ * same bit for bit either way; enable = 0 evaluates every pair each step. */
+int cdet_mcmcmc_set_green_reuse(cdet_mcmcmc* m, int enable);
+
 /* Settings of the factorized histogram seed (MCMCMCConfig's histogram_*
  * fields, mcmcmc_sampler.h:92-95). */
 typedef struct cdet_histogram_config {

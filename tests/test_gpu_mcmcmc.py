@@ -404,3 +404,39 @@ def test_ring_wraps_and_call_boundaries():
         want = orc.mcmcmc_chain(run["order_min"], run["order_max"], run["envelope"], run["lambdas"], 0,
                                 run["adapt_interval"], run["adapt_rate"], steps, int(seed))
         assert np.array_equal(outs[0]["chosen"][:, c], want["chosen"]), c
+
+
+@pytest.mark.parametrize("assembly", ["fp64", "split"])
+def test_green_reuse_keeps_chains_bit_identical(assembly):
+    """Green-pair reuse across steps (the default) against every pair
+    evaluated each step: the same chosen masks, local normalisations and
+    order signals at every step, and the same final vertices and generator
+    states, bit for bit, for both assemblies."""
+    name = "physical_2x2"
+    run = RUNS[name]
+    params, tables, _ = load_case(name)
+    seeds = np.arange(1, 97, dtype=np.uint64) * 7919
+    outs = []
+    for reuse in (False, True):
+        gpu = CdetIntegrand(params, tables)
+        gpu.set_assembly(assembly)
+        chains = McmcmcChains(gpu, run["order_min"], run["order_max"], run["envelope"], seeds, run["lambdas"],
+                              run["adapt_interval"], run["adapt_rate"])
+        chains.set_green_reuse(reuse)
+        w = chains.run(40, warmup=True, record=True)
+        chains.end_warmup()
+        p = chains.run(60, warmup=False, record=True)
+        verts, lams, rng = chains.state()
+        outs.append((w, p, verts, lams, rng))
+        chains.close()
+    (w0, p0, v0, l0, r0), (w1, p1, v1, l1, r1) = outs
+    for key in ("chosen", "norms", "signal"):
+        a = np.concatenate([w0[key], p0[key]]) if key != "signal" else p0[key]
+        b = np.concatenate([w1[key], p1[key]]) if key != "signal" else p1[key]
+        assert np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64)), key
+    assert np.array_equal(v0.view(np.uint64), v1.view(np.uint64))
+    assert np.array_equal(l0.view(np.uint64), l1.view(np.uint64))
+    assert np.array_equal(r0, r1)
+    # every step retains the chosen order's vertices (order_min >= 1), so the copies ran
+    kept = np.vectorize(lambda m: bin(int(m)).count("1"))(np.asarray(p1["chosen"]))
+    assert kept.min() >= run["order_min"] and kept.mean() > 1.0
