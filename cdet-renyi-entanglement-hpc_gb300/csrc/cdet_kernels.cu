@@ -507,6 +507,195 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
     return false;
 }
 
+// ---- orders 11..14: the Schur recursion in chunks of subtrees ----------
+// The whole-level lists of these orders (up to 2 x 18,432 doubles at order
+// 14) do not fit shared memory, and in the global workspace every level
+// streams them through DRAM. Here only the top T levels run breadth-first
+// in the warp's global workspace (small lists); the 2^T nodes of level T are
+// then taken G at a time, and each group's subtrees run breadth-first in
+// shared memory. A node's pivot, factors and Schur complement depend only on
+// its parent, and each shifted minor receives its one addition, so every
+// value is the whole-level recursion's bit for bit; the same pivots are
+// checked, so the LU fallback is taken exactly when it is there.
+struct ChunkGeom {
+    int T, log2g;     // chunk level and log2 of the nodes per chunk
+    int list, aux;    // doubles of one chunk list buffer and of the chunk's pivot/factor buffer
+    __host__ __device__ int doubles() const { return 2 * list + aux; }
+};
+
+__host__ __device__ inline ChunkGeom chunk_geom(int n) {
+    ChunkGeom g;
+    g.T = n <= 11 ? 4 : (n <= 13 ? 5 : 6);
+    g.log2g = 2;
+    const int G = 1 << g.log2g, m = n - g.T;
+    int list = 0, aux = 0;
+    for (int j = 0; j < m; ++j) list = max(list, (G << j) * (m - j) * (m - j));
+    for (int j = 0; j + 1 < m; ++j) aux = max(aux, (G << j) * (m - j));  // pivots' inverses + factors
+    g.list = (list + 1) & ~1;
+    g.aux = (aux + 1) & ~1;
+    return g;
+}
+
+constexpr int kChunkMinOrder = 11, kChunkMaxOrder = 14;
+
+// Shared doubles per warp of the chunked minors for a batch of orders up to nmax.
+__host__ __device__ inline int chunk_doubles_upto(int nmax) {
+    int d = 0;
+    for (int n = kChunkMinOrder; n <= min(nmax, kChunkMaxOrder); ++n) d = max(d, chunk_geom(n).doubles());
+    return d;
+}
+
+// One level of the shifted Schur recursion on `nodes` matrices of old_size^2
+// in old_list, writing their 2 * nodes children (old_size - 1)^2 to new_list:
+// the first `nodes` without the pivot row and column, the next `nodes` the
+// Schur complements (mat2pm_from_buffer, fast_principle_minors.h:165-215).
+// Child q's shifted minor is shifted[base + index(q)], index(q) = c0 + (q mod
+// G) + (q div G) * 2^T (G = 2^log2g): the identity for whole levels (c0 = 0,
+// log2g = 30), the global node numbers of a chunk's subtrees otherwise.
+// Returns false when a pivot sends the matrix to the LU fallback. Each
+// shifted minor receives exactly one addition, p + the child's pivot entry,
+// written directly (the whole-level form adds it to the p it initialised).
+__device__ bool schur_level(const double* old_list, double* new_list, double* inv, int nodes, int old_size,
+                            double p, double fallback_eps, double* shifted, uint32_t base, uint32_t c0,
+                            int log2g, int T, int lane) {
+    const int old_msize = old_size * old_size;
+    const int new_size = old_size - 1;
+    const int new_msize = new_size * new_size;
+    bool bad_pivot = false;
+    for (int set = lane; set < nodes; set += kWarp) {
+        const double pivot = dadd(old_list[set * old_msize], p);
+        const double pa = fabs(pivot);
+        if (pa == 0.0 || (fallback_eps > 0.0 && pa <= fallback_eps)) bad_pivot = true;
+        inv[set] = __drcp_rn(pivot);  // 1.0 / pivot, correctly rounded (IEEE): the same value
+    }
+    if (__any_sync(0xffffffffu, bad_pivot)) return false;
+    __syncwarp();
+    double* factor = inv + nodes;
+    for (int item = lane; item < nodes * new_size; item += kWarp) {
+        const int set = item / new_size;
+        const int row = item - set * new_size;
+        factor[item] = dmul(old_list[set * old_msize + (row + 1) * old_size], inv[set]);
+    }
+    __syncwarp();
+    const int items = nodes * new_msize;
+    for (int item = lane; item < items; item += kWarp) {
+        const int set = item / new_msize;
+        const int e = item - set * new_msize;
+        const int row = e / new_size;
+        const int col = e - row * new_size;
+        const int src = set * old_msize;
+        const double b = old_list[src + (row + 1) * old_size + col + 1];
+        new_list[item] = b;
+        new_list[items + item] = dfma(-old_list[src + 1 + col], factor[set * new_size + row], b);
+    }
+    __syncwarp();
+    const uint32_t gmask = (1u << log2g) - 1u;
+    for (int q = lane; q < 2 * nodes; q += kWarp) {
+        const uint32_t idx = base + c0 + (static_cast<uint32_t>(q) & gmask) +
+                             ((static_cast<uint32_t>(q) >> log2g) << T);
+        shifted[idx] = dadd(p, new_list[q * new_msize]);
+    }
+    __syncwarp();
+    return true;
+}
+
+// The prefix product of mat2pm (fast_principle_minors.h:217-228) on a global
+// array: shifted[step + 1 + t] *= shifted[1 + t], eight elements per lane in
+// flight.
+__device__ __forceinline__ void prefix_product_global(double* shifted, uint32_t subsets, int lane) {
+    for (uint32_t step = 2; step < subsets; step <<= 1) {
+        const uint32_t count = step - 1;
+        for (uint32_t t0 = 0; t0 < count; t0 += 8 * kWarp) {
+            double x[8], y[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t t = t0 + u * kWarp + lane;
+                x[u] = t < count ? shifted[step + 1 + t] : 0.0;
+                y[u] = t < count ? shifted[1 + t] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t t = t0 + u * kWarp + lane;
+                if (t < count) shifted[step + 1 + t] = dmul(x[u], y[u]);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// mat2pm_warp for orders 11..14 with the chunked recursion: the top levels'
+// lists in the global workspace ws, the chunks' in `chunk` (shared memory,
+// chunk_geom(n).doubles()), the shifted minors in global memory.
+__device__ bool mat2pm_chunked(const double* A, int n, double tol, double shift_param, const WsLayout& lay,
+                               double* ws, double* shifted, double* lu_lane, double* chunk, int lane) {
+    const int msize = n * n;
+    const uint32_t subsets = 1u << n;
+    double max_abs = 0.0;
+    for (int k = lane; k < msize; k += kWarp) {
+        const double e = fabs(A[k]);
+        if (e > max_abs) max_abs = e;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_xor_sync(0xffffffffu, max_abs, off);
+        if (o > max_abs) max_abs = o;
+    }
+    const bool explicit_shift = !(shift_param < 0.0);
+    const double p = explicit_shift ? shift_param : ddiv(max_abs, static_cast<double>(msize));
+    if (max_abs == 0.0 && p == 0.0) {
+        for (uint32_t m = lane; m < subsets; m += kWarp) shifted[m] = 0.0;
+        __syncwarp();
+        return false;
+    }
+    const double fallback_eps = (tol > 0.0 && max_abs > 0.0) ? dmul(tol, max_abs) : 0.0;
+    double* old_list = ws + lay.old_list;
+    double* new_list = ws + lay.new_list;
+    double* inv = ws + lay.aux;
+    for (int k = lane; k < msize; k += kWarp) old_list[k] = A[k];
+    // every shifted minor from 2 on is written once by its node below
+    if (lane == 0) {
+        shifted[0] = 1.0;
+        shifted[1] = dadd(p, A[0]);
+    }
+    __syncwarp();
+    const ChunkGeom g = chunk_geom(n);
+    bool ok = true;
+    for (int level = 0; level < g.T && ok; ++level) {
+        ok = schur_level(old_list, new_list, inv, 1 << level, n - level, p, fallback_eps, shifted,
+                         2u << level, 0u, 30, 0, lane);
+        double* t = old_list;
+        old_list = new_list;
+        new_list = t;
+    }
+    // old_list: the 2^T matrices of level T, (n - T)^2 each
+    const int m = n - g.T, msz = m * m, G = 1 << g.log2g;
+    for (uint32_t c0 = 0; ok && c0 < (1u << g.T); c0 += G) {
+        double* co = chunk;
+        double* cn = chunk + g.list;
+        double* caux = chunk + 2 * g.list;
+        for (int k = lane; k < G * msz; k += kWarp) co[k] = old_list[c0 * msz + k];
+        __syncwarp();
+        for (int j = 0; j + 1 < m && ok; ++j) {
+            ok = schur_level(co, cn, caux, G << j, m - j, p, fallback_eps, shifted, 2u << (g.T + j), c0,
+                             g.log2g, g.T, lane);
+            double* t = co;
+            co = cn;
+            cn = t;
+        }
+    }
+    if (!ok) {
+        // determinant_principal_minors_from_buffer (fast_principle_minors.h:107-115)
+        for (uint32_t mk = 1 + lane; mk < subsets; mk += kWarp) shifted[mk] = minor_by_lu(A, n, mk, lu_lane);
+        __syncwarp();
+        return true;
+    }
+    prefix_product_global(shifted, subsets, lane);
+    remove_shift_blocked(shifted, n, p, lane);
+    return false;
+}
+
+// use_smem: 1 = the whole workspace in shared memory; 0 = in the global
+// workspace; 2 = chunked (orders 11..14): lists of the chunks in shared
+// memory, the top levels' lists and the shifted minors in the global workspace.
 __global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_constant__ Problem p,
                                                             const __grid_constant__ Scratch w,
                                                             int use_smem) {
@@ -518,10 +707,16 @@ __global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_consta
     const int64_t total_warps = static_cast<int64_t>(gridDim.x) * warps_per_block;
     const int nmax = p.max_order;
     // the global workspace is laid out for two spins; shared memory for what the sets need
-    const WsLayout lay = ws_layout(nmax, !use_smem || !(p.same_spin[0] && p.same_spin[1]));
-    double* ws = use_smem ? smem + static_cast<size_t>(warp_in_block) * lay.total
-                          : w.ws_global + static_cast<size_t>(global_warp) * lay.total;
+    const WsLayout lay = ws_layout(nmax, use_smem != 1 || !(p.same_spin[0] && p.same_spin[1]));
+    double* ws = use_smem == 1 ? smem + static_cast<size_t>(warp_in_block) * lay.total
+                               : w.ws_global + static_cast<size_t>(global_warp) * lay.total;
     double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
+    double* chunk = use_smem == 2 ? smem + static_cast<size_t>(warp_in_block) * chunk_doubles_upto(nmax) : nullptr;
+    auto minors = [&](const double* A, int n, double* shifted) {
+        return (chunk && n >= kChunkMinOrder && n <= kChunkMaxOrder)
+                   ? mat2pm_chunked(A, n, p.s.tol_fpm, p.s.fpm_shift, lay, ws, shifted, lu_lane, chunk, lane)
+                   : mat2pm_warp(A, n, p.s.tol_fpm, p.s.fpm_shift, lay, ws, shifted, lu_lane, lane);
+    };
     const uint32_t full = 1u << nmax;
     const int64_t items = p.batch * 2;
     for (int64_t item = global_warp; item < items; item += total_warps) {
@@ -534,21 +729,32 @@ __global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_consta
         bool fb = false;
         for (int k = lane; k < n * n; k += kWarp) A[k] = green[k];
         __syncwarp();
-        fb |= mat2pm_warp(A, n, p.s.tol_fpm, p.s.fpm_shift, lay, ws, ws + lay.shifted_up, lu_lane, lane);
+        fb |= minors(A, n, ws + lay.shifted_up);
         const bool one_spin = p.same_spin[set] != 0;
         if (!one_spin) {
             for (int k = lane; k < n * n; k += kWarp) A[k] = green[static_cast<int64_t>(nmax) * nmax + k];
             __syncwarp();
-            fb |= mat2pm_warp(A, n, p.s.tol_fpm, p.s.fpm_shift, lay, ws, ws + lay.shifted_down,
-                              lu_lane, lane);
+            fb |= minors(A, n, ws + lay.shifted_down);
         }
         const double* su = ws + lay.shifted_up;
         const double* sd = one_spin ? su : ws + lay.shifted_down;
         // a[mask] = up[mask-1] * down[mask-1] (integrand_replica_randomly_sampled.h:254-257)
         const int64_t slot = p.sorted ? __ldg(w.slot_of + c) : c;  // lane-interleaved position
         double* a = w.a_int + ((slot >> 5) * 2 + set) * static_cast<int64_t>(full) * kWarp + (slot & 31);
-        for (uint32_t m = lane; m < (1u << n); m += kWarp)
-            a[static_cast<int64_t>(m) * kWarp] = m == 0 ? 0.0 : dmul(su[m], sd[m]);
+        for (uint32_t m0 = 0; m0 < (1u << n); m0 += 8 * kWarp) {  // eight products per lane in flight
+            double x[8], y[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t m = m0 + u * kWarp + lane;
+                x[u] = m < (1u << n) ? su[m] : 0.0;
+                y[u] = m < (1u << n) ? sd[m] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t m = m0 + u * kWarp + lane;
+                if (m < (1u << n)) a[static_cast<int64_t>(m) * kWarp] = m == 0 ? 0.0 : dmul(x[u], y[u]);
+            }
+        }
         if (fb && lane == 0) atomicOr(p.status + c, kStatusFpmFallback);
         __syncwarp();
     }
@@ -1583,20 +1789,29 @@ static cudaError_t post_assembly(const Problem& p_in, const Scratch& w, int sm_c
     const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(double);
     const int fit = minors_warps_in_shared_memory(p.max_order, two_spins);
     const bool use_smem = fit >= 4;
-    const int warps_per_block = use_smem ? fit : 4;
+    // orders 11..14 in the global workspace: the chunked recursion, eight
+    // warps per block, as many blocks per SM as their chunk buffers allow
+    const bool chunked = !use_smem && p.max_order >= kChunkMinOrder && p.max_order <= kChunkMaxOrder;
+    const size_t chunk_bytes = chunked ? chunk_doubles_upto(p.max_order) * sizeof(double) : 0;
+    const int warps_per_block = use_smem ? fit : (chunked ? 8 : 4);
     const int64_t items = p.batch * 2;
     int64_t blocks = (items + warps_per_block - 1) / warps_per_block;
     const int64_t max_blocks = static_cast<int64_t>(w.ws_warps) / warps_per_block;
     blocks = std::min<int64_t>(blocks, std::max<int64_t>(1, max_blocks));
-    if (use_smem) blocks = std::min<int64_t>(blocks, sm_count > 0 ? sm_count : 152);  // one wave
-    const size_t smem = use_smem ? ws_bytes * warps_per_block : 0;
+    const int sms = sm_count > 0 ? sm_count : 152;
+    if (use_smem) blocks = std::min<int64_t>(blocks, sms);  // one wave
+    if (chunked) {
+        const int64_t per_sm = std::max<int64_t>(1, (227 * 1024) / (chunk_bytes * warps_per_block + 1024));
+        blocks = std::min<int64_t>(blocks, per_sm * sms);  // one wave
+    }
+    const size_t smem = use_smem ? ws_bytes * warps_per_block : chunk_bytes * warps_per_block;
     if (smem > 48 * 1024) {
         err = cudaFuncSetAttribute(principal_minors_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem));
         if (err != cudaSuccess) return err;
     }
     principal_minors_fp64<<<static_cast<unsigned>(blocks), warps_per_block * kWarp, smem, stream>>>(
-        p, w, use_smem ? 1 : 0);
+        p, w, use_smem ? 1 : (chunked ? 2 : 0));
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     mark(3);

@@ -156,6 +156,33 @@ def test_oracle_mixed_orders_and_high_orders():
     assert bits_equal(got, want)
 
 
+def test_oracle_high_orders_two_spins_fallback_and_envelope():
+    """Orders 11..14, whose minors run the chunked Schur recursion (top levels
+    in the global workspace, subtrees in shared memory), on tables with
+    distinct up and down spins, with the LU fallback forced (TOL_FPM = 1) and
+    as an all-subsets envelope of 12: bit for bit the oracle's."""
+    import dataclasses
+    params, tables, _ = load_case("physical_2x2")
+    for over in ({}, {"tol_fpm": "1"}):
+        p2 = dataclasses.replace(params, **over)
+        gpu = CdetIntegrand(p2, tables)
+        orc = Oracle(p2.runtime_scalars(), tables)
+        for n, count in ((11, 24), (12, 16), (13, 8), (14, 6)):
+            v = uniform_configurations(300 + n, count, n)
+            orders = np.full(count, n, dtype=np.int32)
+            got, st = gpu.integrand_batch(v, orders)
+            want, wst = orc.integrand_batch(v, orders, threads=THREADS)
+            assert np.array_equal(st, wst) and bits_equal(got, want), (over, n)
+            if over:
+                assert np.all(st & L.CONFIG_FPM_FALLBACK)
+    gpu = CdetIntegrand(params, tables)
+    orc = Oracle(params.runtime_scalars(), tables)
+    v = uniform_configurations(399, 4, 12)
+    got, _ = gpu.all_subsets_batch(v)
+    want, _ = orc.all_subsets_batch(v, threads=THREADS)
+    assert bits_equal(got, want)
+
+
 def test_oracle_8x8_d128_order10():
     """The 8x8 / 4x4-corner / degree-128 configuration at order 10 on a
     512-configuration sample, GPU against the oracle bit for bit."""
