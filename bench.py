@@ -45,12 +45,13 @@ BATCH = 65536
 # packed slot: 24 B read) and its two Green-entry writes (8 B each, a 32-byte
 # DRAM sector each: 64 B). SPLIT_TRAFFIC_RATIO is measured / model from one
 # ncu capture of the small 6x6 / degree-96 case (dram__bytes_read.sum +
-# dram__bytes_write.sum = 4.658 GB against a model of 3.701 GB,
+# dram__bytes_write.sum = 3.009 GB against a model of 3.701 GB; below 1
+# because the kernel skips the zero digit slices before each K step's lead,
 # profiles/split_assembly_traffic_6x6_d96_n10.md); the bench's traffic is
 # that ratio times the model of its own workload.
-SPLIT_TRAFFIC_RATIO = 4.658041856e9 / 3.70147328e9
+SPLIT_TRAFFIC_RATIO = 3.009076224e9 / 3.70147328e9
 SPLIT_TRAFFIC_RULE = ("model (distinct coefficient blocks x slice bytes + 88 B per lookup) x the measured/model "
-                      "ratio 1.258 of the 6x6-d96 ncu capture")
+                      "ratio 0.813 of the 6x6-d96 ncu capture")
 ORDER = 10
 L2_FLUSH_BYTES = 512 << 20
 PRESET = "8x8-d128"
