@@ -12,8 +12,8 @@ LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libcdet_gb300.so")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 
-SOURCES = ["cdet_kernels.cu", "cdet_split.cu", "cdet_capi.cu", "cdet_noalloc.cu", "cdet_diagonal.cu",
-           "cdet_mcmcmc.cu", "cdet_mcmcmc_host.cu"]
+SOURCES = ["cdet_kernels.cu", "cdet_dd.cu", "cdet_split.cu", "cdet_capi.cu", "cdet_noalloc.cu",
+           "cdet_diagonal.cu", "cdet_mcmcmc.cu", "cdet_mcmcmc_host.cu"]
 HEADERS = ["cdet_device.cuh", "cdet_kernels.cuh", "cdet_capi_internal.h"]
 
 NVCC_FLAGS = [

@@ -225,6 +225,22 @@ class CdetIntegrand:
             return {"form": form}
         return {"form": form, "warps_per_sm": out[1].value, "pair": bool(out[2].value), "grab": out[3].value}
 
+    def set_integrand_real(self, real: str, significand_bits: int = 0) -> None:
+        """INTEGRAND_REAL: "double" (the FP64 drop-in, default) or
+        "double_double" (with VECTOR_REAL=double: the FP64 Green matrices,
+        then minors, CDet and the order-1 branch in the reference's
+        DoubleDouble arithmetic). significand_bits = 113 takes the parameters'
+        DoubleDouble values as a quad-precision MP_Real gives them."""
+        from .params import dd_scalars
+        if real == "double":
+            L.check(self._lib.cdet_set_integrand_real(self._ctx, L.INTEGRAND_REAL_DOUBLE, None))
+            return
+        if real != "double_double":
+            raise ValueError("INTEGRAND_REAL must be double or double_double")
+        values = dd_scalars(self.params, significand_bits)
+        scalars = L.DDScalars(**{k: L.DD(*v) for k, v in values.items()})
+        L.check(self._lib.cdet_set_integrand_real(self._ctx, L.INTEGRAND_REAL_DOUBLE_DOUBLE, C.byref(scalars)))
+
     def set_assembly(self, mode: str) -> None:
         """"fp64": the reference's Clenshaw in FP64, bit-identical (default);
         "split": batched split-bf16 tcgen05 assembly, FP64-level accuracy."""

@@ -36,7 +36,7 @@ EXPORTED = (
     "cdet_mcmcmc_summary", "cdet_mcmcmc_estimates", "cdet_write_mcmcmc_checkpoint", "cdet_read_mcmcmc_checkpoint",
     "cdet_mcmcmc_save_checkpoints", "cdet_mcmcmc_load_checkpoints", "cdet_mcmcmc_launch_count", "cdet_set_all_subsets_form", "cdet_all_subsets_form_tuned", "cdet_load_chunks",
     "cdet_split_counters", "cdet_set_integrand_form", "cdet_integrand_form_tuned",
-    "cdet_mcmcmc_set_green_reuse",
+    "cdet_mcmcmc_set_green_reuse", "cdet_set_integrand_real",
 )
 
 ASSEMBLY_FP64 = 0
@@ -86,6 +86,20 @@ class Checkpoint(C.Structure):
                 ("rng_state", C.c_uint64 * 313), ("lambdas", C.c_double * (MAX_ENVELOPE + 1)),
                 ("warmup_block_counts", C.c_uint64 * (MAX_ENVELOPE + 1)),
                 ("vertices", (C.c_double * 4) * MAX_ENVELOPE), ("result", ChainResult)]
+
+
+class DD(C.Structure):
+    _fields_ = [("hi", C.c_double), ("lo", C.c_double)]
+
+
+class DDScalars(C.Structure):
+    """cdet_dd_scalars: the DoubleDouble parameters of the double-double integrand."""
+    _fields_ = [(name, DD) for name in ("beta", "u", "alpha_up", "alpha_down", "tol_fpm", "fpm_shift",
+                                        "z_eps0", "z_safety")]
+
+
+INTEGRAND_REAL_DOUBLE = 0
+INTEGRAND_REAL_DOUBLE_DOUBLE = 1
 
 
 class RunInfo(C.Structure):
@@ -155,6 +169,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cdet_all_subsets_form_tuned.argtypes = [vp, i32, i32, i64, C.POINTER(C.c_int)]
     lib.cdet_set_integrand_form.argtypes = [vp, i32, i32, i32, i32]
     lib.cdet_mcmcmc_set_green_reuse.argtypes = [vp, i32]
+    lib.cdet_set_integrand_real.argtypes = [vp, i32, C.POINTER(DDScalars)]
     lib.cdet_integrand_form_tuned.argtypes = [vp, i32, i32, i64] + [C.POINTER(C.c_int)] * 4
     lib.cdet_mcmcmc_launch_count.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.cdet_mcmcmc_learn_histogram.argtypes = [vp, C.POINTER(McmcmcConfig), C.POINTER(HistogramConfig), C.c_uint64,

@@ -90,6 +90,51 @@ class CdetParams:
         }
 
 
+def dd_of_literal(literal, significand_bits: int = 0) -> Tuple[float, float]:
+    """DoubleDouble(MP_Real(literal)) (utility/types.h:41-45): the nearest
+    double to the value, then the nearest double to the rest. The reference's
+    MP_Real holds 100 decimal digits, so the value is the literal itself
+    (significand_bits = 0); significand_bits = 113 first rounds it to IEEE
+    binary128, as a build whose MP_Real is quad precision does."""
+    from fractions import Fraction
+    x = Fraction(_dec(literal))
+    if significand_bits and x != 0:
+        sign = -1 if x < 0 else 1
+        a = abs(x)
+        e = a.numerator.bit_length() - a.denominator.bit_length()  # 2^e <= a < 2^(e+2)
+        if Fraction(2) ** e > a:
+            e -= 1
+        scale = Fraction(2) ** (significand_bits - 1 - e)
+        n = a * scale
+        q, r = divmod(n.numerator, n.denominator)
+        twice = 2 * r
+        if twice > n.denominator or (twice == n.denominator and q % 2 == 1):
+            q += 1
+        x = sign * Fraction(q) / scale
+    hi = float(x)
+    lo = float(x - Fraction(hi))
+    return hi, lo
+
+
+def dd_scalars(params: "CdetParams", significand_bits: int = 0) -> dict:
+    """The DoubleDouble values the reference's INTEGRAND_REAL=double_double
+    mode reads (cdet_dd_scalars): beta, U, the alphas, TOL_FPM,
+    FPM_GLOBAL_SHIFT (-1 when auto), ZTRANSFORM_EPSILON0 (1e-31 when auto,
+    precision_config.h:173-186) and ZTRANSFORM_SAFETY_FACTOR."""
+    def lit(v: str, auto: str) -> str:
+        return auto if v.strip().lower() == "auto" else v
+    return {
+        "beta": dd_of_literal(params.beta, significand_bits),
+        "u": dd_of_literal(params.u, significand_bits),
+        "alpha_up": dd_of_literal(params.alpha_up, significand_bits),
+        "alpha_down": dd_of_literal(params.alpha_down, significand_bits),
+        "tol_fpm": dd_of_literal(params.tol_fpm, significand_bits),
+        "fpm_shift": dd_of_literal(lit(params.fpm_global_shift, "-1"), significand_bits),
+        "z_eps0": dd_of_literal(lit(params.z_epsilon0, "1e-31"), significand_bits),
+        "z_safety": dd_of_literal(params.z_safety, significand_bits),
+    }
+
+
 def site_index(x: int, y: int, n1: int) -> int:
     return y * n1 + x
 

@@ -225,6 +225,15 @@ int build_problem(cdet_context* ctx, const double* vertices, const int32_t* orde
     p->reuse_green = nullptr;
     p->reuse_diag = nullptr;
     p->reuse_mask = nullptr;
+    p->dd_mode = ctx->integrand_real == CDET_INTEGRAND_REAL_DOUBLE_DOUBLE ? 1 : 0;
+    p->raw_diag = p->dd_mode;
+    p->dd_shift[0] = ctx->dd_shift[0];
+    p->dd_shift[1] = ctx->dd_shift[1];
+    p->dd_threshold = ctx->dd_threshold;
+    p->dd_u = ctx->dd_u;
+    p->dd_beta = ctx->dd_beta;
+    p->dd_tol = ctx->dd_tol;
+    p->dd_fpm_shift = ctx->dd_fpm_shift;
     for (int set = 0; set < 2; ++set) {
         const int r = set == 0 ? 2 : 1;
         for (int n = 0; n <= cdet::kMaxOrder; ++n) {
@@ -426,6 +435,9 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
     if (batch == 0) return CDET_OK;
     if (!vertices || !values || !status || (!all_subsets && !orders))
         return fail(CDET_ERR_INVALID, "null buffer");
+    if (ctx->integrand_real == CDET_INTEGRAND_REAL_DOUBLE_DOUBLE && !assembly_only &&
+        (all_subsets || max_order > cdet::kDDMaxOrder))
+        return fail(CDET_ERR_INVALID, "double-double integrand: single-configuration integrands of order <= 10 only");
     int rc = ensure_scratch(ctx, batch, max_order);
     if (rc != CDET_OK) return rc;
     cdet::Problem p;
@@ -484,7 +496,7 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
     // (order, fused, batch size class) outside a capture (staged until then).
     bool tune_post = false;
     std::tuple<int, int, int> post_key;
-    if (!p.all_subsets && !assembly_only && max_order <= cdet::kQueueMaxOrder) {
+    if (!p.all_subsets && !assembly_only && !p.dd_mode && max_order <= cdet::kQueueMaxOrder) {
         if (ctx->integrand_form != CDET_INTEGRAND_AUTO) {
             p.integrand_form = ctx->integrand_form;
             p.queue = ctx->queue_shape;
@@ -513,7 +525,7 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         p.queue = best.second;
         return CDET_OK;
     };
-    if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16) {
+    if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16 && !p.dd_mode) {
         cdet::SplitPlan plan;
         rc = build_split_plan(ctx, &plan);
         if (rc != CDET_OK) return rc;
@@ -555,7 +567,8 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
             err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events);
         }
         if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
-        launches = cdet::uses_queue_form(p) ? 2 : 3;  // assembly + minors, CDet (or the queue kernel)
+        // assembly + minors, CDet (or the queue kernel, or the double-double kernel)
+        launches = (cdet::uses_queue_form(p) || p.dd_mode) ? 2 : 3;
         if (p.reuse_mask && p.all_subsets) launches += 2;  // the reuse scan and the copies
     } else {
         launches = 1;
@@ -650,6 +663,8 @@ int run_fp64_on_scratch(cdet_context* ctx, const double* vertices, const int32_t
     int rc = build_problem(ctx, vertices, orders, batch, max_order, 0, values, status, &p);
     if (rc != CDET_OK) return rc;
     p.fused_cdet = 0;  // the FP64 form throughout, whatever assembly the context selects
+    p.dd_mode = 0;     // and the FP64 integrand, whatever INTEGRAND_REAL the context selects
+    p.raw_diag = 0;
     Scratch w;
     carve_scratch(scratch, batch, max_order, ws_warps, &w, regions);
     cudaError_t err = cudaMemsetAsync(status, 0, static_cast<size_t>(batch) * sizeof(int32_t), stream);
@@ -885,6 +900,31 @@ int cdet_integrand_form_tuned(const cdet_context* ctx, int max_order, int fused,
     *warps_per_sm = q.warps_per_sm;
     *pair = q.pair;
     *grab = q.grab;
+    return CDET_OK;
+}
+
+int cdet_set_integrand_real(cdet_context* ctx, int real_type, const cdet_dd_scalars* dd) {
+    if (!ctx) return fail(CDET_ERR_INVALID, "null context");
+    if (real_type == CDET_INTEGRAND_REAL_DOUBLE) {
+        ctx->integrand_real = real_type;
+        return CDET_OK;
+    }
+    if (real_type != CDET_INTEGRAND_REAL_DOUBLE_DOUBLE) return fail(CDET_ERR_INVALID, "unknown INTEGRAND_REAL");
+    if (!dd) return fail(CDET_ERR_INVALID, "double-double integrand: null scalars");
+    auto h = [](cdet_dd x) { return HostDD{x.hi, x.lo}; };
+    auto d = [](HostDD x) { return cdet::DDPair{x.hi, x.lo}; };
+    if (dd->u.hi == 0.0 && dd->u.lo == 0.0) return fail(CDET_ERR_INVALID, "U must be non-zero");
+    // make_integrand_runtime_scalars<DoubleDouble> (integrand_replica_randomly_sampled.h:98-119):
+    // diagonal_up_shift = alpha_down / U, diagonal_down_shift = alpha_up / U
+    ctx->dd_shift[0] = d(h_div(h(dd->alpha_down), h(dd->u)));
+    ctx->dd_shift[1] = d(h_div(h(dd->alpha_up), h(dd->u)));
+    // compute_dp_ztransform's roundoff_threshold = epsilon0 * safety_factor (:251)
+    ctx->dd_threshold = d(h_mul(h(dd->z_eps0), h(dd->z_safety)));
+    ctx->dd_u = d(h(dd->u));
+    ctx->dd_beta = d(h(dd->beta));
+    ctx->dd_tol = d(h(dd->tol_fpm));
+    ctx->dd_fpm_shift = d(h(dd->fpm_shift));
+    ctx->integrand_real = real_type;
     return CDET_OK;
 }
 

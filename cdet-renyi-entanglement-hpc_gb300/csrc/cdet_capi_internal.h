@@ -63,6 +63,9 @@ struct cdet_context {
     int integrand_form = CDET_INTEGRAND_AUTO;
     cdet::QueueShape queue_shape{};
     std::map<std::tuple<int, int, int>, std::pair<int, cdet::QueueShape>> integrand_tuned;
+    // INTEGRAND_REAL (CDET_INTEGRAND_REAL_*) and the double-double mode's scalars
+    int integrand_real = CDET_INTEGRAND_REAL_DOUBLE;
+    cdet::DDPair dd_shift[2]{}, dd_threshold{}, dd_u{}, dd_beta{}, dd_tol{}, dd_fpm_shift{};
     std::map<std::pair<const double*, size_t>, capi::SlicedBranch> sliced;  // (coeffs, blocks) -> slices
     void* split_scratch = nullptr;
     size_t split_scratch_bytes = 0;

@@ -134,10 +134,12 @@ __device__ __forceinline__ void assemble_entry(const Problem& p, const Scratch& 
     // fill_pair_range (integrand_replica_randomly_sampled.h:467-473).
     const int64_t mslot = (c * 2 + set) * 2;
     if (i == j) {
+        const double up_raw = up, down_raw = down;
         up = dadd(up, s.diag_up_shift);
         down = dadd(down, s.diag_down_shift);
-        w.diag[mslot * nmax + i] = up;
-        w.diag[(mslot + 1) * nmax + i] = down;
+        // the double-double order-1 branch adds its own shifts to the unshifted value
+        w.diag[mslot * nmax + i] = p.raw_diag ? up_raw : up;
+        w.diag[(mslot + 1) * nmax + i] = p.raw_diag ? down_raw : down;
     }
     w.green[mslot * per_set + i * n + j] = dmul(up, s.scale);
     w.green[(mslot + 1) * per_set + i * n + j] = dmul(down, s.scale);
@@ -261,34 +263,6 @@ __global__ void __launch_bounds__(128) green_assembly_fp64_fresh(const __grid_co
 }
 
 // ------------------------------------------------- 2. principal minors ----
-struct WsLayout {
-    int list;      // doubles per Schur-complement list
-    size_t a, old_list, new_list, aux, shifted_up, shifted_down, total;
-};
-
-// two_spins = false when both sets evaluate one spin only (up and down tables
-// and shifts identical): the spin-down minors then need no space.
-__host__ __device__ inline WsLayout ws_layout(int nmax, bool two_spins = true) {
-    WsLayout l;
-    size_t list = static_cast<size_t>(nmax) * nmax;
-    for (int level = 0; level < nmax - 1; ++level) {
-        const size_t ns = static_cast<size_t>(nmax - level - 1);
-        const size_t cand = (static_cast<size_t>(1) << (level + 1)) * ns * ns;
-        if (cand > list) list = cand;
-    }
-    l.list = static_cast<int>(list);
-    const size_t subsets = static_cast<size_t>(1) << nmax;
-    auto even = [](size_t x) { return (x + 1) & ~static_cast<size_t>(1); };
-    l.a = 0;
-    l.old_list = even(static_cast<size_t>(nmax) * nmax);
-    l.new_list = l.old_list + even(list);
-    l.aux = l.new_list + even(list);
-    l.shifted_up = l.aux + even(subsets / 2 + 2);
-    l.shifted_down = l.shifted_up + subsets;
-    l.total = two_spins ? l.shifted_down + subsets : l.shifted_down;
-    return l;
-}
-
 // Partial-pivot LU minor of the principal submatrix selected by mask
 // (determinant_principal_minor_from_buffer, fast_principle_minors.h:39-105);
 // m is this lane's n*n scratch.
@@ -1489,8 +1463,6 @@ __global__ void __launch_bounds__(kBlockCdetThreads) cdet_block(const __grid_con
 // reference's descending submask sums), so the values are the staged form's
 // bit for bit.
 
-constexpr uint32_t kQueueHeadIndex = 48;  // the queue head's uint32 slot in Scratch::order_count
-
 // compute_dp_ztransform (integrand_replica_randomly_sampled.h:226-290) on one
 // warp, for order n >= 2: a[mask] for every mask, dp of the odd masks into
 // dp_s[mask >> 1]. The masks of a popcount level are dealt to the lanes by
@@ -1765,6 +1737,14 @@ static cudaError_t post_assembly(const Problem& p_in, const Scratch& w, int sm_c
         if (err != cudaSuccess) return err;
     }
 
+    if (p.dd_mode) {
+        err = launch_integrand_dd(p, w, sm_count, stream);
+        if (err != cudaSuccess) return err;
+        mark(3);
+        mark(4);
+        return cudaSuccess;
+    }
+
     if (uses_queue_form(p)) {
         int wpb = 0, blocks = 0;
         size_t smem = 0;
@@ -1868,14 +1848,15 @@ static cudaError_t post_assembly(const Problem& p_in, const Scratch& w, int sm_c
 
 
 bool uses_queue_form(const Problem& p) {
-    return p.integrand_form == kIntegrandQueue && !p.all_subsets && p.max_order >= 1 &&
+    return !p.dd_mode && p.integrand_form == kIntegrandQueue && !p.all_subsets && p.max_order >= 1 &&
            p.max_order <= kQueueMaxOrder;
 }
 
 bool sorts_orders(const Problem& p) {
     // the lane CDet of a single-order batch (the split path's warp CDet and the
     // all-subsets forms have no lanes of different orders), and the queue form
-    return !p.all_subsets && (uses_queue_form(p) || !(p.fused_cdet && p.max_order <= kWarpCdetMaxOrder));
+    return !p.all_subsets &&
+           (p.dd_mode || uses_queue_form(p) || !(p.fused_cdet && p.max_order <= kWarpCdetMaxOrder));
 }
 
 void queue_launch_shape(const Problem& p, const Scratch& w, int sm_count, int* warps_per_block, int* blocks,

@@ -51,6 +51,39 @@ struct Scratch {
     uint32_t* order_count;  // [64] counting-sort buckets
 };
 
+// Per-warp workspace of the minors recursion (mat2pm), in elements of the
+// arithmetic type: the matrix, two Schur-complement lists, the pivots'
+// inverses and factors, and the shifted minors of each spin.
+struct WsLayout {
+    int list;      // elements per Schur-complement list
+    size_t a, old_list, new_list, aux, shifted_up, shifted_down, total;
+};
+
+// two_spins = false when both sets evaluate one spin only (up and down tables
+// and shifts identical): the spin-down minors then need no space.
+__host__ __device__ inline WsLayout ws_layout(int nmax, bool two_spins = true) {
+    WsLayout l;
+    size_t list = static_cast<size_t>(nmax) * nmax;
+    for (int level = 0; level < nmax - 1; ++level) {
+        const size_t ns = static_cast<size_t>(nmax - level - 1);
+        const size_t cand = (static_cast<size_t>(1) << (level + 1)) * ns * ns;
+        if (cand > list) list = cand;
+    }
+    l.list = static_cast<int>(list);
+    const size_t subsets = static_cast<size_t>(1) << nmax;
+    auto even = [](size_t x) { return (x + 1) & ~static_cast<size_t>(1); };
+    l.a = 0;
+    l.old_list = even(static_cast<size_t>(nmax) * nmax);
+    l.new_list = l.old_list + even(list);
+    l.aux = l.new_list + even(list);
+    l.shifted_up = l.aux + even(subsets / 2 + 2);
+    l.shifted_down = l.shifted_up + subsets;
+    l.total = two_spins ? l.shifted_down + subsets : l.shifted_down;
+    return l;
+}
+
+constexpr uint32_t kQueueHeadIndex = 48;  // the queue head's uint32 slot in Scratch::order_count
+
 // all-subsets CDet work layouts, the values of the C ABI's CDET_FORM_*
 constexpr int kFormAuto = 0, kFormLane = 1, kFormWarp = 2;
 constexpr int kAllWarpMaxOrder = 11;  // the warp form holds a and dp of one set in shared memory
@@ -93,6 +126,16 @@ struct Problem {
     const double* reuse_green;
     const double* reuse_diag;
     const uint64_t* reuse_mask;
+    // INTEGRAND_REAL=double_double with VECTOR_REAL=double
+    // (cdet_integrand_evaluator.h:431-465): the Green matrices as in the FP64
+    // form, then minors, CDet and the order-1 branch in the reference's
+    // DoubleDouble arithmetic (integrand_replica_randomly_sampled.h:486-546)
+    int dd_mode;
+    int raw_diag;             // the assembly stores the unshifted diagonal Green values in diag
+    DDPair dd_shift[2];       // IntegrandRuntimeScalars<DoubleDouble> diagonal_up_shift, diagonal_down_shift
+    DDPair dd_threshold;      // ZTRANSFORM_EPSILON0 * ZTRANSFORM_SAFETY_FACTOR in DoubleDouble
+    DDPair dd_u, dd_beta;     // DoubleDouble(U), DoubleDouble(beta)
+    DDPair dd_tol, dd_fpm_shift;  // DoubleDouble(TOL_FPM), DoubleDouble(FPM_GLOBAL_SHIFT)
     DDPair pref_dd[2][kMaxOrder + 1];   // cdet_order_prefactor<DoubleDouble>, [set][order]
     double pref_ld[2][kMaxOrder + 1];   // cdet_order_prefactor<double> (host long double)
     double* values;
@@ -271,6 +314,11 @@ cudaError_t launch_fp64_integrand(const Problem& p, const Scratch& scratch, int 
 bool sorts_orders(const Problem& p);
 // Whether the batch runs the queue form (p.integrand_form and the orders it supports).
 bool uses_queue_form(const Problem& p);
+// The double-double integrand after the FP64 assembly (orders <= kDDMaxOrder,
+// single-top batches): one persistent kernel over the order-sorted slots
+// (the sort already launched), its workspace in shared memory.
+constexpr int kDDMaxOrder = 10;
+cudaError_t launch_integrand_dd(const Problem& p, const Scratch& scratch, int sm_count, cudaStream_t stream);
 // The post-assembly stages alone (sort, minors, CDet, or the queue kernel),
 // on Green matrices already in scratch: what the autotuner times.
 cudaError_t launch_post_assembly(const Problem& p, const Scratch& scratch, int sm_count, cudaStream_t stream);

@@ -453,6 +453,41 @@ int cdet_set_integrand_form(cdet_context* ctx, int form, int warps_per_sm, int p
 int cdet_integrand_form_tuned(const cdet_context* ctx, int max_order, int fused, int64_t batch, int* form,
                               int* warps_per_sm, int* pair, int* grab);
 
+/* The DoubleDouble value of one of the reference's MP_Real parameters,
+ * DoubleDouble(MP_Real(literal)) = {the nearest double, the nearest double to
+ * the rest} (utility/types.h:41-45). */
+typedef struct cdet_dd {
+    double hi, lo;
+} cdet_dd;
+
+/* What the DoubleDouble integrand reads besides the FP64 scalars:
+ * IntegrandRuntimeScalars<DoubleDouble> as make_integrand_runtime_scalars
+ * builds it from the MP_Real parameters (integrand_replica_randomly_sampled.h:
+ * 98-119: the diagonal shifts are alpha / U in DoubleDouble) and the round-off
+ * filter constants in DoubleDouble (precision_config.h:158-186). */
+typedef struct cdet_dd_scalars {
+    cdet_dd beta, u;                /* beta, U */
+    cdet_dd alpha_up, alpha_down;   /* ALPHA_UP, ALPHA_DOWN */
+    cdet_dd tol_fpm, fpm_shift;     /* TOL_FPM, FPM_GLOBAL_SHIFT (-1 when auto) */
+    cdet_dd z_eps0, z_safety;       /* ZTRANSFORM_EPSILON0 (1e-31 when auto), ZTRANSFORM_SAFETY_FACTOR */
+} cdet_dd_scalars;
+
+enum cdet_integrand_real {
+    CDET_INTEGRAND_REAL_DOUBLE = 0,        /* INTEGRAND_REAL=double (default): the FP64 drop-in */
+    CDET_INTEGRAND_REAL_DOUBLE_DOUBLE = 1  /* INTEGRAND_REAL=double_double with VECTOR_REAL=double */
+};
+
+/* The reference's INTEGRAND_REAL switch (precision_config.h:15-26,
+ * cdet_integrand_evaluator.h:431-465) with VECTOR_REAL=double. In the
+ * double-double mode the Green matrices are the FP64 form's (the FP64
+ * Clenshaw assembly, whatever cdet_set_assembly selected) and the minors, the
+ * CDet recursion and the order-1 branch run in the reference's DoubleDouble
+ * arithmetic, so cdet_integrand_device / _host return the reference's
+ * double-double values bit for bit (dd may be null for
+ * CDET_INTEGRAND_REAL_DOUBLE). Single-configuration integrands of order <= 10
+ * only: an all-subsets call or a higher order fails with CDET_ERR_INVALID. */
+int cdet_set_integrand_real(cdet_context* ctx, int real_type, const cdet_dd_scalars* dd);
+
 /* Builds the bf16 slices of every uploaded table for the split assembly
  * (otherwise done by the first split evaluation). Allocates about twice the
  * FP64 table size of device memory. */
