@@ -182,8 +182,10 @@ def precision_by_order(params, tables, host, integrand, device, threads, per_ord
     configurations of the same lattice, tables and vertex distribution),
     against the oracle's long double truth (the checker, not a measured path),
     with the round-off filter on (the reference's default) and off, in the
-    three error forms of oracle/precision.py. The contract the line states:
-    condition-scaled error <= 1e-10 at every order."""
+    three error forms of oracle/precision.py; and the double-double form
+    (INTEGRAND_REAL=double_double, the reference's own high-precision mode)
+    with its default filter. The contract the line states: condition-scaled
+    error <= 1e-10 at every order."""
     import torch
     from cdet_gb300.integrand import CdetIntegrand
     from cdet_gb300.synthetic import uniform_configurations
@@ -219,6 +221,13 @@ def precision_by_order(params, tables, host, integrand, device, threads, per_ord
                 ctx.integrand_device(dv, do, vals, status)
                 torch.cuda.synchronize(dev)
                 got[(filt, path)] = (vals.cpu().numpy().copy(), status.cpu().numpy().copy())
+        integrand.set_integrand_real("double_double")
+        for path, key in (("fp64", "dd"), ("split", "dd_split")):  # the reference's mode; on split Green matrices
+            integrand.set_assembly(path)
+            integrand.integrand_device(dv, do, vals, status)
+            torch.cuda.synchronize(dev)
+            got[("filter_on", key)] = (vals.cpu().numpy().copy(), status.cpu().numpy().copy())
+        integrand.set_integrand_real("double")
         ok = st == 0
         for key in got:
             ok &= got[key][1] == 0
@@ -227,6 +236,8 @@ def precision_by_order(params, tables, host, integrand, device, threads, per_ord
             for path in ("split", "fp64"):
                 entry[f"{path}_vs_truth_{filt}"] = error_forms(got[(filt, path)][0], truth, parts, ok)
                 worst = max(worst, entry[f"{path}_vs_truth_{filt}"]["condition_scaled"]["max"])
+        entry["dd_vs_truth_filter_on"] = error_forms(got[("filter_on", "dd")][0], truth, parts, ok)
+        entry["dd_split_vs_truth_filter_on"] = error_forms(got[("filter_on", "dd_split")][0], truth, parts, ok)
         entry["split_vs_fp64_filter_on"] = error_forms(got[("filter_on", "split")][0],
                                                        got[("filter_on", "fp64")][0], parts, ok)
         entry["configs"] = int(ok.sum())
@@ -236,6 +247,48 @@ def precision_by_order(params, tables, host, integrand, device, threads, per_ord
     out["worst_condition_scaled"] = worst
     out["contract_met"] = bool(worst <= 1e-10)
     out["seconds"] = time.perf_counter() - t0
+    return out
+
+
+def time_dd_forms(integrand, d_vertices, d_orders, stream, args, flush):
+    """The double-double integrand (the reference's INTEGRAND_REAL=double_double
+    mode) on the same batches: with the FP64 assembly (the reference's mode, bit
+    for bit; its Clenshaw sums make a step long, so 8,192 configurations of the
+    batch) and on the split assembly's Green matrices (the whole batch); CUDA
+    events around `steps` evaluations after one warm-up each."""
+    import torch
+    out = {}
+    for assembly, count in (("split", BATCH), ("fp64", min(BATCH, 8192))):
+        integrand.set_assembly(assembly)
+        integrand.set_integrand_real("double_double")
+        v = [d_vertices[k][:count].contiguous() for k in range(args.steps)]
+        o = d_orders[:count].contiguous()
+        vals = torch.empty(count, dtype=torch.float64, device=o.device)
+        st = torch.empty(count, dtype=torch.int32, device=o.device)
+        integrand.integrand_device(v[0], o, vals, st, stream)
+        torch.cuda.synchronize(o.device)
+        integrand.profile(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            flush.zero_()
+            integrand.integrand_device(v[k], o, vals, st, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(o.device)
+        stage_ms, _ = integrand.profile_read()
+        integrand.profile(False)
+        integrand.set_integrand_real("double")
+        ms = e0.elapsed_time(e1) / args.steps
+        out[f"{assembly}_assembly"] = {
+            "value": count / (ms / 1e3), "unit": UNIT, "configs_per_step": count, "ms_per_step": ms,
+            "stages_ms_per_step": {"assembly": (stage_ms[0] + stage_ms[1]) / args.steps,
+                                   "minors_and_cdet_dd": (stage_ms[2] + stage_ms[3]) / args.steps},
+            "flagged_configs": int((st.cpu().numpy() & 5).astype(bool).sum())}
+    integrand.set_assembly("split")
+    out["note"] = ("fp64_assembly is the reference's INTEGRAND_REAL=double_double mode with VECTOR_REAL=double, "
+                   "bit-identical to it; split_assembly runs the same double-double recursion on the tensor-core "
+                   "Green matrices; their errors per order are in precision_by_order (dd_vs_truth_filter_on "
+                   "is the reference mode's)")
     return out
 
 
@@ -480,6 +533,8 @@ def run_gpu(args):
         torch.cuda.synchronize(dev)
         scale = g64.abs().amax(dim=3, keepdim=True).clamp_min(1e-300)
         line["green_split_vs_fp64_max_rel"] = float(((gsp - g64).abs() / scale).max().item())
+    if rank == 0 and head == "split" and not args.no_dd:
+        line["dd_path"] = time_dd_forms(integrand, d_vertices, d_orders, stream, args, flush)
 
     if rank == 0 and not args.no_cpu_baseline:
         host = {k: {kk: vv.cpu().numpy() for kk, vv in t.items()} for k, t in tables.items()}
@@ -859,6 +914,7 @@ def main():
                     help="configurations in the CPU-baseline sample (default 64 per thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-order precision study")
+    ap.add_argument("--no-dd", action="store_true", help="skip timing the double-double integrand")
     ap.add_argument("--precision-configs", type=int, default=512,
                     help="configurations per order in the precision study")
     ap.add_argument("--preset", choices=["8x8-d128", "6x6-d96"], default="8x8-d128",

@@ -525,7 +525,7 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
         p.queue = best.second;
         return CDET_OK;
     };
-    if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16 && !p.dd_mode) {
+    if (ctx->assembly == CDET_ASSEMBLY_SPLIT_BF16) {
         cdet::SplitPlan plan;
         rc = build_split_plan(ctx, &plan);
         if (rc != CDET_OK) return rc;
@@ -550,8 +550,9 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
             if (rc != CDET_OK) return rc;
             err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events, false);
             if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
-            // descriptors, scan, scatter, tiles, tensor assembly + minors, CDet (or the queue kernel)
-            launches = 5 + (cdet::uses_queue_form(p) ? 1 : 2);
+            // descriptors, scan, scatter, tiles, tensor assembly + minors, CDet (or the queue
+            // kernel, or the double-double kernel)
+            launches = 5 + ((cdet::uses_queue_form(p) || p.dd_mode) ? 1 : 2);
         } else {
             launches = 5;
         }

@@ -475,10 +475,11 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
             double down = p.same_spin[set] ? up
                                            : __ldg((upper ? td.upper_corners : td.lower_corners) + sitepair);
             if (i == j) {
+                const double up_raw = up, down_raw = down;
                 up = dadd(up, s.diag_up_shift);
                 down = dadd(down, s.diag_down_shift);
-                w.diag[mslot * nmax + i] = up;
-                w.diag[(mslot + 1) * nmax + i] = down;
+                w.diag[mslot * nmax + i] = p.raw_diag ? up_raw : up;
+                w.diag[(mslot + 1) * nmax + i] = p.raw_diag ? down_raw : down;
             }
             w.green[mslot * per_c + i * n + j] = dmul(up, s.scale);
             w.green[(mslot + 1) * per_c + i * n + j] = dmul(down, s.scale);
@@ -780,7 +781,7 @@ __device__ __forceinline__ void store_green(const Problem& p, const Scratch& w, 
         double g = value;
         if (i == jj) {
             g = dadd(g, spin == 0 ? p.s.diag_up_shift : p.s.diag_down_shift);
-            w.diag[(mslot + spin) * nmax + i] = g;
+            w.diag[(mslot + spin) * nmax + i] = p.raw_diag ? value : g;  // unshifted for the double-double order 1
         }
         w.green[(mslot + spin) * per_c + i * n + jj] = dmul(g, p.s.scale);
     }

@@ -478,14 +478,17 @@ enum cdet_integrand_real {
 };
 
 /* The reference's INTEGRAND_REAL switch (precision_config.h:15-26,
- * cdet_integrand_evaluator.h:431-465) with VECTOR_REAL=double. In the
- * double-double mode the Green matrices are the FP64 form's (the FP64
- * Clenshaw assembly, whatever cdet_set_assembly selected) and the minors, the
- * CDet recursion and the order-1 branch run in the reference's DoubleDouble
- * arithmetic, so cdet_integrand_device / _host return the reference's
- * double-double values bit for bit (dd may be null for
- * CDET_INTEGRAND_REAL_DOUBLE). Single-configuration integrands of order <= 10
- * only: an all-subsets call or a higher order fails with CDET_ERR_INVALID. */
+ * cdet_integrand_evaluator.h:431-465). In the double-double mode the minors,
+ * the CDet recursion and the order-1 branch run in the reference's
+ * DoubleDouble arithmetic on the Green matrices of the context's assembly:
+ * with CDET_ASSEMBLY_FP64 (VECTOR_REAL=double) cdet_integrand_device / _host
+ * return the reference's double-double values bit for bit; with
+ * CDET_ASSEMBLY_SPLIT_BF16 the same arithmetic runs on the tensor-core
+ * Green matrices (no counterpart in the reference: its values differ from
+ * the reference mode's by what the Green entries' last bits move, not by the
+ * FP64 recursion's round-off). dd may be null for CDET_INTEGRAND_REAL_DOUBLE.
+ * Single-configuration integrands of order <= 10 only: an all-subsets call or
+ * a higher order fails with CDET_ERR_INVALID. */
 int cdet_set_integrand_real(cdet_context* ctx, int real_type, const cdet_dd_scalars* dd);
 
 /* Builds the bf16 slices of every uploaded table for the split assembly
