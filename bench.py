@@ -565,6 +565,23 @@ def run_gpu(args):
         if head == "split" and not args.no_precision:
             line["precision_by_order"] = precision_by_order(params, tables, host, integrand, local_rank, threads,
                                                             args.precision_configs)
+    if rank == 0 and "dd_path" in line and "fp64_path" in line:
+        # the literal contract: relative error <= 1e-10 at every order, met by
+        # the double-double recursion on the split assembly's Green matrices
+        dd = line["dd_path"]["split_assembly"]
+        summary = {"form": "split tcgen05 assembly + double-double minors and CDet (the reference's "
+                           "INTEGRAND_REAL=double_double arithmetic)",
+                   "value": dd["value"], "unit": UNIT, "ms_per_step": dd["ms_per_step"],
+                   "over_fp64_path": dd["value"] / line["fp64_path"]["value"]}
+        if "precision_by_order" in line:
+            orders = line["precision_by_order"]["orders"]
+            rel = [orders[str(n)]["dd_split_vs_truth_filter_on"]["relative"]["max"] for n in range(2, ORDER + 1)]
+            summary["worst_relative_error_orders_2_10"] = max(rel)
+            summary["worst_combine_scaled_error_order_1"] = \
+                orders["1"]["dd_split_vs_truth_filter_on"]["combine_scaled"]["max"]
+            summary["contract_met"] = bool(max(rel) <= 1e-10 and summary["worst_combine_scaled_error_order_1"] <= 1e-10)
+            summary["against"] = "the oracle's long double truth, pinned to the reference's high-precision mode"
+        line["at_1e-10_relative"] = summary
     if rank == 0:
         print(json.dumps(line))
     integrand.close()

@@ -156,8 +156,17 @@ void forget_slices(cdet_context* ctx, const TableSlot& slot) {
     }
 }
 
+// The optional regions the context's scratch holds.
+cdet::ScratchRegions scratch_regions(const cdet_context* ctx) {
+    cdet::ScratchRegions r;
+    r.dd_lanes = ctx->scratch_dd;
+    return r;
+}
+
 int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
-    if (ctx->scratch && batch <= ctx->scratch_batch && max_order <= ctx->scratch_order) return CDET_OK;
+    const bool dd = ctx->integrand_real == CDET_INTEGRAND_REAL_DOUBLE_DOUBLE;
+    if (ctx->scratch && batch <= ctx->scratch_batch && max_order <= ctx->scratch_order && (!dd || ctx->scratch_dd))
+        return CDET_OK;
     const int64_t new_batch = batch > ctx->scratch_batch ? batch : ctx->scratch_batch;
     const int new_order = max_order > ctx->scratch_order ? max_order : ctx->scratch_order;
     // minors warps with a global workspace (orders whose workspace does not
@@ -170,7 +179,9 @@ int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
     const size_t ws_cap = (size_t{4} << 30) / per_warp;
     if (ws_warps > ws_cap) ws_warps = ws_cap;
     if (ws_warps < 8) ws_warps = 8;
-    const size_t bytes = cdet::scratch_bytes(new_batch, new_order, ws_warps);
+    cdet::ScratchRegions regions;
+    regions.dd_lanes = dd || ctx->scratch_dd;
+    const size_t bytes = cdet::scratch_bytes(new_batch, new_order, ws_warps, regions);
     if (ctx->scratch) {
         cudaDeviceSynchronize();
         cudaFree(ctx->scratch);
@@ -180,6 +191,7 @@ int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
     if (err != cudaSuccess) {
         ctx->scratch_batch = 0;
         ctx->scratch_order = 0;
+        ctx->scratch_dd = false;
         return cuda_fail(err, "cudaMalloc(scratch)");
     }
     ++ctx->generation;
@@ -187,6 +199,7 @@ int ensure_scratch(cdet_context* ctx, int64_t batch, int max_order) {
     ctx->scratch_batch = new_batch;
     ctx->scratch_order = new_order;
     ctx->ws_warps = ws_warps;
+    ctx->scratch_dd = regions.dd_lanes;
     return CDET_OK;
 }
 
@@ -444,7 +457,8 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
     rc = build_problem(ctx, vertices, orders, batch, max_order, all_subsets, values, status, &p);
     if (rc != CDET_OK) return rc;
     cdet::Scratch w;
-    cdet::carve_scratch(ctx->scratch, ctx->scratch_batch, ctx->scratch_order, ctx->ws_warps, &w);
+    cdet::carve_scratch(ctx->scratch, ctx->scratch_batch, ctx->scratch_order, ctx->ws_warps, &w,
+                        scratch_regions(ctx));
     // The carve above is for the reserved (batch, order); the kernels index
     // with the call's max_order, which only needs less.
     if (reuse) {
@@ -960,7 +974,8 @@ int cdet_assemble_device(cdet_context* ctx, const double* vertices, const int32_
     int rc = run(ctx, vertices, orders, batch, max_order, 0, &scratch_dummy, status, st, true);
     if (rc != CDET_OK) return rc;
     cdet::Scratch w;
-    cdet::carve_scratch(ctx->scratch, ctx->scratch_batch, ctx->scratch_order, ctx->ws_warps, &w);
+    cdet::carve_scratch(ctx->scratch, ctx->scratch_batch, ctx->scratch_order, ctx->ws_warps, &w,
+                        scratch_regions(ctx));
     const size_t gbytes = static_cast<size_t>(batch) * 4 * max_order * max_order * sizeof(double);
     const size_t dbytes = static_cast<size_t>(batch) * 4 * max_order * sizeof(double);
     cudaError_t err = cudaMemcpyAsync(green, w.green, gbytes, cudaMemcpyDeviceToDevice, st);

@@ -48,6 +48,7 @@ struct cdet_context {
     int64_t scratch_batch = 0;
     int scratch_order = 0;
     size_t ws_warps = 0;
+    bool scratch_dd = false;  // the scratch holds the double-double lane region
     // staging for the host-buffer entry points
     void* staging = nullptr;
     size_t staging_bytes = 0;

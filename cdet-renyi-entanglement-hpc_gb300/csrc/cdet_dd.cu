@@ -312,11 +312,147 @@ __global__ void __launch_bounds__(128) integrand_dd(const __grid_constant__ Prob
     }
 }
 
+// ---- lane form: minors by warps into lane-interleaved a, CDet by lanes ----
+// For large batches: principal_minors_dd gives each (configuration, set) a
+// warp, as the FP64 form does, and writes a = up * down into [group][set]
+// [mask][lane] (the slot's lane of its order-sorted group of 32); cdet_dd_lane
+// then gives each slot a lane, so the 32 lanes of a warp run the recursions of
+// 32 configurations of (nearly) one order in step, every load a coalesced
+// 512-byte row. The same operations as the warp form: the same values.
+__device__ __forceinline__ DD* lane_a(const Scratch& w, int64_t slot, int set, int nmax) {
+    const int64_t subsets = int64_t{1} << nmax;
+    return reinterpret_cast<DD*>(w.dd_lanes) + ((slot >> 5) * 2 + set) * subsets * kWarp + (slot & 31);
+}
+__device__ __forceinline__ DD* lane_dp(const Scratch& w, int64_t slot, int set, int nmax, int64_t groups) {
+    const int64_t subsets = int64_t{1} << nmax;
+    return reinterpret_cast<DD*>(w.dd_lanes) + groups * 2 * subsets * kWarp +
+           ((slot >> 5) * 2 + set) * (subsets / 2) * kWarp + (slot & 31);
+}
+
+__global__ void __launch_bounds__(128) principal_minors_dd(const __grid_constant__ Problem p,
+                                                          const __grid_constant__ Scratch w) {
+    extern __shared__ double dd_smem[];
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int warp_in_block = threadIdx.x / kWarp;
+    const int warps_per_block = blockDim.x / kWarp;
+    const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
+    const int64_t total_warps = static_cast<int64_t>(gridDim.x) * warps_per_block;
+    const int nmax = p.max_order;
+    const WsLayout lay = ws_layout(nmax, !(p.same_spin[0] && p.same_spin[1]));
+    DD* ws = reinterpret_cast<DD*>(dd_smem) + static_cast<size_t>(warp_in_block) * lay.total;
+    DD* lu_lane = reinterpret_cast<DD*>(w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * 2 *
+                                                           nmax * nmax);
+    const DD tol{p.dd_tol.hi, p.dd_tol.lo}, thresh{p.dd_fpm_shift.hi, p.dd_fpm_shift.lo};
+    for (int64_t item = global_warp; item < p.batch * 2; item += total_warps) {
+        const int64_t c = item >> 1;
+        const int set = static_cast<int>(item & 1);
+        const int n = __ldg(p.orders + c);
+        if (n < 2 || n > nmax) continue;  // order 1 needs no minors
+        const double* green = w.green + (c * 2 + set) * 2 * static_cast<int64_t>(nmax) * nmax;
+        DD* A = ws + lay.a;
+        bool fb = false;
+        for (int k = lane; k < n * n; k += kWarp) A[k] = DD{green[k], 0.0};
+        __syncwarp();
+        DD* su = ws + lay.shifted_up;
+        fb |= mat2pm_dd_warp(A, n, tol, thresh, lay, ws, su, lu_lane, lane);
+        const bool one_spin = p.same_spin[set] != 0;
+        if (!one_spin) {
+            for (int k = lane; k < n * n; k += kWarp) A[k] = DD{green[static_cast<int64_t>(nmax) * nmax + k], 0.0};
+            __syncwarp();
+            fb |= mat2pm_dd_warp(A, n, tol, thresh, lay, ws, ws + lay.shifted_down, lu_lane, lane);
+        }
+        const DD* sd = one_spin ? su : ws + lay.shifted_down;
+        DD* a = lane_a(w, __ldg(w.slot_of + c), set, nmax);
+        for (uint32_t m = lane; m < (1u << n); m += kWarp)
+            a[static_cast<int64_t>(m) * kWarp] = m == 0 ? DD{0.0, 0.0} : dd_mul(su[m], sd[m]);
+        if (fb && lane == 0) atomicOr(p.status + c, kStatusFpmFallback);
+        __syncwarp();
+    }
+}
+
+// compute_dp_ztransform<DoubleDouble> for the slot's configuration on one
+// lane, masks holding vertex 0 in popcount order, each one's submasks in the
+// reference's descending order; then the prefactors and the combine.
+__global__ void __launch_bounds__(128) cdet_dd_lane(const __grid_constant__ Problem p,
+                                                   const __grid_constant__ Scratch w) {
+    const int64_t slot = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (slot >= p.batch) return;
+    const int64_t c = __ldg(w.config_at + slot);
+    const int n = __ldg(p.orders + c);
+    const int nmax = p.max_order;
+    if (n < 1 || n > nmax) return;
+    const int64_t groups = (p.batch + kWarp - 1) / kWarp;
+    const DD zero{0.0, 0.0};
+    const DD threshold{p.dd_threshold.hi, p.dd_threshold.lo};
+    const bool filter = dd_gt(threshold, zero);
+    int32_t status = 0;
+    DD value[2];
+    for (int set = 0; set < 2; ++set) {
+        const int r = set == 0 ? 2 : 1;
+        if (n == 1) {
+            const double* diag = w.diag + c * 2 * 2 * nmax;
+            const DD shu{p.dd_shift[0].hi, p.dd_shift[0].lo}, shd{p.dd_shift[1].hi, p.dd_shift[1].lo};
+            const DD su = dd_add(DD{diag[(set * 2) * nmax], 0.0}, shu);
+            const DD sd = dd_add(DD{diag[(set * 2 + 1) * nmax], 0.0}, shd);
+            const DD ru = dd_mul(dd_mul(DD{static_cast<double>(-r), 0.0}, DD{p.dd_u.hi, p.dd_u.lo}),
+                                 DD{p.dd_beta.hi, p.dd_beta.lo});
+            value[set] = dd_mul(ru, dd_sub(dd_mul(su, sd), dd_mul(shu, shd)));
+            continue;
+        }
+        const DD* a = lane_a(w, slot, set, nmax);
+        DD* dp = lane_dp(w, slot, set, nmax, groups);
+        dp[0] = a[1 * kWarp];
+        const uint32_t rest_limit = 1u << (n - 1);
+        for (int bits = 2; bits <= n; ++bits) {
+            for (uint32_t rest = (1u << (bits - 1)) - 1u; rest < rest_limit; rest = next_same_popcount(rest)) {
+                DD acc = a[static_cast<int64_t>((rest << 1) | 1u) * kWarp];
+                DD rhs = dd_abs(acc);
+                for (uint32_t sm = (rest - 1u) & rest;; sm = (sm - 1u) & rest) {
+                    const DD term = dd_mul(dp[static_cast<int64_t>(sm) * kWarp],
+                                           a[static_cast<int64_t>((rest ^ sm) << 1) * kWarp]);
+                    acc = dd_sub(acc, term);
+                    rhs = dd_add(rhs, dd_abs(term));
+                    if (sm == 0) break;
+                }
+                if (filter && dd_lt(dd_abs(acc), dd_mul(threshold, rhs))) acc = zero;
+                dp[static_cast<int64_t>(rest) * kWarp] = acc;
+                if (bits == n) break;  // one mask at the top level
+            }
+        }
+        const DD top = dp[static_cast<int64_t>(rest_limit - 1u) * kWarp];
+        value[set] = dd_mul(DD{p.pref_dd[set][n].hi, p.pref_dd[set][n].lo}, top);
+        if (!dd_finite(value[set])) status |= kStatusNonFinite;
+    }
+    const DD result = dd_sub(value[0], dd_mul(DD{2.0, 0.0}, value[1]));
+    p.values[c] = dadd(result.hi, result.lo);
+    if (status) atomicOr(p.status + c, status);
+}
+
 }  // namespace
+
+// Smallest batch that runs the lane form (a warp of configurations per SM).
+static int64_t dd_lane_min_batch(int sm_count) { return static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * kWarp; }
 
 cudaError_t launch_integrand_dd(const Problem& p, const Scratch& w, int sm_count, cudaStream_t stream) {
     if (p.batch <= 0) return cudaSuccess;
     const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
+    if (w.dd_lanes && p.batch >= dd_lane_min_batch(sm_count)) {
+        const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(DD);
+        const int wpb = static_cast<int>(std::max<size_t>(1, std::min<size_t>(4, (227 * 1024) / ws_bytes)));
+        const int sms = sm_count > 0 ? sm_count : 152;
+        const int per_sm = std::max(1, static_cast<int>((227 * 1024) / (ws_bytes * wpb + 1024)));
+        int64_t blocks = std::min<int64_t>(static_cast<int64_t>(sms) * per_sm, (p.batch * 2 + wpb - 1) / wpb);
+        blocks = std::min<int64_t>(blocks, std::max<int64_t>(1, static_cast<int64_t>(w.ws_warps) / (2 * wpb)));
+        const size_t smem = ws_bytes * wpb;
+        cudaError_t err = cudaFuncSetAttribute(principal_minors_dd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(smem));
+        if (err != cudaSuccess) return err;
+        principal_minors_dd<<<static_cast<unsigned>(blocks), wpb * kWarp, smem, stream>>>(p, w);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        cdet_dd_lane<<<static_cast<unsigned>((p.batch + 127) / 128), 128, 0, stream>>>(p, w);
+        return cudaGetLastError();
+    }
     const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(DD);
     const size_t budget = 227 * 1024;
     const int wpb = static_cast<int>(std::max<size_t>(1, std::min<size_t>(4, budget / ws_bytes)));

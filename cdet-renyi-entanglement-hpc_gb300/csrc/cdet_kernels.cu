@@ -1688,7 +1688,8 @@ size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps, ScratchRegio
     if (regions.minors_workspace) total += ws_warps * minors_workspace_doubles(max_order);  // minors workspace
     total += ws_warps * kWarp * n2;                                 // LU fallback scratch
     total += 2 * ((static_cast<size_t>(batch) * 4 + 7) / 8) + 32;   // order-sorted slots, buckets
-    return total * sizeof(double) + 64 * 9;
+    if (regions.dd_lanes) total += 3 * groups * 2 * subsets * kWarp;  // double-double a and dp
+    return total * sizeof(double) + 64 * (regions.dd_lanes ? 10 : 9);
 }
 
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out,
@@ -1712,6 +1713,7 @@ void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Sc
     out->slot_of = reinterpret_cast<int32_t*>(take((static_cast<size_t>(batch) * 4 + 7) / 8));
     out->config_at = reinterpret_cast<int32_t*>(take((static_cast<size_t>(batch) * 4 + 7) / 8));
     out->order_count = reinterpret_cast<uint32_t*>(take(32));
+    out->dd_lanes = regions.dd_lanes ? take(3 * groups * 2 * subsets * kWarp) : nullptr;
 }
 
 // Sort, minors and CDet (or the queue kernel) on the Green matrices in scratch.

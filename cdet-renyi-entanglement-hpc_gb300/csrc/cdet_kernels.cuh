@@ -49,6 +49,8 @@ struct Scratch {
     int32_t* slot_of;   // [batch] order-sorted slot of each configuration (single-order FP64 CDet)
     int32_t* config_at; // [batch] configuration in each slot
     uint32_t* order_count;  // [64] counting-sort buckets
+    double* dd_lanes;   // double-double lane form: a [groups][2][2^max_order][32] and dp of the
+                        // masks holding vertex 0 [groups][2][2^(max_order-1)][32], (hi, lo) pairs
 };
 
 // Per-warp workspace of the minors recursion (mat2pm), in elements of the
@@ -248,6 +250,7 @@ bool fp64_single_order_uses_dp_lanes(int max_order);
 struct ScratchRegions {
     bool minors_workspace = true;
     bool dp_lanes = true;
+    bool dd_lanes = false;  // the double-double integrand's lane-interleaved a and dp
 };
 size_t scratch_bytes(int64_t batch, int max_order, size_t ws_warps, ScratchRegions regions = {});
 void carve_scratch(void* base, int64_t batch, int max_order, size_t ws_warps, Scratch* out,

@@ -57,6 +57,25 @@ def test_dd_mode_equals_reference(case, variant):
 
 
 @pytest.mark.parametrize("case", ["physical_2x2", "column_3x3"])
+@pytest.mark.parametrize("variant", ["default", "fallback"])
+def test_dd_lane_form_equals_reference(case, variant):
+    """A batch large enough for the lane form (minors by warps into
+    lane-interleaved arrays, the recursion one lane per configuration over
+    order-sorted slots): the golden configurations repeated to 6,300, every
+    value the reference's bit for bit."""
+    params, tables, _ = load_case(case)
+    params = dataclasses.replace(params, **VARIANTS[variant])
+    gpu = CdetIntegrand(params, tables)
+    gpu.set_integrand_real("double_double", significand_bits=113)
+    v, o = DD[f"{case}.vertices"], DD[f"{case}.orders"]
+    reps = 50
+    got, st = gpu.integrand_batch(np.tile(v, (reps, 1, 1)), np.tile(o, reps))
+    want = np.tile(DD[f"{case}.{variant}.values"], reps)
+    assert (st & ~L.CONFIG_FPM_FALLBACK).max() == 0
+    assert bits_equal(got, want)
+
+
+@pytest.mark.parametrize("case", ["physical_2x2", "column_3x3"])
 def test_dd_on_split_assembly_and_what_it_rejects(case):
     """The double-double recursion on the tensor-core Green matrices: not
     the reference's mode, but its values stay within 1e-12 relative of it at

@@ -103,3 +103,31 @@ def test_precision_contract_order_14_degree_192():
     params = CdetParams(n1=3, n2=3, beta="10", mu="-0.5", u="6", alpha_up="0", alpha_down="0",
                         mask_sites=half_lattice_mask(3, 3), cheb_nu=192, cheb_nv=192)
     _check_orders(params, [14], 16, 42000)
+
+
+def test_double_double_meets_relative_contract_8x8():
+    """The literal contract, relative error <= 1e-10 at every order, on the
+    benchmark lattice: the double-double recursion (the reference's
+    INTEGRAND_REAL=double_double on the FP64 assembly, and the same recursion
+    on the split assembly's Green matrices), with the reference's default
+    round-off filter, against the long double truth at orders 2..10; at
+    order 1, whose twisted - 2 ordinary cancels to the round-off of its
+    inputs, scaled by |twisted| + 2 |ordinary|."""
+    params = CdetParams(n1=8, n2=8, beta="8", mu="0", u="4", alpha_up="0", alpha_down="0",
+                        mask_sites=named_mask("origin_square", 8, 8, 2), cheb_nu=128, cheb_nv=128)
+    tables = build_tables(params, device="cuda")
+    orc = Oracle(params.runtime_scalars(), _host(tables))
+    ctx = CdetIntegrand(params, tables)
+    ctx.set_integrand_real("double_double")
+    for n in range(1, 11):
+        v = uniform_configurations(43000 + n, 64, n)
+        o = np.full(64, n, np.int32)
+        truth, parts, st = orc.integrand_ld_parts_batch(v, o, threads=8)
+        for path in ("fp64", "split"):
+            got, gst = _evaluate(ctx, path, v, o)
+            ok = (st == 0) & (gst == 0)
+            assert ok.sum() >= 32, (n, path)
+            e = error_forms(got, truth, parts, ok)
+            form = "combine_scaled" if n == 1 else "relative"
+            assert e[form]["max"] <= CONTRACT, (n, path, e[form])
+    ctx.close()
