@@ -222,12 +222,14 @@ def precision_by_order(params, tables, host, integrand, device, threads, per_ord
                 torch.cuda.synchronize(dev)
                 got[(filt, path)] = (vals.cpu().numpy().copy(), status.cpu().numpy().copy())
         integrand.set_integrand_real("double_double")
+        integrand.set_integrand_form("staged")  # the lane layout, as the timed batch runs it
         for path, key in (("fp64", "dd"), ("split", "dd_split")):  # the reference's mode; on split Green matrices
             integrand.set_assembly(path)
             integrand.integrand_device(dv, do, vals, status)
             torch.cuda.synchronize(dev)
             got[("filter_on", key)] = (vals.cpu().numpy().copy(), status.cpu().numpy().copy())
         integrand.set_integrand_real("double")
+        integrand.set_integrand_form("auto")
         ok = st == 0
         for key in got:
             ok &= got[key][1] == 0
@@ -569,8 +571,8 @@ def run_gpu(args):
         # the literal contract: relative error <= 1e-10 at every order, met by
         # the double-double recursion on the split assembly's Green matrices
         dd = line["dd_path"]["split_assembly"]
-        summary = {"form": "split tcgen05 assembly + double-double minors and CDet (the reference's "
-                           "INTEGRAND_REAL=double_double arithmetic)",
+        summary = {"form": "split tcgen05 assembly + double-double minors (the reference's DoubleDouble "
+                           "arithmetic) and CDet recursion (FMA double-double steps, lane layout)",
                    "value": dd["value"], "unit": UNIT, "ms_per_step": dd["ms_per_step"],
                    "over_fp64_path": dd["value"] / line["fp64_path"]["value"]}
         if "precision_by_order" in line:

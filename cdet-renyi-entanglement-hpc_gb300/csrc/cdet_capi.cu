@@ -510,7 +510,11 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
     // (order, fused, batch size class) outside a capture (staged until then).
     bool tune_post = false;
     std::tuple<int, int, int> post_key;
-    if (!p.all_subsets && !assembly_only && !p.dd_mode && max_order <= cdet::kQueueMaxOrder) {
+    if (p.dd_mode) {
+        // the double-double integrand: STAGED = its lane form, QUEUE = its warp
+        // form, AUTO = the lane form from one warp of configurations per SM
+        p.integrand_form = ctx->integrand_form;
+    } else if (!p.all_subsets && !assembly_only && max_order <= cdet::kQueueMaxOrder) {
         if (ctx->integrand_form != CDET_INTEGRAND_AUTO) {
             p.integrand_form = ctx->integrand_form;
             p.queue = ctx->queue_shape;

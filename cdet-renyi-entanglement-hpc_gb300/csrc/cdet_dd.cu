@@ -373,6 +373,14 @@ __global__ void __launch_bounds__(128) principal_minors_dd(const __grid_constant
 // compute_dp_ztransform<DoubleDouble> for the slot's configuration on one
 // lane, masks holding vertex 0 in popcount order, each one's submasks in the
 // reference's descending order; then the prefactors and the combine.
+// Exact: the reference's DoubleDouble operations (51 FP64 operations per
+// pair update). Otherwise (the split assembly's Green matrices, where the
+// reference's values are not the contract): the product as FMAs without the
+// lo x lo term, the subtraction as one two-sum of the highs plus the lows and
+// one renormalisation, and the round-off filter's magnitude sum in FP64 on
+// the products' high parts (16 operations; the accumulated error stays near
+// 1e-32 of the terms' magnitude sum).
+template <bool Exact>
 __global__ void __launch_bounds__(128) cdet_dd_lane(const __grid_constant__ Problem p,
                                                    const __grid_constant__ Scratch w) {
     const int64_t slot = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -406,15 +414,34 @@ __global__ void __launch_bounds__(128) cdet_dd_lane(const __grid_constant__ Prob
         for (int bits = 2; bits <= n; ++bits) {
             for (uint32_t rest = (1u << (bits - 1)) - 1u; rest < rest_limit; rest = next_same_popcount(rest)) {
                 DD acc = a[static_cast<int64_t>((rest << 1) | 1u) * kWarp];
-                DD rhs = dd_abs(acc);
-                for (uint32_t sm = (rest - 1u) & rest;; sm = (sm - 1u) & rest) {
-                    const DD term = dd_mul(dp[static_cast<int64_t>(sm) * kWarp],
-                                           a[static_cast<int64_t>((rest ^ sm) << 1) * kWarp]);
-                    acc = dd_sub(acc, term);
-                    rhs = dd_add(rhs, dd_abs(term));
-                    if (sm == 0) break;
+                if constexpr (Exact) {
+                    DD rhs = dd_abs(acc);
+                    for (uint32_t sm = (rest - 1u) & rest;; sm = (sm - 1u) & rest) {
+                        const DD term = dd_mul(dp[static_cast<int64_t>(sm) * kWarp],
+                                               a[static_cast<int64_t>((rest ^ sm) << 1) * kWarp]);
+                        acc = dd_sub(acc, term);
+                        rhs = dd_add(rhs, dd_abs(term));
+                        if (sm == 0) break;
+                    }
+                    if (filter && dd_lt(dd_abs(acc), dd_mul(threshold, rhs))) acc = zero;
+                } else {
+                    double rhs = fabs(acc.hi);
+                    for (uint32_t sm = (rest - 1u) & rest;; sm = (sm - 1u) & rest) {
+                        const DD x = dp[static_cast<int64_t>(sm) * kWarp];
+                        const DD y = a[static_cast<int64_t>((rest ^ sm) << 1) * kWarp];
+                        const double ph = dmul(x.hi, y.hi);
+                        double pe = dfma(x.hi, y.hi, -ph);
+                        pe = dfma(x.hi, y.lo, pe);
+                        pe = dfma(x.lo, y.hi, pe);
+                        double e;
+                        const double s = two_sum(acc.hi, -ph, e);
+                        e = dadd(e, dsub(acc.lo, pe));
+                        acc.hi = quick_two_sum(s, e, acc.lo);
+                        rhs = dadd(rhs, fabs(ph));
+                        if (sm == 0) break;
+                    }
+                    if (filter && fabs(acc.hi) < dmul(threshold.hi, rhs)) acc = zero;
                 }
-                if (filter && dd_lt(dd_abs(acc), dd_mul(threshold, rhs))) acc = zero;
                 dp[static_cast<int64_t>(rest) * kWarp] = acc;
                 if (bits == n) break;  // one mask at the top level
             }
@@ -436,7 +463,9 @@ static int64_t dd_lane_min_batch(int sm_count) { return static_cast<int64_t>(sm_
 cudaError_t launch_integrand_dd(const Problem& p, const Scratch& w, int sm_count, cudaStream_t stream) {
     if (p.batch <= 0) return cudaSuccess;
     const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
-    if (w.dd_lanes && p.batch >= dd_lane_min_batch(sm_count)) {
+    const bool lanes = p.integrand_form == kIntegrandStaged ||
+                       (p.integrand_form == kIntegrandAuto && p.batch >= dd_lane_min_batch(sm_count));
+    if (w.dd_lanes && lanes) {
         const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(DD);
         const int wpb = static_cast<int>(std::max<size_t>(1, std::min<size_t>(4, (227 * 1024) / ws_bytes)));
         const int sms = sm_count > 0 ? sm_count : 152;
@@ -450,7 +479,11 @@ cudaError_t launch_integrand_dd(const Problem& p, const Scratch& w, int sm_count
         principal_minors_dd<<<static_cast<unsigned>(blocks), wpb * kWarp, smem, stream>>>(p, w);
         err = cudaGetLastError();
         if (err != cudaSuccess) return err;
-        cdet_dd_lane<<<static_cast<unsigned>((p.batch + 127) / 128), 128, 0, stream>>>(p, w);
+        // the reference's arithmetic on the FP64 assembly; the lighter one on the split assembly
+        if (p.fused_cdet)
+            cdet_dd_lane<false><<<static_cast<unsigned>((p.batch + 127) / 128), 128, 0, stream>>>(p, w);
+        else
+            cdet_dd_lane<true><<<static_cast<unsigned>((p.batch + 127) / 128), 128, 0, stream>>>(p, w);
         return cudaGetLastError();
     }
     const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(DD);

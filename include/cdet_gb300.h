@@ -488,7 +488,14 @@ enum cdet_integrand_real {
  * the reference mode's by what the Green entries' last bits move, not by the
  * FP64 recursion's round-off). dd may be null for CDET_INTEGRAND_REAL_DOUBLE.
  * Single-configuration integrands of order <= 10 only: an all-subsets call or
- * a higher order fails with CDET_ERR_INVALID. */
+ * a higher order fails with CDET_ERR_INVALID. Its work layout follows
+ * cdet_set_integrand_form: CDET_INTEGRAND_STAGED = minors by warps, then the
+ * recursion one lane per configuration; CDET_INTEGRAND_QUEUE = one warp per
+ * configuration; AUTO = the lane layout from one warp of configurations per
+ * SM. On the FP64 assembly both layouts give the reference's values; on the
+ * split assembly the lane layout's recursion uses the lighter double-double
+ * steps (FMA products, one renormalisation per subtraction, FP64 magnitude
+ * sum), so there they differ in the last bits. */
 int cdet_set_integrand_real(cdet_context* ctx, int real_type, const cdet_dd_scalars* dd);
 
 /* Builds the bf16 slices of every uploaded table for the split assembly

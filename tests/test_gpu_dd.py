@@ -41,11 +41,14 @@ def test_dd_mode_equals_reference(case, variant):
     gpu = CdetIntegrand(params, tables)
     gpu.set_integrand_real("double_double", significand_bits=113)
     v, o = DD[f"{case}.vertices"], DD[f"{case}.orders"]
-    got, st = gpu.integrand_batch(v, o)
     want = DD[f"{case}.{variant}.values"]
-    assert (st & ~L.CONFIG_FPM_FALLBACK).max() == 0
-    bad = np.flatnonzero(got.view(np.uint64) != want.view(np.uint64))
-    assert bad.size == 0, (bad[:8], o[bad[:8]], got[bad[:8]], want[bad[:8]])
+    for form in ("auto", "staged", "queue"):  # every layout gives the reference's values on the FP64 assembly
+        gpu.set_integrand_form(form)
+        got, st = gpu.integrand_batch(v, o)
+        assert (st & ~L.CONFIG_FPM_FALLBACK).max() == 0
+        bad = np.flatnonzero(got.view(np.uint64) != want.view(np.uint64))
+        assert bad.size == 0, (form, bad[:8], o[bad[:8]], got[bad[:8]], want[bad[:8]])
+    gpu.set_integrand_form("auto")
     if variant == "fallback":
         assert np.all(st[o >= 2] & L.CONFIG_FPM_FALLBACK)
     # back to the FP64 drop-in: the FP64 values again
@@ -87,14 +90,16 @@ def test_dd_on_split_assembly_and_what_it_rejects(case):
     gpu.set_integrand_real("double_double", significand_bits=113)
     gpu.set_assembly("split")
     v, o = DD[f"{case}.vertices"], DD[f"{case}.orders"]
-    got, st = gpu.integrand_batch(v, o)
     want = DD[f"{case}.default.values"]
-    assert st.max() == 0
-    scale = np.maximum(np.abs(want), 1e-300)
-    rel = np.abs(got - want) / scale
-    big = o >= 2  # order 1 cancels to round-off residue (compare absolutely)
-    assert rel[big].max() <= 1e-12, (rel[big].max(), o[big][np.argmax(rel[big])])
-    assert np.abs(got - want)[o == 1].max() <= 1e-13
+    for form in ("queue", "staged"):  # the warp layout (exact steps) and the lane layout (lighter ones)
+        gpu.set_integrand_form(form)
+        got, st = gpu.integrand_batch(v, o)
+        assert st.max() == 0
+        scale = np.maximum(np.abs(want), 1e-300)
+        rel = np.abs(got - want) / scale
+        big = o >= 2  # order 1 cancels to round-off residue (compare absolutely)
+        assert rel[big].max() <= 1e-12, (form, rel[big].max(), o[big][np.argmax(rel[big])])
+        assert np.abs(got - want)[o == 1].max() <= 1e-13
     with pytest.raises(RuntimeError, match="order <= 10"):
         gpu.all_subsets_batch(uniform_configurations(3, 4, 5))
     with pytest.raises(RuntimeError, match="order <= 10"):

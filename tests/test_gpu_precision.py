@@ -119,6 +119,7 @@ def test_double_double_meets_relative_contract_8x8():
     orc = Oracle(params.runtime_scalars(), _host(tables))
     ctx = CdetIntegrand(params, tables)
     ctx.set_integrand_real("double_double")
+    ctx.set_integrand_form("staged")  # the lane layout a large batch runs (lighter steps on the split assembly)
     for n in range(1, 11):
         v = uniform_configurations(43000 + n, 64, n)
         o = np.full(64, n, np.int32)
