@@ -571,8 +571,8 @@ def run_gpu(args):
         # the literal contract: relative error <= 1e-10 at every order, met by
         # the double-double recursion on the split assembly's Green matrices
         dd = line["dd_path"]["split_assembly"]
-        summary = {"form": "split tcgen05 assembly + double-double minors (the reference's DoubleDouble "
-                           "arithmetic) and CDet recursion (FMA double-double steps, lane layout)",
+        summary = {"form": "split tcgen05 assembly + double-double minors and CDet recursion (lighter "
+                           "double-double steps: FMA products, one renormalisation per sum; lane layout)",
                    "value": dd["value"], "unit": UNIT, "ms_per_step": dd["ms_per_step"],
                    "over_fp64_path": dd["value"] / line["fp64_path"]["value"]}
         if "precision_by_order" in line:

@@ -52,6 +52,49 @@ __device__ __forceinline__ bool dd_zero(DD a) { return a.hi == 0.0 && a.lo == 0.
 // subtract_product for DoubleDouble (fast_principle_minors.h:30-37): base - left * right
 __device__ __forceinline__ DD dd_sub_prod(DD left, DD right, DD base) { return dd_sub(base, dd_mul(left, right)); }
 
+// The lighter steps used on the split assembly's Green matrices, where the
+// reference's values are not the contract: products as FMAs without the
+// lo x lo term, sums as one two-sum of the highs plus the lows and one
+// renormalisation (relative error a few 2^-104 of the operands).
+__device__ __forceinline__ DD dd_mul_light(DD x, DD y) {
+    const double p = dmul(x.hi, y.hi);
+    double e = dfma(x.hi, y.hi, -p);
+    e = dfma(x.hi, y.lo, e);
+    e = dfma(x.lo, y.hi, e);
+    DD r;
+    r.hi = quick_two_sum(p, e, r.lo);
+    return r;
+}
+__device__ __forceinline__ DD dd_add_light(DD x, DD y) {
+    double e;
+    const double s = two_sum(x.hi, y.hi, e);
+    e = dadd(e, dadd(x.lo, y.lo));
+    DD r;
+    r.hi = quick_two_sum(s, e, r.lo);
+    return r;
+}
+// base - left * right with the product as FMAs
+__device__ __forceinline__ DD dd_sub_prod_light(DD left, DD right, DD base) {
+    const double p = dmul(left.hi, right.hi);
+    double pe = dfma(left.hi, right.hi, -p);
+    pe = dfma(left.hi, right.lo, pe);
+    pe = dfma(left.lo, right.hi, pe);
+    double e;
+    const double s = two_sum(base.hi, -p, e);
+    e = dadd(e, dsub(base.lo, pe));
+    DD r;
+    r.hi = quick_two_sum(s, e, r.lo);
+    return r;
+}
+template <bool Exact>
+__device__ __forceinline__ DD mul_t(DD x, DD y) { return Exact ? dd_mul(x, y) : dd_mul_light(x, y); }
+template <bool Exact>
+__device__ __forceinline__ DD add_t(DD x, DD y) { return Exact ? dd_add(x, y) : dd_add_light(x, y); }
+template <bool Exact>
+__device__ __forceinline__ DD sub_prod_t(DD l, DD r, DD b) {
+    return Exact ? dd_sub_prod(l, r, b) : dd_sub_prod_light(l, r, b);
+}
+
 __device__ __forceinline__ DD shfl_dd(DD v, int src_lane_xor) {
     return DD{__shfl_xor_sync(0xffffffffu, v.hi, src_lane_xor), __shfl_xor_sync(0xffffffffu, v.lo, src_lane_xor)};
 }
@@ -102,6 +145,10 @@ __device__ DD minor_by_lu_dd(const DD* a, int n, uint32_t mask, DD* m) {
 // mat2pm_from_buffer<DoubleDouble> (fast_principle_minors.h:120-246) for one
 // matrix on one warp: shifted[mask] (mask >= 1) ends as the principal minor of
 // the rows and columns in mask. Returns true when the LU fallback ran.
+// Exact: the reference's operations; otherwise the lighter steps for the
+// Schur updates, the minor sums and products and the shift removal (the
+// pivots, their inverses and the fallback decision stay exact).
+template <bool Exact>
 __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLayout& lay, DD* ws, DD* shifted,
                                DD* lu_lane, int lane) {
     const int msize = n * n;
@@ -157,7 +204,7 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
         for (int item = lane; item < sets * new_size; item += kWarp) {
             const int set = item / new_size;
             const int row = item - set * new_size;
-            factor[item] = dd_mul(old_list[set * old_msize + (row + 1) * old_size], inv[set]);
+            factor[item] = mul_t<Exact>(old_list[set * old_msize + (row + 1) * old_size], inv[set]);
         }
         __syncwarp();
         const int items = sets * new_msize;
@@ -169,11 +216,11 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
             const int src = set * old_msize;
             const DD base = old_list[src + (row + 1) * old_size + col + 1];
             new_list[item] = base;
-            new_list[items + item] = dd_sub_prod(old_list[src + 1 + col], factor[set * new_size + row], base);
+            new_list[items + item] = sub_prod_t<Exact>(old_list[src + 1 + col], factor[set * new_size + row], base);
         }
         __syncwarp();
         for (int m = lane; m < 2 * sets; m += kWarp)
-            shifted[minor_index + m] = dd_add(shifted[minor_index + m], new_list[m * new_msize]);
+            shifted[minor_index + m] = add_t<Exact>(shifted[minor_index + m], new_list[m * new_msize]);
         minor_index += 2 * sets;
         DD* t = old_list;
         old_list = new_list;
@@ -188,7 +235,7 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
     }
     for (uint32_t step = 1; step < subsets; step <<= 1) {  // the prefix product over levels
         for (uint32_t set = step + 1 + lane; set < 2 * step; set += kWarp)
-            shifted[set] = dd_mul(shifted[set], shifted[set - step]);
+            shifted[set] = mul_t<Exact>(shifted[set], shifted[set - step]);
         __syncwarp();
     }
     for (uint32_t step = subsets; step > 1; step >>= 1) {  // the shift removal, bit by bit from the top
@@ -196,7 +243,7 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
         for (uint32_t q = lane; q < subsets / 2; q += kWarp) {
             const uint32_t t = q / half;
             const uint32_t ss = t * step + half + (q - t * half);
-            shifted[ss] = dd_sub_prod(p, shifted[ss - half], shifted[ss]);
+            shifted[ss] = sub_prod_t<Exact>(p, shifted[ss - half], shifted[ss]);
         }
         __syncwarp();
     }
@@ -258,12 +305,12 @@ __device__ DD dd_set_value(const Problem& p, const Scratch& w, int64_t c, int se
     for (int k = lane; k < n * n; k += kWarp) A[k] = DD{green[k], 0.0};
     __syncwarp();
     DD* su = ws + lay.shifted_up;
-    fb |= mat2pm_dd_warp(A, n, tol, thresh, lay, ws, su, lu_lane, lane);
+    fb |= mat2pm_dd_warp<true>(A, n, tol, thresh, lay, ws, su, lu_lane, lane);
     const bool one_spin = p.same_spin[set] != 0;
     if (!one_spin) {
         for (int k = lane; k < n * n; k += kWarp) A[k] = DD{green[static_cast<int64_t>(nmax) * nmax + k], 0.0};
         __syncwarp();
-        fb |= mat2pm_dd_warp(A, n, tol, thresh, lay, ws, ws + lay.shifted_down, lu_lane, lane);
+        fb |= mat2pm_dd_warp<true>(A, n, tol, thresh, lay, ws, ws + lay.shifted_down, lu_lane, lane);
     }
     const DD* sd = one_spin ? su : ws + lay.shifted_down;
     // a[mask] = up[mask - 1] * down[mask - 1] (:254-257), in place of the up minors
@@ -329,6 +376,7 @@ __device__ __forceinline__ DD* lane_dp(const Scratch& w, int64_t slot, int set, 
            ((slot >> 5) * 2 + set) * (subsets / 2) * kWarp + (slot & 31);
 }
 
+template <bool Exact>
 __global__ void __launch_bounds__(128) principal_minors_dd(const __grid_constant__ Problem p,
                                                           const __grid_constant__ Scratch w) {
     extern __shared__ double dd_smem[];
@@ -354,17 +402,17 @@ __global__ void __launch_bounds__(128) principal_minors_dd(const __grid_constant
         for (int k = lane; k < n * n; k += kWarp) A[k] = DD{green[k], 0.0};
         __syncwarp();
         DD* su = ws + lay.shifted_up;
-        fb |= mat2pm_dd_warp(A, n, tol, thresh, lay, ws, su, lu_lane, lane);
+        fb |= mat2pm_dd_warp<Exact>(A, n, tol, thresh, lay, ws, su, lu_lane, lane);
         const bool one_spin = p.same_spin[set] != 0;
         if (!one_spin) {
             for (int k = lane; k < n * n; k += kWarp) A[k] = DD{green[static_cast<int64_t>(nmax) * nmax + k], 0.0};
             __syncwarp();
-            fb |= mat2pm_dd_warp(A, n, tol, thresh, lay, ws, ws + lay.shifted_down, lu_lane, lane);
+            fb |= mat2pm_dd_warp<Exact>(A, n, tol, thresh, lay, ws, ws + lay.shifted_down, lu_lane, lane);
         }
         const DD* sd = one_spin ? su : ws + lay.shifted_down;
         DD* a = lane_a(w, __ldg(w.slot_of + c), set, nmax);
         for (uint32_t m = lane; m < (1u << n); m += kWarp)
-            a[static_cast<int64_t>(m) * kWarp] = m == 0 ? DD{0.0, 0.0} : dd_mul(su[m], sd[m]);
+            a[static_cast<int64_t>(m) * kWarp] = m == 0 ? DD{0.0, 0.0} : mul_t<Exact>(su[m], sd[m]);
         if (fb && lane == 0) atomicOr(p.status + c, kStatusFpmFallback);
         __syncwarp();
     }
@@ -473,10 +521,11 @@ cudaError_t launch_integrand_dd(const Problem& p, const Scratch& w, int sm_count
         int64_t blocks = std::min<int64_t>(static_cast<int64_t>(sms) * per_sm, (p.batch * 2 + wpb - 1) / wpb);
         blocks = std::min<int64_t>(blocks, std::max<int64_t>(1, static_cast<int64_t>(w.ws_warps) / (2 * wpb)));
         const size_t smem = ws_bytes * wpb;
-        cudaError_t err = cudaFuncSetAttribute(principal_minors_dd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        auto minors = p.fused_cdet ? principal_minors_dd<false> : principal_minors_dd<true>;
+        cudaError_t err = cudaFuncSetAttribute(minors, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                static_cast<int>(smem));
         if (err != cudaSuccess) return err;
-        principal_minors_dd<<<static_cast<unsigned>(blocks), wpb * kWarp, smem, stream>>>(p, w);
+        minors<<<static_cast<unsigned>(blocks), wpb * kWarp, smem, stream>>>(p, w);
         err = cudaGetLastError();
         if (err != cudaSuccess) return err;
         // the reference's arithmetic on the FP64 assembly; the lighter one on the split assembly

@@ -493,9 +493,9 @@ enum cdet_integrand_real {
  * recursion one lane per configuration; CDET_INTEGRAND_QUEUE = one warp per
  * configuration; AUTO = the lane layout from one warp of configurations per
  * SM. On the FP64 assembly both layouts give the reference's values; on the
- * split assembly the lane layout's recursion uses the lighter double-double
- * steps (FMA products, one renormalisation per subtraction, FP64 magnitude
- * sum), so there they differ in the last bits. */
+ * split assembly the lane layout's minors and recursion take lighter
+ * double-double steps (FMA products, one renormalisation per sum, the
+ * filter's magnitude sum in FP64), so there they differ in the last bits. */
 int cdet_set_integrand_real(cdet_context* ctx, int real_type, const cdet_dd_scalars* dd);
 
 /* Builds the bf16 slices of every uploaded table for the split assembly
