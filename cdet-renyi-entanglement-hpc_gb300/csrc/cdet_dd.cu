@@ -208,7 +208,8 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
         }
         __syncwarp();
         const int items = sets * new_msize;
-        for (int item = lane; item < items; item += kWarp) {
+#pragma unroll 4
+        for (int item = lane; item < items; item += kWarp) {  // independent items: chains in flight
             const int set = item / new_msize;
             const int e = item - set * new_msize;
             const int row = e / new_size;
@@ -234,12 +235,14 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
         return true;
     }
     for (uint32_t step = 1; step < subsets; step <<= 1) {  // the prefix product over levels
+#pragma unroll 4
         for (uint32_t set = step + 1 + lane; set < 2 * step; set += kWarp)
             shifted[set] = mul_t<Exact>(shifted[set], shifted[set - step]);
         __syncwarp();
     }
     for (uint32_t step = subsets; step > 1; step >>= 1) {  // the shift removal, bit by bit from the top
         const uint32_t half = step >> 1;
+#pragma unroll 4
         for (uint32_t q = lane; q < subsets / 2; q += kWarp) {
             const uint32_t t = q / half;
             const uint32_t ss = t * step + half + (q - t * half);
@@ -429,7 +432,7 @@ __global__ void __launch_bounds__(128) principal_minors_dd(const __grid_constant
 // the products' high parts (16 operations; the accumulated error stays near
 // 1e-32 of the terms' magnitude sum).
 template <bool Exact>
-__global__ void __launch_bounds__(128) cdet_dd_lane(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(32) cdet_dd_lane(const __grid_constant__ Problem p,
                                                    const __grid_constant__ Scratch w) {
     const int64_t slot = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (slot >= p.batch) return;
@@ -529,10 +532,11 @@ cudaError_t launch_integrand_dd(const Problem& p, const Scratch& w, int sm_count
         err = cudaGetLastError();
         if (err != cudaSuccess) return err;
         // the reference's arithmetic on the FP64 assembly; the lighter one on the split assembly
+        // one warp per block, so that a small batch still spreads over every SM
         if (p.fused_cdet)
-            cdet_dd_lane<false><<<static_cast<unsigned>((p.batch + 127) / 128), 128, 0, stream>>>(p, w);
+            cdet_dd_lane<false><<<static_cast<unsigned>((p.batch + kWarp - 1) / kWarp), kWarp, 0, stream>>>(p, w);
         else
-            cdet_dd_lane<true><<<static_cast<unsigned>((p.batch + 127) / 128), 128, 0, stream>>>(p, w);
+            cdet_dd_lane<true><<<static_cast<unsigned>((p.batch + kWarp - 1) / kWarp), kWarp, 0, stream>>>(p, w);
         return cudaGetLastError();
     }
     const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(DD);
