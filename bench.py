@@ -86,8 +86,19 @@ def split_dram_bytes(params, lookups: int):
 
 def line_config(head: str, world: int) -> dict:
     """The `config` of the bench line, shared by both arms so that the
-    reference arm's line names the same workload."""
-    return dict(WORKLOAD, path=head, parallelism=f"replicas x{world}",
+    reference arm's line names the same workload (the profiling preset and a
+    non-default batch name themselves)."""
+    if PRESET == "6x6-d96":
+        work = {"workload": f"6x6 Hubbard U=4 beta=5, half-lattice subsystem, Chebyshev degree 96, order n=10, "
+                            f"{BATCH} configurations per step (per GPU): the profiling preset, not the benchmark",
+                "lattice": "6x6", "U": 4, "beta": 5, "mu": 0, "mask": "half lattice", "cheb_degree": 96,
+                "order": ORDER, "batch_per_gpu": BATCH}
+        return dict(work, path=head, parallelism=f"replicas x{world}", l2="flushed between steps (512 MiB write)")
+    work = dict(WORKLOAD)
+    if BATCH != WORKLOAD["batch_per_gpu"]:
+        work["workload"] = work["workload"].replace("65536", str(BATCH))
+        work["batch_per_gpu"] = BATCH
+    return dict(work, path=head, parallelism=f"replicas x{world}",
                 l2="flushed between steps (512 MiB write); tables 8.6 GB > L2")
 
 
