@@ -242,10 +242,10 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
     }
     for (uint32_t step = subsets; step > 1; step >>= 1) {  // the shift removal, bit by bit from the top
         const uint32_t half = step >> 1;
+        const int hb = __ffs(half) - 1;  // half = 2^hb
 #pragma unroll 4
         for (uint32_t q = lane; q < subsets / 2; q += kWarp) {
-            const uint32_t t = q / half;
-            const uint32_t ss = t * step + half + (q - t * half);
+            const uint32_t ss = ((q >> hb) << (hb + 1)) + half + (q & (half - 1u));
             shifted[ss] = sub_prod_t<Exact>(p, shifted[ss - half], shifted[ss]);
         }
         __syncwarp();

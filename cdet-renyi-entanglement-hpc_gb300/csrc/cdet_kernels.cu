@@ -433,7 +433,8 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
         __syncwarp();
         // submatrix without the pivot, and its Schur complement
         const int items = sets * new_msize;
-        for (int item = lane; item < items; item += kWarp) {
+#pragma unroll 4
+        for (int item = lane; item < items; item += kWarp) {  // independent items, several in flight
             const int set = item / new_msize;
             const int e = item - set * new_msize;
             const int row = e / new_size;
@@ -460,6 +461,7 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
     }
     // prefix product over levels
     for (uint32_t step = 1; step < subsets; step <<= 1) {
+#pragma unroll 4
         for (uint32_t set = step + 1 + lane; set < 2 * step; set += kWarp)
             shifted[set] = dmul(shifted[set], shifted[set - step]);
         __syncwarp();
@@ -471,9 +473,10 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
     }
     for (uint32_t step = subsets; step > 1; step >>= 1) {
         const uint32_t half = step >> 1;
+        const int hb = __ffs(half) - 1;  // half = 2^hb: the element's bit hb is set, its partner's clear
+#pragma unroll 4
         for (uint32_t q = lane; q < subsets / 2; q += kWarp) {
-            const uint32_t t = q / half;
-            const uint32_t ss = t * step + half + (q - t * half);
+            const uint32_t ss = ((q >> hb) << (hb + 1)) + half + (q & (half - 1u));
             shifted[ss] = dfma(-p, shifted[ss - half], shifted[ss]);
         }
         __syncwarp();
