@@ -337,7 +337,8 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform vertices)",
-        "config": line_config("split", args.gpus),
+        # the workload's config, with the sample this arm times per step of it
+        "config": dict(line_config("split", args.gpus), reference_batch_per_step=sample),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "batch_per_step": sample,
                          "sample": f"{sample} configurations per step of the workload's 65,536 "
