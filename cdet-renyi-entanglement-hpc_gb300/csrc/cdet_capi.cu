@@ -272,18 +272,24 @@ int slice_branch(cdet_context* ctx, const double* coeffs, size_t blocks, SlicedB
     const size_t sbytes = cdet::split_slices_bytes(s.cheb_nu, s.cheb_nv, blocks);
     const size_t rbytes = cdet::split_level_rows_bytes(s.cheb_nu, s.cheb_nv, blocks);
     const size_t lbytes = cdet::split_leads_bytes(s.cheb_nu, s.cheb_nv, blocks);
+    // then the sub-blocks' tile costs (4-byte aligned)
+    int nrb = 0, nkc = 0, ksteps_last = 0;
+    cdet::split_geometry(s.cheb_nu, s.cheb_nv, &nrb, &nkc, &ksteps_last);
+    const size_t cost_at = (sbytes + rbytes + blocks * sizeof(int32_t) + lbytes + 15) & ~static_cast<size_t>(15);
+    const size_t cbytes = blocks * static_cast<size_t>(nrb) * nkc * sizeof(uint32_t);
     SlicedBranch b;
-    cudaError_t err = cudaMalloc(&b.mem, sbytes + rbytes + blocks * sizeof(int32_t) + lbytes + 256);
+    cudaError_t err = cudaMalloc(&b.mem, cost_at + cbytes + 256);
     if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(split slices)");
     char* base = static_cast<char*>(b.mem);
     b.slices = reinterpret_cast<const uint16_t*>(base);
     b.level_rows = reinterpret_cast<const uint64_t*>(base + sbytes);
     b.exponents = reinterpret_cast<const int32_t*>(base + sbytes + rbytes);
     b.leads = reinterpret_cast<const uint8_t*>(base + sbytes + rbytes + blocks * sizeof(int32_t));
+    b.key_costs = reinterpret_cast<const uint32_t*>(base + cost_at);
     b.blocks = blocks;
     err = cdet::launch_slice_table(coeffs, s.cheb_nu, s.cheb_nv, blocks, const_cast<uint16_t*>(b.slices),
                                    const_cast<int32_t*>(b.exponents), const_cast<uint8_t*>(b.leads),
-                                   const_cast<uint64_t*>(b.level_rows), nullptr);
+                                   const_cast<uint64_t*>(b.level_rows), const_cast<uint32_t*>(b.key_costs), nullptr);
     if (err == cudaSuccess) err = cudaDeviceSynchronize();
     if (err != cudaSuccess) {
         cudaFree(b.mem);
@@ -327,6 +333,7 @@ int build_split_plan(cdet_context* ctx, cdet::SplitPlan* plan) {
                 plan->exponents[seg] = sb->exponents;
                 plan->leads[seg] = sb->leads;
                 plan->level_rows[seg] = sb->level_rows;
+                plan->key_costs[seg] = sb->key_costs;
                 plan->segment_of[set][r][br] = seg;
                 base += static_cast<uint32_t>(blocks * nsub);
                 ++seg;
@@ -568,8 +575,8 @@ int run(cdet_context* ctx, const double* vertices, const int32_t* orders, int64_
             if (rc != CDET_OK) return rc;
             err = cdet::launch_fp64_integrand(p, w, ctx->sm_count, stream, events, false);
             if (err != cudaSuccess) return cuda_fail(err, "kernel launch");
-            // descriptors, scan, scatter, tiles, tensor assembly + minors, CDet (or the queue
-            // kernel, or the double-double kernel)
+            // descriptors, scan, scatter, tiles and per-CTA ranges, tensor assembly + minors,
+            // CDet (or the queue kernel, or the double-double kernel)
             launches = 5 + ((cdet::uses_queue_form(p) || p.dd_mode) ? 1 : 2);
         } else {
             launches = 5;

@@ -31,6 +31,7 @@ struct SlicedBranch {
     const int32_t* exponents = nullptr;
     const uint64_t* level_rows = nullptr;  // rows reaching each accumulator level, per sub-block
     const uint8_t* leads = nullptr;        // first nonzero slice per K step
+    const uint32_t* key_costs = nullptr;   // estimated tile time per sub-block
     size_t blocks = 0;
 };
 

@@ -205,6 +205,7 @@ struct SplitPlan {
     const int32_t* exponents[8];    // binary exponent of each block
     const uint8_t* leads[8];        // first nonzero slice of each K step of each sub-block row
     const uint64_t* level_rows[8];  // per sub-block: rows reaching each accumulator level (a byte per level)
+    const uint32_t* key_costs[8];   // per sub-block: the estimated time of one of its tiles (relative clocks)
     int records_per_set[2];         // 1 when up and down share one table, else 2
     int segment_of[2][2][2];        // [set][record][0 upper, 1 lower] -> segment
     int spin_mask[2][2];            // [set][record] -> spins the record writes
@@ -221,8 +222,12 @@ size_t split_slices_bytes(int nu, int nv, size_t blocks);
 size_t split_leads_bytes(int nu, int nv, size_t blocks);
 // bytes of the per-sub-block level rows of `blocks` blocks (8 per sub-block)
 size_t split_level_rows_bytes(int nu, int nv, size_t blocks);
+// Slices `blocks` coefficient blocks and estimates each sub-block's tile
+// time (key_costs, one uint32 per sub-block, used to balance the assembly's
+// per-CTA tile ranges).
 cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
-                               int32_t* exponents, uint8_t* leads, uint64_t* level_rows, cudaStream_t stream);
+                               int32_t* exponents, uint8_t* leads, uint64_t* level_rows, uint32_t* key_costs,
+                               cudaStream_t stream);
 size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan);
 // Bytes of the split assembly's status region: its error flag (int32 at
 // byte 0) and counters (uint64 at byte 8: the accumulator columns its

@@ -503,45 +503,70 @@ __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__
 
 // Exclusive scan of block counts (offsets) and of their 128-lookup tile counts
 // (tile offsets); one CTA of 1024 threads. totals[0] = lookups, totals[1] = tiles.
-__global__ void __launch_bounds__(1024) split_scan(const uint32_t* __restrict__ counts, uint32_t nblocks,
+// The estimated time of one tile of sub-block `key` (its branch's key_costs).
+__device__ __forceinline__ uint32_t key_cost(const SplitPlan& plan, uint32_t key) {
+    int seg = 0;
+    while (seg + 1 < plan.segments && key >= plan.segment_base[seg + 1]) ++seg;
+    return __ldg(plan.key_costs[seg] + (key - plan.segment_base[seg]));
+}
+
+// Exclusive scans over the keys of their lookup counts (offsets), tile counts
+// (tile_offsets) and estimated tile time (cost_prefix: tiles x key cost);
+// totals[0] = lookups, totals[1] = tiles, totals[2..3] = the time as uint64.
+__global__ void __launch_bounds__(1024) split_scan(const SplitPlan plan, const uint32_t* __restrict__ counts,
                                                    uint32_t* __restrict__ offsets,
                                                    uint32_t* __restrict__ tile_offsets,
                                                    uint32_t* __restrict__ cursors,
+                                                   unsigned long long* __restrict__ cost_prefix,
                                                    uint32_t* __restrict__ totals) {
     __shared__ uint32_t s_sum[1024], s_tiles[1024];
+    __shared__ unsigned long long s_cost[1024];
+    const uint32_t nblocks = plan.nblocks;
     const uint32_t per = (nblocks + 1023) / 1024;
     const uint32_t begin = threadIdx.x * per;
     const uint32_t end = min(nblocks, begin + per);
     uint32_t sum = 0, tiles = 0;
+    unsigned long long cost = 0;
     for (uint32_t b = begin; b < end; ++b) {
-        sum += counts[b];
-        tiles += (counts[b] + kTileN - 1) / kTileN;
+        const uint32_t c = counts[b], m = (c + kTileN - 1) / kTileN;
+        sum += c;
+        tiles += m;
+        if (m) cost += static_cast<unsigned long long>(m) * key_cost(plan, b);
     }
     s_sum[threadIdx.x] = sum;
     s_tiles[threadIdx.x] = tiles;
+    s_cost[threadIdx.x] = cost;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {
         uint32_t a = 0, t = 0;
+        unsigned long long e = 0;
         if (threadIdx.x >= static_cast<unsigned>(off)) {
             a = s_sum[threadIdx.x - off];
             t = s_tiles[threadIdx.x - off];
+            e = s_cost[threadIdx.x - off];
         }
         __syncthreads();
         s_sum[threadIdx.x] += a;
         s_tiles[threadIdx.x] += t;
+        s_cost[threadIdx.x] += e;
         __syncthreads();
     }
     uint32_t run = s_sum[threadIdx.x] - sum, trun = s_tiles[threadIdx.x] - tiles;
+    unsigned long long crun = s_cost[threadIdx.x] - cost;
     for (uint32_t b = begin; b < end; ++b) {
+        const uint32_t c = counts[b], m = (c + kTileN - 1) / kTileN;
         offsets[b] = run;
         tile_offsets[b] = trun;
+        cost_prefix[b] = crun;
         cursors[b] = 0;
-        run += counts[b];
-        trun += (counts[b] + kTileN - 1) / kTileN;
+        run += c;
+        trun += m;
+        if (m) crun += static_cast<unsigned long long>(m) * key_cost(plan, b);
     }
     if (threadIdx.x == 1023) {
         totals[0] = s_sum[1023];
         totals[1] = s_tiles[1023];
+        *reinterpret_cast<unsigned long long*>(totals + 2) = s_cost[1023];
     }
 }
 
@@ -564,16 +589,6 @@ __global__ void __launch_bounds__(256) split_scatter(const SplitRecordArrays rec
     sorted.info[pos] = rec.info[idx];
 }
 
-__global__ void __launch_bounds__(256) split_tiles(const uint32_t* __restrict__ counts, uint32_t nblocks,
-                                                   const uint32_t* __restrict__ offsets,
-                                                   const uint32_t* __restrict__ tile_offsets,
-                                                   SplitTile* __restrict__ tiles) {
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nblocks) return;
-    const uint32_t n = counts[b];
-    uint32_t t = tile_offsets[b];
-    for (uint32_t s = 0; s < n; s += kTileN, ++t) tiles[t] = SplitTile{b, offsets[b] + s, min(kTileN * 1u, n - s), 0};
-}
 
 // ------------------------------------------------------------- assembly --
 // Warp-specialised persistent kernel, one CTA of 14 warps per SM. A tile is
@@ -877,6 +892,93 @@ __device__ __forceinline__ void issue_kstep(const uint32_t (&d)[kLevels], const 
     }
 }
 
+// The time a tile takes, estimated from its sub-block (in clocks, roughly):
+// the MMA phase (each MMA moves its 128 x 16 basis slice and its N x 16
+// coefficient slice at ~128 B per clock, about twice that in the loaded
+// kernel) and, after it, the epilogue (~3.6 K clocks per 16-column chunk of
+// rows some level below 7 reaches, ~0.6 K per chunk of the others, ~1.5 K
+// to finish). Only the relative costs matter: they split the tile list into
+// per-CTA ranges of equal estimated time.
+template <bool Chunked>
+__device__ uint32_t tile_cost(const SplitPlan& plan, uint32_t key) {
+    const TileSource src = tile_source<Chunked>(plan, key);
+    const uint64_t packed = __ldg(src.rows);
+    const int npass = pass_geom(packed, 0).npass;
+    uint32_t cost = 0;
+    for (int pass = 0; pass < npass; ++pass) {
+        const PassGeom g = pass_geom(packed, pass);
+        uint32_t mma = 0, cols = 0;
+        for (int ks = 0; ks < src.ksteps; ++ks) {
+            const int lead = step_lead(src.leads, ks);
+            for (int i = 0; i < kIssue; ++i) {
+                const int t = kIssueT[i], tp = kIssueTp[i];
+                if (t < lead) continue;
+                const int lv = t == 8 ? kLevels - 1 : t + tp - 2;
+                ++mma;
+                cols += static_cast<uint32_t>(g.n[lv]);
+            }
+        }
+        const int head = min(g.n[kLevels - 3], g.cols) / 16;
+        const int tail = (g.cols - min(g.n[kLevels - 3], g.cols)) / 16;
+        cost += 2u * (32u * mma + cols / 4u) + 3600u * head + 580u * tail + 1500u;
+    }
+    return cost;
+}
+
+// Each sub-block's estimated tile time, once per sliced branch (`plan` holds
+// that branch alone as its one segment).
+template <bool Chunked>
+__global__ void __launch_bounds__(256) split_key_costs(const SplitPlan plan, uint32_t* __restrict__ costs) {
+    const uint32_t key = blockIdx.x * blockDim.x + threadIdx.x;
+    if (key < plan.nblocks) costs[key] = tile_cost<Chunked>(plan, key);
+}
+
+// The tile list and the per-CTA tile ranges, one thread per key (sub-block).
+// Each key's lookups go into tiles of up to 128. CTA b of the assembly takes
+// the tiles ranges[b] .. ranges[b + 1] of the block-sorted list, a
+// contiguous part of (nearly) equal estimated time: a tile weighs its key's
+// cost plus the mean cost (half the tile count's share, half the estimate's:
+// measured, that balances the CTAs better than either alone). With C(t) the
+// weight of the tiles before tile t and T the total, CTA b starts at the
+// first tile with C(t) >= thr(b) = ceil(T * b / ctas). Key q's tiles cover
+// the weights [P(q), P(q + 1)) with P(q) = cost_prefix[q] + mean *
+// tile_offsets[q], so the key writes the starts of the CTAs whose thr falls
+// there; thread 0 writes the CTAs past the last tile (and ranges[ctas]).
+__global__ void __launch_bounds__(256) split_tiles(const SplitPlan plan, const uint32_t* __restrict__ counts,
+                                                   const uint32_t* __restrict__ offsets,
+                                                   const uint32_t* __restrict__ tile_offsets,
+                                                   const unsigned long long* __restrict__ cost_prefix,
+                                                   const uint32_t* __restrict__ totals, int ctas,
+                                                   SplitTile* __restrict__ tiles, uint32_t* __restrict__ ranges) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t ntiles = totals[1];
+    const unsigned long long n = static_cast<unsigned long long>(ctas);
+    if (ntiles == 0) {
+        if (b <= static_cast<uint32_t>(ctas)) ranges[b] = 0;
+        return;
+    }
+    const unsigned long long raw = *reinterpret_cast<const unsigned long long*>(totals + 2);
+    const unsigned long long mean = raw / ntiles, total = raw + mean * ntiles;
+    if (b == 0)
+        for (unsigned long long c = (total - 1) * n / total + 1; c <= n; ++c) ranges[c] = ntiles;
+    if (b >= plan.nblocks) return;
+    const uint32_t cnt = counts[b];
+    if (cnt == 0) return;
+    uint32_t t = tile_offsets[b];
+    for (uint32_t s = 0; s < cnt; s += kTileN, ++t) tiles[t] = SplitTile{b, offsets[b] + s, min(kTileN * 1u, cnt - s), 0};
+    const uint32_t m = (cnt + kTileN - 1) / kTileN;
+    const unsigned long long wq = key_cost(plan, b) + mean;
+    const unsigned long long p0 = cost_prefix[b] + mean * tile_offsets[b], p1 = p0 + m * wq;
+    // CTAs c with p0 <= ceil(T * c / n) < p1
+    const unsigned long long c_lo = p0 == 0 ? 0 : (p0 - 1) * n / total + 1;
+    const unsigned long long c_hi = min((p1 - 1) * n / total, n - 1);
+    for (unsigned long long c = c_lo; c <= c_hi; ++c) {
+        const unsigned long long thr = (total * c + n - 1) / n;
+        const unsigned long long j = thr > p0 ? (thr - p0 + wq - 1) / wq : 0;
+        ranges[c] = tile_offsets[b] + static_cast<uint32_t>(j);
+    }
+}
+
 template <bool Chunked>
 __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __grid_constant__ Problem p,
                                                                       const __grid_constant__ Scratch w,
@@ -886,19 +988,18 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
                                                                       const uint32_t* __restrict__ totals,
                                                                       int64_t* __restrict__ parts,
                                                                       int32_t* __restrict__ error_flag,
-                                                                      unsigned long long* __restrict__ counters) {
+                                                                      unsigned long long* __restrict__ counters,
+                                                                      const uint32_t* __restrict__ ranges) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SplitShared& sh = *reinterpret_cast<SplitShared*>(smem_raw);
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
     const int lane = tid & 31;
-    const uint32_t ntiles = totals[1];
-    // each CTA takes a contiguous range of the block-sorted tile list, so the
-    // later tiles of a coefficient block find its slices in L2
-    const uint32_t tile_begin =
-        static_cast<uint32_t>((static_cast<uint64_t>(ntiles) * blockIdx.x) / gridDim.x);
-    const uint32_t tile_end =
-        static_cast<uint32_t>((static_cast<uint64_t>(ntiles) * (blockIdx.x + 1)) / gridDim.x);
+    // each CTA takes a contiguous range of the block-sorted tile list (so the
+    // later tiles of a coefficient block find its slices in L2), the ranges
+    // of equal estimated time (split_tiles writes them)
+    const uint32_t tile_begin = ranges[blockIdx.x];
+    const uint32_t tile_end = max(tile_begin, ranges[blockIdx.x + 1]);
 
     if (tid == 0) {
         for (int i = 0; i < kCStages; ++i) {
@@ -1430,7 +1531,8 @@ size_t split_level_rows_bytes(int nu, int nv, size_t blocks) {
 }
 
 cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t blocks, uint16_t* slices,
-                               int32_t* exponents, uint8_t* leads, uint64_t* level_rows, cudaStream_t stream) {
+                               int32_t* exponents, uint8_t* leads, uint64_t* level_rows, uint32_t* key_costs,
+                               cudaStream_t stream) {
     if (blocks == 0) return cudaSuccess;
     int nrb, nkc, ksteps_last;
     split_geometry(nu, nv, &nrb, &nkc, &ksteps_last);
@@ -1438,6 +1540,26 @@ cudaError_t launch_slice_table(const double* coeffs, int nu, int nv, size_t bloc
     if (grid > 0x7FFFFFFFu) return cudaErrorInvalidValue;
     slice_blocks<<<static_cast<unsigned>(grid), 256, 0, stream>>>(coeffs, nu, nv, nrb, nkc, ksteps_last, slices,
                                                                   exponents, leads, level_rows);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    // the branch alone as a one-segment plan: its sub-blocks' tile costs
+    SplitPlan one{};
+    one.segments = 1;
+    one.segment_base[0] = 0;
+    one.segment_base[1] = static_cast<uint32_t>(grid);
+    one.slices[0] = slices;
+    one.exponents[0] = exponents;
+    one.leads[0] = leads;
+    one.level_rows[0] = level_rows;
+    one.nblocks = static_cast<uint32_t>(grid);
+    one.nrb = nrb;
+    one.nkc = nkc;
+    one.ksteps_last = ksteps_last;
+    const unsigned cgrid = static_cast<unsigned>((grid + 255) / 256);
+    if (nrb * nkc > 1)
+        split_key_costs<true><<<cgrid, 256, 0, stream>>>(one, key_costs);
+    else
+        split_key_costs<false><<<cgrid, 256, 0, stream>>>(one, key_costs);
     return cudaGetLastError();
 }
 
@@ -1448,10 +1570,12 @@ size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan) 
     total += nrec * (4 + 8 + 8 + 8);          // unsorted records
     total += nrec * (8 + 8 + 8);              // sorted records
     total += static_cast<size_t>(plan.nblocks) * 4 * 4;  // counts, offsets, tile offsets, cursors
+    total += static_cast<size_t>(plan.nblocks) * 8;      // estimated-time prefix
     total += (nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile);  // tiles
     if (nsub > 1) total += nrec * 16;         // 128-bit sub-block parts
-    total += 16 + kSplitStatusBytes;          // totals, error flag and counters
-    return total + 16 * 256;
+    total += 32 + kSplitStatusBytes;          // totals, error flag and counters
+    total += (1024 + 1) * 4;                  // per-CTA tile ranges (up to 1,024 SMs)
+    return total + 18 * 256;
 }
 
 cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const SplitPlan& plan, void* scratch,
@@ -1474,9 +1598,11 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     uint32_t* offsets = static_cast<uint32_t*>(take(plan.nblocks * 4u));
     uint32_t* tile_offsets = static_cast<uint32_t*>(take(plan.nblocks * 4u));
     uint32_t* cursors = static_cast<uint32_t*>(take(plan.nblocks * 4u));
+    unsigned long long* cost_prefix = static_cast<unsigned long long*>(take(plan.nblocks * 8u));
     SplitTile* tiles = static_cast<SplitTile*>(take((nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile)));
     int64_t* parts = nsub > 1 ? static_cast<int64_t*>(take(nrec * 16)) : nullptr;
-    uint32_t* totals = static_cast<uint32_t*>(take(16));
+    uint32_t* totals = static_cast<uint32_t*>(take(32));
+    uint32_t* ranges = static_cast<uint32_t*>(take((static_cast<size_t>(sm_count) + 1) * 4));
     // the error flag (int32 at byte 0) and the assembly's counters (uint64 at
     // bytes 8 and 16: MMAs issued, coefficient-slice bytes streamed)
     int32_t* error_flag = static_cast<int32_t*>(take(kSplitStatusBytes));
@@ -1490,13 +1616,14 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     if (err != cudaSuccess) return err;
     split_descriptors<<<static_cast<unsigned>((pairs + 127) / 128), 128, 0, stream>>>(p, w, plan, rec, counts);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    split_scan<<<1, 1024, 0, stream>>>(counts, plan.nblocks, offsets, tile_offsets, cursors, totals);
+    split_scan<<<1, 1024, 0, stream>>>(plan, counts, offsets, tile_offsets, cursors, cost_prefix, totals);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     split_scatter<<<static_cast<unsigned>((nrec + 255) / 256), 256, 0, stream>>>(rec, nrec, offsets, cursors,
                                                                                  sorted);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    split_tiles<<<(plan.nblocks + 255) / 256, 256, 0, stream>>>(counts, plan.nblocks, offsets, tile_offsets,
-                                                                tiles);
+    const uint32_t tile_threads = std::max(plan.nblocks, static_cast<uint32_t>(sm_count) + 1);
+    split_tiles<<<(tile_threads + 255) / 256, 256, 0, stream>>>(plan, counts, offsets, tile_offsets, cost_prefix,
+                                                                totals, sm_count, tiles, ranges);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     if (events && events->marks[1]) cudaEventRecord(events->marks[1], stream);
     const size_t smem = sizeof(SplitShared);
@@ -1504,7 +1631,7 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (err != cudaSuccess) return err;
     kernel<<<sm_count, kAssemblyThreads, smem, stream>>>(p, w, plan, sorted, tiles, totals, parts, error_flag,
-                                                         counters);
+                                                         counters, ranges);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     if (nsub > 1) {
         split_combine<<<static_cast<unsigned>((pairs + 127) / 128), 128, 0, stream>>>(p, w, plan, rec, parts);
