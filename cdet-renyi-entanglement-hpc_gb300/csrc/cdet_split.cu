@@ -513,60 +513,92 @@ __device__ __forceinline__ uint32_t key_cost(const SplitPlan& plan, uint32_t key
 // Exclusive scans over the keys of their lookup counts (offsets), tile counts
 // (tile_offsets) and estimated tile time (cost_prefix: tiles x key cost);
 // totals[0] = lookups, totals[1] = tiles, totals[2..3] = the time as uint64.
+// One block of 32 warps, each a contiguous chunk of the keys read 32 at a
+// time (coalesced), a warp scan by shuffles carrying the running sums.
+struct KeySums {
+    uint32_t lookups, tiles;
+    unsigned long long cost;
+};
+
+__device__ __forceinline__ KeySums key_sums(const SplitPlan& plan, const uint32_t* counts, uint32_t b, uint32_t end) {
+    KeySums k{0, 0, 0};
+    if (b < end) {
+        k.lookups = counts[b];
+        k.tiles = (k.lookups + kTileN - 1) / kTileN;
+        if (k.tiles) k.cost = static_cast<unsigned long long>(k.tiles) * key_cost(plan, b);
+    }
+    return k;
+}
+
 __global__ void __launch_bounds__(1024) split_scan(const SplitPlan plan, const uint32_t* __restrict__ counts,
                                                    uint32_t* __restrict__ offsets,
                                                    uint32_t* __restrict__ tile_offsets,
                                                    uint32_t* __restrict__ cursors,
                                                    unsigned long long* __restrict__ cost_prefix,
                                                    uint32_t* __restrict__ totals) {
-    __shared__ uint32_t s_sum[1024], s_tiles[1024];
-    __shared__ unsigned long long s_cost[1024];
+    __shared__ KeySums s_warp[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t nblocks = plan.nblocks;
-    const uint32_t per = (nblocks + 1023) / 1024;
-    const uint32_t begin = threadIdx.x * per;
-    const uint32_t end = min(nblocks, begin + per);
-    uint32_t sum = 0, tiles = 0;
-    unsigned long long cost = 0;
-    for (uint32_t b = begin; b < end; ++b) {
-        const uint32_t c = counts[b], m = (c + kTileN - 1) / kTileN;
-        sum += c;
-        tiles += m;
-        if (m) cost += static_cast<unsigned long long>(m) * key_cost(plan, b);
+    const uint32_t chunk = ((nblocks + 32 * 32 - 1) / (32 * 32)) * 32;  // keys per warp, a multiple of 32
+    const uint32_t begin = min(nblocks, warp * chunk), end = min(nblocks, begin + chunk);
+    // pass 1: the warp's sums
+    KeySums mine{0, 0, 0};
+    for (uint32_t b = begin + lane; b < end; b += 32) {
+        const KeySums k = key_sums(plan, counts, b, end);
+        mine.lookups += k.lookups;
+        mine.tiles += k.tiles;
+        mine.cost += k.cost;
     }
-    s_sum[threadIdx.x] = sum;
-    s_tiles[threadIdx.x] = tiles;
-    s_cost[threadIdx.x] = cost;
+    for (int off = 16; off > 0; off >>= 1) {
+        mine.lookups += __shfl_xor_sync(0xffffffffu, mine.lookups, off);
+        mine.tiles += __shfl_xor_sync(0xffffffffu, mine.tiles, off);
+        mine.cost += __shfl_xor_sync(0xffffffffu, mine.cost, off);
+    }
+    if (lane == 0) s_warp[warp] = mine;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t a = 0, t = 0;
-        unsigned long long e = 0;
-        if (threadIdx.x >= static_cast<unsigned>(off)) {
-            a = s_sum[threadIdx.x - off];
-            t = s_tiles[threadIdx.x - off];
-            e = s_cost[threadIdx.x - off];
+    KeySums run{0, 0, 0};
+    for (int w = 0; w < warp; ++w) {
+        run.lookups += s_warp[w].lookups;
+        run.tiles += s_warp[w].tiles;
+        run.cost += s_warp[w].cost;
+    }
+    if (threadIdx.x == 0) {
+        KeySums all{0, 0, 0};
+        for (int w = 0; w < 32; ++w) {
+            all.lookups += s_warp[w].lookups;
+            all.tiles += s_warp[w].tiles;
+            all.cost += s_warp[w].cost;
         }
-        __syncthreads();
-        s_sum[threadIdx.x] += a;
-        s_tiles[threadIdx.x] += t;
-        s_cost[threadIdx.x] += e;
-        __syncthreads();
+        totals[0] = all.lookups;
+        totals[1] = all.tiles;
+        *reinterpret_cast<unsigned long long*>(totals + 2) = all.cost;
     }
-    uint32_t run = s_sum[threadIdx.x] - sum, trun = s_tiles[threadIdx.x] - tiles;
-    unsigned long long crun = s_cost[threadIdx.x] - cost;
-    for (uint32_t b = begin; b < end; ++b) {
-        const uint32_t c = counts[b], m = (c + kTileN - 1) / kTileN;
-        offsets[b] = run;
-        tile_offsets[b] = trun;
-        cost_prefix[b] = crun;
-        cursors[b] = 0;
-        run += c;
-        trun += m;
-        if (m) crun += static_cast<unsigned long long>(m) * key_cost(plan, b);
-    }
-    if (threadIdx.x == 1023) {
-        totals[0] = s_sum[1023];
-        totals[1] = s_tiles[1023];
-        *reinterpret_cast<unsigned long long*>(totals + 2) = s_cost[1023];
+    // pass 2: the exclusive prefixes, 32 keys a round
+    KeySums next = key_sums(plan, counts, begin + lane, end);
+    for (uint32_t b0 = begin; b0 < end; b0 += 32) {
+        const KeySums k = next;
+        next = key_sums(plan, counts, b0 + 32 + lane, end);  // the next round's keys, in flight meanwhile
+        KeySums incl = k;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t a = __shfl_up_sync(0xffffffffu, incl.lookups, off);
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl.tiles, off);
+            const unsigned long long c = __shfl_up_sync(0xffffffffu, incl.cost, off);
+            if (lane >= off) {
+                incl.lookups += a;
+                incl.tiles += t;
+                incl.cost += c;
+            }
+        }
+        const uint32_t b = b0 + lane;
+        if (b < end) {
+            offsets[b] = run.lookups + incl.lookups - k.lookups;
+            tile_offsets[b] = run.tiles + incl.tiles - k.tiles;
+            cost_prefix[b] = run.cost + incl.cost - k.cost;
+            cursors[b] = 0;
+        }
+        run.lookups += __shfl_sync(0xffffffffu, incl.lookups, 31);
+        run.tiles += __shfl_sync(0xffffffffu, incl.tiles, 31);
+        run.cost += __shfl_sync(0xffffffffu, incl.cost, 31);
     }
 }
 
