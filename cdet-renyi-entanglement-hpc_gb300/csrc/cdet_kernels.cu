@@ -394,9 +394,12 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
     }
     const double fallback_eps = (tol > 0.0 && max_abs > 0.0) ? dmul(tol, max_abs) : 0.0;
 
+    // A node's pivot inverse replaces its pivot entry and its first-column
+    // factors replace column 0 of rows 1.. (the children take only rows and
+    // columns 1.., and the first minor has read the pivot entry already), so
+    // the recursion needs no space besides its two lists.
     double* old_list = ws + lay.old_list;
     double* new_list = ws + lay.new_list;
-    double* inv = ws + lay.aux;
     for (int k = lane; k < msize; k += kWarp) old_list[k] = A[k];
     for (uint32_t m = lane; m < subsets; m += kWarp) shifted[m] = m == 0 ? 1.0 : p;
     __syncwarp();
@@ -416,19 +419,20 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
             const double pivot = dadd(old_list[set * old_msize], p);
             const double pa = fabs(pivot);
             if (pa == 0.0 || (fallback_eps > 0.0 && pa <= fallback_eps)) bad_pivot = true;
-            inv[set] = __drcp_rn(pivot);  // 1.0 / pivot, correctly rounded (IEEE): the same value
+            // 1.0 / pivot, correctly rounded (IEEE): the same value
+            old_list[set * old_msize] = __drcp_rn(pivot);
         }
         if (__any_sync(0xffffffffu, bad_pivot)) {
             fell_back = true;
             break;
         }
         __syncwarp();
-        // first-column factors, one per (set, row)
-        double* factor = inv + sets;
+        // first-column factors, one per (set, row), in place of the column
         for (int item = lane; item < sets * new_size; item += kWarp) {
             const int set = item / new_size;
             const int row = item - set * new_size;
-            factor[item] = dmul(old_list[set * old_msize + (row + 1) * old_size], inv[set]);
+            double* entry = old_list + set * old_msize + (row + 1) * old_size;
+            *entry = dmul(*entry, old_list[set * old_msize]);
         }
         __syncwarp();
         // submatrix without the pivot, and its Schur complement
@@ -442,7 +446,7 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
             const int src = set * old_msize;
             const double base = old_list[src + (row + 1) * old_size + col + 1];
             new_list[item] = base;
-            new_list[items + item] = dfma(-old_list[src + 1 + col], factor[set * new_size + row], base);
+            new_list[items + item] = dfma(-old_list[src + 1 + col], old_list[src + (row + 1) * old_size], base);
         }
         __syncwarp();
         for (int m = lane; m < 2 * sets; m += kWarp)
@@ -514,6 +518,12 @@ __host__ __device__ inline ChunkGeom chunk_geom(int n) {
 }
 
 constexpr int kChunkMinOrder = 11, kChunkMaxOrder = 14;
+
+// The FP64 minors' workspace of a batch of orders up to nmax: the aux region
+// only where the chunked recursion can run (mat2pm_warp needs none).
+__host__ __device__ inline WsLayout fp64_minors_layout(int nmax, bool two_spins) {
+    return ws_layout(nmax, two_spins, nmax >= kChunkMinOrder);
+}
 
 // Shared doubles per warp of the chunked minors for a batch of orders up to nmax.
 __host__ __device__ inline int chunk_doubles_upto(int nmax) {
@@ -684,7 +694,7 @@ __global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_consta
     const int64_t total_warps = static_cast<int64_t>(gridDim.x) * warps_per_block;
     const int nmax = p.max_order;
     // the global workspace is laid out for two spins; shared memory for what the sets need
-    const WsLayout lay = ws_layout(nmax, use_smem != 1 || !(p.same_spin[0] && p.same_spin[1]));
+    const WsLayout lay = fp64_minors_layout(nmax, use_smem != 1 || !(p.same_spin[0] && p.same_spin[1]));
     double* ws = use_smem == 1 ? smem + static_cast<size_t>(warp_in_block) * lay.total
                                : w.ws_global + static_cast<size_t>(global_warp) * lay.total;
     double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
@@ -1563,7 +1573,7 @@ __global__ void __launch_bounds__(256) integrand_queue(const __grid_constant__ P
     const int warps_per_block = blockDim.x / kWarp;
     const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
     const int nmax = p.max_order;
-    const WsLayout lay = ws_layout(nmax, !(p.same_spin[0] && p.same_spin[1]));
+    const WsLayout lay = fp64_minors_layout(nmax, !(p.same_spin[0] && p.same_spin[1]));
     double* ws = queue_smem + static_cast<size_t>(warp_in_block) * lay.total;
     double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
     uint32_t* head = w.order_count + kQueueHeadIndex;
@@ -1623,7 +1633,7 @@ size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).tot
 // Warps of the minors kernel whose workspaces fit one block's shared memory
 // (at most 8); the kernel uses shared memory when this is at least 4.
 static int minors_warps_in_shared_memory(int max_order, bool two_spins) {
-    const size_t ws_bytes = ws_layout(max_order, two_spins).total * sizeof(double);
+    const size_t ws_bytes = fp64_minors_layout(max_order, two_spins).total * sizeof(double);
     const size_t smem_budget = 227 * 1024;
     return static_cast<int>(std::min<size_t>(8, smem_budget / ws_bytes));
 }
@@ -1771,7 +1781,7 @@ static cudaError_t post_assembly(const Problem& p_in, const Scratch& w, int sm_c
     // most 8; without the spin-down minors when both sets have one spin),
     // otherwise to the global workspace (4 warps per block).
     const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
-    const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(double);
+    const size_t ws_bytes = fp64_minors_layout(p.max_order, two_spins).total * sizeof(double);
     const int fit = minors_warps_in_shared_memory(p.max_order, two_spins);
     const bool use_smem = fit >= 4;
     // orders 11..14 in the global workspace: the chunked recursion, eight
@@ -1867,7 +1877,7 @@ bool sorts_orders(const Problem& p) {
 void queue_launch_shape(const Problem& p, const Scratch& w, int sm_count, int* warps_per_block, int* blocks,
                         size_t* smem) {
     const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
-    const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(double);
+    const size_t ws_bytes = fp64_minors_layout(p.max_order, two_spins).total * sizeof(double);
     const size_t sm_bytes = 227 * 1024;  // shared memory of one SM this kernel can use (a block's limit too)
     const int sms = sm_count > 0 ? sm_count : 152;
     int per_sm = static_cast<int>(std::min<size_t>(32, sm_bytes / (ws_bytes + 16)));

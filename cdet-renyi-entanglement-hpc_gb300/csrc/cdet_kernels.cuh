@@ -62,8 +62,11 @@ struct WsLayout {
 };
 
 // two_spins = false when both sets evaluate one spin only (up and down tables
-// and shifts identical): the spin-down minors then need no space.
-__host__ __device__ inline WsLayout ws_layout(int nmax, bool two_spins = true) {
+// and shifts identical): the spin-down minors then need no space. with_aux =
+// false leaves out the pivots' inverses and factors (aux): the FP64 warp
+// recursion keeps them in its lists, only the chunked recursion of orders
+// 11..14 and the double-double one need the region.
+__host__ __device__ inline WsLayout ws_layout(int nmax, bool two_spins = true, bool with_aux = true) {
     WsLayout l;
     size_t list = static_cast<size_t>(nmax) * nmax;
     for (int level = 0; level < nmax - 1; ++level) {
@@ -78,7 +81,7 @@ __host__ __device__ inline WsLayout ws_layout(int nmax, bool two_spins = true) {
     l.old_list = even(static_cast<size_t>(nmax) * nmax);
     l.new_list = l.old_list + even(list);
     l.aux = l.new_list + even(list);
-    l.shifted_up = l.aux + even(subsets / 2 + 2);
+    l.shifted_up = l.aux + (with_aux ? even(subsets / 2 + 2) : 0);
     l.shifted_down = l.shifted_up + subsets;
     l.total = two_spins ? l.shifted_down + subsets : l.shifted_down;
     return l;
