@@ -370,7 +370,10 @@ __device__ __forceinline__ void remove_shift_blocked(double* shifted, int n, dou
 // mat2pm_from_buffer (fast_principle_minors.h:120-246) for one matrix, by a
 // whole warp. On return shifted[mask] (mask >= 1) holds the principal minor
 // of the rows/columns in mask. Returns true when a pivot sent the matrix to
-// the whole-matrix LU fallback (which this function then also runs).
+// the whole-matrix LU fallback (which this function then also runs). With
+// the compact layout (lay.arena > 0) the level lists live in shifted's arena
+// (compact_minors_layout), and each shifted minor is written once as p + its
+// pivot entry, the value the initialise-then-add form gives.
 __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_param,
                             const WsLayout& lay, double* ws, double* shifted, double* lu_lane,
                             int lane) {
@@ -398,12 +401,17 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
     // factors replace column 0 of rows 1.. (the children take only rows and
     // columns 1.., and the first minor has read the pivot entry already), so
     // the recursion needs no space besides its two lists.
-    double* old_list = ws + lay.old_list;
-    double* new_list = ws + lay.new_list;
+    const bool compact = lay.arena > 0;
+    double* old_list = compact ? shifted + compact_list_offset(n, 0, lay.arena) : ws + lay.old_list;
+    double* new_list = compact ? nullptr : ws + lay.new_list;
     for (int k = lane; k < msize; k += kWarp) old_list[k] = A[k];
-    for (uint32_t m = lane; m < subsets; m += kWarp) shifted[m] = m == 0 ? 1.0 : p;
+    if (compact) {
+        if (lane == 0) shifted[0] = 1.0;
+    } else {
+        for (uint32_t m = lane; m < subsets; m += kWarp) shifted[m] = m == 0 ? 1.0 : p;
+    }
     __syncwarp();
-    if (lane == 0) shifted[1] = dadd(shifted[1], old_list[0]);
+    if (lane == 0) shifted[1] = dadd(compact ? p : shifted[1], old_list[0]);
 
     uint32_t minor_index = 2;
     bool fell_back = false;
@@ -435,6 +443,21 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
             *entry = dmul(*entry, old_list[set * old_msize]);
         }
         __syncwarp();
+        if (compact) {
+            if (level == n - 2) {
+                // the last level's 1 x 1 children, straight to their shifted minors
+                for (int set = lane; set < sets; set += kWarp) {
+                    const double* m = old_list + set * 4;
+                    const double base = m[3];
+                    shifted[minor_index + set] = dadd(p, base);
+                    shifted[minor_index + sets + set] = dadd(p, dfma(-m[1], m[2], base));
+                }
+                __syncwarp();
+                minor_index += 2 * sets;
+                break;
+            }
+            new_list = shifted + compact_list_offset(n, level + 1, lay.arena);
+        }
         // submatrix without the pivot, and its Schur complement
         const int items = sets * new_msize;
 #pragma unroll 4
@@ -450,7 +473,7 @@ __device__ bool mat2pm_warp(const double* A, int n, double tol, double shift_par
         }
         __syncwarp();
         for (int m = lane; m < 2 * sets; m += kWarp)
-            shifted[minor_index + m] = dadd(shifted[minor_index + m], new_list[m * new_msize]);
+            shifted[minor_index + m] = dadd(compact ? p : shifted[minor_index + m], new_list[m * new_msize]);
         minor_index += 2 * sets;
         double* t = old_list;
         old_list = new_list;
@@ -523,6 +546,13 @@ constexpr int kChunkMinOrder = 11, kChunkMaxOrder = 14;
 // only where the chunked recursion can run (mat2pm_warp needs none).
 __host__ __device__ inline WsLayout fp64_minors_layout(int nmax, bool two_spins) {
     return ws_layout(nmax, two_spins, nmax >= kChunkMinOrder);
+}
+
+// The FP64 warp minors' workspace: compact up to order 10 in shared memory,
+// else the list layout above.
+__host__ __device__ inline WsLayout minors_layout(int nmax, bool two_spins, bool shared) {
+    return shared && nmax <= kCompactMaxOrder ? compact_minors_layout(nmax, two_spins)
+                                              : fp64_minors_layout(nmax, two_spins);
 }
 
 // Shared doubles per warp of the chunked minors for a batch of orders up to nmax.
@@ -683,7 +713,7 @@ __device__ bool mat2pm_chunked(const double* A, int n, double tol, double shift_
 // use_smem: 1 = the whole workspace in shared memory; 0 = in the global
 // workspace; 2 = chunked (orders 11..14): lists of the chunks in shared
 // memory, the top levels' lists and the shifted minors in the global workspace.
-__global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(384) principal_minors_fp64(const __grid_constant__ Problem p,
                                                             const __grid_constant__ Scratch w,
                                                             int use_smem) {
     extern __shared__ double smem[];
@@ -693,8 +723,9 @@ __global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_consta
     const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
     const int64_t total_warps = static_cast<int64_t>(gridDim.x) * warps_per_block;
     const int nmax = p.max_order;
-    // the global workspace is laid out for two spins; shared memory for what the sets need
-    const WsLayout lay = fp64_minors_layout(nmax, use_smem != 1 || !(p.same_spin[0] && p.same_spin[1]));
+    // the global workspace is laid out for two spins; shared memory for what
+    // the sets need, compact up to order 10 (A then read from the Green matrices)
+    const WsLayout lay = minors_layout(nmax, use_smem != 1 || !(p.same_spin[0] && p.same_spin[1]), use_smem == 1);
     double* ws = use_smem == 1 ? smem + static_cast<size_t>(warp_in_block) * lay.total
                                : w.ws_global + static_cast<size_t>(global_warp) * lay.total;
     double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
@@ -712,16 +743,21 @@ __global__ void __launch_bounds__(256) principal_minors_fp64(const __grid_consta
         const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
         if (n < 2 || n > nmax) continue;  // order 1 needs no minors; bad orders are flagged by step 1
         const double* green = w.green + (c * 2 + set) * 2 * static_cast<int64_t>(nmax) * nmax;
-        double* A = ws + lay.a;
         bool fb = false;
-        for (int k = lane; k < n * n; k += kWarp) A[k] = green[k];
-        __syncwarp();
-        fb |= minors(A, n, ws + lay.shifted_up);
         const bool one_spin = p.same_spin[set] != 0;
-        if (!one_spin) {
-            for (int k = lane; k < n * n; k += kWarp) A[k] = green[static_cast<int64_t>(nmax) * nmax + k];
+        if (lay.arena > 0) {
+            fb |= minors(green, n, ws + lay.shifted_up);
+            if (!one_spin) fb |= minors(green + static_cast<int64_t>(nmax) * nmax, n, ws + lay.shifted_down);
+        } else {
+            double* A = ws + lay.a;
+            for (int k = lane; k < n * n; k += kWarp) A[k] = green[k];
             __syncwarp();
-            fb |= minors(A, n, ws + lay.shifted_down);
+            fb |= minors(A, n, ws + lay.shifted_up);
+            if (!one_spin) {
+                for (int k = lane; k < n * n; k += kWarp) A[k] = green[static_cast<int64_t>(nmax) * nmax + k];
+                __syncwarp();
+                fb |= minors(A, n, ws + lay.shifted_down);
+            }
         }
         const double* su = ws + lay.shifted_up;
         const double* sd = one_spin ? su : ws + lay.shifted_down;
@@ -1519,17 +1555,24 @@ __device__ __forceinline__ DD queue_set_value(const Problem& p, const Scratch& w
         return DD{order1_value(s, diag[(set * 2) * nmax], diag[(set * 2 + 1) * nmax], set == 0 ? 2 : 1), 0.0};
     }
     const double* green = w.green + (c * 2 + set) * 2 * static_cast<int64_t>(nmax) * nmax;
-    double* A = ws + lay.a;
+    const bool compact = lay.arena > 0;  // A read from the Green matrices, else copied in
+    double* A = compact ? nullptr : ws + lay.a;
     bool fb = false;
-    for (int k = lane; k < n * n; k += kWarp) A[k] = green[k];
-    __syncwarp();
+    if (!compact) {
+        for (int k = lane; k < n * n; k += kWarp) A[k] = green[k];
+        __syncwarp();
+    }
     double* su = ws + lay.shifted_up;
-    fb |= mat2pm_warp(A, n, s.tol_fpm, s.fpm_shift, lay, ws, su, lu_lane, lane);
+    fb |= mat2pm_warp(compact ? green : A, n, s.tol_fpm, s.fpm_shift, lay, ws, su, lu_lane, lane);
     const bool one_spin = p.same_spin[set] != 0;
     if (!one_spin) {
-        for (int k = lane; k < n * n; k += kWarp) A[k] = green[static_cast<int64_t>(nmax) * nmax + k];
-        __syncwarp();
-        fb |= mat2pm_warp(A, n, s.tol_fpm, s.fpm_shift, lay, ws, ws + lay.shifted_down, lu_lane, lane);
+        const double* green_down = green + static_cast<int64_t>(nmax) * nmax;
+        if (!compact) {
+            for (int k = lane; k < n * n; k += kWarp) A[k] = green_down[k];
+            __syncwarp();
+        }
+        fb |= mat2pm_warp(compact ? green_down : A, n, s.tol_fpm, s.fpm_shift, lay, ws, ws + lay.shifted_down,
+                          lu_lane, lane);
     }
     const double* sd = one_spin ? su : ws + lay.shifted_down;
     const uint32_t count = 1u << n;
@@ -1565,7 +1608,7 @@ __device__ __forceinline__ void pair_barrier(int pair) {
 }
 
 template <bool Fused, bool Pair>
-__global__ void __launch_bounds__(256) integrand_queue(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(384) integrand_queue(const __grid_constant__ Problem p,
                                                       const __grid_constant__ Scratch w, int grab) {
     extern __shared__ double queue_smem[];
     const int lane = threadIdx.x & (kWarp - 1);
@@ -1573,7 +1616,7 @@ __global__ void __launch_bounds__(256) integrand_queue(const __grid_constant__ P
     const int warps_per_block = blockDim.x / kWarp;
     const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
     const int nmax = p.max_order;
-    const WsLayout lay = fp64_minors_layout(nmax, !(p.same_spin[0] && p.same_spin[1]));
+    const WsLayout lay = minors_layout(nmax, !(p.same_spin[0] && p.same_spin[1]), true);
     double* ws = queue_smem + static_cast<size_t>(warp_in_block) * lay.total;
     double* lu_lane = w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * nmax * nmax;
     uint32_t* head = w.order_count + kQueueHeadIndex;
@@ -1631,11 +1674,12 @@ __global__ void __launch_bounds__(256) integrand_queue(const __grid_constant__ P
 size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).total; }
 
 // Warps of the minors kernel whose workspaces fit one block's shared memory
-// (at most 8); the kernel uses shared memory when this is at least 4.
+// (at most kMinorsMaxWarps); the kernel uses shared memory when this is at least 4.
+constexpr int kMinorsMaxWarps = 12;
 static int minors_warps_in_shared_memory(int max_order, bool two_spins) {
-    const size_t ws_bytes = fp64_minors_layout(max_order, two_spins).total * sizeof(double);
+    const size_t ws_bytes = minors_layout(max_order, two_spins, true).total * sizeof(double);
     const size_t smem_budget = 227 * 1024;
-    return static_cast<int>(std::min<size_t>(8, smem_budget / ws_bytes));
+    return static_cast<int>(std::min<size_t>(kMinorsMaxWarps, smem_budget / ws_bytes));
 }
 
 bool minors_use_global_workspace(int max_order, bool two_spins) {
@@ -1778,10 +1822,11 @@ static cudaError_t post_assembly(const Problem& p_in, const Scratch& w, int sm_c
 
     // Minors: the per-warp workspace goes to shared memory when at least four
     // warps' worth fits a block (one block per SM, as many warps as fit, at
-    // most 8; without the spin-down minors when both sets have one spin),
-    // otherwise to the global workspace (4 warps per block).
+    // most 16; the compact arena up to order 10; without the spin-down minors
+    // when both sets have one spin), otherwise to the global workspace (4
+    // warps per block).
     const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
-    const size_t ws_bytes = fp64_minors_layout(p.max_order, two_spins).total * sizeof(double);
+    const size_t ws_bytes = minors_layout(p.max_order, two_spins, true).total * sizeof(double);
     const int fit = minors_warps_in_shared_memory(p.max_order, two_spins);
     const bool use_smem = fit >= 4;
     // orders 11..14 in the global workspace: the chunked recursion, eight
@@ -1877,16 +1922,18 @@ bool sorts_orders(const Problem& p) {
 void queue_launch_shape(const Problem& p, const Scratch& w, int sm_count, int* warps_per_block, int* blocks,
                         size_t* smem) {
     const bool two_spins = !(p.same_spin[0] && p.same_spin[1]);
-    const size_t ws_bytes = fp64_minors_layout(p.max_order, two_spins).total * sizeof(double);
+    const size_t ws_bytes = minors_layout(p.max_order, two_spins, true).total * sizeof(double);
     const size_t sm_bytes = 227 * 1024;  // shared memory of one SM this kernel can use (a block's limit too)
     const int sms = sm_count > 0 ? sm_count : 152;
     int per_sm = static_cast<int>(std::min<size_t>(32, sm_bytes / (ws_bytes + 16)));
     if (p.queue.warps_per_sm > 0) per_sm = std::min(per_sm, p.queue.warps_per_sm);
     if (p.queue.pair) per_sm &= ~1;
     per_sm = std::max(per_sm, p.queue.pair ? 2 : 1);
-    int wpb = std::min(8, per_sm);
+    // as few blocks per SM as blocks of at most kQueueMaxWarps allow
+    int wpb = per_sm / ((per_sm + kQueueMaxWarps - 1) / kQueueMaxWarps);
     if (p.queue.pair) wpb &= ~1;
-    size_t bytes = ws_bytes * wpb + (p.queue.pair ? 16 * sizeof(double) : 0);
+    // the pair exchange: four doubles per pair of warps
+    size_t bytes = ws_bytes * wpb + (p.queue.pair ? 2 * static_cast<size_t>(wpb) * sizeof(double) : 0);
     int per_sm_blocks = std::max(1, per_sm / wpb);
     while (per_sm_blocks > 1 && per_sm_blocks * (bytes + 1024) > sm_bytes + 1024) --per_sm_blocks;
     int64_t grid = static_cast<int64_t>(sms) * per_sm_blocks;

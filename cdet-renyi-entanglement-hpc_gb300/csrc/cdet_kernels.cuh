@@ -59,7 +59,58 @@ struct Scratch {
 struct WsLayout {
     int list;      // elements per Schur-complement list
     size_t a, old_list, new_list, aux, shifted_up, shifted_down, total;
+    int arena = 0;  // > 0: the compact form (compact_minors_layout), doubles per spin's arena
 };
+
+// ---- compact workspace of the FP64 warp recursion (orders <= 10) ----------
+// The shifted minors of an order-n matrix fill [0, 2^n) level by level (level
+// l writes [2^(l+1), 2^(l+2)) after its Schur complements), so the level
+// lists can share one arena with them: list L_k (2^k matrices of (n-k)^2)
+// sits low, at 2^(k+1) (only minors below that are written while it lives),
+// or high, ending at the arena's end, alternating so that a level's two lists
+// never meet. L_{n-2}, read while the last level writes [2^(n-1), 2^n), is
+// high; the last level's 1 x 1 children go straight to the minors.
+constexpr int kCompactMaxOrder = 10;
+__host__ __device__ inline int compact_list_doubles(int n, int k) { return (1 << k) * (n - k) * (n - k); }
+__host__ __device__ inline bool compact_list_high(int n, int k) { return ((n - 2 - k) & 1) == 0; }
+__host__ __device__ inline int compact_list_offset(int n, int k, int arena) {
+    return compact_list_high(n, k) ? arena - compact_list_doubles(n, k) : (1 << (k + 1));
+}
+// Doubles an order-n arena needs: the minors, each level's two lists apart,
+// each high list above the minors written before it is last read.
+__host__ __device__ inline int compact_arena_doubles(int n) {
+    int t = 1 << n;
+    for (int k = 0; k + 2 < n; ++k) {  // level k holds L_k and L_{k+1}
+        const int lo = compact_list_high(n, k) ? k + 1 : k;
+        t = max(t, (1 << (lo + 1)) + compact_list_doubles(n, k) + compact_list_doubles(n, k + 1));
+    }
+    for (int k = 0; k + 1 < n; ++k)
+        if (compact_list_high(n, k))
+            t = max(t, (k == n - 2 ? (1 << n) : (1 << (k + 1))) + compact_list_doubles(n, k));
+    return t;
+}
+
+// The compact workspace of a batch of orders up to nmax (<= 10) in shared
+// memory: one arena per spin (the spin-up minors at 0, the spin-down ones at
+// `arena`); A is read from the Green matrices. The arena is at least
+// 2^(nmax+1), so that after the minors its doubles from 2^nmax on hold the
+// queue form's recursion arrays (old_list: dp, new_list: a of the even masks).
+__host__ __device__ inline WsLayout compact_minors_layout(int nmax, bool two_spins) {
+    WsLayout l{};
+    int arena = compact_arena_doubles(nmax);
+    if (arena < (2 << nmax)) arena = 2 << nmax;
+    arena = (arena + 1) & ~1;
+    l.arena = arena;
+    l.list = 0;
+    l.a = 0;
+    l.aux = 0;
+    l.shifted_up = 0;
+    l.shifted_down = static_cast<size_t>(arena);
+    l.old_list = static_cast<size_t>(1) << nmax;
+    l.new_list = l.old_list + (static_cast<size_t>(1) << (nmax - 1));
+    l.total = static_cast<size_t>(arena) * (two_spins ? 2 : 1);
+    return l;
+}
 
 // two_spins = false when both sets evaluate one spin only (up and down tables
 // and shifts identical): the spin-down minors then need no space. with_aux =
@@ -100,6 +151,7 @@ constexpr int kAllWarpMaxOrder = 11;  // the warp form holds a and dp of one set
 // slots). Both give the same values bit for bit.
 constexpr int kIntegrandAuto = 0, kIntegrandStaged = 1, kIntegrandQueue = 2;
 constexpr int kQueueMaxOrder = 10;  // the queue form keeps a configuration's workspace in shared memory
+constexpr int kQueueMaxWarps = 12;  // warps per block of the queue kernel (384 threads)
 struct QueueShape {
     int warps_per_sm = 0;  // resident warps per SM (0: as many as the shared memory holds)
     int pair = 0;          // 1: two warps per configuration (one per set)
