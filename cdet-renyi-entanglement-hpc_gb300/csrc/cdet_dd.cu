@@ -17,9 +17,10 @@
 // One persistent kernel after the assembly: warps take configurations from
 // the order-sorted slots (decreasing order) through an atomic queue head; a
 // warp runs one configuration's minors and recursion in its shared-memory
-// workspace (the minors layout in DoubleDouble elements: 63 KB per warp at
-// order 10 with one spin per set), the masks of a popcount level dealt to its
-// lanes, each mask's submask sum on one lane in the reference's order.
+// workspace (the compact minors layout in DoubleDouble elements, A and one
+// arena per spin: 40.5 KB per warp at order 10 with one spin per set, five
+// warps per SM), the masks of a popcount level dealt to its lanes, each mask's
+// submask sum on one lane in the reference's order.
 #include "cdet_device.cuh"
 #include "cdet_kernels.cuh"
 
@@ -172,13 +173,16 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
     }
     const DD fallback_eps = (dd_gt(tol, zero) && dd_gt(max_abs, zero)) ? dd_mul(tol, max_abs) : zero;
     const bool eps_on = dd_gt(fallback_eps, zero);
-    DD* old_list = ws + lay.old_list;
-    DD* new_list = ws + lay.new_list;
-    DD* inv = ws + lay.aux;
+    // The compact arena (compact_minors_layout): the level lists share
+    // shifted's arena with the minors, each node's pivot inverse replaces its
+    // pivot entry and its factors column 0, each shifted minor is written once
+    // as p + its pivot entry (the initialise-then-add form's value).
+    DD* old_list = shifted + compact_list_offset(n, 0, lay.arena);
+    DD* new_list = nullptr;
     for (int k = lane; k < msize; k += kWarp) old_list[k] = A[k];
-    for (uint32_t m = lane; m < subsets; m += kWarp) shifted[m] = m == 0 ? DD{1.0, 0.0} : p;
+    if (lane == 0) shifted[0] = DD{1.0, 0.0};
     __syncwarp();
-    if (lane == 0) shifted[1] = dd_add(shifted[1], old_list[0]);
+    if (lane == 0) shifted[1] = dd_add(p, old_list[0]);
     __syncwarp();
     uint32_t minor_index = 2;
     bool fell_back = false;
@@ -193,20 +197,33 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
             const DD pivot = dd_add(old_list[set * old_msize], p);
             const DD pa = dd_abs(pivot);
             if (dd_eq(pa, zero) || (eps_on && !dd_gt(pa, fallback_eps))) bad_pivot = true;
-            inv[set] = dd_div(DD{1.0, 0.0}, pivot);
+            old_list[set * old_msize] = dd_div(DD{1.0, 0.0}, pivot);
         }
         if (__any_sync(0xffffffffu, bad_pivot)) {
             fell_back = true;
             break;
         }
         __syncwarp();
-        DD* factor = inv + sets;
         for (int item = lane; item < sets * new_size; item += kWarp) {
             const int set = item / new_size;
             const int row = item - set * new_size;
-            factor[item] = mul_t<Exact>(old_list[set * old_msize + (row + 1) * old_size], inv[set]);
+            DD* entry = old_list + set * old_msize + (row + 1) * old_size;
+            *entry = mul_t<Exact>(*entry, old_list[set * old_msize]);
         }
         __syncwarp();
+        if (level == n - 2) {
+            // the last level's 1 x 1 children, straight to their shifted minors
+            for (int set = lane; set < sets; set += kWarp) {
+                const DD* m = old_list + set * 4;
+                const DD base = m[3];
+                shifted[minor_index + set] = add_t<Exact>(p, base);
+                shifted[minor_index + sets + set] = add_t<Exact>(p, sub_prod_t<Exact>(m[1], m[2], base));
+            }
+            __syncwarp();
+            minor_index += 2 * sets;
+            break;
+        }
+        new_list = shifted + compact_list_offset(n, level + 1, lay.arena);
         const int items = sets * new_msize;
 #pragma unroll 4
         for (int item = lane; item < items; item += kWarp) {  // independent items: chains in flight
@@ -217,15 +234,14 @@ __device__ bool mat2pm_dd_warp(const DD* A, int n, DD tol, DD thresh, const WsLa
             const int src = set * old_msize;
             const DD base = old_list[src + (row + 1) * old_size + col + 1];
             new_list[item] = base;
-            new_list[items + item] = sub_prod_t<Exact>(old_list[src + 1 + col], factor[set * new_size + row], base);
+            new_list[items + item] =
+                sub_prod_t<Exact>(old_list[src + 1 + col], old_list[src + (row + 1) * old_size], base);
         }
         __syncwarp();
         for (int m = lane; m < 2 * sets; m += kWarp)
-            shifted[minor_index + m] = add_t<Exact>(shifted[minor_index + m], new_list[m * new_msize]);
+            shifted[minor_index + m] = add_t<Exact>(p, new_list[m * new_msize]);
         minor_index += 2 * sets;
-        DD* t = old_list;
         old_list = new_list;
-        new_list = t;
         __syncwarp();
     }
     if (fell_back) {
@@ -327,7 +343,7 @@ __device__ DD dd_set_value(const Problem& p, const Scratch& w, int64_t c, int se
     return value;
 }
 
-__global__ void __launch_bounds__(128) integrand_dd(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(kDDMaxWarps * 32) integrand_dd(const __grid_constant__ Problem p,
                                                    const __grid_constant__ Scratch w) {
     extern __shared__ double dd_smem[];
     const int lane = threadIdx.x & (kWarp - 1);
@@ -335,7 +351,7 @@ __global__ void __launch_bounds__(128) integrand_dd(const __grid_constant__ Prob
     const int warps_per_block = blockDim.x / kWarp;
     const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
     const int nmax = p.max_order;
-    const WsLayout lay = ws_layout(nmax, !(p.same_spin[0] && p.same_spin[1]));
+    const WsLayout lay = compact_minors_layout(nmax, !(p.same_spin[0] && p.same_spin[1]), true);
     DD* ws = reinterpret_cast<DD*>(dd_smem) + static_cast<size_t>(warp_in_block) * lay.total;
     // a lane's LU-fallback matrix: two lanes' FP64 regions of the scratch
     DD* lu_lane = reinterpret_cast<DD*>(w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * 2 *
@@ -380,7 +396,7 @@ __device__ __forceinline__ DD* lane_dp(const Scratch& w, int64_t slot, int set, 
 }
 
 template <bool Exact>
-__global__ void __launch_bounds__(128) principal_minors_dd(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(kDDMaxWarps * 32) principal_minors_dd(const __grid_constant__ Problem p,
                                                           const __grid_constant__ Scratch w) {
     extern __shared__ double dd_smem[];
     const int lane = threadIdx.x & (kWarp - 1);
@@ -389,7 +405,7 @@ __global__ void __launch_bounds__(128) principal_minors_dd(const __grid_constant
     const int64_t global_warp = static_cast<int64_t>(blockIdx.x) * warps_per_block + warp_in_block;
     const int64_t total_warps = static_cast<int64_t>(gridDim.x) * warps_per_block;
     const int nmax = p.max_order;
-    const WsLayout lay = ws_layout(nmax, !(p.same_spin[0] && p.same_spin[1]));
+    const WsLayout lay = compact_minors_layout(nmax, !(p.same_spin[0] && p.same_spin[1]), true);
     DD* ws = reinterpret_cast<DD*>(dd_smem) + static_cast<size_t>(warp_in_block) * lay.total;
     DD* lu_lane = reinterpret_cast<DD*>(w.lu_scratch + (static_cast<size_t>(global_warp) * kWarp + lane) * 2 *
                                                            nmax * nmax);
@@ -517,8 +533,8 @@ cudaError_t launch_integrand_dd(const Problem& p, const Scratch& w, int sm_count
     const bool lanes = p.integrand_form == kIntegrandStaged ||
                        (p.integrand_form == kIntegrandAuto && p.batch >= dd_lane_min_batch(sm_count));
     if (w.dd_lanes && lanes) {
-        const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(DD);
-        const int wpb = static_cast<int>(std::max<size_t>(1, std::min<size_t>(4, (227 * 1024) / ws_bytes)));
+        const size_t ws_bytes = compact_minors_layout(p.max_order, two_spins, true).total * sizeof(DD);
+        const int wpb = static_cast<int>(std::max<size_t>(1, std::min<size_t>(kDDMaxWarps, (227 * 1024) / ws_bytes)));
         const int sms = sm_count > 0 ? sm_count : 152;
         const int per_sm = std::max(1, static_cast<int>((227 * 1024) / (ws_bytes * wpb + 1024)));
         int64_t blocks = std::min<int64_t>(static_cast<int64_t>(sms) * per_sm, (p.batch * 2 + wpb - 1) / wpb);
@@ -539,9 +555,9 @@ cudaError_t launch_integrand_dd(const Problem& p, const Scratch& w, int sm_count
             cdet_dd_lane<true><<<static_cast<unsigned>((p.batch + kWarp - 1) / kWarp), kWarp, 0, stream>>>(p, w);
         return cudaGetLastError();
     }
-    const size_t ws_bytes = ws_layout(p.max_order, two_spins).total * sizeof(DD);
+    const size_t ws_bytes = compact_minors_layout(p.max_order, two_spins, true).total * sizeof(DD);
     const size_t budget = 227 * 1024;
-    const int wpb = static_cast<int>(std::max<size_t>(1, std::min<size_t>(4, budget / ws_bytes)));
+    const int wpb = static_cast<int>(std::max<size_t>(1, std::min<size_t>(kDDMaxWarps, budget / ws_bytes)));
     const int sms = sm_count > 0 ? sm_count : 152;
     const int per_sm = std::max(1, static_cast<int>(budget / (ws_bytes * wpb + 1024)));
     int64_t blocks = static_cast<int64_t>(sms) * per_sm;

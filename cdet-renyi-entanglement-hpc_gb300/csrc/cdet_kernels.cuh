@@ -91,24 +91,27 @@ __host__ __device__ inline int compact_arena_doubles(int n) {
 }
 
 // The compact workspace of a batch of orders up to nmax (<= 10) in shared
-// memory: one arena per spin (the spin-up minors at 0, the spin-down ones at
-// `arena`); A is read from the Green matrices. The arena is at least
-// 2^(nmax+1), so that after the minors its doubles from 2^nmax on hold the
-// queue form's recursion arrays (old_list: dp, new_list: a of the even masks).
-__host__ __device__ inline WsLayout compact_minors_layout(int nmax, bool two_spins) {
+// memory: one arena per spin (the spin-up minors at its start, the spin-down
+// ones one arena later), after the matrix A when with_a (the double-double
+// form widens A into it; the FP64 form reads A from the Green matrices). The
+// arena is at least 2^(nmax+1) elements, so that after the minors its
+// elements from 2^nmax on hold the recursion arrays of the forms that run the
+// CDet on the same warp (old_list: dp, new_list: a of the even masks).
+__host__ __device__ inline WsLayout compact_minors_layout(int nmax, bool two_spins, bool with_a = false) {
     WsLayout l{};
     int arena = compact_arena_doubles(nmax);
     if (arena < (2 << nmax)) arena = 2 << nmax;
     arena = (arena + 1) & ~1;
+    const size_t base = with_a ? (static_cast<size_t>(nmax) * nmax + 1) & ~static_cast<size_t>(1) : 0;
     l.arena = arena;
     l.list = 0;
     l.a = 0;
     l.aux = 0;
-    l.shifted_up = 0;
-    l.shifted_down = static_cast<size_t>(arena);
-    l.old_list = static_cast<size_t>(1) << nmax;
+    l.shifted_up = base;
+    l.shifted_down = base + static_cast<size_t>(arena);
+    l.old_list = base + (static_cast<size_t>(1) << nmax);
     l.new_list = l.old_list + (static_cast<size_t>(1) << (nmax - 1));
-    l.total = static_cast<size_t>(arena) * (two_spins ? 2 : 1);
+    l.total = base + static_cast<size_t>(arena) * (two_spins ? 2 : 1);
     return l;
 }
 
@@ -381,6 +384,7 @@ bool uses_queue_form(const Problem& p);
 // single-top batches): one persistent kernel over the order-sorted slots
 // (the sort already launched), its workspace in shared memory.
 constexpr int kDDMaxOrder = 10;
+constexpr int kDDMaxWarps = 8;  // warps per block of the double-double minors and warp-form kernels
 cudaError_t launch_integrand_dd(const Problem& p, const Scratch& scratch, int sm_count, cudaStream_t stream);
 // The post-assembly stages alone (sort, minors, CDet, or the queue kernel),
 // on Green matrices already in scratch: what the autotuner times.
