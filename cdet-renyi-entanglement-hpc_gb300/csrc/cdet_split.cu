@@ -958,11 +958,15 @@ __device__ uint32_t tile_cost(const SplitPlan& plan, uint32_t key) {
 }
 
 // Each sub-block's estimated tile time, once per sliced branch (`plan` holds
-// that branch alone as its one segment).
+// that branch alone as its one segment). Tables cut into sub-blocks (degrees
+// above 128) get one cost for all: measured at 12x12 / degree 192 / order 14
+// (tiles of ~31 lookups, whose time the estimate, made for full tiles, does
+// not follow), ranges of equal tile count took 73.0 ms against 74.6-75.4 ms
+// with the estimate.
 template <bool Chunked>
 __global__ void __launch_bounds__(256) split_key_costs(const SplitPlan plan, uint32_t* __restrict__ costs) {
     const uint32_t key = blockIdx.x * blockDim.x + threadIdx.x;
-    if (key < plan.nblocks) costs[key] = tile_cost<Chunked>(plan, key);
+    if (key < plan.nblocks) costs[key] = Chunked ? 1u : tile_cost<Chunked>(plan, key);
 }
 
 // The tile list and the per-CTA tile ranges, one thread per key (sub-block).
