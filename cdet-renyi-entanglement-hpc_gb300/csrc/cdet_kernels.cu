@@ -1029,7 +1029,9 @@ __global__ void __launch_bounds__(128) cdet_all_warp(const __grid_constant__ Pro
 // doubles from shared memory. Magnitudes are clamped to the FP32 range, and a
 // non-finite accumulator is never zeroed.
 constexpr int kWarpCdetMaxOrder = 10;
-constexpr int kWarpCdetWarps = 8;
+// warps per block of cdet_split_warp: two blocks of 14 warps (8 KB each at
+// order 10) fill an SM's shared memory, 28 warps per SM
+constexpr int kWarpCdetWarps = 14;
 
 __device__ const uint16_t kBinom[11][11] = {
     {1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
@@ -1215,7 +1217,7 @@ __device__ __forceinline__ double split_cdet_recursion(const double* a_s, double
     return dp_s[swz((count - 1) >> 1)];
 }
 
-__global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const __grid_constant__ Problem p,
+__global__ void __launch_bounds__(kWarpCdetWarps * 32, 2) cdet_split_warp(const __grid_constant__ Problem p,
                                                                        const __grid_constant__ Scratch w) {
     extern __shared__ __align__(16) unsigned char cdet_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1228,12 +1230,13 @@ __global__ void __launch_bounds__(kWarpCdetWarps * 32, 3) cdet_split_warp(const 
     double* dp_s = a_s + full_n / 2;
     const Scalars& s = p.s;
     const double threshold = dmul(s.z_eps0, s.z_safety);
-    const int64_t g = blockIdx.x;
-    for (int cl = warp; cl < kWarp; cl += kWarpCdetWarps) {
-        const int64_t c = g * kWarp + cl;
-        if (c >= p.batch) break;
+    {  // one configuration per warp: lane cl of 32-configuration group g
+        const int64_t c = static_cast<int64_t>(blockIdx.x) * kWarpCdetWarps + warp;
+        if (c >= p.batch) return;
+        const int64_t g = c >> 5;
+        const int cl = static_cast<int>(c & 31);
         const int n = __ldg(p.orders + c);
-        if (n < 1 || n > nmax) continue;
+        if (n < 1 || n > nmax) return;
         const double* diag = w.diag + c * 2 * 2 * nmax;
         int32_t status = 0;
         DD value_twisted{0.0, 0.0}, value_ordinary{0.0, 0.0};
@@ -1862,8 +1865,8 @@ static cudaError_t post_assembly(const Problem& p_in, const Scratch& w, int sm_c
         err = cudaFuncSetAttribute(cdet_split_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(csmem));
         if (err != cudaSuccess) return err;
-        cdet_split_warp<<<static_cast<unsigned>((p.batch + kWarp - 1) / kWarp), kWarpCdetWarps * kWarp, csmem,
-                          stream>>>(p, w);
+        cdet_split_warp<<<static_cast<unsigned>((p.batch + kWarpCdetWarps - 1) / kWarpCdetWarps),
+                          kWarpCdetWarps * kWarp, csmem, stream>>>(p, w);
     } else if (p.all_subsets && p.max_order <= kAllWarpMaxOrder && p.all_subsets_form != kFormLane &&
                (p.all_subsets_form == kFormWarp ||
                 p.batch < static_cast<int64_t>(all_subsets_lane_form_min_batch(sm_count)))) {
