@@ -1678,7 +1678,6 @@ size_t minors_workspace_doubles(int max_order) { return ws_layout(max_order).tot
 
 // Warps of the minors kernel whose workspaces fit one block's shared memory
 // (at most kMinorsMaxWarps); the kernel uses shared memory when this is at least 4.
-constexpr int kMinorsMaxWarps = 12;
 static int minors_warps_in_shared_memory(int max_order, bool two_spins) {
     const size_t ws_bytes = minors_layout(max_order, two_spins, true).total * sizeof(double);
     const size_t smem_budget = 227 * 1024;

@@ -155,6 +155,7 @@ constexpr int kAllWarpMaxOrder = 11;  // the warp form holds a and dp of one set
 constexpr int kIntegrandAuto = 0, kIntegrandStaged = 1, kIntegrandQueue = 2;
 constexpr int kQueueMaxOrder = 10;  // the queue form keeps a configuration's workspace in shared memory
 constexpr int kQueueMaxWarps = 12;  // warps per block of the queue kernel (384 threads)
+constexpr int kMinorsMaxWarps = 12;  // warps per block (one block per SM) of the shared-memory minors kernel
 struct QueueShape {
     int warps_per_sm = 0;  // resident warps per SM (0: as many as the shared memory holds)
     int pair = 0;          // 1: two warps per configuration (one per set)

@@ -102,9 +102,9 @@ extern "C" int cdet_integrand_device_noalloc(cdet_context* ctx, const double* ve
     const size_t fixed = cdet::scratch_bytes(batch, max_order, 0, regions);
     const size_t per_warp = cdet::scratch_bytes(batch, max_order, 1, regions) - fixed;
     // the warps the minors kernel can use: 32 per SM from the global
-    // workspace, one block of at most 8 per SM from shared memory
+    // workspace, one block of at most kMinorsMaxWarps per SM from shared memory
     const size_t sms = static_cast<size_t>(std::max(1, cdet::context_sm_count(ctx)));
-    const size_t useful = sms * (regions.minors_workspace ? 32 : 8);
+    const size_t useful = sms * (regions.minors_workspace ? 32 : cdet::kMinorsMaxWarps);
     const size_t room = fixed < kNoAllocScratchBytes ? (kNoAllocScratchBytes - fixed) / per_warp : 0;
     const size_t ws_warps = std::min(useful, room);
     if (ws_warps < kMinWarps) {
