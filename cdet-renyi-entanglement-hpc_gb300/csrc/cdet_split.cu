@@ -406,96 +406,132 @@ __host__ __device__ __forceinline__ int records_per_pair(const SplitPlan& plan) 
     return plan.records_per_set[0] + plan.records_per_set[1];
 }
 
-// One thread per (configuration, i, j): branch and (u, v) are shared by both
-// table sets; the corner path is evaluated here, every other lookup becomes
-// one record per sub-block of its coefficient block, keyed by the sub-block.
-// Record slots are fixed: ((c * nmax^2 + pair) * records_per_pair + record)
-// * nsub + sub, the set's records after those of the sets before it.
+// Configurations per warp of split_descriptors: as many whole
+// configurations' vertices as 32 lanes hold (max_order <= 24).
+__host__ __device__ inline int descriptor_configs_per_warp(int nmax) { return nmax >= 1 && nmax <= 32 ? 32 / nmax : 1; }
+
+// One warp per K = 32 / max_order configurations (at least one): each
+// vertex is decoded once, on its lane (tau = beta u_tau, the site and
+// replica indices, and u = 2 tau / beta - 1, the vertex's value when it is
+// the outer one of a pair), then the warp takes the vertex pairs 32 at a time,
+// the two vertices' values by shuffles, and computes per pair only v = 2
+// tau_inner / tau_outer - 1 (the same operations as per-pair decoding, so the
+// same values). Branch and (u, v) are shared by both table sets; the corner
+// path is evaluated here, every other lookup becomes one record per sub-block
+// of its coefficient block, keyed by the sub-block. Record slots are fixed:
+// ((c * nmax^2 + pair) * records_per_pair + record) * nsub + sub, the set's
+// records after those of the sets before it.
 __global__ void __launch_bounds__(128) split_descriptors(const __grid_constant__ Problem p,
                                                          const __grid_constant__ Scratch w,
                                                          const __grid_constant__ SplitPlan plan,
                                                          SplitRecordArrays rec, uint32_t* counts) {
     const int nmax = p.max_order;
-    const int64_t per_c = static_cast<int64_t>(nmax) * nmax;
-    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= p.batch * per_c) return;
-    const int64_t c = idx / per_c;
-    const int pair = static_cast<int>(idx - c * per_c);
-    const int i = pair / nmax, j = pair - (pair / nmax) * nmax;
+    const int per_c = nmax * nmax;
+    const int K = descriptor_configs_per_warp(nmax);
+    const int lane = threadIdx.x & 31;
+    const int64_t c0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * K;
+    if (c0 >= p.batch) return;  // the whole warp
+    const Scalars& s = p.s;
     const int nsub = plan.nrb * plan.nkc;
     const int rpp = records_per_pair(plan);
-    const int64_t slot0 = idx * rpp * nsub;
-    for (int k = 0; k < rpp * nsub; ++k) rec.key[slot0 + k] = kNoKey;
-    const int n = p.all_subsets ? nmax : __ldg(p.orders + c);
-    if (n < 1 || n > nmax) {
-        if (pair == 0) atomicOr(p.status + c, kStatusBadInput);
-        return;
+    // this lane's vertex: vertex vv of configuration c0 + vc
+    const int vc = lane / nmax, vv = lane - (lane / nmax) * nmax;
+    const int64_t cv = c0 + vc;
+    int nv = 0, xv = 0, yv = 0, rv = 0;
+    bool vbad = false;
+    double tuv = 0.0, tauv = 0.0, uv = 0.0;
+    if (vc < K && cv < p.batch) {
+        nv = p.all_subsets ? nmax : __ldg(p.orders + cv);
+        if (nv >= 1 && nv <= nmax && vv < nv) {
+            const double* vb = p.vertices + (cv * nmax + vv) * 4;
+            tuv = __ldg(vb);
+            if (!isfinite(tuv)) vbad = true;
+            tauv = dmul(s.beta, tuv);
+            xv = coordinate_index_s(dmul(static_cast<double>(s.n1), __ldg(vb + 1)), s.n1, vbad);
+            yv = coordinate_index_s(dmul(static_cast<double>(s.n2), __ldg(vb + 2)), s.n2, vbad);
+            rv = coordinate_index_s(dmul(2.0, __ldg(vb + 3)), 2, vbad);
+            uv = clamp_unit_s(dsub(ddiv(dmul(2.0, tauv), s.beta), 1.0));
+        }
     }
-    if (i >= n || j >= n) return;
-    const Scalars& s = p.s;
-    const double* vb = p.vertices + c * static_cast<int64_t>(nmax) * 4;
-    bool bad = false;
-    const double tui = __ldg(vb + 4 * i), tuj = __ldg(vb + 4 * j);
-    if (!isfinite(tui) || !isfinite(tuj)) bad = true;
-    const double taui = dmul(s.beta, tui), tauj = dmul(s.beta, tuj);
-    const int xi = coordinate_index_s(dmul(static_cast<double>(s.n1), __ldg(vb + 4 * i + 1)), s.n1, bad);
-    const int yi = coordinate_index_s(dmul(static_cast<double>(s.n2), __ldg(vb + 4 * i + 2)), s.n2, bad);
-    const int xj = coordinate_index_s(dmul(static_cast<double>(s.n1), __ldg(vb + 4 * j + 1)), s.n1, bad);
-    const int yj = coordinate_index_s(dmul(static_cast<double>(s.n2), __ldg(vb + 4 * j + 2)), s.n2, bad);
-    const int ri = coordinate_index_s(dmul(2.0, __ldg(vb + 4 * i + 3)), 2, bad);
-    const int rj = coordinate_index_s(dmul(2.0, __ldg(vb + 4 * j + 3)), 2, bad);
-    if (bad) {
-        atomicOr(p.status + c, kStatusBadInput);
-        return;
-    }
-    if (copy_reused_pair(p, w.green, w.diag, c, 0, i, j, n)) {  // both vertices retained: no records
-        copy_reused_pair(p, w.green, w.diag, c, 1, i, j, n);
-        return;
-    }
-    const bool upper = (i != j) && (tui > tuj);
-    const double t_outer = upper ? taui : tauj;
-    const double t_inner = upper ? tauj : taui;
-    const bool corner = t_outer < s.branch_eps;
-    double u = 0.0, v = 0.0;
-    if (!corner) {
-        u = clamp_unit_s(dsub(ddiv(dmul(2.0, t_outer), s.beta), 1.0));
-        v = clamp_unit_s(dsub(ddiv(dmul(2.0, t_inner), t_outer), 1.0));
-    }
-    const uint64_t site_part =
-        ((static_cast<uint64_t>(xi) * s.n2 + yi) * s.n1 + xj) * s.n2 + yj;
-    const uint64_t sites2 = static_cast<uint64_t>(s.n1) * s.n2 * s.n1 * s.n2;
-    for (int set = 0; set < 2; ++set) {
-        const uint64_t sitepair =
-            set == 0 ? (static_cast<uint64_t>(ri) * 2 + rj) * sites2 + site_part : site_part;
-        const int64_t mslot = (c * 2 + set) * 2;
-        if (corner) {
-            const TableDev& tu = p.up[set];
-            const TableDev& td = p.down[set];
-            double up = __ldg((upper ? tu.upper_corners : tu.lower_corners) + sitepair);
-            double down = p.same_spin[set] ? up
-                                           : __ldg((upper ? td.upper_corners : td.lower_corners) + sitepair);
-            if (i == j) {
-                const double up_raw = up, down_raw = down;
-                up = dadd(up, s.diag_up_shift);
-                down = dadd(down, s.diag_down_shift);
-                w.diag[mslot * nmax + i] = p.raw_diag ? up_raw : up;
-                w.diag[(mslot + 1) * nmax + i] = p.raw_diag ? down_raw : down;
-            }
-            w.green[mslot * per_c + i * n + j] = dmul(up, s.scale);
-            w.green[(mslot + 1) * per_c + i * n + j] = dmul(down, s.scale);
+    const int total = K * per_c;
+    for (int q0 = 0; q0 < total; q0 += 32) {
+        const int q = q0 + lane;
+        const bool valid = q < total;
+        const int cq = valid ? q / per_c : 0;
+        const int pair = valid ? q - cq * per_c : 0;
+        const int i = pair / nmax, j = pair - (pair / nmax) * nmax;
+        const int li = cq * nmax + i, lj = cq * nmax + j;  // the two vertices' lanes (< K nmax <= 32)
+        const int n = __shfl_sync(0xffffffffu, nv, li);
+        const double tui = __shfl_sync(0xffffffffu, tuv, li), tuj = __shfl_sync(0xffffffffu, tuv, lj);
+        const double taui = __shfl_sync(0xffffffffu, tauv, li), tauj = __shfl_sync(0xffffffffu, tauv, lj);
+        const double ui = __shfl_sync(0xffffffffu, uv, li), uj = __shfl_sync(0xffffffffu, uv, lj);
+        const int xi = __shfl_sync(0xffffffffu, xv, li), xj = __shfl_sync(0xffffffffu, xv, lj);
+        const int yi = __shfl_sync(0xffffffffu, yv, li), yj = __shfl_sync(0xffffffffu, yv, lj);
+        const int ri = __shfl_sync(0xffffffffu, rv, li), rj = __shfl_sync(0xffffffffu, rv, lj);
+        const bool bad = __shfl_sync(0xffffffffu, static_cast<int>(vbad), li) != 0 ||
+                         __shfl_sync(0xffffffffu, static_cast<int>(vbad), lj) != 0;
+        const int64_t c = c0 + cq;
+        if (!valid || c >= p.batch) continue;
+        const int64_t slot0 = (c * per_c + pair) * rpp * nsub;
+        for (int k = 0; k < rpp * nsub; ++k) rec.key[slot0 + k] = kNoKey;
+        if (n < 1 || n > nmax) {
+            if (pair == 0) atomicOr(p.status + c, kStatusBadInput);
             continue;
         }
-        for (int r = 0; r < plan.records_per_set[set]; ++r) {
-            const int seg = plan.segment_of[set][r][upper ? 0 : 1];
-            const uint64_t info = pack_info(c, set, plan.spin_mask[set][r], i, j, n);
-            for (int sub = 0; sub < nsub; ++sub) {
-                const uint32_t key = plan.segment_base[seg] + static_cast<uint32_t>(sitepair * nsub + sub);
-                const int64_t slot = slot0 + ((set ? plan.records_per_set[0] : 0) + r) * nsub + sub;
-                rec.key[slot] = key;
-                rec.u[slot] = u;
-                rec.v[slot] = v;
-                rec.info[slot] = info;
-                atomicAdd(counts + key, 1u);
+        if (i >= n || j >= n) continue;
+        if (bad) {
+            atomicOr(p.status + c, kStatusBadInput);
+            continue;
+        }
+        if (copy_reused_pair(p, w.green, w.diag, c, 0, i, j, n)) {  // both vertices retained: no records
+            copy_reused_pair(p, w.green, w.diag, c, 1, i, j, n);
+            continue;
+        }
+        const bool upper = (i != j) && (tui > tuj);
+        const double t_outer = upper ? taui : tauj;
+        const double t_inner = upper ? tauj : taui;
+        const bool corner = t_outer < s.branch_eps;
+        double u = 0.0, v = 0.0;
+        if (!corner) {
+            u = upper ? ui : uj;  // clamp(2 t_outer / beta - 1), decoded with the outer vertex
+            v = clamp_unit_s(dsub(ddiv(dmul(2.0, t_inner), t_outer), 1.0));
+        }
+        const uint64_t site_part =
+            ((static_cast<uint64_t>(xi) * s.n2 + yi) * s.n1 + xj) * s.n2 + yj;
+        const uint64_t sites2 = static_cast<uint64_t>(s.n1) * s.n2 * s.n1 * s.n2;
+        for (int set = 0; set < 2; ++set) {
+            const uint64_t sitepair =
+                set == 0 ? (static_cast<uint64_t>(ri) * 2 + rj) * sites2 + site_part : site_part;
+            const int64_t mslot = (c * 2 + set) * 2;
+            if (corner) {
+                const TableDev& tu = p.up[set];
+                const TableDev& td = p.down[set];
+                double up = __ldg((upper ? tu.upper_corners : tu.lower_corners) + sitepair);
+                double down = p.same_spin[set] ? up
+                                               : __ldg((upper ? td.upper_corners : td.lower_corners) + sitepair);
+                if (i == j) {
+                    const double up_raw = up, down_raw = down;
+                    up = dadd(up, s.diag_up_shift);
+                    down = dadd(down, s.diag_down_shift);
+                    w.diag[mslot * nmax + i] = p.raw_diag ? up_raw : up;
+                    w.diag[(mslot + 1) * nmax + i] = p.raw_diag ? down_raw : down;
+                }
+                w.green[mslot * per_c + i * n + j] = dmul(up, s.scale);
+                w.green[(mslot + 1) * per_c + i * n + j] = dmul(down, s.scale);
+                continue;
+            }
+            for (int r = 0; r < plan.records_per_set[set]; ++r) {
+                const int seg = plan.segment_of[set][r][upper ? 0 : 1];
+                const uint64_t info = pack_info(c, set, plan.spin_mask[set][r], i, j, n);
+                for (int sub = 0; sub < nsub; ++sub) {
+                    const uint32_t key = plan.segment_base[seg] + static_cast<uint32_t>(sitepair * nsub + sub);
+                    const int64_t slot = slot0 + ((set ? plan.records_per_set[0] : 0) + r) * nsub + sub;
+                    rec.key[slot] = key;
+                    rec.u[slot] = u;
+                    rec.v[slot] = v;
+                    rec.info[slot] = info;
+                    atomicAdd(counts + key, 1u);
+                }
             }
         }
     }
@@ -1650,7 +1686,11 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     if (err != cudaSuccess) return err;
     err = cudaMemsetAsync(error_flag, 0, kSplitStatusBytes, stream);
     if (err != cudaSuccess) return err;
-    split_descriptors<<<static_cast<unsigned>((pairs + 127) / 128), 128, 0, stream>>>(p, w, plan, rec, counts);
+    {
+        const int64_t per_warp = descriptor_configs_per_warp(p.max_order);
+        const int64_t warps = (p.batch + per_warp - 1) / per_warp;
+        split_descriptors<<<static_cast<unsigned>((warps + 3) / 4), 128, 0, stream>>>(p, w, plan, rec, counts);
+    }
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     split_scan<<<1, 1024, 0, stream>>>(plan, counts, offsets, tile_offsets, cursors, cost_prefix, totals);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
