@@ -378,6 +378,13 @@ struct SplitRecordArrays {
 };
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;
 
+// A lookup after the sort by sub-block: one 32-byte record, so that the
+// scatter writes one sector per lookup (its positions are scattered).
+struct __align__(32) SortedLookup {
+    double u, v;
+    uint64_t info, pad;
+};
+
 __device__ __forceinline__ uint64_t pack_info(int64_t c, int set, int spins, int i, int j, int n) {
     return static_cast<uint64_t>(c) | (static_cast<uint64_t>(set) << 32) |
            (static_cast<uint64_t>(spins) << 33) | (static_cast<uint64_t>(i) << 35) |
@@ -646,15 +653,15 @@ struct SplitTile {
 __global__ void __launch_bounds__(256) split_scatter(const SplitRecordArrays rec, int64_t nrec,
                                                      const uint32_t* __restrict__ offsets,
                                                      uint32_t* __restrict__ cursors,
-                                                     SplitRecordArrays sorted) {
+                                                     SortedLookup* __restrict__ sorted) {
     const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= nrec) return;
     const uint32_t key = rec.key[idx];
     if (key == kNoKey) return;
     const uint32_t pos = offsets[key] + atomicAdd(cursors + key, 1u);
-    sorted.u[pos] = rec.u[idx];
-    sorted.v[pos] = rec.v[idx];
-    sorted.info[pos] = rec.info[idx];
+    double2* out = reinterpret_cast<double2*>(sorted + pos);
+    out[0] = make_double2(rec.u[idx], rec.v[idx]);
+    reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(rec.info[idx], 0ull);
 }
 
 
@@ -1055,7 +1062,7 @@ template <bool Chunked>
 __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __grid_constant__ Problem p,
                                                                       const __grid_constant__ Scratch w,
                                                                       const __grid_constant__ SplitPlan plan,
-                                                                      const SplitRecordArrays sorted,
+                                                                      const SortedLookup* __restrict__ sorted,
                                                                       const SplitTile* __restrict__ tiles,
                                                                       const uint32_t* __restrict__ totals,
                                                                       int64_t* __restrict__ parts,
@@ -1117,9 +1124,11 @@ __global__ void __launch_bounds__(kAssemblyThreads, 1) split_assembly(const __gr
             const TileSource src = tile_source<Chunked>(plan, tl.block);
             const uint64_t rows = __ldg(reinterpret_cast<const unsigned long long*>(src.rows));
             const bool live = static_cast<uint32_t>(l) < tl.count;
-            const double v = live ? sorted.v[tl.start + l] : 0.0;
-            sh.meta[mb].u[l] = live ? sorted.u[tl.start + l] : 0.0;
-            sh.meta[mb].info[l] = live ? sorted.info[tl.start + l] : ~uint64_t{0};
+            SortedLookup look{0.0, 0.0, ~uint64_t{0}, 0};
+            if (live) look = sorted[tl.start + l];
+            const double v = look.v;
+            sh.meta[mb].u[l] = look.u;
+            sh.meta[mb].info[l] = look.info;
             if (l == 0) {
                 sh.meta[mb].count = tl.count;
                 sh.meta[mb].exponent = __ldg(src.exponent);
@@ -1640,7 +1649,7 @@ size_t split_scratch_bytes(int64_t batch, int max_order, const SplitPlan& plan) 
     const size_t nrec = static_cast<size_t>(batch) * max_order * max_order * records_per_pair(plan) * nsub;
     size_t total = 0;
     total += nrec * (4 + 8 + 8 + 8);          // unsorted records
-    total += nrec * (8 + 8 + 8);              // sorted records
+    total += nrec * sizeof(SortedLookup);     // sorted records
     total += static_cast<size_t>(plan.nblocks) * 4 * 4;  // counts, offsets, tile offsets, cursors
     total += static_cast<size_t>(plan.nblocks) * 8;      // estimated-time prefix
     total += (nrec / kTileN + plan.nblocks + 1) * sizeof(SplitTile);  // tiles
@@ -1664,8 +1673,7 @@ cudaError_t launch_split_assembly(const Problem& p, const Scratch& w, const Spli
     };
     SplitRecordArrays rec{static_cast<uint32_t*>(take(nrec * 4)), static_cast<double*>(take(nrec * 8)),
                           static_cast<double*>(take(nrec * 8)), static_cast<uint64_t*>(take(nrec * 8))};
-    SplitRecordArrays sorted{nullptr, static_cast<double*>(take(nrec * 8)), static_cast<double*>(take(nrec * 8)),
-                             static_cast<uint64_t*>(take(nrec * 8))};
+    SortedLookup* sorted = static_cast<SortedLookup*>(take(nrec * sizeof(SortedLookup)));
     uint32_t* counts = static_cast<uint32_t*>(take(plan.nblocks * 4u));
     uint32_t* offsets = static_cast<uint32_t*>(take(plan.nblocks * 4u));
     uint32_t* tile_offsets = static_cast<uint32_t*>(take(plan.nblocks * 4u));
