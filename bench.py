@@ -402,6 +402,7 @@ def run_gpu(args):
         stream, barrier + synchronize on both sides); returns the elapsed ms
         (max over ranks), per-stage kernel ms, launches, last values/status."""
         integrand.set_assembly(path)
+        integrand.set_integrand_form(args.integrand_form)
         for w in range(args.warmup):
             flush.zero_()
             integrand.integrand_device(d_vertices[args.steps + w], d_orders, d_values, d_status, stream)
@@ -418,7 +419,8 @@ def run_gpu(args):
         elapsed = max_over_ranks(start.elapsed_time(stop))
         stage_ms, launches = integrand.profile_read()
         integrand.profile(False)
-        tuned_forms[path] = integrand.integrand_form_tuned(ORDER, BATCH)
+        tuned_forms[path] = (integrand.integrand_form_tuned(ORDER, BATCH) if args.integrand_form == "auto"
+                             else {"form": args.integrand_form, "chosen_by": "--integrand-form"})
         return elapsed, stage_ms, launches, d_values.cpu().numpy(), d_status.cpu().numpy()
 
     tuned_forms = {}
@@ -946,6 +948,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-order precision study")
     ap.add_argument("--no-dd", action="store_true", help="skip timing the double-double integrand")
+    ap.add_argument("--integrand-form", choices=["auto", "staged", "queue"], default="auto",
+                    help="the headline's layout after the assembly: the autotuner's choice (default) or a fixed one")
     ap.add_argument("--precision-configs", type=int, default=512,
                     help="configurations per order in the precision study")
     ap.add_argument("--preset", choices=["8x8-d128", "6x6-d96"], default="8x8-d128",
