@@ -8,7 +8,9 @@ for it (split_slices_bytes, split_leads_bytes, split_level_rows_bytes); every
 pass geometry pass_geom can produce keeps the copy warp's bulk copies inside
 one K step of the table and inside its ring stage, the MMA's operand rows
 inside the copied rows, and the accumulator columns below the sink; the tile
-list fits the capacity the scratch carve gives it.
+list fits the capacity the scratch carve gives it; the descriptor kernel's
+warps take every (configuration, vertex pair) once and shuffle only from
+lanes holding that configuration's vertices.
 """
 import itertools
 
@@ -128,3 +130,38 @@ def test_tile_list_capacity(seed):
     counts = np.bincount(rng.integers(0, nblocks, nrec), minlength=nblocks) if nrec else np.zeros(nblocks, int)
     tiles = int(sum((c + TILE_N - 1) // TILE_N for c in counts))
     assert tiles <= nrec // TILE_N + nblocks + 1
+
+
+def descriptor_configs_per_warp(nmax):
+    """descriptor_configs_per_warp: whole configurations' vertices per 32 lanes."""
+    return 32 // nmax if 1 <= nmax <= 32 else 1
+
+
+@pytest.mark.parametrize("nmax", range(1, 25))
+def test_descriptor_warp_mapping(nmax):
+    """split_descriptors: one warp per K configurations, each vertex on a lane,
+    the pairs 32 at a time. Every (configuration, pair) of the batch is taken
+    exactly once, and both vertices of a pair are read from lanes holding that
+    configuration's vertices (lane < K nmax <= 32)."""
+    K = descriptor_configs_per_warp(nmax)
+    per_c = nmax * nmax
+    for batch in (1, 2, K, K + 1, 3 * K + 2, 97):
+        warps = (batch + K - 1) // K
+        seen = set()
+        for warp in range(warps):
+            c0 = warp * K
+            assert c0 < batch
+            total = K * per_c
+            for q0 in range(0, total, 32):
+                for lane in range(32):
+                    q = q0 + lane
+                    valid = q < total
+                    cq = q // per_c if valid else 0
+                    pair = q - cq * per_c if valid else 0
+                    i, j = divmod(pair, nmax)
+                    li, lj = cq * nmax + i, cq * nmax + j
+                    assert li < 32 and lj < 32 and li // nmax == cq and lj // nmax == cq
+                    if valid and c0 + cq < batch:
+                        assert (c0 + cq, pair) not in seen
+                        seen.add((c0 + cq, pair))
+        assert len(seen) == batch * per_c
