@@ -8,8 +8,9 @@ minors run from shared memory and at orders 12 and 14, whose minors use the
 workspace carved from the array. The first call on a device is the set-up
 call: it looks up the array's device address, which loads the library's
 module holding the array (the 64 MiB then stays with the GPU until exit). The
-calls after it must leave the device's free memory unchanged. A batch too
-large for the fixed scratch must be refused with a message. This file sorts
+calls after it must leave the device's free memory unchanged, also when one
+is captured into a CUDA graph and replayed. A batch too large for the fixed
+scratch must be refused with a message. This file sorts
 last so that a run stopping at the first failure has already run every other
 test.
 """
@@ -55,6 +56,47 @@ def test_noalloc_matches_device_entry_twice():
     for k in range(3):
         assert np.array_equal(values[k].cpu().numpy().view(np.uint64), want)
         assert np.array_equal(status[k].cpu().numpy(), ref_status.cpu().numpy())
+
+
+def test_noalloc_in_a_cuda_graph():
+    """The use the entry exists for: after the set-up call (outside any
+    capture), one call captured into a CUDA graph on a side stream and
+    replayed twice; every replay gives the ordinary entry point's values and
+    statuses bit for bit and leaves the device's free memory as it was."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    params = CdetParams(n1=4, n2=4, beta="6", mu="0", u="2",
+                        mask_sites=named_mask("origin_square", 4, 4, 1), cheb_nu=32, cheb_nv=32)
+    gpu = CdetIntegrand(params, build_tables(params, device="cuda"))
+    batch, nmax = 384, 8
+    v = torch.from_numpy(uniform_configurations(5252, batch, nmax)).cuda()
+    o = torch.from_numpy(truncated_geometric_orders(5253, batch, 0.3, nmax)).cuda()
+    ref_values = torch.empty(batch, dtype=torch.float64, device="cuda")
+    ref_status = torch.empty(batch, dtype=torch.int32, device="cuda")
+    gpu.integrand_device(v, o, ref_values, ref_status)
+    values = torch.full((batch,), float("nan"), dtype=torch.float64, device="cuda")
+    status = torch.full((batch,), -1, dtype=torch.int32, device="cuda")
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        assert gpu.integrand_device_noalloc(v, o, values, status, side) == L.CDET_OK, L.last_error()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        rc = gpu.integrand_device_noalloc(v, o, values, status, torch.cuda.current_stream())
+    assert rc == L.CDET_OK, L.last_error()
+    values.fill_(float("nan"))
+    status.fill_(-1)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    want_v, want_s = ref_values.cpu().numpy().view(np.uint64), ref_status.cpu().numpy()
+    for _ in range(2):
+        graph.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(values.cpu().numpy().view(np.uint64), want_v)
+        assert np.array_equal(status.cpu().numpy(), want_s)
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
 
 
 def test_noalloc_rejects_oversized_batch():
